@@ -1,0 +1,381 @@
+"""GB300 compressed precomputed shadows: Python mirror of the reference API.
+
+The reference (TobiasRp/cpvs) exposes the shadow path as C++ classes:
+``MinMaxHierarchy(const ImageF&)``, ``CompressedShadow::create(minMax,
+zTileIndex, zTileNum)``, ``CompressedShadow::traverse(ndc, tryLeafmasks)``,
+``getDAG()``, ``getTotalVisibility()``, ``getNumLevels()`` and
+``CompressedShadowContainer``.  This package keeps those names and argument
+meanings over the library's C ABI (include/cpvs.h, libcpvs_gb300.so); every
+computation runs on the GPU.  The library is loaded from this directory and
+is required: importing the API without it raises, there is no fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcpvs_gb300.so")
+
+SHADOW, VISIBLE, PARTIAL = 0, 1, 2
+FLAG_LEAFMASKS = 0x1
+IO_DEVICE = 0x100
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "device wait timed out",
+          4: "CUDA device error", 5: "unimplemented", 6: "memory budget exceeded", 7: "cancelled",
+          8: "output buffer too small"}
+
+
+class CpvsError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+# name -> (restype, argtypes)
+_vp, _u32, _u64, _i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
+_SIGS = {
+    "cpvs_abi_version": (C.c_int, []),
+    "cpvs_status_string": (C.c_char_p, [C.c_int]),
+    "cpvs_last_error": (C.c_char_p, []),
+    "cpvs_ctx_create": (C.c_int, [C.c_int, C.POINTER(_vp)]),
+    "cpvs_ctx_destroy": (None, [_vp]),
+    "cpvs_ctx_set_budget": (C.c_int, [_vp, _u64]),
+    "cpvs_ctx_bytes_in_use": (_u64, [_vp]),
+    "cpvs_hierarchy_create": (C.c_int, [_vp, _vp, _u32, _u32, _vp, C.POINTER(_vp)]),
+    "cpvs_hierarchy_destroy": (None, [_vp]),
+    "cpvs_hierarchy_num_levels": (_u32, [_vp]),
+    "cpvs_hierarchy_size": (_u32, [_vp]),
+    "cpvs_hierarchy_level": (C.c_int, [_vp, _u32, _vp, _u64, _vp]),
+    "cpvs_shadow_create": (C.c_int, [_vp, _vp, _u32, _u32, _u32, _vp, C.POINTER(_vp)]),
+    "cpvs_shadow_create_from_depth": (C.c_int, [_vp, _vp, _u32, _u32, _u32, _u32, _vp, C.POINTER(_vp)]),
+    "cpvs_shadow_destroy": (None, [_vp]),
+    "cpvs_shadow_num_levels": (_u32, [_vp]),
+    "cpvs_shadow_uses_leafmasks": (C.c_int, [_vp]),
+    "cpvs_shadow_total_visibility": (C.c_int, [_vp]),
+    "cpvs_shadow_dag_size": (_u64, [_vp]),
+    "cpvs_shadow_dag_words": (C.c_int, [_vp, _vp, _u64, C.POINTER(_u64), _vp]),
+    "cpvs_shadow_device_dag": (_vp, [_vp]),
+    "cpvs_shadow_level_counts": (C.c_int, [_vp, _vp, _vp, _u32]),
+    "cpvs_shadow_lookup_ndc": (C.c_int, [_vp, _vp, _u64, _vp, _u32, _vp]),
+    "cpvs_shadow_lookup_voxel": (C.c_int, [_vp, _vp, _u64, _vp, _u32, _vp]),
+    "cpvs_grid_create": (C.c_int, [_vp, _u32, C.POINTER(_vp)]),
+    "cpvs_grid_destroy": (None, [_vp]),
+    "cpvs_grid_length": (_u32, [_vp]),
+    "cpvs_grid_set": (C.c_int, [_vp, _u32, _u32, _u32, _vp]),
+    "cpvs_grid_get": (_vp, [_vp, _u32, _u32, _u32]),
+    "cpvs_grid_finalize": (C.c_int, [_vp, C.c_int, _vp]),
+    "cpvs_grid_dag_size": (_u64, [_vp]),
+    "cpvs_grid_words": (C.c_int, [_vp, _vp, _u64, _vp, _u64, _vp]),
+    "cpvs_grid_lookup_ndc": (C.c_int, [_vp, _vp, _u64, _vp, _u32, _vp]),
+}
+
+_lib: Optional[C.CDLL] = None
+
+
+def library_path() -> str:
+    return LIB_PATH
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Loads libcpvs_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -m cpvs_gb300.build` "
+                          "(the shadow path has no CPU fallback)")
+    lib = C.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols() -> list:
+    return list(_SIGS)
+
+
+def _check(status: int):
+    if status != 0:
+        msg = _lib.cpvs_last_error().decode(errors="replace") if _lib else ""
+        raise CpvsError(status, msg)
+
+
+def _ptr(a) -> int:
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return int(a.data_ptr())  # torch tensor
+
+
+def _is_device(a) -> bool:
+    return not isinstance(a, np.ndarray) and getattr(a, "is_cuda", False)
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        return 0
+    if isinstance(stream, int):
+        return stream
+    return int(stream.cuda_stream)
+
+
+class Context:
+    """One device (cpvs_ctx).  A process-wide default is created lazily."""
+
+    _default: Optional["Context"] = None
+
+    def __init__(self, device: int = 0):
+        lib = load_library()
+        h = _vp()
+        _check(lib.cpvs_ctx_create(device, C.byref(h)))
+        self.handle = h.value
+        self.device = device
+
+    @classmethod
+    def default(cls) -> "Context":
+        if cls._default is None:
+            cls._default = Context(0)
+        return cls._default
+
+    def set_budget(self, nbytes: int):
+        _check(_lib.cpvs_ctx_set_budget(self.handle, int(nbytes)))
+
+    def bytes_in_use(self) -> int:
+        return int(_lib.cpvs_ctx_bytes_in_use(self.handle))
+
+    def __del__(self):
+        if getattr(self, "handle", None) and _lib is not None:
+            _lib.cpvs_ctx_destroy(self.handle)
+            self.handle = None
+
+
+def unpack_bits(words: np.ndarray, n: int) -> np.ndarray:
+    """Bit-packed lookup result -> uint8 class per point (1 lit, 0 shadow)."""
+    b = np.unpackbits(np.ascontiguousarray(words, np.uint32).view(np.uint8), bitorder="little")
+    return b[:n].astype(np.uint8)
+
+
+class MinMaxHierarchy:
+    """Device min-max pyramid of a square power-of-two depth map
+    (src/MinMaxHierarchy.h:12-92).  `depth` is an (n, n) float32 numpy array
+    or CUDA tensor."""
+
+    def __init__(self, depth, ctx: Optional[Context] = None, stream=None):
+        self.ctx = ctx or Context.default()
+        n = int(depth.shape[0])
+        if depth.shape != (n, n):
+            raise ValueError("depth map must be square")
+        dev = _is_device(depth)
+        if not dev:
+            depth = np.ascontiguousarray(depth, np.float32)
+        h = _vp()
+        _check(_lib.cpvs_hierarchy_create(self.ctx.handle, _ptr(depth), n, IO_DEVICE if dev else 0,
+                                          _stream(stream), C.byref(h)))
+        self.handle = h.value
+        self.n = n
+        self._levels = {}
+
+    def get_num_levels(self) -> int:
+        return int(_lib.cpvs_hierarchy_num_levels(self.handle))
+
+    getNumLevels = get_num_levels
+
+    def level(self, level: int) -> np.ndarray:
+        """(s, s, 2) array of (min, max) of pyramid level `level` >= 1."""
+        if level not in self._levels:
+            s = self.n >> level
+            out = np.zeros((s, s, 2), np.float32)
+            _check(_lib.cpvs_hierarchy_level(self.handle, level, out.ctypes.data, out.size, 0))
+            self._levels[level] = out
+        return self._levels[level]
+
+    def get_min(self, level: int, x: int, y: int) -> float:
+        return float(self.level(level)[y, x, 0])
+
+    def get_max(self, level: int, x: int, y: int) -> float:
+        return float(self.level(level)[y, x, 1])
+
+    getMin, getMax = get_min, get_max
+
+    def __del__(self):
+        if getattr(self, "handle", None) and _lib is not None:
+            _lib.cpvs_hierarchy_destroy(self.handle)
+            self.handle = None
+
+
+class CompressedShadow:
+    """A resident shadow DAG (src/CompressedShadow.h:20-125)."""
+
+    SHADOW, VISIBLE, PARTIAL = SHADOW, VISIBLE, PARTIAL
+
+    def __init__(self, handle: int, ctx: Context, owned: bool = True):
+        self.handle = handle
+        self.ctx = ctx
+        self._owned = owned
+        self._dag = None
+
+    @staticmethod
+    def create(min_max: MinMaxHierarchy, z_tile_index: int = 0, z_tile_num: int = 1, leafmasks: bool = True,
+               stream=None) -> "CompressedShadow":
+        """CompressedShadow::create(minMax, zTileIndex, zTileNum)."""
+        h = _vp()
+        _check(_lib.cpvs_shadow_create(min_max.ctx.handle, min_max.handle, z_tile_index, z_tile_num,
+                                       FLAG_LEAFMASKS if leafmasks else 0, _stream(stream), C.byref(h)))
+        return CompressedShadow(h.value, min_max.ctx)
+
+    @staticmethod
+    def from_depth(depth, z_tile_index: int = 0, z_tile_num: int = 1, leafmasks: bool = True,
+                   ctx: Optional[Context] = None, stream=None) -> "CompressedShadow":
+        """CompressedShadow::create(const ShadowMap*, ...): depth map -> DAG."""
+        ctx = ctx or Context.default()
+        n = int(depth.shape[0])
+        dev = _is_device(depth)
+        if not dev:
+            depth = np.ascontiguousarray(depth, np.float32)
+        flags = (FLAG_LEAFMASKS if leafmasks else 0) | (IO_DEVICE if dev else 0)
+        h = _vp()
+        _check(_lib.cpvs_shadow_create_from_depth(ctx.handle, _ptr(depth), n, z_tile_index, z_tile_num, flags,
+                                                  _stream(stream), C.byref(h)))
+        return CompressedShadow(h.value, ctx)
+
+    def get_num_levels(self) -> int:
+        return int(_lib.cpvs_shadow_num_levels(self.handle))
+
+    def uses_leafmasks(self) -> bool:
+        return bool(_lib.cpvs_shadow_uses_leafmasks(self.handle))
+
+    def get_total_visibility(self) -> int:
+        return int(_lib.cpvs_shadow_total_visibility(self.handle))
+
+    def dag_size(self) -> int:
+        return int(_lib.cpvs_shadow_dag_size(self.handle))
+
+    def get_dag(self) -> np.ndarray:
+        """CompressedShadow::getDAG(): the DAG words, copied to the host."""
+        if self._dag is None:
+            n = self.dag_size()
+            out = np.zeros(max(n, 1), np.uint32)
+            _check(_lib.cpvs_shadow_dag_words(self.handle, out.ctypes.data, out.size, None, 0))
+            self._dag = out[:n]
+        return self._dag
+
+    getNumLevels, getTotalVisibility, getDAG = get_num_levels, get_total_visibility, get_dag
+
+    def device_dag(self) -> int:
+        return int(_lib.cpvs_shadow_device_dag(self.handle) or 0)
+
+    def level_counts(self):
+        nl = self.get_num_levels()
+        t = np.zeros(nl, np.uint64)
+        u = np.zeros(nl, np.uint64)
+        _check(_lib.cpvs_shadow_level_counts(self.handle, t.ctypes.data, u.ctypes.data, nl))
+        return t.astype(np.int64).tolist(), u.astype(np.int64).tolist()
+
+    def lookup_ndc(self, points, out=None, stream=None):
+        """Visibility of (n, 3) float32 NDC points.  numpy in -> uint8 classes
+        out; CUDA tensor in -> bit-packed int32 CUDA tensor out."""
+        return self._lookup(points, True, out, stream)
+
+    def lookup_voxel(self, points, out=None, stream=None):
+        """Visibility of (n, 3) int32 voxel coordinates."""
+        return self._lookup(points, False, out, stream)
+
+    def _lookup(self, points, ndc: bool, out, stream):
+        fn = _lib.cpvs_shadow_lookup_ndc if ndc else _lib.cpvs_shadow_lookup_voxel
+        n = int(points.shape[0])
+        if _is_device(points):
+            import torch
+            if out is None:
+                out = torch.empty((n + 31) // 32, dtype=torch.int32, device=points.device)
+            _check(fn(self.handle, _ptr(points), n, _ptr(out), IO_DEVICE, _stream(stream)))
+            return out
+        pts = np.ascontiguousarray(points, np.float32 if ndc else np.int32)
+        words = np.zeros(max((n + 31) // 32, 1), np.uint32)
+        _check(fn(self.handle, pts.ctypes.data, n, words.ctypes.data, 0, _stream(stream)))
+        return unpack_bits(words, n)
+
+    def traverse(self, position, try_leafmasks: bool = True) -> int:
+        """CompressedShadow::traverse(ndc, tryLeafmasks) for one point (a
+        one-element GPU lookup; batch with lookup_ndc).  `try_leafmasks` must
+        match how the DAG was built, as in the reference."""
+        if bool(try_leafmasks) != self.uses_leafmasks():
+            raise ValueError("try_leafmasks must match the DAG's leafmask mode")
+        return int(self.lookup_ndc(np.asarray(position, np.float32).reshape(1, 3))[0])
+
+    def release(self):
+        if getattr(self, "handle", None) and self._owned and _lib is not None:
+            _lib.cpvs_shadow_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        self.release()
+
+
+class CompressedShadowContainer:
+    """Cubic length^3 top-level grid of DAGs (src/CompressedShadowContainer.h:21-73)."""
+
+    def __init__(self, length: int = 1, ctx: Optional[Context] = None):
+        self.ctx = ctx or Context.default()
+        h = _vp()
+        _check(_lib.cpvs_grid_create(self.ctx.handle, length, C.byref(h)))
+        self.handle = h.value
+        self.length = length
+        self._cells = {}
+
+    @classmethod
+    def of(cls, shadow: CompressedShadow) -> "CompressedShadowContainer":
+        c = cls(1, shadow.ctx)
+        c.set(shadow, 0, 0, 0)
+        return c
+
+    def set(self, shadow: CompressedShadow, x: int, y: int, z: int):
+        """Cell (x,y,z) takes ownership of the shadow's DAG."""
+        _check(_lib.cpvs_grid_set(self.handle, x, y, z, shadow.handle))
+        shadow._owned = False
+        self._cells[(x, y, z)] = shadow
+
+    def get(self, x: int, y: int, z: int) -> Optional[CompressedShadow]:
+        return self._cells.get((x, y, z))
+
+    def copy_to_gpu(self, stream=None):
+        _check(_lib.cpvs_grid_finalize(self.handle, 0, _stream(stream)))
+
+    def move_to_gpu(self, stream=None):
+        _check(_lib.cpvs_grid_finalize(self.handle, 1, _stream(stream)))
+        for s in self._cells.values():
+            s.handle = None
+        self._cells.clear()
+
+    copyToGPU, moveToGPU = copy_to_gpu, move_to_gpu
+
+    def words(self):
+        """(combined DAG words, per-cell words) after copy_to_gpu."""
+        n = int(_lib.cpvs_grid_dag_size(self.handle))
+        dag = np.zeros(max(n, 1), np.uint32)
+        cells = np.zeros(self.length ** 3, np.uint32)
+        _check(_lib.cpvs_grid_words(self.handle, dag.ctypes.data, dag.size, cells.ctypes.data, cells.size, 0))
+        return dag[:n], cells
+
+    def lookup_ndc(self, points, out=None, stream=None):
+        n = int(points.shape[0])
+        if _is_device(points):
+            import torch
+            if out is None:
+                out = torch.empty((n + 31) // 32, dtype=torch.int32, device=points.device)
+            _check(_lib.cpvs_grid_lookup_ndc(self.handle, _ptr(points), n, _ptr(out), IO_DEVICE, _stream(stream)))
+            return out
+        pts = np.ascontiguousarray(points, np.float32)
+        words = np.zeros(max((n + 31) // 32, 1), np.uint32)
+        _check(_lib.cpvs_grid_lookup_ndc(self.handle, pts.ctypes.data, n, words.ctypes.data, 0, _stream(stream)))
+        return unpack_bits(words, n)
+
+    def __del__(self):
+        if getattr(self, "handle", None) and _lib is not None:
+            _lib.cpvs_grid_destroy(self.handle)
+            self.handle = None

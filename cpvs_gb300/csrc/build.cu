@@ -1,0 +1,778 @@
+// Sparse-voxel-DAG build of one or many shadow z-tiles on the device.
+//
+// Replaces CompressedShadow::create (src/CompressedShadow.cpp:49-59):
+// constructSvo + constructLastLevels (:87-190), mergeCommonSubtrees with
+// cs::mergeLevel (:215-259, src/CompressedShadowUtil.h:137-182),
+// removeUnusedNodes (:261-304) and compress (:306-392).  The DAG words equal
+// the reference's whenever its own build is defined.
+//
+// The reference's output is fully determined by three facts, which the
+// kernels below reproduce level-synchronously instead of with pointer
+// rewriting:
+//   1. the SVO lists every level's nodes in breadth-first order (parents in
+//      order, children in child-index order x | y<<1 | z<<2);
+//   2. the merge keeps, per level, the FIRST occurrence of each distinct
+//      node, where a node is its 16-bit mask plus the merged identities of
+//      its children (inner levels) or its mask plus 64-bit leafmasks
+//      (leaf level), and
+//   3. the final array holds the levels top-down, each level's kept nodes in
+//      first-occurrence order, an inner node as 1+k words (mask, absolute
+//      child offsets) and a leaf as 1+2k words (mask, lo/hi of each partial
+//      slice's leafmask).
+//
+// Pipeline per build (all DAGs of a batch at once; each node carries its
+// job id and never merges across jobs):
+//   top-down, per level L:  expand_count + expand_write  (classify, scan,
+//                           write children)            -- breadth-first order
+//   leaf level:             leaf_masks (one warp per leaf, 16 ballots)
+//   bottom-up, per level L: dedup_insert (open-addressing hash, 64-bit keys
+//                           = 32-bit tag | node index, atomicMin keeps the
+//                           first occurrence, full-signature compare on tag
+//                           match), dedup_resolve, dedup_scan (ranks and word
+//                           offsets in one pair scan), dedup_remap
+//   layout:                 per-job level bases, then emit per level.
+// Scans are reduce-then-scan over contiguous per-CTA chunks: no CTA waits on
+// another, so nothing can hang.
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "common.cuh"
+
+namespace cpvs {
+namespace {
+
+constexpr int kThreads = 256;
+
+struct JobDev {
+    const float2* pyr;  // pyramid levels 1..log2(n)
+    const float* depth;  // level 0
+    uint32_t n, num_levels, z_idx, z_num;
+};
+
+// Per-level node arrays (capacity `cap`).
+struct LevelDev {
+    uint64_t* coord;   // packed node coordinate at this level
+    uint32_t* job;
+    uint32_t* mask;
+    uint32_t* first;   // index of the first child in the level below
+    uint32_t* uid;     // merged identity (rank among the level's kept nodes)
+    uint32_t* slot;    // hash slot during the merge
+    uint32_t* uniq;    // rank -> node index of the first occurrence
+    uint32_t* woff;    // rank -> word offset (running over the level)
+    uint64_t* slices;  // leaf level: 8 leafmasks per node
+    uint64_t* hash;    // leaf level: signature hash per node
+};
+
+// Per-job, per-level bookkeeping of segment boundaries (jobs are contiguous
+// in every level).
+struct SegDev {
+    uint32_t* nstart;  // [job * L_MAX + level]
+    uint32_t* nend;
+    uint32_t* ustart;
+    uint32_t* uend;
+    uint32_t* wstart;
+    uint32_t* wend;
+};
+
+struct Injected {  // a job's root, entering at its root level
+    uint64_t coord;
+    uint32_t job;
+    uint32_t pad;
+};
+
+__device__ __forceinline__ uint32_t seg_index(uint32_t job, int L) { return job * CPVS_MAX_LEVELS + (uint32_t)L; }
+
+// cs::createChildmask (src/CompressedShadowUtil.cpp:20-54) for the node at
+// `c` (level-L texel units): children x|y<<1|z<<2 over the 2x2 texels of
+// level L and z-cells z, z+1; 2 bits each (01 lit, 00 shadow, 10 partial).
+// Level 0 uses cs::absoluteVisible and never yields partial children.
+// A node whose 2x2 texels would fall outside its level (only possible after
+// an internal check already failed) reads nothing and yields mask 0.
+__device__ __forceinline__ uint32_t node_mask(const JobDev& J, int L, uint64_t c, uint32_t* err) {
+    const uint32_t x = unpack_x(c), y = unpack_y(c), z = unpack_z(c);
+    const uint32_t W = J.n >> L;
+    if (x + 1u >= W || y + 1u >= W) {
+        atomicOr(err, 4u);
+        return 0u;
+    }
+    const float H = __uint2float_rn((J.n >> L) * J.z_num);
+    float mn[4], mx[4];
+    if (L == 0) {
+        const float2 r0 = *reinterpret_cast<const float2*>(J.depth + (size_t)y * J.n + x);
+        const float2 r1 = *reinterpret_cast<const float2*>(J.depth + (size_t)(y + 1) * J.n + x);
+        mn[0] = mx[0] = r0.x;
+        mn[1] = mx[1] = r0.y;
+        mn[2] = mx[2] = r1.x;
+        mn[3] = mx[3] = r1.y;
+    } else {
+        const float2* P = J.pyr + pyramid_level_offset_dev(J.n, L);
+        const float4 r0 = *reinterpret_cast<const float4*>(P + (size_t)y * W + x);
+        const float4 r1 = *reinterpret_cast<const float4*>(P + (size_t)(y + 1) * W + x);
+        mn[0] = r0.x; mx[0] = r0.y;
+        mn[1] = r0.z; mx[1] = r0.w;
+        mn[2] = r1.x; mx[2] = r1.y;
+        mn[3] = r1.z; mx[3] = r1.w;
+    }
+    uint32_t m = 0;
+#pragma unroll
+    for (uint32_t ch = 0; ch < 8; ++ch) {
+        const uint32_t t = ch & 3u, zc = z + (ch >> 2);
+        uint32_t v;
+        if (L > 0)
+            v = classify_cell(zc, __fmul_rn(mn[t], H), __fmul_rn(mx[t], H));
+        else
+            v = voxel_lit(zc, __fmul_rn(mn[t], H)) ? kVisible : kShadow;
+        m |= v << (2u * ch);
+    }
+    return m;
+}
+
+// ---------------------------------------------------------------- top-down
+// Pass 1: per-CTA sum of partial children over its chunk of level L.
+__global__ void __launch_bounds__(kThreads)
+    k_expand_count(LevelDev cur, const uint32_t* __restrict__ counts, const JobDev* __restrict__ jobs, uint32_t njobs,
+                   int L, uint2* partials, uint32_t* err) {
+    __shared__ uint64_t red[32];
+    uint32_t b, e;
+    block_chunk(counts[L], b, e);
+    uint64_t s = 0;
+    for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        const uint32_t j = cur.job[i];
+        uint32_t m = 0;
+        if (j < njobs) {
+            m = node_mask(jobs[j], L, cur.coord[i], err);
+        } else {
+            atomicOr(err, 8u);
+            cur.job[i] = 0;  // keep later passes' job lookups in range
+        }
+        cur.mask[i] = m;
+        s += partial_children(m);
+    }
+    s = block_sum_u64(s, red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = make_uint2((uint32_t)s, 0u);
+}
+
+// Pass 2: scan the partials, then write first[], the children's coordinates
+// and jobs (children after the `ninj` roots that enter level L-1), and the
+// level L-1 count.  Also records each job's node range at level L.
+__global__ void __launch_bounds__(kThreads)
+    k_expand_write(LevelDev cur, LevelDev nxt, uint32_t* counts, int L, const uint2* __restrict__ partials,
+                   const Injected* __restrict__ inj, uint32_t ninj, SegDev seg, uint32_t cap_next, uint32_t* err) {
+    __shared__ uint32_t sm[64];
+    const uint32_t n = counts[L];
+    uint32_t b, e;
+    block_chunk(n, b, e);
+    uint32_t run = ninj + block_prefix_of_partials(partials, blockIdx.x, sm).x;
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+        // total children = prefix of the last block + its own partial
+        counts[L - 1] = run + partials[blockIdx.x].x;
+    }
+    if (blockIdx.x == 0)
+        for (uint32_t r = threadIdx.x; r < ninj; r += blockDim.x) {
+            nxt.coord[r] = inj[r].coord;
+            nxt.job[r] = inj[r].job;
+        }
+    for (uint32_t t0 = b; t0 < e; t0 += blockDim.x) {
+        const uint32_t i = t0 + threadIdx.x;
+        const bool valid = i < e;
+        const uint32_t m = valid ? cur.mask[i] : 0u;
+        const uint32_t k = partial_children(m);
+        uint2 tot;
+        const uint2 p = block_exclusive_scan2(make_uint2(k, 0u), tot, sm);
+        if (valid && run + p.x + k > cap_next) {
+            // more children than the level bound: drop them (the count
+            // already includes them; their slots keep stale coordinates,
+            // which node_mask rejects) and report
+            atomicOr(err, 1u);
+            cur.mask[i] = m & 0x5555u;
+            cur.first[i] = 0;
+        } else if (valid) {
+            const uint32_t f = run + p.x;
+            cur.first[i] = f;
+            const uint64_t c = cur.coord[i];
+            const uint32_t x = unpack_x(c), y = unpack_y(c), z = unpack_z(c), j = cur.job[i];
+            uint32_t r = 0;
+#pragma unroll
+            for (uint32_t ch = 0; ch < 8; ++ch)
+                if (m & (2u << (2u * ch))) {
+                    // cs::getChildCoordinates (src/CompressedShadowUtil.cpp:101-117)
+                    nxt.coord[f + r] = pack_xyz((x + (ch & 1u)) * 2u, (y + ((ch >> 1) & 1u)) * 2u, (z + (ch >> 2)) * 2u);
+                    nxt.job[f + r] = j;
+                    ++r;
+                }
+            if (i == 0 || cur.job[i - 1] != j) seg.nstart[seg_index(j, L)] = i;
+            if (i == n - 1 || cur.job[i + 1] != j) seg.nend[seg_index(j, L)] = i + 1;
+        }
+        run += tot.x;
+    }
+}
+
+// Bottom level without leafmasks (level 0): masks only, no children.
+__global__ void __launch_bounds__(kThreads)
+    k_classify_bottom(LevelDev cur, const uint32_t* __restrict__ counts, const JobDev* __restrict__ jobs,
+                      uint32_t njobs, int L, SegDev seg, uint32_t* err) {
+    const uint32_t n = counts[L];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t j = cur.job[i];
+        if (j >= njobs) {
+            atomicOr(err, 8u);
+            cur.mask[i] = 0;
+            cur.job[i] = 0;
+            continue;
+        }
+        cur.mask[i] = node_mask(jobs[j], L, cur.coord[i], err);
+        if (i == 0 || cur.job[i - 1] != j) seg.nstart[seg_index(j, L)] = i;
+        if (i == n - 1 || cur.job[i + 1] != j) seg.nend[seg_index(j, L)] = i + 1;
+    }
+}
+
+// Leaf level (level 2 with leafmasks): createChildmask1x1x8 + createLeafmask
+// (src/CompressedShadowUtil.cpp:59-99).  One warp per leaf: lane l holds the
+// voxel columns (x,y) = (l&7, l>>3) and (l&7, 4+(l>>3)) of the 8x8 footprint,
+// so slice s's 64-bit mask is ballot(lit(row<4)) | ballot(lit(row>=4)) << 32,
+// bit x+8y exactly as the reference.  Also the leaf's mask, signature hash
+// and job-range bookkeeping.
+__global__ void __launch_bounds__(kThreads)
+    k_leaf_masks(LevelDev lv, const uint32_t* __restrict__ counts, const JobDev* __restrict__ jobs, uint32_t njobs,
+                 int L, SegDev seg, uint32_t* err) {
+    const uint32_t n = counts[L];
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nw) {
+        const uint64_t c = lv.coord[i];
+        const uint32_t j = lv.job[i];
+        const uint32_t bx = unpack_x(c) * 4u, by = unpack_y(c) * 4u, bz = unpack_z(c) * 4u;
+        if (j >= njobs || bx + 8u > jobs[j].n || by + 8u > jobs[j].n) {
+            // stale slot (an internal check already failed): inert leaf
+            if (lane < 8) lv.slices[(size_t)i * 8 + lane] = 0;
+            if (lane == 0) {
+                atomicOr(err, 4u);
+                lv.mask[i] = 0;
+                lv.job[i] = 0;
+                lv.hash[i] = 0;
+            }
+            continue;
+        }
+        const JobDev J = jobs[j];
+        const float H = __uint2float_rn(J.n * J.z_num);
+        const uint32_t col = bx + (uint32_t)(lane & 7), row = by + (uint32_t)(lane >> 3);
+        const float d0 = __fmul_rn(J.depth[(size_t)row * J.n + col], H);
+        const float d1 = __fmul_rn(J.depth[(size_t)(row + 4) * J.n + col], H);
+        uint64_t mine = 0;
+#pragma unroll
+        for (uint32_t s = 0; s < 8; ++s) {
+            const uint32_t lo = __ballot_sync(0xffffffffu, voxel_lit(bz + s, d0));
+            const uint32_t hi = __ballot_sync(0xffffffffu, voxel_lit(bz + s, d1));
+            if ((uint32_t)lane == s) mine = (uint64_t)lo | ((uint64_t)hi << 32);
+        }
+        const bool full = mine == ~0ull, empty = mine == 0ull;
+        const uint32_t vis = __ballot_sync(0xffffffffu, lane < 8 && full) & 0xFFu;
+        const uint32_t part = __ballot_sync(0xffffffffu, lane < 8 && !full && !empty) & 0xFFu;
+        const uint32_t mask = spread8(vis) | (spread8(part) << 1);
+        uint64_t h = (lane < 8) ? fmix64(mine + (uint64_t)(lane + 1) * kGolden) : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) h ^= __shfl_xor_sync(0xffffffffu, h, o);
+        if (lane < 8) lv.slices[(size_t)i * 8 + lane] = mine;
+        if (lane == 0) {
+            lv.mask[i] = mask;
+            lv.hash[i] = fmix64(h ^ ((uint64_t)(j + 1) * kGolden));
+            if (i == 0 || lv.job[i - 1] != j) seg.nstart[seg_index(j, L)] = i;
+            if (i == n - 1 || lv.job[i + 1] != j) seg.nend[seg_index(j, L)] = i + 1;
+        }
+    }
+}
+
+// --------------------------------------------------------------- bottom-up
+__device__ __forceinline__ uint64_t inner_hash(const LevelDev& cur, const LevelDev& child, uint32_t i) {
+    const uint32_t m = cur.mask[i];
+    uint64_t h = fmix64((((uint64_t)cur.job[i] + 1) << 32 | m) ^ kGolden);
+    const uint32_t k = partial_children(m), f = cur.first[i];
+    for (uint32_t r = 0; r < k; ++r) h = fmix64(h ^ ((uint64_t)child.uid[f + r] + (uint64_t)(r + 1) * kGolden));
+    return h;
+}
+
+template <bool LEAF>
+__device__ __forceinline__ bool same_node(const LevelDev& cur, const LevelDev& child, uint32_t a, uint32_t b) {
+    if (cur.job[a] != cur.job[b]) return false;
+    if (LEAF) {
+        const ulonglong2* sa = reinterpret_cast<const ulonglong2*>(cur.slices + (size_t)a * 8);
+        const ulonglong2* sb = reinterpret_cast<const ulonglong2*>(cur.slices + (size_t)b * 8);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const ulonglong2 x = sa[q], y = sb[q];
+            if (x.x != y.x || x.y != y.y) return false;
+        }
+        return true;
+    } else {
+        const uint32_t m = cur.mask[a];
+        if (m != cur.mask[b]) return false;
+        const uint32_t k = partial_children(m), fa = cur.first[a], fb = cur.first[b];
+        for (uint32_t r = 0; r < k; ++r)
+            if (child.uid[fa + r] != child.uid[fb + r]) return false;
+        return true;
+    }
+}
+
+// Inserts every node of level L into the table.  A slot holds
+// (tag << 32 | node index); the first node of a signature class claims an
+// empty slot with CAS, later equal nodes lower it with atomicMin, so the slot
+// ends with the class's smallest (first-occurring) index.  The probe is
+// bounded by the table size (the table is at least twice the node count).
+template <bool LEAF>
+__global__ void __launch_bounds__(kThreads)
+    k_dedup_insert(LevelDev cur, LevelDev child, const uint32_t* __restrict__ counts, int L,
+                   unsigned long long* table, uint64_t cap_mask) {
+    const uint32_t n = counts[L];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint64_t h = LEAF ? cur.hash[i] : inner_hash(cur, child, i);
+        const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | i;
+        uint64_t s = h & cap_mask;
+        for (uint64_t probe = 0; probe <= cap_mask; ++probe) {
+            unsigned long long cur_e = __ldcg(&table[s]);
+            if (cur_e == kEmptySlot) {
+                const unsigned long long prev = atomicCAS(&table[s], kEmptySlot, key);
+                if (prev == kEmptySlot) break;
+                cur_e = prev;
+            }
+            if ((cur_e >> 32) == (key >> 32) && same_node<LEAF>(cur, child, i, (uint32_t)cur_e)) {
+                atomicMin(&table[s], key);
+                break;
+            }
+            s = (s + 1) & cap_mask;
+        }
+        cur.slot[i] = (uint32_t)s;
+    }
+}
+
+__device__ __forceinline__ uint32_t node_words(uint32_t m, bool leaf) {
+    return 1u + (leaf ? 2u : 1u) * partial_children(m);
+}
+
+// Representative of every node; per-CTA (kept count, kept words).
+template <bool LEAF>
+__global__ void __launch_bounds__(kThreads)
+    k_dedup_resolve(LevelDev cur, const uint32_t* __restrict__ counts, int L,
+                    const unsigned long long* __restrict__ table, uint2* partials) {
+    __shared__ uint64_t red[32];
+    uint32_t b, e;
+    block_chunk(counts[L], b, e);
+    uint64_t kept = 0, words = 0;
+    for (uint32_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        const uint32_t rep = (uint32_t)table[cur.slot[i]];
+        cur.uid[i] = rep;
+        if (rep == i) {
+            ++kept;
+            words += node_words(cur.mask[i], LEAF);
+        }
+    }
+    kept = block_sum_u64(kept, red);
+    words = block_sum_u64(words, red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = make_uint2((uint32_t)kept, (uint32_t)words);
+}
+
+// Ranks and word offsets of the kept nodes in node order; each kept node
+// writes its rank into its table slot for dedup_remap.
+template <bool LEAF>
+__global__ void __launch_bounds__(kThreads)
+    k_dedup_scan(LevelDev cur, const uint32_t* __restrict__ counts, uint32_t* level_u, int L,
+                 unsigned long long* table, const uint2* __restrict__ partials, SegDev seg) {
+    __shared__ uint32_t sm[64];
+    const uint32_t n = counts[L];
+    uint32_t b, e;
+    block_chunk(n, b, e);
+    uint2 run = block_prefix_of_partials(partials, blockIdx.x, sm);
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+        level_u[2 * L] = run.x + partials[blockIdx.x].x;
+        level_u[2 * L + 1] = run.y + partials[blockIdx.x].y;
+    }
+    for (uint32_t t0 = b; t0 < e; t0 += blockDim.x) {
+        const uint32_t i = t0 + threadIdx.x;
+        const bool valid = i < e;
+        const bool kept = valid && cur.uid[i] == i;
+        const uint32_t w = kept ? node_words(cur.mask[i], LEAF) : 0u;
+        uint2 tot;
+        const uint2 p = block_exclusive_scan2(make_uint2(kept ? 1u : 0u, w), tot, sm);
+        const uint2 q = make_uint2(run.x + p.x, run.y + p.y);
+        if (kept) {
+            cur.uniq[q.x] = i;
+            cur.woff[q.x] = q.y;
+            table[cur.slot[i]] = q.x;
+        }
+        if (valid) {
+            const uint32_t j = cur.job[i];
+            if (i == 0 || cur.job[i - 1] != j) {
+                seg.ustart[seg_index(j, L)] = q.x;
+                seg.wstart[seg_index(j, L)] = q.y;
+            }
+            if (i == n - 1 || cur.job[i + 1] != j) {
+                seg.uend[seg_index(j, L)] = q.x + (kept ? 1u : 0u);
+                seg.wend[seg_index(j, L)] = q.y + w;
+            }
+        }
+        run.x += tot.x;
+        run.y += tot.y;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads)
+    k_dedup_remap(LevelDev cur, const uint32_t* __restrict__ counts, int L, const unsigned long long* __restrict__ table) {
+    const uint32_t n = counts[L];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        cur.uid[i] = (uint32_t)table[cur.slot[i]];
+}
+
+// ------------------------------------------------------------------ layout
+// Per job: level bases top-down and the DAG size; then job offsets.
+struct JobLayout {
+    uint64_t* job_off;  // [njobs + 1]
+    uint32_t* base;     // [job * L_MAX + level]: word offset of the level in the job's DAG
+};
+
+__global__ void k_layout(SegDev seg, JobLayout lay, const uint32_t* __restrict__ root_level, uint32_t njobs, int bottom) {
+    // single block: each thread sums its jobs, then a block scan over jobs in
+    // rounds of blockDim
+    __shared__ uint32_t sm[64];
+    uint64_t carry = 0;
+    for (uint32_t j0 = 0; j0 < njobs; j0 += blockDim.x) {
+        const uint32_t j = j0 + threadIdx.x;
+        uint64_t total = 0;
+        if (j < njobs) {
+            for (int L = (int)root_level[j]; L >= bottom; --L) {
+                const uint32_t s = seg_index(j, L);
+                lay.base[s] = (uint32_t)total;
+                total += seg.wend[s] - seg.wstart[s];
+            }
+        }
+        // totals stay below 2^32 words per job (checked on the host)
+        uint2 tot;
+        const uint2 p = block_exclusive_scan2(make_uint2((uint32_t)total, 0u), tot, sm);
+        if (j < njobs) lay.job_off[j] = carry + p.x;
+        carry += tot.x;
+    }
+    if (threadIdx.x == 0) lay.job_off[njobs] = carry;
+}
+
+template <bool LEAF>
+__global__ void __launch_bounds__(kThreads)
+    k_emit(LevelDev cur, LevelDev child, const uint32_t* __restrict__ level_u, int L, SegDev seg, JobLayout lay,
+           uint32_t* __restrict__ out, uint64_t total_words, uint32_t* err) {
+    const uint32_t U = level_u[2 * L];
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < U; u += gridDim.x * blockDim.x) {
+        const uint32_t i = cur.uniq[u];
+        const uint32_t j = cur.job[i];
+        const uint32_t sj = seg_index(j, L);
+        const uint32_t m = cur.mask[i];
+        const uint64_t at = lay.job_off[j] + lay.base[sj] + (cur.woff[u] - seg.wstart[sj]);
+        if (at + node_words(m, LEAF) > total_words) {
+            atomicOr(err, 2u);  // layout out of range: skip, report
+            continue;
+        }
+        uint32_t* dst = out + at;
+        dst[0] = m;
+        if (LEAF) {
+            uint32_t r = 0;
+#pragma unroll
+            for (uint32_t s = 0; s < 8; ++s)
+                if (((m >> (2u * s)) & 3u) == kPartial) {
+                    const uint64_t v = cur.slices[(size_t)i * 8 + s];
+                    dst[1 + 2 * r] = (uint32_t)v;
+                    dst[2 + 2 * r] = (uint32_t)(v >> 32);
+                    ++r;
+                }
+        } else {
+            const uint32_t k = partial_children(m), f = cur.first[i];
+            const uint32_t sc = seg_index(j, L - 1);
+            const uint32_t cb = lay.base[sc] - seg.wstart[sc];
+            for (uint32_t r = 0; r < k; ++r) dst[1 + r] = cb + child.woff[child.uid[f + r]];
+        }
+    }
+}
+
+// --------------------------------------------------------------- host side
+inline uint64_t next_pow2(uint64_t v) {
+    uint64_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// A bump allocator over one device block.
+struct Arena {
+    char* base = nullptr;
+    size_t size = 0, used = 0;
+    template <class T>
+    T* take(size_t count) {
+        const size_t b = align256(count * sizeof(T));
+        T* p = reinterpret_cast<T*>(base + used);
+        used += b;
+        return p;
+    }
+};
+
+}  // namespace
+
+cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const std::vector<JobSpec>& jobs,
+                       bool leafmasks, cudaStream_t st, BuildOutput& out) {
+    const uint32_t njobs = (uint32_t)jobs.size();
+    if (njobs == 0) return fail(CPVS_ERR_INVALID_ARG, "build_dags: no jobs");
+    const int bottom = leafmasks ? 2 : 0;
+    const int lmin = bottom + 1;  // pyramid level whose cells become bottom nodes
+
+    // ---- per-job geometry
+    std::vector<uint32_t> root_level(njobs);
+    int maxR = 0;
+    for (uint32_t j = 0; j < njobs; ++j) {
+        const SourceSpec& S = sources[jobs[j].source];
+        const int nl = log2_u32(S.n) + 1;
+        root_level[j] = (uint32_t)(nl - 2);
+        maxR = std::max(maxR, nl - 2);
+        if ((nl - 3 >= 2) != leafmasks) return fail(CPVS_ERR_INVALID_ARG, "build_dags: mixed leafmask modes");
+    }
+
+    // ---- level bounds (one pass over each source's pyramid), one sync
+    const size_t bounds_bytes = (size_t)njobs * CPVS_MAX_LEVELS * sizeof(unsigned long long);
+    unsigned long long* bounds_dev = nullptr;
+    BoundJob* bj_dev = nullptr;
+    std::vector<BoundJob> bj(njobs);
+    for (uint32_t j = 0; j < njobs; ++j) bj[j] = BoundJob{jobs[j].z_idx, jobs[j].z_num, j};
+    CPVS_CUDA(cudaMallocAsync((void**)&bounds_dev, bounds_bytes, st));
+    CPVS_CUDA(cudaMallocAsync((void**)&bj_dev, njobs * sizeof(BoundJob), st));
+    CPVS_CUDA(cudaMemsetAsync(bounds_dev, 0, bounds_bytes, st));
+    {
+        // jobs grouped by source (jobs of one source need not be adjacent)
+        std::vector<std::vector<uint32_t>> by_src(sources.size());
+        for (uint32_t j = 0; j < njobs; ++j) by_src[jobs[j].source].push_back(j);
+        std::vector<BoundJob> grouped;
+        std::vector<std::pair<size_t, size_t>> ranges(sources.size());
+        for (size_t s = 0; s < sources.size(); ++s) {
+            ranges[s] = {grouped.size(), by_src[s].size()};
+            for (uint32_t j : by_src[s]) grouped.push_back(bj[j]);
+        }
+        CPVS_CUDA(cudaMemcpyAsync(bj_dev, grouped.data(), njobs * sizeof(BoundJob), cudaMemcpyHostToDevice, st));
+        for (size_t s = 0; s < sources.size(); ++s) {
+            if (!ranges[s].second) continue;
+            cpvs_status r = launch_level_bounds(sources[s].levels, sources[s].n, lmin, bj_dev + ranges[s].first,
+                                                (int)ranges[s].second, bounds_dev, st);
+            if (r != CPVS_OK) return r;
+        }
+    }
+    std::vector<unsigned long long> bounds((size_t)njobs * CPVS_MAX_LEVELS);
+    CPVS_CUDA(cudaMemcpyAsync(bounds.data(), bounds_dev, bounds_bytes, cudaMemcpyDeviceToHost, st));
+    CPVS_CUDA(cudaStreamSynchronize(st));
+    cudaFreeAsync(bounds_dev, st);
+    cudaFreeAsync(bj_dev, st);
+
+    // capacity per level: bounded children + roots entering there
+    std::vector<uint64_t> cap(CPVS_MAX_LEVELS, 0), ninj(CPVS_MAX_LEVELS, 0);
+    for (uint32_t j = 0; j < njobs; ++j) {
+        ninj[root_level[j]] += 1;
+        for (int L = bottom; L < (int)root_level[j]; ++L) cap[L] += bounds[(size_t)j * CPVS_MAX_LEVELS + L];
+    }
+    uint64_t maxcap = 0;
+    for (int L = 0; L < CPVS_MAX_LEVELS; ++L) {
+        cap[L] += ninj[L];
+        if (cap[L] >= (1ull << 31)) return fail(CPVS_ERR_BUDGET, "build_dags: a level exceeds 2^31 nodes");
+        maxcap = std::max(maxcap, cap[L]);
+    }
+    const uint64_t table_cap = next_pow2(std::max<uint64_t>(2 * maxcap, 1024));
+
+    // ---- launch shapes
+    const uint32_t max_grid = (uint32_t)std::max(ctx.num_sms, 1) * 8;
+    auto grid_for = [&](uint64_t items, uint64_t per_block) -> uint32_t {
+        uint64_t g = (items + per_block - 1) / per_block;
+        return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, max_grid));
+    };
+
+    // ---- scratch arena
+    size_t bytes = 0;
+    auto add = [&](size_t count, size_t elem) { bytes += align256(count * elem); };
+    for (int L = bottom; L <= maxR; ++L) {
+        const uint64_t c = std::max<uint64_t>(cap[L], 1);
+        add(c, 8); add(c, 4); add(c, 4); add(c, 4); add(c, 4); add(c, 4); add(c, 4); add(c, 4);
+        if (leafmasks && L == 2) { add(c * 8, 8); add(c, 8); }
+    }
+    add(table_cap, 8);
+    add(max_grid, sizeof(uint2));
+    add(CPVS_MAX_LEVELS, 4);       // counts
+    add(2 * CPVS_MAX_LEVELS, 4);   // level (U, W)
+    add(1, 4);                     // error word
+    add((size_t)njobs * CPVS_MAX_LEVELS * 7, 4);  // seg arrays + base
+    add(njobs + 1, 8);             // job_off
+    add(njobs, 4);                 // root levels
+    add(njobs, sizeof(JobDev));
+    add(njobs, sizeof(Injected));
+    Arena A;
+    A.size = bytes;
+    {
+        cpvs_status r = ctx.alloc((void**)&A.base, bytes, false, st);
+        if (r != CPVS_OK) return r;
+    }
+    struct Free {
+        Ctx& c; Arena& a; cudaStream_t s;
+        ~Free() {
+            if (a.base) c.release(a.base, a.size, false, s);
+        }
+    } free_guard{ctx, A, st};
+
+    LevelDev lv[CPVS_MAX_LEVELS];
+    std::memset(lv, 0, sizeof(lv));
+    for (int L = bottom; L <= maxR; ++L) {
+        const uint64_t c = std::max<uint64_t>(cap[L], 1);
+        lv[L].coord = A.take<uint64_t>(c);
+        lv[L].job = A.take<uint32_t>(c);
+        lv[L].mask = A.take<uint32_t>(c);
+        lv[L].first = A.take<uint32_t>(c);
+        lv[L].uid = A.take<uint32_t>(c);
+        lv[L].slot = A.take<uint32_t>(c);
+        lv[L].uniq = A.take<uint32_t>(c);
+        lv[L].woff = A.take<uint32_t>(c);
+        if (leafmasks && L == 2) {
+            lv[L].slices = A.take<uint64_t>(c * 8);
+            lv[L].hash = A.take<uint64_t>(c);
+        }
+    }
+    unsigned long long* table = A.take<unsigned long long>(table_cap);
+    uint2* partials = A.take<uint2>(max_grid);
+    uint32_t* counts = A.take<uint32_t>(CPVS_MAX_LEVELS);
+    uint32_t* level_u = A.take<uint32_t>(2 * CPVS_MAX_LEVELS);
+    uint32_t* err = A.take<uint32_t>(1);
+    const size_t segn = (size_t)njobs * CPVS_MAX_LEVELS;
+    uint32_t* segbuf = A.take<uint32_t>(segn * 7);
+    SegDev seg{segbuf, segbuf + segn, segbuf + 2 * segn, segbuf + 3 * segn, segbuf + 4 * segn, segbuf + 5 * segn};
+    JobLayout lay{A.take<uint64_t>(njobs + 1), segbuf + 6 * segn};
+    uint32_t* root_dev = A.take<uint32_t>(njobs);
+    JobDev* jobs_dev = A.take<JobDev>(njobs);
+    Injected* inj_dev = A.take<Injected>(njobs);
+
+    // ---- job table and roots (grouped by root level, in job order)
+    std::vector<JobDev> jd(njobs);
+    std::vector<Injected> inj;
+    std::vector<uint64_t> inj_off(CPVS_MAX_LEVELS + 1, 0);
+    for (uint32_t j = 0; j < njobs; ++j) {
+        const SourceSpec& S = sources[jobs[j].source];
+        jd[j] = JobDev{S.levels, S.depth, S.n, root_level[j] + 2, jobs[j].z_idx, jobs[j].z_num};
+    }
+    for (int L = 0; L < CPVS_MAX_LEVELS; ++L) {
+        inj_off[L] = inj.size();
+        for (uint32_t j = 0; j < njobs; ++j)
+            if ((int)root_level[j] == L) inj.push_back(Injected{pack_xyz(0, 0, 2 * jobs[j].z_idx), j, 0});
+    }
+    inj_off[CPVS_MAX_LEVELS] = inj.size();
+    CPVS_CUDA(cudaMemsetAsync(segbuf, 0, segn * 7 * sizeof(uint32_t), st));
+    CPVS_CUDA(cudaMemsetAsync(counts, 0, CPVS_MAX_LEVELS * sizeof(uint32_t), st));
+    CPVS_CUDA(cudaMemsetAsync(level_u, 0, 2 * CPVS_MAX_LEVELS * sizeof(uint32_t), st));
+    CPVS_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
+    CPVS_CUDA(cudaMemcpyAsync(jobs_dev, jd.data(), njobs * sizeof(JobDev), cudaMemcpyHostToDevice, st));
+    CPVS_CUDA(cudaMemcpyAsync(inj_dev, inj.data(), inj.size() * sizeof(Injected), cudaMemcpyHostToDevice, st));
+    CPVS_CUDA(cudaMemcpyAsync(root_dev, root_level.data(), njobs * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+
+    // top level: its roots only
+    {
+        const uint32_t c = (uint32_t)ninj[maxR];
+        std::vector<uint64_t> coords(c);
+        std::vector<uint32_t> js(c);
+        for (uint32_t r = 0; r < c; ++r) {
+            coords[r] = inj[inj_off[maxR] + r].coord;
+            js[r] = inj[inj_off[maxR] + r].job;
+        }
+        CPVS_CUDA(cudaMemcpyAsync(lv[maxR].coord, coords.data(), c * 8, cudaMemcpyHostToDevice, st));
+        CPVS_CUDA(cudaMemcpyAsync(lv[maxR].job, js.data(), c * 4, cudaMemcpyHostToDevice, st));
+        CPVS_CUDA(cudaMemcpyAsync(counts + maxR, &c, 4, cudaMemcpyHostToDevice, st));
+        CPVS_CUDA(cudaStreamSynchronize(st));  // `c` and the vectors leave scope
+    }
+
+    // ---- top-down
+    for (int L = maxR; L > bottom; --L) {
+        const uint32_t g = grid_for(cap[L], kThreads * 4);
+        k_expand_count<<<g, kThreads, 0, st>>>(lv[L], counts, jobs_dev, njobs, L, partials, err);
+        k_expand_write<<<g, kThreads, 0, st>>>(lv[L], lv[L - 1], counts, L, partials, inj_dev + inj_off[L - 1],
+                                               (uint32_t)ninj[L - 1], seg, (uint32_t)cap[L - 1], err);
+    }
+    if (leafmasks)
+        k_leaf_masks<<<grid_for(cap[2] * 32, kThreads), kThreads, 0, st>>>(lv[2], counts, jobs_dev, njobs, 2, seg, err);
+    else
+        k_classify_bottom<<<grid_for(cap[0], kThreads), kThreads, 0, st>>>(lv[0], counts, jobs_dev, njobs, 0, seg, err);
+    CPVS_CUDA(cudaGetLastError());
+
+    // ---- bottom-up merge
+    for (int L = bottom; L <= maxR; ++L) {
+        const uint64_t tcap = next_pow2(std::max<uint64_t>(2 * cap[L], 1024));
+        const uint64_t cmask = tcap - 1;
+        const bool leaf = leafmasks && L == 2;
+        const uint32_t gs = grid_for(cap[L], kThreads * 4);
+        const uint32_t gi = grid_for(cap[L], kThreads);
+        const LevelDev child = (L > bottom) ? lv[L - 1] : lv[L];
+        CPVS_CUDA(cudaMemsetAsync(table, 0xFF, tcap * sizeof(unsigned long long), st));
+        if (leaf) {
+            k_dedup_insert<true><<<gi, kThreads, 0, st>>>(lv[L], child, counts, L, table, cmask);
+            k_dedup_resolve<true><<<gs, kThreads, 0, st>>>(lv[L], counts, L, table, partials);
+            k_dedup_scan<true><<<gs, kThreads, 0, st>>>(lv[L], counts, level_u, L, table, partials, seg);
+        } else {
+            k_dedup_insert<false><<<gi, kThreads, 0, st>>>(lv[L], child, counts, L, table, cmask);
+            k_dedup_resolve<false><<<gs, kThreads, 0, st>>>(lv[L], counts, L, table, partials);
+            k_dedup_scan<false><<<gs, kThreads, 0, st>>>(lv[L], counts, level_u, L, table, partials, seg);
+        }
+        k_dedup_remap<<<gi, kThreads, 0, st>>>(lv[L], counts, L, table);
+        CPVS_CUDA(cudaGetLastError());
+    }
+
+    // ---- layout, one sync for the sizes
+    k_layout<<<1, 1024, 0, st>>>(seg, lay, root_dev, njobs, bottom);
+    CPVS_CUDA(cudaGetLastError());
+    std::vector<uint64_t> job_off(njobs + 1);
+    std::vector<uint32_t> hseg(segn * 6);
+    std::vector<uint32_t> hcounts(CPVS_MAX_LEVELS), hlu(2 * CPVS_MAX_LEVELS);
+    CPVS_CUDA(cudaMemcpyAsync(job_off.data(), lay.job_off, (njobs + 1) * 8, cudaMemcpyDeviceToHost, st));
+    CPVS_CUDA(cudaMemcpyAsync(hseg.data(), segbuf, segn * 6 * 4, cudaMemcpyDeviceToHost, st));
+    CPVS_CUDA(cudaMemcpyAsync(hlu.data(), level_u, 2 * CPVS_MAX_LEVELS * 4, cudaMemcpyDeviceToHost, st));
+    uint32_t herr = 0;
+    CPVS_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+    CPVS_CUDA(cudaStreamSynchronize(st));
+    if (herr) return fail(CPVS_ERR_DEVICE, "build_dags: a level outgrew its bound (internal check " + std::to_string(herr) + ")");
+    const uint64_t total = job_off[njobs];
+
+    out.leafmasks = leafmasks;
+    out.dag_words = total;
+    out.job_offset.assign(job_off.begin(), job_off.begin() + njobs);
+    out.job_words.resize(njobs);
+    out.tree_nodes.assign(njobs, std::vector<uint64_t>());
+    out.unique_nodes.assign(njobs, std::vector<uint64_t>());
+    for (uint32_t j = 0; j < njobs; ++j) {
+        out.job_words[j] = job_off[j + 1] - job_off[j];
+        if (out.job_words[j] >= (1ull << 32)) return fail(CPVS_ERR_BUDGET, "build_dags: DAG exceeds 2^32 words");
+        const int nl = (int)root_level[j] + 2;
+        out.tree_nodes[j].assign(nl, 0);
+        out.unique_nodes[j].assign(nl, 0);
+        for (int L = bottom; L <= (int)root_level[j]; ++L) {
+            const size_t s = (size_t)j * CPVS_MAX_LEVELS + L;
+            out.tree_nodes[j][L] = hseg[1 * segn + s] - hseg[0 * segn + s];
+            out.unique_nodes[j][L] = hseg[3 * segn + s] - hseg[2 * segn + s];
+        }
+    }
+    {
+        cpvs_status r = ctx.alloc((void**)&out.dag, std::max<uint64_t>(total, 1) * 4, true, st);
+        if (r != CPVS_OK) return r;
+    }
+    for (int L = maxR; L >= bottom; --L) {
+        const uint32_t U = hlu[2 * L];
+        if (!U) continue;
+        const uint32_t g = grid_for(U, kThreads);
+        const LevelDev child = (L > bottom) ? lv[L - 1] : lv[L];
+        if (leafmasks && L == 2)
+            k_emit<true><<<g, kThreads, 0, st>>>(lv[L], child, level_u, L, seg, lay, out.dag, total, err);
+        else
+            k_emit<false><<<g, kThreads, 0, st>>>(lv[L], child, level_u, L, seg, lay, out.dag, total, err);
+    }
+    CPVS_CUDA(cudaGetLastError());
+    // root masks of every job (the first word of each DAG)
+    out.root_mask.resize(njobs);
+    for (uint32_t j = 0; j < njobs; ++j)
+        CPVS_CUDA(cudaMemcpyAsync(&out.root_mask[j], out.dag + job_off[j], 4, cudaMemcpyDeviceToHost, st));
+    CPVS_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+    CPVS_CUDA(cudaStreamSynchronize(st));
+    if (herr) return fail(CPVS_ERR_DEVICE, "build_dags: DAG layout out of range (internal check " + std::to_string(herr) + ")");
+    return CPVS_OK;
+}
+
+}  // namespace cpvs

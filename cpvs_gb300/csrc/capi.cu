@@ -1,0 +1,521 @@
+// C ABI of the library (include/cpvs.h): handles, validation, memory budget,
+// host <-> device staging.  All compute is in pyramid.cu, build.cu and
+// lookup.cu; nothing here computes a result on the host.
+#include <algorithm>
+#include <cstring>
+#include <functional>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace cpvs {
+
+static thread_local std::string g_last_error;
+
+cpvs_status fail(cpvs_status s, const std::string& msg) {
+    g_last_error = msg;
+    return s;
+}
+
+cpvs_status cuda_fail(cudaError_t e, const char* what) {
+    const cpvs_status s = (e == cudaErrorMemoryAllocation) ? CPVS_ERR_OOM : CPVS_ERR_DEVICE;
+    cudaGetLastError();  // clear a non-sticky error
+    return fail(s, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+cpvs_status Ctx::alloc(void** p, uint64_t bytes, bool persistent, cudaStream_t st) {
+    *p = nullptr;
+    if (budget && in_use + scratch + bytes > budget)
+        return fail(CPVS_ERR_BUDGET, "allocation of " + std::to_string(bytes) + " bytes exceeds the context budget");
+    cudaError_t e = persistent ? cudaMalloc(p, bytes) : cudaMallocAsync(p, bytes, st);
+    if (e != cudaSuccess) return cuda_fail(e, persistent ? "cudaMalloc" : "cudaMallocAsync");
+    if (persistent)
+        in_use += bytes;
+    else
+        scratch += bytes;
+    return CPVS_OK;
+}
+
+void Ctx::release(void* p, uint64_t bytes, bool persistent, cudaStream_t st) {
+    if (persistent) {
+        if (p) cudaFree(p);
+        in_use -= std::min(in_use, bytes);
+    } else {
+        if (p) cudaFreeAsync(p, st);
+        scratch -= std::min(scratch, bytes);
+    }
+}
+
+}  // namespace cpvs
+
+using cpvs::fail;
+
+struct cpvs_ctx {
+    cpvs::Ctx c;
+};
+
+struct cpvs_hierarchy {
+    cpvs_ctx* ctx = nullptr;
+    uint32_t n = 0;
+    float* depth = nullptr;    // device n*n
+    float2* levels = nullptr;  // device pyramid
+    uint64_t bytes = 0;
+};
+
+struct cpvs_shadow {
+    cpvs_ctx* ctx = nullptr;
+    uint32_t* dag = nullptr;
+    uint64_t words = 0;
+    uint64_t bytes = 0;
+    uint32_t num_levels = 0;
+    bool leafmasks = false;
+    uint32_t root_mask = 0;
+    std::vector<uint64_t> tree, uniq;
+};
+
+struct cpvs_grid {
+    cpvs_ctx* ctx = nullptr;
+    uint32_t length = 0;
+    std::vector<cpvs_shadow*> cells;
+    uint32_t* dag = nullptr;
+    uint64_t words = 0;
+    uint32_t* cell_words = nullptr;
+    uint32_t dag_levels = 0;
+    bool leafmasks = false;
+    bool finalized = false;
+};
+
+namespace {
+
+bool is_pow2(uint64_t v) { return v && !(v & (v - 1)); }
+
+cpvs_status set_device(const cpvs_ctx* ctx) {
+    cudaError_t e = cudaSetDevice(ctx->c.device);
+    if (e != cudaSuccess) return cpvs::cuda_fail(e, "cudaSetDevice");
+    return CPVS_OK;
+}
+
+// A hierarchy needs a square power-of-two map (src/MinMaxHierarchy.cpp:12-14);
+// a DAG needs numLevels > 3, i.e. n >= 8 (src/CompressedShadow.cpp:46).
+cpvs_status check_map_size(uint32_t n, uint32_t min_n) {
+    if (!is_pow2(n) || n < min_n || n > 65536)
+        return fail(CPVS_ERR_INVALID_ARG, "map side must be a power of two in [" + std::to_string(min_n) +
+                                              ", 65536], got " + std::to_string(n));
+    return CPVS_OK;
+}
+
+// Device copy of a host or device input; `owned` tells whether to free it.
+cpvs_status stage_in(cpvs::Ctx& c, const void* src, uint64_t bytes, uint32_t flags, cudaStream_t st, void** dev,
+                     bool* owned) {
+    if (flags & CPVS_IO_DEVICE) {
+        *dev = const_cast<void*>(src);
+        *owned = false;
+        return CPVS_OK;
+    }
+    cpvs_status r = c.alloc(dev, std::max<uint64_t>(bytes, 4), false, st);
+    if (r != CPVS_OK) return r;
+    *owned = true;
+    if (bytes) CPVS_CUDA(cudaMemcpyAsync(*dev, src, bytes, cudaMemcpyHostToDevice, st));
+    return CPVS_OK;
+}
+
+cpvs_status lookup_common(cpvs_ctx* ctx, const void* xyz, uint64_t n, uint32_t* bits_out, uint32_t flags,
+                          cudaStream_t st, const std::function<cpvs_status(const void*, uint32_t*)>& run) {
+    if (!xyz && n) return fail(CPVS_ERR_INVALID_ARG, "lookup: null input");
+    if (!bits_out && n) return fail(CPVS_ERR_INVALID_ARG, "lookup: null output");
+    if (n == 0) return CPVS_OK;
+    if (n >= (1ull << 40)) return fail(CPVS_ERR_INVALID_ARG, "lookup: batch too large");
+    cpvs_status r = set_device(ctx);
+    if (r != CPVS_OK) return r;
+    cpvs::Ctx& c = ctx->c;
+    const uint64_t qbytes = n * 12, bbytes = (n + 31) / 32 * 4;
+    void* q = nullptr;
+    bool qowned = false;
+    r = stage_in(c, xyz, qbytes, flags, st, &q, &qowned);
+    if (r != CPVS_OK) return r;
+    uint32_t* bits = bits_out;
+    bool bowned = false;
+    if (!(flags & CPVS_IO_DEVICE)) {
+        r = c.alloc((void**)&bits, bbytes, false, st);
+        if (r != CPVS_OK) {
+            if (qowned) c.release(q, qbytes, false, st);
+            return r;
+        }
+        bowned = true;
+    }
+    r = run(q, bits);
+    if (r == CPVS_OK && bowned) {
+        cudaError_t e = cudaMemcpyAsync(bits_out, bits, bbytes, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) r = cpvs::cuda_fail(e, "lookup read-back");
+    }
+    if (qowned) c.release(q, std::max<uint64_t>(qbytes, 4), false, st);
+    if (bowned) c.release(bits, bbytes, false, st);
+    return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* cpvs_status_string(cpvs_status s) {
+    switch (s) {
+        case CPVS_OK: return "ok";
+        case CPVS_ERR_INVALID_ARG: return "invalid argument";
+        case CPVS_ERR_OOM: return "out of device memory";
+        case CPVS_ERR_TIMEOUT: return "device wait timed out";
+        case CPVS_ERR_DEVICE: return "CUDA device error";
+        case CPVS_ERR_UNIMPLEMENTED: return "unimplemented";
+        case CPVS_ERR_BUDGET: return "memory budget exceeded";
+        case CPVS_ERR_CANCELLED: return "cancelled";
+        case CPVS_ERR_CAPACITY: return "output buffer too small";
+    }
+    return "unknown status";
+}
+
+const char* cpvs_last_error(void) { return cpvs::g_last_error.c_str(); }
+int cpvs_abi_version(void) { return CPVS_ABI_VERSION; }
+
+cpvs_status cpvs_ctx_create(int device, cpvs_ctx** out) {
+    if (!out) return fail(CPVS_ERR_INVALID_ARG, "ctx_create: null out");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return fail(CPVS_ERR_DEVICE, "no CUDA device available");
+    }
+    if (device < 0 || device >= count) return fail(CPVS_ERR_INVALID_ARG, "ctx_create: bad device index");
+    CPVS_CUDA(cudaSetDevice(device));
+    auto* c = new cpvs_ctx;
+    c->c.device = device;
+    cudaDeviceGetAttribute(&c->c.num_sms, cudaDevAttrMultiProcessorCount, device);
+    *out = c;
+    return CPVS_OK;
+}
+
+void cpvs_ctx_destroy(cpvs_ctx* ctx) { delete ctx; }
+
+cpvs_status cpvs_ctx_set_budget(cpvs_ctx* ctx, uint64_t bytes) {
+    if (!ctx) return fail(CPVS_ERR_INVALID_ARG, "null ctx");
+    ctx->c.budget = bytes;
+    return CPVS_OK;
+}
+
+uint64_t cpvs_ctx_bytes_in_use(const cpvs_ctx* ctx) { return ctx ? ctx->c.in_use + ctx->c.scratch : 0; }
+
+// ------------------------------------------------------------- hierarchy
+cpvs_status cpvs_hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n, uint32_t flags, void* stream,
+                                  cpvs_hierarchy** out) {
+    if (!ctx || !depth || !out) return fail(CPVS_ERR_INVALID_ARG, "hierarchy_create: null argument");
+    *out = nullptr;
+    cpvs_status r = check_map_size(n, 2);
+    if (r != CPVS_OK) return r;
+    r = set_device(ctx);
+    if (r != CPVS_OK) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    cpvs::Ctx& c = ctx->c;
+    const uint64_t dbytes = (uint64_t)n * n * 4;
+    const uint64_t lbytes = cpvs::pyramid_texels(n) * 8;
+    auto* h = new cpvs_hierarchy;
+    h->ctx = ctx;
+    h->n = n;
+    r = c.alloc((void**)&h->depth, dbytes, true, st);
+    if (r == CPVS_OK) {
+        h->bytes += dbytes;
+        r = c.alloc((void**)&h->levels, lbytes, true, st);
+        if (r == CPVS_OK) h->bytes += lbytes;
+    }
+    if (r == CPVS_OK) {
+        cudaError_t e = cudaMemcpyAsync(h->depth, depth, dbytes,
+                                        (flags & CPVS_IO_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) r = cpvs::cuda_fail(e, "hierarchy upload");
+    }
+    if (r == CPVS_OK) r = cpvs::launch_pyramid(h->depth, n, h->levels, st);
+    if (r != CPVS_OK) {
+        cpvs_hierarchy_destroy(h);
+        return r;
+    }
+    *out = h;
+    return CPVS_OK;
+}
+
+void cpvs_hierarchy_destroy(cpvs_hierarchy* h) {
+    if (!h) return;
+    cpvs::Ctx& c = h->ctx->c;
+    cudaSetDevice(c.device);
+    if (h->depth) c.release(h->depth, (uint64_t)h->n * h->n * 4, true, nullptr);
+    if (h->levels) c.release(h->levels, cpvs::pyramid_texels(h->n) * 8, true, nullptr);
+    delete h;
+}
+
+uint32_t cpvs_hierarchy_num_levels(const cpvs_hierarchy* h) { return h ? (uint32_t)cpvs::log2_u32(h->n) + 1 : 0; }
+uint32_t cpvs_hierarchy_size(const cpvs_hierarchy* h) { return h ? h->n : 0; }
+
+cpvs_status cpvs_hierarchy_level(const cpvs_hierarchy* h, uint32_t level, float* host_out, uint64_t capacity,
+                                 void* stream) {
+    if (!h || !host_out) return fail(CPVS_ERR_INVALID_ARG, "hierarchy_level: null argument");
+    const uint32_t nl = cpvs_hierarchy_num_levels(h);
+    if (level < 1 || level >= nl) return fail(CPVS_ERR_INVALID_ARG, "hierarchy_level: level out of range");
+    const uint64_t s = h->n >> level;
+    if (capacity < 2 * s * s) return fail(CPVS_ERR_CAPACITY, "hierarchy_level: buffer too small");
+    cpvs_status r = set_device(h->ctx);
+    if (r != CPVS_OK) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    CPVS_CUDA(cudaMemcpyAsync(host_out, h->levels + cpvs::pyramid_level_offset(h->n, (int)level), 2 * s * s * 4,
+                              cudaMemcpyDeviceToHost, st));
+    CPVS_CUDA(cudaStreamSynchronize(st));
+    return CPVS_OK;
+}
+
+// ---------------------------------------------------------------- shadow
+cpvs_status cpvs_shadow_create(cpvs_ctx* ctx, const cpvs_hierarchy* h, uint32_t z_tile_index, uint32_t z_tile_num,
+                               uint32_t flags, void* stream, cpvs_shadow** out) {
+    if (!ctx || !h || !out) return fail(CPVS_ERR_INVALID_ARG, "shadow_create: null argument");
+    *out = nullptr;
+    cpvs_status r0 = check_map_size(h->n, 8);
+    if (r0 != CPVS_OK) return r0;
+    if (z_tile_num == 0 || z_tile_index >= z_tile_num)
+        return fail(CPVS_ERR_INVALID_ARG, "shadow_create: need z_tile_index < z_tile_num");
+    // every z-cell index must be exact in float32, as the classification
+    // converts it (src/CompressedShadowUtil.cpp:36-40)
+    if ((uint64_t)h->n * z_tile_num > (1ull << 24))
+        return fail(CPVS_ERR_INVALID_ARG, "shadow_create: n * z_tile_num must not exceed 2^24");
+    cpvs_status r = set_device(ctx);
+    if (r != CPVS_OK) return r;
+    const uint32_t nl = (uint32_t)cpvs::log2_u32(h->n) + 1;
+    const bool leaf = (flags & CPVS_FLAG_LEAFMASKS) && (nl - 3 >= 2);
+    std::vector<cpvs::SourceSpec> src{{h->depth, h->levels, h->n}};
+    std::vector<cpvs::JobSpec> jobs{{0, z_tile_index, z_tile_num}};
+    cpvs::BuildOutput bo;
+    r = cpvs::build_dags(ctx->c, src, jobs, leaf, (cudaStream_t)stream, bo);
+    if (r != CPVS_OK) {
+        if (bo.dag) ctx->c.release(bo.dag, std::max<uint64_t>(bo.dag_words, 1) * 4, true, nullptr);
+        return r;
+    }
+    auto* s = new cpvs_shadow;
+    s->ctx = ctx;
+    s->dag = bo.dag;
+    s->words = bo.dag_words;
+    s->bytes = std::max<uint64_t>(bo.dag_words, 1) * 4;
+    s->num_levels = nl;
+    s->leafmasks = leaf;
+    s->root_mask = bo.root_mask[0];
+    s->tree = bo.tree_nodes[0];
+    s->uniq = bo.unique_nodes[0];
+    *out = s;
+    return CPVS_OK;
+}
+
+cpvs_status cpvs_shadow_create_from_depth(cpvs_ctx* ctx, const float* depth, uint32_t n, uint32_t z_tile_index,
+                                          uint32_t z_tile_num, uint32_t flags, void* stream, cpvs_shadow** out) {
+    if (out) *out = nullptr;
+    cpvs_status r = check_map_size(n, 8);
+    if (r != CPVS_OK) return r;
+    cpvs_hierarchy* h = nullptr;
+    r = cpvs_hierarchy_create(ctx, depth, n, flags, stream, &h);
+    if (r != CPVS_OK) return r;
+    r = cpvs_shadow_create(ctx, h, z_tile_index, z_tile_num, flags, stream, out);
+    cudaStreamSynchronize((cudaStream_t)stream);
+    cpvs_hierarchy_destroy(h);
+    return r;
+}
+
+void cpvs_shadow_destroy(cpvs_shadow* s) {
+    if (!s) return;
+    cudaSetDevice(s->ctx->c.device);
+    s->ctx->c.release(s->dag, s->bytes, true, nullptr);
+    delete s;
+}
+
+uint32_t cpvs_shadow_num_levels(const cpvs_shadow* s) { return s ? s->num_levels : 0; }
+int cpvs_shadow_uses_leafmasks(const cpvs_shadow* s) { return s && s->leafmasks ? 1 : 0; }
+
+cpvs_visibility cpvs_shadow_total_visibility(const cpvs_shadow* s) {
+    if (!s) return CPVS_PARTIAL;
+    if (s->root_mask == 0x5555u) return CPVS_VISIBLE;
+    if (s->root_mask == 0u) return CPVS_SHADOW;
+    return CPVS_PARTIAL;
+}
+
+uint64_t cpvs_shadow_dag_size(const cpvs_shadow* s) { return s ? s->words : 0; }
+const uint32_t* cpvs_shadow_device_dag(const cpvs_shadow* s) { return s ? s->dag : nullptr; }
+
+cpvs_status cpvs_shadow_dag_words(const cpvs_shadow* s, uint32_t* host_out, uint64_t capacity, uint64_t* n_out,
+                                  void* stream) {
+    if (!s) return fail(CPVS_ERR_INVALID_ARG, "dag_words: null shadow");
+    if (n_out) *n_out = s->words;
+    if (!host_out) return CPVS_OK;
+    if (capacity < s->words) return fail(CPVS_ERR_CAPACITY, "dag_words: buffer too small");
+    cpvs_status r = set_device(s->ctx);
+    if (r != CPVS_OK) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    CPVS_CUDA(cudaMemcpyAsync(host_out, s->dag, s->words * 4, cudaMemcpyDeviceToHost, st));
+    CPVS_CUDA(cudaStreamSynchronize(st));
+    return CPVS_OK;
+}
+
+cpvs_status cpvs_shadow_level_counts(const cpvs_shadow* s, uint64_t* tree, uint64_t* unique, uint32_t capacity) {
+    if (!s) return fail(CPVS_ERR_INVALID_ARG, "level_counts: null shadow");
+    if (capacity < s->num_levels) return fail(CPVS_ERR_CAPACITY, "level_counts: capacity below numLevels");
+    for (uint32_t L = 0; L < s->num_levels; ++L) {
+        if (tree) tree[L] = L < s->tree.size() ? s->tree[L] : 0;
+        if (unique) unique[L] = L < s->uniq.size() ? s->uniq[L] : 0;
+    }
+    return CPVS_OK;
+}
+
+cpvs_status cpvs_shadow_lookup_ndc(const cpvs_shadow* s, const float* xyz, uint64_t n, uint32_t* bits_out,
+                                   uint32_t flags, void* stream) {
+    if (!s) return fail(CPVS_ERR_INVALID_ARG, "lookup_ndc: null shadow");
+    cudaStream_t st = (cudaStream_t)stream;
+    return lookup_common(s->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
+        return cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, q, true, n, bits, st);
+    });
+}
+
+cpvs_status cpvs_shadow_lookup_voxel(const cpvs_shadow* s, const int32_t* xyz, uint64_t n, uint32_t* bits_out,
+                                     uint32_t flags, void* stream) {
+    if (!s) return fail(CPVS_ERR_INVALID_ARG, "lookup_voxel: null shadow");
+    cudaStream_t st = (cudaStream_t)stream;
+    return lookup_common(s->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
+        return cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, q, false, n, bits, st);
+    });
+}
+
+// ------------------------------------------------------------------ grid
+cpvs_status cpvs_grid_create(cpvs_ctx* ctx, uint32_t length, cpvs_grid** out) {
+    if (!ctx || !out) return fail(CPVS_ERR_INVALID_ARG, "grid_create: null argument");
+    *out = nullptr;
+    if (!is_pow2(length) || length > 256) return fail(CPVS_ERR_INVALID_ARG, "grid length must be a power of two <= 256");
+    auto* g = new cpvs_grid;
+    g->ctx = ctx;
+    g->length = length;
+    g->cells.assign((size_t)length * length * length, nullptr);
+    *out = g;
+    return CPVS_OK;
+}
+
+static void grid_release_device(cpvs_grid* g) {
+    cpvs::Ctx& c = g->ctx->c;
+    if (g->dag) c.release(g->dag, std::max<uint64_t>(g->words, 1) * 4, true, nullptr);
+    if (g->cell_words) c.release(g->cell_words, g->cells.size() * 4, true, nullptr);
+    g->dag = nullptr;
+    g->cell_words = nullptr;
+    g->finalized = false;
+}
+
+void cpvs_grid_destroy(cpvs_grid* g) {
+    if (!g) return;
+    cudaSetDevice(g->ctx->c.device);
+    for (auto* s : g->cells) cpvs_shadow_destroy(s);
+    grid_release_device(g);
+    delete g;
+}
+
+uint32_t cpvs_grid_length(const cpvs_grid* g) { return g ? g->length : 0; }
+
+cpvs_status cpvs_grid_set(cpvs_grid* g, uint32_t x, uint32_t y, uint32_t z, cpvs_shadow* s) {
+    if (!g) return fail(CPVS_ERR_INVALID_ARG, "grid_set: null grid");
+    if (x >= g->length || y >= g->length || z >= g->length) return fail(CPVS_ERR_INVALID_ARG, "grid_set: cell out of range");
+    const size_t i = ((size_t)z * g->length + y) * g->length + x;
+    if (g->cells[i] && g->cells[i] != s) cpvs_shadow_destroy(g->cells[i]);
+    g->cells[i] = s;
+    return CPVS_OK;
+}
+
+const cpvs_shadow* cpvs_grid_get(const cpvs_grid* g, uint32_t x, uint32_t y, uint32_t z) {
+    if (!g || x >= g->length || y >= g->length || z >= g->length) return nullptr;
+    return g->cells[((size_t)z * g->length + y) * g->length + x];
+}
+
+cpvs_status cpvs_grid_finalize(cpvs_grid* g, int release_cells, void* stream) {
+    if (!g) return fail(CPVS_ERR_INVALID_ARG, "grid_finalize: null grid");
+    cpvs_status r = set_device(g->ctx);
+    if (r != CPVS_OK) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    uint64_t total = 0;
+    uint32_t nl = 0;
+    bool leaf = false;
+    std::vector<uint32_t> cellw(g->cells.size());
+    for (size_t i = 0; i < g->cells.size(); ++i) {
+        const cpvs_shadow* s = g->cells[i];
+        if (!s) return fail(CPVS_ERR_INVALID_ARG, "grid_finalize: cell " + std::to_string(i) + " is empty");
+        if (i == 0) {
+            nl = s->num_levels;
+            leaf = s->leafmasks;
+        } else if (s->num_levels != nl || s->leafmasks != leaf) {
+            return fail(CPVS_ERR_INVALID_ARG, "grid_finalize: cells differ in numLevels or leafmask mode");
+        }
+        // createTopLevelGrid (src/CompressedShadowContainer.cpp:71-91), with
+        // the sentinel values the shader tests (shader/traverse.cs:85-88)
+        if (s->root_mask == 0u)
+            cellw[i] = 0xFFFFFFFFu;
+        else if (s->root_mask == 0x5555u)
+            cellw[i] = 0xFFFFFFFEu;
+        else
+            cellw[i] = (uint32_t)total;
+        total += s->words;
+        if (total >= 0xFFFFFFFEull) return fail(CPVS_ERR_BUDGET, "grid_finalize: combined DAG exceeds 2^32-2 words");
+    }
+    grid_release_device(g);
+    cpvs::Ctx& c = g->ctx->c;
+    r = c.alloc((void**)&g->dag, std::max<uint64_t>(total, 1) * 4, true, st);
+    if (r != CPVS_OK) return r;
+    r = c.alloc((void**)&g->cell_words, g->cells.size() * 4, true, st);
+    if (r != CPVS_OK) {
+        grid_release_device(g);
+        return r;
+    }
+    uint64_t off = 0;
+    for (const cpvs_shadow* s : g->cells) {
+        CPVS_CUDA(cudaMemcpyAsync(g->dag + off, s->dag, s->words * 4, cudaMemcpyDeviceToDevice, st));
+        off += s->words;
+    }
+    CPVS_CUDA(cudaMemcpyAsync(g->cell_words, cellw.data(), cellw.size() * 4, cudaMemcpyHostToDevice, st));
+    CPVS_CUDA(cudaStreamSynchronize(st));
+    g->words = total;
+    g->dag_levels = nl;
+    g->leafmasks = leaf;
+    g->finalized = true;
+    if (release_cells) {
+        for (auto*& s : g->cells) {
+            cpvs_shadow_destroy(s);
+            s = nullptr;
+        }
+    }
+    return CPVS_OK;
+}
+
+uint64_t cpvs_grid_dag_size(const cpvs_grid* g) { return g && g->finalized ? g->words : 0; }
+
+cpvs_status cpvs_grid_words(const cpvs_grid* g, uint32_t* dag_out, uint64_t dag_capacity, uint32_t* cells_out,
+                            uint64_t cells_capacity, void* stream) {
+    if (!g || !g->finalized) return fail(CPVS_ERR_INVALID_ARG, "grid_words: grid not finalized");
+    cpvs_status r = set_device(g->ctx);
+    if (r != CPVS_OK) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (dag_out) {
+        if (dag_capacity < g->words) return fail(CPVS_ERR_CAPACITY, "grid_words: DAG buffer too small");
+        CPVS_CUDA(cudaMemcpyAsync(dag_out, g->dag, g->words * 4, cudaMemcpyDeviceToHost, st));
+    }
+    if (cells_out) {
+        if (cells_capacity < g->cells.size()) return fail(CPVS_ERR_CAPACITY, "grid_words: cell buffer too small");
+        CPVS_CUDA(cudaMemcpyAsync(cells_out, g->cell_words, g->cells.size() * 4, cudaMemcpyDeviceToHost, st));
+    }
+    CPVS_CUDA(cudaStreamSynchronize(st));
+    return CPVS_OK;
+}
+
+cpvs_status cpvs_grid_lookup_ndc(const cpvs_grid* g, const float* xyz, uint64_t n, uint32_t* bits_out, uint32_t flags,
+                                 void* stream) {
+    if (!g || !g->finalized) return fail(CPVS_ERR_INVALID_ARG, "grid_lookup_ndc: grid not finalized");
+    cudaStream_t st = (cudaStream_t)stream;
+    return lookup_common(g->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
+        return cpvs::launch_grid_lookup(g->dag, g->words, g->cell_words, g->length, g->dag_levels, g->leafmasks,
+                                        static_cast<const float*>(q), n, bits, st);
+    });
+}
+
+}  // extern "C"

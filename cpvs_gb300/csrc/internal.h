@@ -1,0 +1,103 @@
+// Host-side interfaces shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/cpvs.h"
+
+#define CPVS_MAX_LEVELS 18
+
+namespace cpvs {
+
+// Records `msg` as this thread's last error and returns `s`.
+cpvs_status fail(cpvs_status s, const std::string& msg);
+cpvs_status cuda_fail(cudaError_t e, const char* what);
+
+#define CPVS_CUDA(call)                                          \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
+        if (e_ != cudaSuccess) return ::cpvs::cuda_fail(e_, #call); \
+    } while (0)
+
+// ------------------------------------------------------------- pyramid
+// Float2 offset of pyramid level L (L >= 1) in the packed level array of an
+// n x n map: levels 1..log2(n) of (n>>l)^2 (min,max) pairs back to back.
+inline uint64_t pyramid_level_offset(uint32_t n, int L) {
+    uint64_t o = 0;
+    for (int l = 1; l < L; ++l) o += (uint64_t)(n >> l) * (n >> l);
+    return o;
+}
+inline uint64_t pyramid_texels(uint32_t n) {
+    uint64_t o = 0;
+    for (uint32_t s = n >> 1; s >= 1; s >>= 1) o += (uint64_t)s * s;
+    return o;
+}
+inline int log2_u32(uint32_t n) {
+    int l = 0;
+    while ((1u << l) < n) ++l;
+    return l;
+}
+
+// Builds levels 1..log2(n) of the min-max pyramid of `depth` into `levels`.
+cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaStream_t st);
+
+// One z-tile of a source map whose per-level node bounds are wanted.
+struct BoundJob {
+    uint32_t z_idx, z_num;
+    uint32_t out_row;  // row of `bounds` to accumulate into
+};
+// bounds[row * CPVS_MAX_LEVELS + (L-1)] += number of partial cells of the
+// job's z range at pyramid level L, for L in [lmin, numLevels-2]: an upper
+// bound on the SVO node count at level L-1.
+cpvs_status launch_level_bounds(const float2* levels, uint32_t n, int lmin, const BoundJob* jobs_dev, int njobs,
+                                unsigned long long* bounds, cudaStream_t st);
+
+// --------------------------------------------------------------- build
+struct SourceSpec {
+    const float* depth;    // device, n*n
+    const float2* levels;  // device pyramid (levels 1..log2 n)
+    uint32_t n;
+};
+struct JobSpec {
+    uint32_t source;
+    uint32_t z_idx, z_num;
+};
+struct BuildOutput {
+    uint32_t* dag = nullptr;          // device, all jobs concatenated (cudaMalloc'd, caller owns)
+    uint64_t dag_words = 0;
+    std::vector<uint64_t> job_offset;  // word offset of each job's DAG in `dag`
+    std::vector<uint64_t> job_words;
+    std::vector<uint32_t> root_mask;
+    std::vector<std::vector<uint64_t>> tree_nodes, unique_nodes;  // [job][level]
+    bool leafmasks = false;
+};
+struct Ctx;
+// Builds the DAGs of `jobs` (all with the same leafmask mode).
+cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const std::vector<JobSpec>& jobs,
+                       bool leafmasks, cudaStream_t st, BuildOutput& out);
+
+// -------------------------------------------------------------- lookup
+cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks, const void* xyz,
+                          bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st);
+cpvs_status launch_grid_lookup(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
+                               uint32_t dag_levels, bool leafmasks, const float* xyz, uint64_t n, uint32_t* bits,
+                               cudaStream_t st);
+
+// ----------------------------------------------------------------- ctx
+struct Ctx {
+    int device = 0;
+    int num_sms = 0;
+    uint64_t budget = 0;   // 0 = unlimited
+    uint64_t in_use = 0;   // persistent bytes (hierarchies, DAGs, grids)
+    uint64_t scratch = 0;  // stream-ordered build / staging scratch
+    // Device allocation with budget accounting: persistent blocks come from
+    // cudaMalloc, scratch from the stream-ordered pool on `st`.
+    cpvs_status alloc(void** p, uint64_t bytes, bool persistent, cudaStream_t st);
+    void release(void* p, uint64_t bytes, bool persistent, cudaStream_t st);
+};
+
+}  // namespace cpvs

@@ -1,0 +1,176 @@
+// Min-max pyramid of a depth map, and the per-level SVO node bounds.
+//
+// Replaces MinMaxHierarchy (src/MinMaxHierarchy.cpp:9-97).  Level L >= 1 is
+// (n>>L)^2 (min,max) float pairs; texel (x,y) of level L reduces texels
+// a=(2x,2y), b=(2x+1,2y), c=(2x,2y+1), d=(2x+1,2y+1) of level L-1 as
+// pred(pred(a,b), pred(c,d)) with pred = std::min<float> / std::max<float>
+// (:29-49), so the result is bit-identical to the reference's, signed zeros
+// and NaN included.  Level 1 reads the single-channel depth map for both min
+// and max (:75-97).
+//
+// One CTA reduces a T x T input tile (T = 64, or the whole level when it is
+// smaller) through log2(T) levels: the first level straight from global
+// memory with 16-byte loads, the rest in shared memory.  Three launches cover
+// an 8192^2 map (levels 1-6, 7-12, 13).  HBM-bound: the map is read once and
+// every pyramid texel written once.
+#include "common.cuh"
+
+namespace cpvs {
+namespace {
+
+__device__ __forceinline__ float pmin(float a, float b) { return (b < a) ? b : a; }  // std::min<float>
+__device__ __forceinline__ float pmax(float a, float b) { return (a < b) ? b : a; }  // std::max<float>
+
+constexpr int kTile = 64;
+constexpr int kThreads = 256;
+
+// in: level `L0-1` of side S (the depth map when FROM_DEPTH), out: pyramid
+// level array; writes levels L0 .. L0+log2(T)-1 of this CTA's tile.
+template <bool FROM_DEPTH>
+__global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ in, uint32_t S, float2* __restrict__ out,
+                                                      uint32_t n, int L0, uint32_t T) {
+    __shared__ float2 buf0[(kTile / 2) * (kTile / 2)];
+    __shared__ float2 buf1[(kTile / 4) * (kTile / 4)];
+    const uint32_t tiles_x = S / T;
+    const uint32_t tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+
+    // first level: (T/2)^2 outputs of this tile
+    uint32_t half = T / 2;
+    {
+        const uint32_t So = S / 2;
+        float2* dst = out + pyramid_level_offset_dev(n, L0);
+        for (uint32_t o = threadIdx.x; o < half * half; o += blockDim.x) {
+            const uint32_t ox = o % half, oy = o / half;
+            const uint32_t ix = (tx * T) + 2 * ox, iy = (ty * T) + 2 * oy;
+            float lo, hi;
+            if (FROM_DEPTH) {
+                const float* d = static_cast<const float*>(in);
+                const float2 r0 = *reinterpret_cast<const float2*>(d + (size_t)iy * S + ix);
+                const float2 r1 = *reinterpret_cast<const float2*>(d + (size_t)(iy + 1) * S + ix);
+                lo = pmin(pmin(r0.x, r0.y), pmin(r1.x, r1.y));
+                hi = pmax(pmax(r0.x, r0.y), pmax(r1.x, r1.y));
+            } else {
+                const float2* p = static_cast<const float2*>(in);
+                const float4 r0 = *reinterpret_cast<const float4*>(p + (size_t)iy * S + ix);
+                const float4 r1 = *reinterpret_cast<const float4*>(p + (size_t)(iy + 1) * S + ix);
+                lo = pmin(pmin(r0.x, r0.z), pmin(r1.x, r1.z));
+                hi = pmax(pmax(r0.y, r0.w), pmax(r1.y, r1.w));
+            }
+            const float2 v = make_float2(lo, hi);
+            dst[(size_t)(ty * half + oy) * So + tx * half + ox] = v;
+            buf0[o] = v;
+        }
+    }
+    // remaining levels of the tile in shared memory (ping-pong buf0 <-> buf1)
+    uint32_t So = S / 2;
+    int L = L0 + 1;
+    float2* src = buf0;
+    float2* nxt = buf1;
+    while (half > 1) {
+        __syncthreads();
+        const uint32_t h2 = half / 2;
+        So /= 2;
+        float2* dst = out + pyramid_level_offset_dev(n, L);
+        for (uint32_t o = threadIdx.x; o < h2 * h2; o += blockDim.x) {
+            const uint32_t ox = o % h2, oy = o / h2;
+            const float2 a = src[(2 * oy) * half + 2 * ox], b = src[(2 * oy) * half + 2 * ox + 1];
+            const float2 c = src[(2 * oy + 1) * half + 2 * ox], d = src[(2 * oy + 1) * half + 2 * ox + 1];
+            const float2 v = make_float2(pmin(pmin(a.x, b.x), pmin(c.x, d.x)), pmax(pmax(a.y, b.y), pmax(c.y, d.y)));
+            dst[(size_t)(ty * h2 + oy) * So + tx * h2 + ox] = v;
+            nxt[o] = v;
+        }
+        // the next level reads what this one wrote: swap, and reuse the
+        // larger buffer for the level after (its size only shrinks)
+        float2* t = src;
+        src = nxt;
+        nxt = t;
+        half = h2;
+        ++L;
+    }
+}
+
+// Partial-cell count of one texel for a z range [lo, hi): the cells z with
+// NOT(z+1 <= a) and NOT(z >= b), i.e. z in [floor(a), ceil(b)), where a and
+// b are the scaled min and max; a NaN bound excludes nothing (the
+// comparisons against it are false, as in cs::visible).
+__device__ __forceinline__ uint64_t partial_cells(float a, float b, uint64_t lo, uint64_t hi) {
+    double s = (a != a) ? (double)lo : floor((double)a);
+    double e = (b != b) ? (double)hi : ceil((double)b);
+    if (s < (double)lo) s = (double)lo;
+    if (e > (double)hi) e = (double)hi;
+    return (e > s) ? (uint64_t)(e - s) : 0ull;
+}
+
+constexpr int kBoundThreads = 256;
+
+// One block per (level, texel chunk); block_level[] maps a block to its
+// pyramid level.  For every z-tile job of this map, sums the partial cells of
+// the job's z range at that level.
+struct BlockTable {
+    uint32_t first[CPVS_MAX_LEVELS + 1];
+};
+
+__global__ void __launch_bounds__(kBoundThreads)
+    k_level_bounds(const float2* __restrict__ levels, uint32_t n, int num_levels, const BlockTable bt, int lmin, const BoundJob* __restrict__ jobs, int njobs, unsigned long long* bounds) {
+    __shared__ uint64_t red[32];
+    int L = lmin;
+    while (L + 1 <= num_levels - 2 && blockIdx.x >= bt.first[L + 1 - lmin]) ++L;
+    const uint32_t W = n >> L;
+    const uint64_t texels = (uint64_t)W * W;
+    const uint64_t t = (uint64_t)(blockIdx.x - bt.first[L - lmin]) * blockDim.x + threadIdx.x;
+    const int R = num_levels - 2;
+    float2 mm = make_float2(0.f, 0.f);
+    const bool valid = t < texels;
+    if (valid) mm = levels[pyramid_level_offset_dev(n, L) + t];
+    for (int j = 0; j < njobs; ++j) {
+        const BoundJob J = jobs[j];
+        const float H = __uint2float_rn((n >> L) * J.z_num);
+        const uint64_t span = 2ull << (R - L);
+        uint64_t c = 0;
+        if (valid) c = partial_cells(__fmul_rn(mm.x, H), __fmul_rn(mm.y, H), J.z_idx * span, (J.z_idx + 1) * span);
+        const uint64_t s = block_sum_u64(c, red);
+        if (threadIdx.x == 0 && s) atomicAdd(&bounds[(size_t)J.out_row * CPVS_MAX_LEVELS + (L - 1)], (unsigned long long)s);
+    }
+}
+
+}  // namespace
+
+cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaStream_t st) {
+    uint32_t S = n;
+    int L0 = 1;
+    bool first = true;
+    while (S > 1) {
+        const uint32_t T = S < (uint32_t)kTile ? S : (uint32_t)kTile;
+        const uint32_t tiles = (S / T) * (S / T);
+        if (first)
+            k_pyramid<true><<<tiles, kThreads, 0, st>>>(depth, S, levels, n, L0, T);
+        else
+            k_pyramid<false><<<tiles, kThreads, 0, st>>>(levels + pyramid_level_offset(n, L0 - 1), S, levels, n, L0, T);
+        CPVS_CUDA(cudaGetLastError());
+        first = false;
+        L0 += log2_u32(T);
+        S /= T;
+    }
+    return CPVS_OK;
+}
+
+cpvs_status launch_level_bounds(const float2* levels, uint32_t n, int lmin, const BoundJob* jobs_dev, int njobs,
+                                unsigned long long* bounds, cudaStream_t st) {
+    const int num_levels = log2_u32(n) + 1;
+    const int R = num_levels - 2;
+    if (lmin > R || njobs == 0) return CPVS_OK;
+    // bt.first[k] = first block of level lmin+k
+    BlockTable bt{};
+    uint32_t blocks = 0;
+    for (int L = lmin; L <= R; ++L) {
+        bt.first[L - lmin] = blocks;
+        const uint64_t tex = (uint64_t)(n >> L) * (n >> L);
+        blocks += (uint32_t)((tex + kBoundThreads - 1) / kBoundThreads);
+    }
+    bt.first[R + 1 - lmin] = blocks;
+    k_level_bounds<<<blocks, kBoundThreads, 0, st>>>(levels, n, num_levels, bt, lmin, jobs_dev, njobs, bounds);
+    CPVS_CUDA(cudaGetLastError());
+    return CPVS_OK;
+}
+
+}  // namespace cpvs

@@ -1,0 +1,188 @@
+/*
+ * cpvs.h -- C ABI of the GB300 precomputed-voxelized-shadow library.
+ *
+ * Builds the sparse-voxel DAG of a shadow volume ("compressed shadow") from a
+ * float32 depth map on the GPU and answers batched visibility lookups for
+ * light-space points.  Every entry point returns a cpvs_status; the library
+ * never falls back to the CPU: without a usable CUDA device every call that
+ * needs one returns CPVS_ERR_DEVICE.
+ *
+ * Conventions
+ *   - All sizes are in elements unless named *_bytes.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = the legacy default
+ *     stream).  Calls are stream-ordered; calls that return host data
+ *     synchronise that stream before returning.
+ *   - Pointers are host memory unless the call's flags say CPVS_IO_DEVICE.
+ *   - Handles are immutable after creation and may be read from several host
+ *     threads; a cpvs_ctx must not be used by two host threads at once.
+ *   - Visibility classes follow the reference's NodeVisibility
+ *     (src/CompressedShadow.h:22-26): SHADOW 0, VISIBLE 1, PARTIAL 2.
+ *     Lookup results are bit-packed: bit (i % 32) of word (i / 32) is 1 when
+ *     point i is lit (VISIBLE) and 0 when it is in shadow.
+ */
+#ifndef CPVS_H
+#define CPVS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CPVS_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define CPVS_API __attribute__((visibility("default")))
+#else
+#define CPVS_API
+#endif
+
+typedef enum cpvs_status {
+    CPVS_OK = 0,
+    CPVS_ERR_INVALID_ARG = 1,  /* a size, flag or pointer the call cannot accept */
+    CPVS_ERR_OOM = 2,          /* device allocation failed */
+    CPVS_ERR_TIMEOUT = 3,      /* a bounded device wait gave up */
+    CPVS_ERR_DEVICE = 4,       /* CUDA error, or no usable device */
+    CPVS_ERR_UNIMPLEMENTED = 5,
+    CPVS_ERR_BUDGET = 6,       /* request exceeds the context's memory budget */
+    CPVS_ERR_CANCELLED = 7,    /* request cancelled before it ran */
+    CPVS_ERR_CAPACITY = 8      /* a caller-provided buffer is too small */
+} cpvs_status;
+
+typedef enum cpvs_visibility {
+    CPVS_SHADOW = 0,
+    CPVS_VISIBLE = 1,
+    CPVS_PARTIAL = 2
+} cpvs_visibility;
+
+/* Build flags. */
+#define CPVS_FLAG_LEAFMASKS 0x1u     /* 64-bit leafmasks for the last 3 levels
+                                        (the reference's #define LEAFMASKS,
+                                        src/CompressedShadow.cpp:16-27); used only
+                                        when numLevels-3 >= 2, as there */
+#define CPVS_IO_DEVICE 0x100u        /* input/output pointers are device memory */
+
+typedef struct cpvs_ctx cpvs_ctx;
+typedef struct cpvs_hierarchy cpvs_hierarchy;
+typedef struct cpvs_shadow cpvs_shadow;
+typedef struct cpvs_grid cpvs_grid;
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Opens the library on CUDA device `device`.  Replaces the GL context the
+ * reference renders and dispatches through (src/cpvs.h, src/ShaderProgram.*). */
+CPVS_API cpvs_status cpvs_ctx_create(int device, cpvs_ctx** out);
+CPVS_API void cpvs_ctx_destroy(cpvs_ctx* ctx);
+/* Upper bound on device bytes this context may hold in build scratch plus
+ * resident DAGs; 0 = unlimited.  Builds that would exceed it fail with
+ * CPVS_ERR_BUDGET. */
+CPVS_API cpvs_status cpvs_ctx_set_budget(cpvs_ctx* ctx, uint64_t bytes);
+CPVS_API uint64_t cpvs_ctx_bytes_in_use(const cpvs_ctx* ctx);
+CPVS_API const char* cpvs_status_string(cpvs_status s);
+/* Message of the last failed call on this host thread ("" if none). */
+CPVS_API const char* cpvs_last_error(void);
+CPVS_API int cpvs_abi_version(void);
+
+/* ---- min-max hierarchy ------------------------------------------------ */
+
+/* Device min-max pyramid of an n x n depth map (n a power of two, 2 <= n <=
+ * 65536; building a DAG from it needs n >= 8).  Replaces MinMaxHierarchy(const ImageF&)
+ * (src/MinMaxHierarchy.h:23, src/MinMaxHierarchy.cpp:9-27).  `depth` is
+ * row-major n*n float32, host memory unless flags has CPVS_IO_DEVICE.  The
+ * depth map is copied; the caller's buffer may be reused on return. */
+CPVS_API cpvs_status cpvs_hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n, uint32_t flags, void* stream,
+                                  cpvs_hierarchy** out);
+CPVS_API void cpvs_hierarchy_destroy(cpvs_hierarchy* h);
+/* numLevels including the depth map itself (MinMaxHierarchy::getNumLevels,
+ * src/MinMaxHierarchy.h:60-62). */
+CPVS_API uint32_t cpvs_hierarchy_num_levels(const cpvs_hierarchy* h);
+CPVS_API uint32_t cpvs_hierarchy_size(const cpvs_hierarchy* h);
+/* Copies level `level` (1 <= level < numLevels) to host memory as
+ * (n>>level)^2 interleaved (min,max) float pairs, row-major
+ * (MinMaxHierarchy::getMin/getMax, src/MinMaxHierarchy.h:31-55).
+ * `capacity` is in floats. */
+CPVS_API cpvs_status cpvs_hierarchy_level(const cpvs_hierarchy* h, uint32_t level, float* host_out, uint64_t capacity,
+                                 void* stream);
+
+/* ---- compressed shadow (one DAG) ------------------------------------- */
+
+/* Builds the DAG of z-tile `z_tile_index` of `z_tile_num` from a hierarchy.
+ * Replaces CompressedShadow::create(const MinMaxHierarchy&, uint zTileIndex,
+ * uint zTileNum) (src/CompressedShadow.h:48-49, src/CompressedShadow.cpp:49-59):
+ * the SVO classification, subtree merge and pointer compression all run on
+ * the device and the DAG stays resident there.  The DAG words equal the
+ * reference's getDAG() whenever the reference's own build is defined. */
+CPVS_API cpvs_status cpvs_shadow_create(cpvs_ctx* ctx, const cpvs_hierarchy* h, uint32_t z_tile_index, uint32_t z_tile_num,
+                               uint32_t flags, void* stream, cpvs_shadow** out);
+/* Depth map straight to DAG: hierarchy + create in one call.  Replaces
+ * CompressedShadow::create(const ShadowMap*, ...) (src/CompressedShadow.h:55-56),
+ * whose GL read-back becomes a host or device float32 buffer. */
+CPVS_API cpvs_status cpvs_shadow_create_from_depth(cpvs_ctx* ctx, const float* depth, uint32_t n, uint32_t z_tile_index,
+                                          uint32_t z_tile_num, uint32_t flags, void* stream, cpvs_shadow** out);
+CPVS_API void cpvs_shadow_destroy(cpvs_shadow* s);
+/* CompressedShadow::getNumLevels (src/CompressedShadow.h:71-73). */
+CPVS_API uint32_t cpvs_shadow_num_levels(const cpvs_shadow* s);
+/* 1 if the DAG uses 64-bit leafmasks. */
+CPVS_API int cpvs_shadow_uses_leafmasks(const cpvs_shadow* s);
+/* CompressedShadow::getTotalVisibility (src/CompressedShadow.cpp:66-72). */
+CPVS_API cpvs_visibility cpvs_shadow_total_visibility(const cpvs_shadow* s);
+/* Number of 32-bit words in the DAG. */
+CPVS_API uint64_t cpvs_shadow_dag_size(const cpvs_shadow* s);
+/* Copies the DAG words to host memory: CompressedShadow::getDAG()
+ * (src/CompressedShadow.h:75-77).  `capacity` is in words; `n_out` receives
+ * the DAG size (may be NULL). */
+CPVS_API cpvs_status cpvs_shadow_dag_words(const cpvs_shadow* s, uint32_t* host_out, uint64_t capacity, uint64_t* n_out,
+                                  void* stream);
+/* Device address of the resident DAG words (valid until destroy). */
+CPVS_API const uint32_t* cpvs_shadow_device_dag(const cpvs_shadow* s);
+/* Per-level node counts of the last build: `tree` before the subtree merge,
+ * `unique` after it; index = level (0 .. numLevels-1). */
+CPVS_API cpvs_status cpvs_shadow_level_counts(const cpvs_shadow* s, uint64_t* tree, uint64_t* unique, uint32_t capacity);
+
+/* Visibility of n light-space points in NDC ([-1,1]^3), xyz interleaved
+ * float32.  Replaces CompressedShadow::traverse(const vec3, bool)
+ * (src/CompressedShadow.h:64, src/CompressedShadow.cpp:404-463) and the
+ * per-pixel descent of shader/traverse.cs:75-133; the NDC is quantised with
+ * the reference's float32 order (src/CompressedShadowUtil.h:70-75).
+ * `bits_out` holds ceil(n/32) words. */
+CPVS_API cpvs_status cpvs_shadow_lookup_ndc(const cpvs_shadow* s, const float* xyz, uint64_t n, uint32_t* bits_out,
+                                   uint32_t flags, void* stream);
+/* Same, for integer voxel coordinates (the path getPathFromNDC yields),
+ * xyz interleaved int32. */
+CPVS_API cpvs_status cpvs_shadow_lookup_voxel(const cpvs_shadow* s, const int32_t* xyz, uint64_t n, uint32_t* bits_out,
+                                     uint32_t flags, void* stream);
+
+/* ---- top-level grid (container) -------------------------------------- */
+
+/* A cubic length^3 grid of DAGs (length a power of two).  Replaces
+ * CompressedShadowContainer (src/CompressedShadowContainer.h:21-73). */
+CPVS_API cpvs_status cpvs_grid_create(cpvs_ctx* ctx, uint32_t length, cpvs_grid** out);
+CPVS_API void cpvs_grid_destroy(cpvs_grid* g);
+CPVS_API uint32_t cpvs_grid_length(const cpvs_grid* g);
+/* CompressedShadowContainer::set (src/CompressedShadowContainer.h:34-39):
+ * cell (x,y,z) takes ownership of `s` (destroys any previous DAG there). */
+CPVS_API cpvs_status cpvs_grid_set(cpvs_grid* g, uint32_t x, uint32_t y, uint32_t z, cpvs_shadow* s);
+/* CompressedShadowContainer::get: the DAG at (x,y,z), or NULL. */
+CPVS_API const cpvs_shadow* cpvs_grid_get(const cpvs_grid* g, uint32_t x, uint32_t y, uint32_t z);
+/* copyToGPU/moveToGPU (src/CompressedShadowContainer.cpp:31-91): concatenates
+ * the DAGs in cell order z*L^2+y*L+x and writes the top-level grid, one word
+ * per cell: the cell DAG's start offset, or 0xFFFFFFFF / 0xFFFFFFFE for a
+ * uniformly shadowed / lit cell.  All cells must be set and share numLevels.
+ * With `release_cells` the per-cell DAGs are freed afterwards (moveToGPU). */
+CPVS_API cpvs_status cpvs_grid_finalize(cpvs_grid* g, int release_cells, void* stream);
+/* Size in words of the concatenated DAG, and its copy (after finalize). */
+CPVS_API uint64_t cpvs_grid_dag_size(const cpvs_grid* g);
+CPVS_API cpvs_status cpvs_grid_words(const cpvs_grid* g, uint32_t* dag_out, uint64_t dag_capacity, uint32_t* cells_out,
+                            uint64_t cells_capacity, void* stream);
+/* Grid lookup of n NDC points (shader/traverse.cs:41-133): the point is
+ * quantised at resolution 2^(dag_levels+grid_levels-1), routed to its cell
+ * and descended there.  Points outside the grid are lit. */
+CPVS_API cpvs_status cpvs_grid_lookup_ndc(const cpvs_grid* g, const float* xyz, uint64_t n, uint32_t* bits_out,
+                                 uint32_t flags, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CPVS_H */

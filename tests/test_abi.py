@@ -1,0 +1,75 @@
+"""The C ABI library without a GPU: it builds, loads, exports exactly what
+include/cpvs.h declares, and rejects bad arguments before touching the
+device.  No compute call runs here."""
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "cpvs.h")
+
+
+def declared_symbols():
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"^CPVS_API\s+[^(]*?\b(cpvs_\w+)\s*\(", src, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from cpvs_gb300 import build
+    build.build()
+    import cpvs_gb300
+    return cpvs_gb300.load_library()
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    assert len(names) >= 30
+    for must in ("cpvs_shadow_create", "cpvs_shadow_lookup_ndc", "cpvs_grid_lookup_ndc", "cpvs_hierarchy_create"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from cpvs_gb300 import LIB_PATH
+    out = subprocess.run(["nm", "-D", "--defined-only", LIB_PATH], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (cpvs_\w+)$", out, re.M))
+    declared = set(declared_symbols())
+    assert declared <= exported, sorted(declared - exported)
+    # nothing else escapes the library's C ABI
+    assert exported <= declared, sorted(exported - declared)
+    for name in declared:
+        assert getattr(lib, name) is not None
+
+
+def test_python_mirror_binds_every_symbol():
+    import cpvs_gb300
+    assert sorted(cpvs_gb300.exported_symbols()) == declared_symbols()
+
+
+def test_status_strings_and_version(lib):
+    assert lib.cpvs_abi_version() == 1
+    assert lib.cpvs_status_string(0) == b"ok"
+    assert lib.cpvs_status_string(6) == b"memory budget exceeded"
+
+
+def test_null_arguments_are_rejected(lib):
+    import ctypes as C
+    h = C.c_void_p()
+    assert lib.cpvs_hierarchy_create(None, None, 64, 0, None, C.byref(h)) == 1
+    assert lib.cpvs_shadow_create(None, None, 0, 1, 1, None, C.byref(h)) == 1
+    assert lib.cpvs_grid_create(None, 4, C.byref(h)) == 1
+    assert b"null" in lib.cpvs_last_error()
+    assert lib.cpvs_shadow_lookup_ndc(None, None, 0, None, 0, None) == 1
+    assert lib.cpvs_shadow_num_levels(None) == 0
+
+
+def test_no_device_is_an_error_not_a_fallback(lib):
+    import ctypes as C
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = C.c_void_p()
+    assert lib.cpvs_ctx_create(0, C.byref(h)) == 4   # CPVS_ERR_DEVICE
+    assert not h.value

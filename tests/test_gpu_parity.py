@@ -1,0 +1,213 @@
+"""GPU parity: the CUDA path, called through the C ABI, against the
+reference's golden fixtures and the oracle.  Integer/bit work: every
+comparison is exact (DAG words, pyramid bits, visibility bits)."""
+import numpy as np
+import pytest
+
+from cpvs_gb300 import scene
+
+pytestmark = pytest.mark.gpu
+
+
+def split_key(key):
+    name, zt = key.split("/")
+    zi, zn = (int(v) for v in zt[1:].split("of"))
+    return name, zi, zn
+
+
+def hierarchy_levels(cp, mm):
+    return np.concatenate([mm.level(L).reshape(-1) for L in range(1, mm.get_num_levels())])
+
+
+# ------------------------------------------------------------ golden fixtures
+def test_pyramid_matches_reference(cp, golden, golden_cases):
+    names = sorted({k.split("/")[0] for k in golden_cases} | {"test_minmax_4x4_1"})
+    for name in names:
+        depth = golden[f"{name}/depth"]
+        mm = cp.MinMaxHierarchy(depth)
+        assert mm.get_num_levels() == int(np.log2(depth.shape[0])) + 1
+        got = hierarchy_levels(cp, mm)
+        assert np.array_equal(got.view(np.uint32), golden[f"{name}/pyramid"].view(np.uint32)), name
+
+
+def test_build_matches_reference(cp, golden, golden_cases):
+    for key in golden_cases:
+        name, zi, zn = split_key(key)
+        depth = golden[f"{name}/depth"]
+        nl, tv, lm = golden[f"{key}/meta"].tolist()
+        mm = cp.MinMaxHierarchy(depth)
+        sh = cp.CompressedShadow.create(mm, zi, zn)
+        assert sh.get_num_levels() == nl and sh.uses_leafmasks() == bool(lm), key
+        assert np.array_equal(sh.get_dag(), golden[f"{key}/dag"]), key
+        assert sh.get_total_visibility() == tv, key
+        assert np.array_equal(sh.lookup_ndc(golden[f"{name}/ndc"]), golden[f"{key}/vis"]), key
+
+
+def test_reference_unit_test_traversals(cp, golden):
+    """test/CompressedShadowTest.cpp:50-152 through the drop-in traverse()."""
+    sh8 = cp.CompressedShadow.create(cp.MinMaxHierarchy(golden["test_depths8x8/depth"]))
+    assert sh8.traverse((-1, 1, -1), False) == cp.SHADOW
+    assert sh8.traverse((-1, -1, 0), False) == cp.VISIBLE
+    assert sh8.traverse((1, -1, 0.99), False) == cp.VISIBLE
+    sh16 = cp.CompressedShadow.create(cp.MinMaxHierarchy(golden["test_depths16x16/depth"]))
+    s = 2.0 / 16.0
+    assert sh16.traverse((0 + s, 0, .9)) == cp.SHADOW
+    assert sh16.traverse((0 + 3 * s, 0, -.9)) == cp.VISIBLE
+    sh32 = cp.CompressedShadow.create(cp.MinMaxHierarchy(golden["test_depths32x32/depth"]))
+    lit = np.asarray([[x / 32.0, y / 32.0, 0.59] for y in range(31) for x in range(31)], np.float32) * 2 - 1
+    assert (sh32.lookup_ndc(lit) == cp.VISIBLE).all()
+    dark = np.asarray([[x / 32.0, y / 32.0, 0.79] for y in range(8, 26) for x in range(7, 27)], np.float32) * 2 - 1
+    assert (sh32.lookup_ndc(dark) == cp.SHADOW).all()
+
+
+# ------------------------------------------------------------- vs the oracle
+def random_map(rng, n, kind):
+    if kind == 0:
+        return rng.random((n, n), dtype=np.float32)
+    if kind == 1:
+        return (rng.integers(0, 8, (n, n)) / 7).astype(np.float32)
+    if kind == 2:
+        return scene.rasterise(scene.make_scene(n, 0.9, int(rng.integers(1, 30)), int(rng.integers(0, 6)),
+                                                int(rng.integers(1 << 30))))
+    if kind == 3:
+        return (rng.integers(0, 4, (n, n)) / 4).astype(np.float32)  # dyadic: SVOs that stop early
+    return (rng.random((n, n)) * 0.2 + 0.7).astype(np.float32)
+
+
+def check_against_oracle(cp, oracle, depth, zi=0, zn=1, leafmasks=True, nq=4096, seed=0):
+    want = oracle.build(depth, zi, zn, leafmasks=leafmasks)
+    sh = cp.CompressedShadow.create(cp.MinMaxHierarchy(depth), zi, zn, leafmasks=leafmasks)
+    got = sh.get_dag()
+    assert sh.get_num_levels() == want.num_levels
+    assert sh.uses_leafmasks() == want.leafmasks
+    assert got.size == want.dag.size and np.array_equal(got, want.dag)
+    tree, uniq = sh.level_counts()
+    assert tree == want.tree_nodes and uniq == want.unique_nodes
+    n = depth.shape[0]
+    rng = np.random.default_rng(seed)
+    vox = rng.integers(-2, n + 2, (nq, 3)).astype(np.int32)
+    assert np.array_equal(sh.lookup_voxel(vox), oracle.lookup_voxel(want.dag, want.num_levels, want.leafmasks, vox))
+    ndc = rng.uniform(-1.05, 1.05, (nq, 3)).astype(np.float32)
+    assert np.array_equal(sh.lookup_ndc(ndc), oracle.lookup_ndc(want.dag, want.num_levels, want.leafmasks, ndc))
+    return sh
+
+
+def test_random_maps_match_oracle(cp, oracle):
+    rng = np.random.default_rng(1234)
+    for trial in range(60):
+        n = int(rng.choice([8, 16, 32, 64, 128, 256]))
+        zn = int(rng.choice([1, 1, 2, 3, 5, 8]))
+        check_against_oracle(cp, oracle, random_map(rng, n, trial % 5), int(rng.integers(0, zn)), zn, seed=trial)
+
+
+def test_leafmasks_off_matches_oracle(cp, oracle):
+    rng = np.random.default_rng(5)
+    for trial in range(12):
+        n = int(rng.choice([16, 32, 64, 128]))
+        check_against_oracle(cp, oracle, random_map(rng, n, trial % 5), leafmasks=False, seed=trial)
+
+
+def test_special_values_match_oracle(cp, oracle):
+    rng = np.random.default_rng(6)
+    d = (rng.random((64, 64), dtype=np.float32) * 0.6 + 0.2).astype(np.float32)
+    d[rng.random((64, 64)) < 0.1] = np.float32(-0.0)
+    d[rng.random((64, 64)) < 0.1] = np.float32(0.0)
+    d[rng.random((64, 64)) < 0.02] = np.float32(np.nan)
+    d[rng.random((64, 64)) < 0.02] = np.float32(np.inf)
+    d[rng.random((64, 64)) < 0.02] = np.float32(-1.5)
+    mm = cp.MinMaxHierarchy(d)
+    assert np.array_equal(hierarchy_levels(cp, mm).view(np.uint32), oracle.pyramid(d).view(np.uint32))
+    check_against_oracle(cp, oracle, d)
+    for v in (0.0, 1.0, 0.25, 0.5, 0.3):
+        check_against_oracle(cp, oracle, np.full((32, 32), v, np.float32))
+
+
+def test_c0_config_matches_oracle(cp, oracle):
+    """The 1024^2 map of 40 boxes: DAG words and 2^20 voxel lookups."""
+    d = scene.rasterise(scene.config_scene("c0"))
+    want = oracle.build(d)
+    sh = cp.CompressedShadow.from_depth(d)
+    assert np.array_equal(sh.get_dag(), want.dag)
+    q = scene.voxel_queries(1 << 20, 1024, 0)
+    assert np.array_equal(sh.lookup_voxel(q), oracle.lookup_voxel(want.dag, want.num_levels, True, q, threads=8))
+
+
+def test_c1_config_matches_oracle(cp, oracle):
+    """The 8192^2 map of 500 boxes and 64 spheres: DAG words, per-level node
+    counts, and 2^22 of the mixed surface/volume NDC queries."""
+    d = scene.rasterise(scene.config_scene("c1"))
+    want = oracle.build(d, threads=4)
+    import torch
+    sh = cp.CompressedShadow.from_depth(torch.from_numpy(d).cuda())
+    got = sh.get_dag()
+    assert got.size == want.dag.size and np.array_equal(got, want.dag)
+    tree, uniq = sh.level_counts()
+    assert tree == want.tree_nodes and uniq == want.unique_nodes
+    q = scene.ndc_queries_mixed(d, 1 << 22, 1)
+    assert np.array_equal(sh.lookup_ndc(q), oracle.lookup_ndc(want.dag, want.num_levels, True, q, threads=8))
+
+
+def test_repeated_builds_are_identical(cp):
+    d = scene.rasterise(scene.config_scene("c0", n=512))
+    a = cp.CompressedShadow.from_depth(d).get_dag()
+    for _ in range(3):
+        assert np.array_equal(cp.CompressedShadow.from_depth(d).get_dag(), a)
+
+
+def test_device_io_matches_host_io(cp, oracle):
+    import torch
+    d = scene.rasterise(scene.config_scene("c0", n=256))
+    sh = cp.CompressedShadow.from_depth(torch.from_numpy(d).cuda())
+    q = scene.ndc_queries_mixed(d, 100_003, 4)
+    host = sh.lookup_ndc(q)
+    words = sh.lookup_ndc(torch.from_numpy(q).cuda())
+    torch.cuda.synchronize()
+    dev = cp.unpack_bits(words.cpu().numpy().view(np.uint32), q.shape[0])
+    assert np.array_equal(host, dev)
+    assert sh.lookup_ndc(np.zeros((0, 3), np.float32)).size == 0
+
+
+def test_grid_matches_oracle(cp, oracle):
+    """A 2x2x2 grid: 2x2 xy tiles of a 128^2 map, 2 z-tiles each, plus one
+    uniformly lit tile; routing and descent equal the oracle's restatement of
+    shader/traverse.cs."""
+    n, L = 64, 2
+    full = scene.rasterise(scene.make_scene(n * L, 0.9, 20, 4, 77))
+    full[:n, n:] = np.float32(1.0)  # tile (x=1, y=0) lit everywhere
+    grid = cp.CompressedShadowContainer(L)
+    dags, offs, off = [], [], 0
+    for z in range(L):
+        for y in range(L):
+            for x in range(L):
+                tile = np.ascontiguousarray(full[y * n:(y + 1) * n, x * n:(x + 1) * n])
+                b = oracle.build(tile, z, L)
+                dags.append(b.dag)
+                offs.append(off)
+                off += b.dag.size
+                grid.set(cp.CompressedShadow.from_depth(tile, z, L), x, y, z)
+    grid.copy_to_gpu()
+    dag, cells = grid.words()
+    assert np.array_equal(dag, np.concatenate(dags))
+    q = np.random.default_rng(3).uniform(-1.1, 1.1, (200_000, 3)).astype(np.float32)
+    want = oracle.grid_lookup_ndc(np.concatenate(dags).astype(np.uint32), np.asarray(offs, np.uint32), L,
+                                  int(np.log2(n)) + 1, True, q)
+    assert np.array_equal(grid.lookup_ndc(q), want)
+    lit_cells = [(z * L + 0) * L + 1 for z in range(L)]
+    assert any(cells[c] == 0xFFFFFFFE for c in lit_cells)
+
+
+def test_errors(cp):
+    d = scene.rasterise(scene.config_scene("c0", n=256))
+    with pytest.raises(cp.CpvsError) as e:
+        cp.CompressedShadow.from_depth(np.zeros((48, 48), np.float32))
+    assert e.value.status == 1
+    with pytest.raises(cp.CpvsError) as e:
+        cp.CompressedShadow.from_depth(d, 3, 2)
+    assert e.value.status == 1
+    ctx = cp.Context(0)
+    ctx.set_budget(1 << 20)
+    with pytest.raises(cp.CpvsError) as e:
+        cp.CompressedShadow.from_depth(d, ctx=ctx)
+    assert e.value.status == 6
+    ctx.set_budget(0)
+    assert cp.CompressedShadow.from_depth(d, ctx=ctx).dag_size() > 0
