@@ -45,6 +45,9 @@ _SIGS = {
     "cpvs_ctx_destroy": (None, [_vp]),
     "cpvs_ctx_set_budget": (C.c_int, [_vp, _u64]),
     "cpvs_ctx_bytes_in_use": (_u64, [_vp]),
+    "cpvs_ctx_enable_timing": (C.c_int, [_vp, C.c_int]),
+    "cpvs_ctx_kernel_times": (C.c_int, [_vp, _vp, _vp, _u32, C.POINTER(_u32)]),
+    "cpvs_kernel_name": (C.c_char_p, [_u32]),
     "cpvs_hierarchy_create": (C.c_int, [_vp, _vp, _u32, _u32, _vp, C.POINTER(_vp)]),
     "cpvs_hierarchy_destroy": (None, [_vp]),
     "cpvs_hierarchy_num_levels": (_u32, [_vp]),
@@ -148,6 +151,18 @@ class Context:
 
     def bytes_in_use(self) -> int:
         return int(_lib.cpvs_ctx_bytes_in_use(self.handle))
+
+    def enable_timing(self, on: bool = True):
+        _check(_lib.cpvs_ctx_enable_timing(self.handle, int(on)))
+
+    def kernel_times(self) -> dict:
+        """{kernel name: (total ms, launches)} since timing was enabled."""
+        cap = 64
+        ms = (C.c_double * cap)()
+        ln = (C.c_uint64 * cap)()
+        cnt = C.c_uint32()
+        _check(_lib.cpvs_ctx_kernel_times(self.handle, ms, ln, cap, C.byref(cnt)))
+        return {_lib.cpvs_kernel_name(i).decode(): (float(ms[i]), int(ln[i])) for i in range(cnt.value)}
 
     def __del__(self):
         if getattr(self, "handle", None) and _lib is not None:

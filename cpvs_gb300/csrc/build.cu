@@ -287,7 +287,9 @@ __global__ void __launch_bounds__(kThreads)
 __device__ __forceinline__ uint64_t inner_hash(const LevelDev& cur, const LevelDev& child, uint32_t i) {
     const uint32_t m = cur.mask[i];
     uint64_t h = fmix64((((uint64_t)cur.job[i] + 1) << 32 | m) ^ kGolden);
-    const uint32_t k = partial_children(m), f = cur.first[i];
+    const uint32_t k = partial_children(m);
+    if (!k) return h;
+    const uint32_t f = cur.first[i];
     for (uint32_t r = 0; r < k; ++r) h = fmix64(h ^ ((uint64_t)child.uid[f + r] + (uint64_t)(r + 1) * kGolden));
     return h;
 }
@@ -307,7 +309,9 @@ __device__ __forceinline__ bool same_node(const LevelDev& cur, const LevelDev& c
     } else {
         const uint32_t m = cur.mask[a];
         if (m != cur.mask[b]) return false;
-        const uint32_t k = partial_children(m), fa = cur.first[a], fb = cur.first[b];
+        const uint32_t k = partial_children(m);
+        if (!k) return true;
+        const uint32_t fa = cur.first[a], fb = cur.first[b];
         for (uint32_t r = 0; r < k; ++r)
             if (child.uid[fa + r] != child.uid[fb + r]) return false;
         return true;
@@ -481,10 +485,15 @@ __global__ void __launch_bounds__(kThreads)
                     ++r;
                 }
         } else {
-            const uint32_t k = partial_children(m), f = cur.first[i];
-            const uint32_t sc = seg_index(j, L - 1);
-            const uint32_t cb = lay.base[sc] - seg.wstart[sc];
-            for (uint32_t r = 0; r < k; ++r) dst[1 + r] = cb + child.woff[child.uid[f + r]];
+            // only nodes with children touch the level below (which does not
+            // exist under the bottom level)
+            const uint32_t k = partial_children(m);
+            if (k && L > 0) {
+                const uint32_t f = cur.first[i];
+                const uint32_t sc = seg_index(j, L - 1);
+                const uint32_t cb = lay.base[sc] - seg.wstart[sc];
+                for (uint32_t r = 0; r < k; ++r) dst[1 + r] = cb + child.woff[child.uid[f + r]];
+            }
         }
     }
 }
@@ -527,9 +536,11 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         const int nl = log2_u32(S.n) + 1;
         root_level[j] = (uint32_t)(nl - 2);
         maxR = std::max(maxR, nl - 2);
-        if ((nl - 3 >= 2) != leafmasks) return fail(CPVS_ERR_INVALID_ARG, "build_dags: mixed leafmask modes");
+        // leafmasks need numLevels-3 >= 2 (src/CompressedShadow.cpp:20-27)
+        if (leafmasks && nl - 3 < 2) return fail(CPVS_ERR_INVALID_ARG, "build_dags: map too small for leafmasks");
     }
 
+    Timing* tm = &ctx.timing;
     // ---- level bounds (one pass over each source's pyramid), one sync
     const size_t bounds_bytes = (size_t)njobs * CPVS_MAX_LEVELS * sizeof(unsigned long long);
     unsigned long long* bounds_dev = nullptr;
@@ -552,6 +563,7 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         CPVS_CUDA(cudaMemcpyAsync(bj_dev, grouped.data(), njobs * sizeof(BoundJob), cudaMemcpyHostToDevice, st));
         for (size_t s = 0; s < sources.size(); ++s) {
             if (!ranges[s].second) continue;
+            KernelTimer kt(tm, K_LEVEL_BOUNDS, st);
             cpvs_status r = launch_level_bounds(sources[s].levels, sources[s].n, lmin, bj_dev + ranges[s].first,
                                                 (int)ranges[s].second, bounds_dev, st);
             if (r != CPVS_OK) return r;
@@ -685,14 +697,19 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
     // ---- top-down
     for (int L = maxR; L > bottom; --L) {
         const uint32_t g = grid_for(cap[L], kThreads * 4);
-        k_expand_count<<<g, kThreads, 0, st>>>(lv[L], counts, jobs_dev, njobs, L, partials, err);
+        { KernelTimer kt(tm, K_EXPAND_COUNT, st);
+        k_expand_count<<<g, kThreads, 0, st>>>(lv[L], counts, jobs_dev, njobs, L, partials, err); }
+        { KernelTimer kt(tm, K_EXPAND_WRITE, st);
         k_expand_write<<<g, kThreads, 0, st>>>(lv[L], lv[L - 1], counts, L, partials, inj_dev + inj_off[L - 1],
-                                               (uint32_t)ninj[L - 1], seg, (uint32_t)cap[L - 1], err);
+                                               (uint32_t)ninj[L - 1], seg, (uint32_t)cap[L - 1], err); }
     }
-    if (leafmasks)
+    if (leafmasks) {
+        KernelTimer kt(tm, K_LEAF_MASKS, st);
         k_leaf_masks<<<grid_for(cap[2] * 32, kThreads), kThreads, 0, st>>>(lv[2], counts, jobs_dev, njobs, 2, seg, err);
-    else
+    } else {
+        KernelTimer kt(tm, K_CLASSIFY_BOTTOM, st);
         k_classify_bottom<<<grid_for(cap[0], kThreads), kThreads, 0, st>>>(lv[0], counts, jobs_dev, njobs, 0, seg, err);
+    }
     CPVS_CUDA(cudaGetLastError());
 
     // ---- bottom-up merge
@@ -703,22 +720,35 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         const uint32_t gs = grid_for(cap[L], kThreads * 4);
         const uint32_t gi = grid_for(cap[L], kThreads);
         const LevelDev child = (L > bottom) ? lv[L - 1] : lv[L];
-        CPVS_CUDA(cudaMemsetAsync(table, 0xFF, tcap * sizeof(unsigned long long), st));
-        if (leaf) {
-            k_dedup_insert<true><<<gi, kThreads, 0, st>>>(lv[L], child, counts, L, table, cmask);
-            k_dedup_resolve<true><<<gs, kThreads, 0, st>>>(lv[L], counts, L, table, partials);
-            k_dedup_scan<true><<<gs, kThreads, 0, st>>>(lv[L], counts, level_u, L, table, partials, seg);
-        } else {
-            k_dedup_insert<false><<<gi, kThreads, 0, st>>>(lv[L], child, counts, L, table, cmask);
-            k_dedup_resolve<false><<<gs, kThreads, 0, st>>>(lv[L], counts, L, table, partials);
-            k_dedup_scan<false><<<gs, kThreads, 0, st>>>(lv[L], counts, level_u, L, table, partials, seg);
+        {
+            KernelTimer kt(tm, K_TABLE_CLEAR, st);
+            CPVS_CUDA(cudaMemsetAsync(table, 0xFF, tcap * sizeof(unsigned long long), st));
         }
-        k_dedup_remap<<<gi, kThreads, 0, st>>>(lv[L], counts, L, table);
+        if (leaf) {
+            { KernelTimer kt(tm, K_INSERT_LEAF, st);
+              k_dedup_insert<true><<<gi, kThreads, 0, st>>>(lv[L], child, counts, L, table, cmask); }
+            { KernelTimer kt(tm, K_RESOLVE, st);
+              k_dedup_resolve<true><<<gs, kThreads, 0, st>>>(lv[L], counts, L, table, partials); }
+            { KernelTimer kt(tm, K_SCAN, st);
+              k_dedup_scan<true><<<gs, kThreads, 0, st>>>(lv[L], counts, level_u, L, table, partials, seg); }
+        } else {
+            { KernelTimer kt(tm, K_INSERT_INNER, st);
+              k_dedup_insert<false><<<gi, kThreads, 0, st>>>(lv[L], child, counts, L, table, cmask); }
+            { KernelTimer kt(tm, K_RESOLVE, st);
+              k_dedup_resolve<false><<<gs, kThreads, 0, st>>>(lv[L], counts, L, table, partials); }
+            { KernelTimer kt(tm, K_SCAN, st);
+              k_dedup_scan<false><<<gs, kThreads, 0, st>>>(lv[L], counts, level_u, L, table, partials, seg); }
+        }
+        { KernelTimer kt(tm, K_REMAP, st);
+          k_dedup_remap<<<gi, kThreads, 0, st>>>(lv[L], counts, L, table); }
         CPVS_CUDA(cudaGetLastError());
     }
 
     // ---- layout, one sync for the sizes
-    k_layout<<<1, 1024, 0, st>>>(seg, lay, root_dev, njobs, bottom);
+    {
+        KernelTimer kt(tm, K_LAYOUT, st);
+        k_layout<<<1, 1024, 0, st>>>(seg, lay, root_dev, njobs, bottom);
+    }
     CPVS_CUDA(cudaGetLastError());
     std::vector<uint64_t> job_off(njobs + 1);
     std::vector<uint32_t> hseg(segn * 6);
@@ -759,6 +789,7 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         if (!U) continue;
         const uint32_t g = grid_for(U, kThreads);
         const LevelDev child = (L > bottom) ? lv[L - 1] : lv[L];
+        KernelTimer kt(tm, K_EMIT, st);
         if (leafmasks && L == 2)
             k_emit<true><<<g, kThreads, 0, st>>>(lv[L], child, level_u, L, seg, lay, out.dag, total, err);
         else

@@ -205,6 +205,29 @@ cpvs_status cpvs_ctx_set_budget(cpvs_ctx* ctx, uint64_t bytes) {
 
 uint64_t cpvs_ctx_bytes_in_use(const cpvs_ctx* ctx) { return ctx ? ctx->c.in_use + ctx->c.scratch : 0; }
 
+cpvs_status cpvs_ctx_enable_timing(cpvs_ctx* ctx, int on) {
+    if (!ctx) return fail(CPVS_ERR_INVALID_ARG, "null ctx");
+    cudaSetDevice(ctx->c.device);
+    ctx->c.timing.on = on != 0;
+    ctx->c.timing.reset();
+    return CPVS_OK;
+}
+
+cpvs_status cpvs_ctx_kernel_times(cpvs_ctx* ctx, double* total_ms, uint64_t* launches, uint32_t capacity,
+                                  uint32_t* count) {
+    if (!ctx) return fail(CPVS_ERR_INVALID_ARG, "null ctx");
+    if (count) *count = cpvs::K_COUNT;
+    cudaSetDevice(ctx->c.device);
+    ctx->c.timing.collect();
+    for (uint32_t i = 0; i < capacity && i < (uint32_t)cpvs::K_COUNT; ++i) {
+        if (total_ms) total_ms[i] = ctx->c.timing.ms[i];
+        if (launches) launches[i] = ctx->c.timing.launches[i];
+    }
+    return CPVS_OK;
+}
+
+const char* cpvs_kernel_name(uint32_t id) { return cpvs::kernel_name((int)id); }
+
 // ------------------------------------------------------------- hierarchy
 cpvs_status cpvs_hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n, uint32_t flags, void* stream,
                                   cpvs_hierarchy** out) {
@@ -232,7 +255,7 @@ cpvs_status cpvs_hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n,
                                         (flags & CPVS_IO_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) r = cpvs::cuda_fail(e, "hierarchy upload");
     }
-    if (r == CPVS_OK) r = cpvs::launch_pyramid(h->depth, n, h->levels, st);
+    if (r == CPVS_OK) r = cpvs::launch_pyramid(h->depth, n, h->levels, st, &c.timing);
     if (r != CPVS_OK) {
         cpvs_hierarchy_destroy(h);
         return r;
@@ -371,7 +394,7 @@ cpvs_status cpvs_shadow_lookup_ndc(const cpvs_shadow* s, const float* xyz, uint6
     if (!s) return fail(CPVS_ERR_INVALID_ARG, "lookup_ndc: null shadow");
     cudaStream_t st = (cudaStream_t)stream;
     return lookup_common(s->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
-        return cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, q, true, n, bits, st);
+        return cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, q, true, n, bits, st, &s->ctx->c.timing);
     });
 }
 
@@ -380,7 +403,7 @@ cpvs_status cpvs_shadow_lookup_voxel(const cpvs_shadow* s, const int32_t* xyz, u
     if (!s) return fail(CPVS_ERR_INVALID_ARG, "lookup_voxel: null shadow");
     cudaStream_t st = (cudaStream_t)stream;
     return lookup_common(s->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
-        return cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, q, false, n, bits, st);
+        return cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, q, false, n, bits, st, &s->ctx->c.timing);
     });
 }
 
@@ -514,7 +537,7 @@ cpvs_status cpvs_grid_lookup_ndc(const cpvs_grid* g, const float* xyz, uint64_t 
     cudaStream_t st = (cudaStream_t)stream;
     return lookup_common(g->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
         return cpvs::launch_grid_lookup(g->dag, g->words, g->cell_words, g->length, g->dag_levels, g->leafmasks,
-                                        static_cast<const float*>(q), n, bits, st);
+                                        static_cast<const float*>(q), n, bits, st, &g->ctx->c.timing);
     });
 }
 

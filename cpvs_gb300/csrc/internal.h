@@ -43,7 +43,8 @@ inline int log2_u32(uint32_t n) {
 }
 
 // Builds levels 1..log2(n) of the min-max pyramid of `depth` into `levels`.
-cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaStream_t st);
+struct Timing;
+cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaStream_t st, Timing* timing = nullptr);
 
 // One z-tile of a source map whose per-level node bounds are wanted.
 struct BoundJob {
@@ -82,13 +83,64 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
 
 // -------------------------------------------------------------- lookup
 cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks, const void* xyz,
-                          bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st);
+                          bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st, Timing* timing = nullptr);
 cpvs_status launch_grid_lookup(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
                                uint32_t dag_levels, bool leafmasks, const float* xyz, uint64_t n, uint32_t* bits,
-                               cudaStream_t st);
+                               cudaStream_t st, Timing* timing = nullptr);
+
+// ------------------------------------------------------------ timing
+// Kernels timed (when a context's timing is on) with a CUDA event pair on
+// the launching stream around every launch.
+enum KernelId : int {
+    K_PYRAMID = 0,
+    K_LEVEL_BOUNDS,
+    K_EXPAND_COUNT,
+    K_EXPAND_WRITE,
+    K_LEAF_MASKS,
+    K_CLASSIFY_BOTTOM,
+    K_TABLE_CLEAR,
+    K_INSERT_LEAF,
+    K_INSERT_INNER,
+    K_RESOLVE,
+    K_SCAN,
+    K_REMAP,
+    K_LAYOUT,
+    K_EMIT,
+    K_LOOKUP,
+    K_GRID_LOOKUP,
+    K_COUNT
+};
+const char* kernel_name(int id);
+
+struct Timing {
+    bool on = false;
+    std::vector<cudaEvent_t> free_events;
+    struct Pending {
+        int id;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    double ms[K_COUNT] = {0};
+    uint64_t launches[K_COUNT] = {0};
+    cudaEvent_t get();
+    void collect();  // waits for pending events and accumulates
+    void reset();
+    ~Timing();
+};
+
+// Records an event pair around the launches in its scope.
+struct KernelTimer {
+    Timing* t;
+    int id;
+    cudaStream_t st;
+    cudaEvent_t a = nullptr;
+    KernelTimer(Timing* timing, int kid, cudaStream_t s);
+    ~KernelTimer();
+};
 
 // ----------------------------------------------------------------- ctx
 struct Ctx {
+    Timing timing;
     int device = 0;
     int num_sms = 0;
     uint64_t budget = 0;   // 0 = unlimited

@@ -131,8 +131,9 @@ uint32_t lookup_grid(int num_sms, uint64_t n) {
 }  // namespace
 
 cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks, const void* xyz,
-                          bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st) {
+                          bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st, Timing* timing) {
     if (n == 0) return CPVS_OK;
+    KernelTimer kt(timing, K_LOOKUP, st);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -147,8 +148,9 @@ cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_leve
 
 cpvs_status launch_grid_lookup(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
                                uint32_t dag_levels, bool leafmasks, const float* xyz, uint64_t n, uint32_t* bits,
-                               cudaStream_t st) {
+                               cudaStream_t st, Timing* timing) {
     if (n == 0) return CPVS_OK;
+    KernelTimer kt(timing, K_GRID_LOOKUP, st);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

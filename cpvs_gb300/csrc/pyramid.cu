@@ -135,7 +135,8 @@ __global__ void __launch_bounds__(kBoundThreads)
 
 }  // namespace
 
-cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaStream_t st) {
+cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaStream_t st, Timing* timing) {
+    KernelTimer kt(timing, K_PYRAMID, st);
     uint32_t S = n;
     int L0 = 1;
     bool first = true;

@@ -79,6 +79,15 @@ CPVS_API void cpvs_ctx_destroy(cpvs_ctx* ctx);
  * CPVS_ERR_BUDGET. */
 CPVS_API cpvs_status cpvs_ctx_set_budget(cpvs_ctx* ctx, uint64_t bytes);
 CPVS_API uint64_t cpvs_ctx_bytes_in_use(const cpvs_ctx* ctx);
+/* Per-kernel CUDA-event timing (off by default).  When on, every kernel the
+ * context launches is bracketed by an event pair on its stream;
+ * cpvs_ctx_kernel_times waits for those events and returns, per kernel id
+ * (0 .. count-1, names from cpvs_kernel_name), the summed milliseconds and
+ * the launch count since timing was enabled. */
+CPVS_API cpvs_status cpvs_ctx_enable_timing(cpvs_ctx* ctx, int on);
+CPVS_API cpvs_status cpvs_ctx_kernel_times(cpvs_ctx* ctx, double* total_ms, uint64_t* launches, uint32_t capacity,
+                                           uint32_t* count);
+CPVS_API const char* cpvs_kernel_name(uint32_t id);
 CPVS_API const char* cpvs_status_string(cpvs_status s);
 /* Message of the last failed call on this host thread ("" if none). */
 CPVS_API const char* cpvs_last_error(void);
