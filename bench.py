@@ -1,0 +1,393 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 shadow hot path: DAG build + visibility lookups.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config c1|c0]
+
+A step is one full build of the compressed shadow of the workload's depth
+map (min-max pyramid, SVO classification with 64-bit leafmasks, subtree
+merge, pointer compression), from a depth map resident in HBM to a DAG
+resident in HBM.  `value` is whole-job build throughput in Gvoxel/s
+(n^3 voxels per DAG).  `lookup` reports the workload's query batch against
+the built DAG (Glookups/s).  `e2e` repeats both through the public API with
+host buffers: the depth map / queries copied in from pinned host memory and
+the DAG words / visibility bits read back, inside the timed region.
+
+With --gpus N > 1 (under torchrun) every rank builds its own copy of the
+workload (independent shadows, no collective on the data path: weak scaling)
+and the slowest rank's time counts.  `--impl reference` times the CPU
+restatement of the reference's own build and lookup (oracle/) on the host
+cores instead.  Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from cpvs_gb300 import scene  # noqa: E402
+
+WORKLOADS = {
+    "c1": dict(queries=1 << 26, desc="8192^2 float32 depth map (plane 0.95, 500 boxes, 64 spheres; seed 1) -> "
+                                      "8192^3-voxel DAG with 64-bit leafmasks; 2^26 float32 NDC lookups, half on "
+                                      "the depth surface +-0.5 voxel, half uniform"),
+    "c0": dict(queries=1 << 20, desc="1024^2 float32 depth map (plane 0.9, 40 boxes; seed 0) -> 1024^3-voxel DAG "
+                                     "with 64-bit leafmasks; 2^20 NDC lookups"),
+}
+METRIC = "DAG-build Gvoxel/s (shadow DAG from a depth map, bit-exact with the reference)"
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(prefix="cpvs_clocks_", suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={CLOCK_FIELDS}", "--format=csv,noheader,nounits", "-lms", "50",
+                 "-i", str(self.device)], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, ValueError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append(dict(sm=float(f[1]), smax=float(f[2]), power=float(f[3]) if f[3] not in ("", "[N/A]") else 0.0,
+                                 hw=f[5], hwt=f[6], swt=f[7], swp=f[8]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        pmax = max(r["power"] for r in rows)
+        load = [r for r in rows if r["power"] >= 0.3 * pmax] or rows
+        reasons = []
+        for key, name in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"), ("swt", "sw_thermal_slowdown"),
+                          ("swp", "sw_power_cap")):
+            if any(r[key].lower() == "active" for r in load):
+                reasons.append(name)
+        return {"sm_mhz": statistics.median(r["sm"] for r in load), "sm_max_mhz": max(r["smax"] for r in rows),
+                "reasons": reasons, "samples": len(rows), "samples_under_load": len(load),
+                "power_w_max": pmax}
+
+
+# algorithmic bytes per kernel of the build (the units each launch processes)
+def kernel_alg_bytes(name: str, n: int, tree: list, uniq: list, dag_words: int) -> float:
+    texels = sum((n >> L) ** 2 for L in range(1, int(np.log2(n)) + 1))
+    leaves = tree[2] if len(tree) > 2 else 0
+    inner = sum(tree[3:])
+    if name == "pyramid":          # depth read once, every pyramid texel written once
+        return 4.0 * n * n + 8.0 * texels
+    if name == "leaf_masks":       # per leaf: 8x8 depth footprint in, 8 leafmasks + mask + hash out
+        return leaves * (256 + 12 + 64 + 4 + 8)
+    if name == "insert_leaf":      # per leaf: hash + job in, one slot probed, slot index out, 2x64 B compared
+        return leaves * (8 + 4 + 8 + 4 + 128)
+    if name in ("resolve", "scan", "remap"):
+        return (leaves + inner) * 16
+    if name in ("expand_count", "expand_write"):
+        return inner * (12 + 32 + 8) + leaves * 12
+    if name == "emit":
+        return 4.0 * dag_words
+    if name == "table_clear":
+        return 8.0 * 2 * (leaves + inner)
+    return 0.0
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import cpvs_gb300 as cp
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    wl = WORKLOADS[args.config]
+    sc = scene.config_scene(args.config)
+    n = sc.n
+    depth = scene.rasterise(sc)
+    depth_pinned = torch.from_numpy(depth).pin_memory()
+    depth_dev = depth_pinned.to(dev)
+    nq = wl["queries"]
+    q_host = scene.ndc_queries_mixed(depth, nq, 1)
+    q_pinned = torch.from_numpy(q_host).pin_memory()
+    q_dev = q_pinned.to(dev)
+    bits_dev = torch.empty((nq + 31) // 32, dtype=torch.int32, device=dev)
+    bits_host = torch.empty((nq + 31) // 32, dtype=torch.int32).pin_memory()
+
+    ctx = cp.Context(local_rank)
+    stream = torch.cuda.current_stream(dev)
+    keep = {}
+
+    def build_step():
+        mm = cp.MinMaxHierarchy(depth_dev, ctx=ctx, stream=stream, borrow=True)
+        sh = cp.CompressedShadow.create(mm, stream=stream)
+        keep["sh"] = sh  # the previous step's DAG is freed as this one replaces it
+        return sh
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    for _ in range(args.warmup):
+        build_step()
+    barrier()
+    ctx.enable_timing(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        build_step()
+    e1.record(stream)
+    barrier()
+    build_ms = e0.elapsed_time(e1) / args.steps
+    ktimes = ctx.kernel_times()
+    ctx.enable_timing(False)
+    sh = keep["sh"]
+    tree, uniq = sh.level_counts()
+    dag_words = sh.dag_size()
+
+    # lookups against the resident DAG, queries resident in HBM
+    for _ in range(args.warmup):
+        sh.lookup_ndc(q_dev, bits_dev, stream=stream)
+    barrier()
+    ctx.enable_timing(True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        sh.lookup_ndc(q_dev, bits_dev, stream=stream)
+    e1.record(stream)
+    barrier()
+    lookup_ms = e0.elapsed_time(e1) / args.steps
+    lk = ctx.kernel_times()["lookup"]
+    ctx.enable_timing(False)
+
+    # end to end through the public API with host buffers
+    def e2e_build():
+        s = cp.CompressedShadow.from_depth(depth_pinned, ctx=ctx, stream=stream)
+        s.get_dag()
+        return s
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_build()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        s = e2e_build()
+    barrier()
+    e2e_build_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    dag_bytes = s.dag_size() * 4
+    del s
+    for _ in range(max(1, args.warmup // 2)):
+        sh.lookup_ndc_packed(q_pinned, bits_host, stream=stream)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sh.lookup_ndc_packed(q_pinned, bits_host, stream=stream)
+    barrier()
+    e2e_lookup_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    clk = clocks.stop()
+
+    # slowest rank
+    t = torch.tensor([build_ms, lookup_ms, e2e_build_ms, e2e_lookup_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    build_ms, lookup_ms, e2e_build_ms, e2e_lookup_ms = t.tolist()
+    voxels = float(n) ** 3
+
+    launches = sum(v[1] for k, v in ktimes.items() if k != "table_clear")
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    peak, peak_kind = peaks()
+    build_kernels = {k: v for k, v in ktimes.items() if v[1] and k not in ("lookup", "grid_lookup")}
+    dom = max(build_kernels, key=lambda k: build_kernels[k][0])
+    dom_ms_launch = build_kernels[dom][0] / build_kernels[dom][1]
+    dom_launches_per_step = build_kernels[dom][1] / args.steps
+    dom_bytes = kernel_alg_bytes(dom, n, tree, uniq, dag_words) / dom_launches_per_step
+    achieved = dom_bytes / (dom_ms_launch * 1e-3) / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", f"traffic_{args.config}.json")
+    if os.path.exists(prof):
+        traffic = json.load(open(prof)).get(dom)
+    build_alg = 4.0 * n * n + 8.0 * sum((n >> L) ** 2 for L in range(1, int(np.log2(n)) + 1)) + 4.0 * dag_words
+    lookup_alg = nq * 12.125 + 4.0 * dag_words
+    lk_ms_launch = lk[0] / max(lk[1], 1)
+    line = {
+        "metric": METRIC,
+        "value": round(world * voxels / (build_ms * 1e-3) / 1e9, 1),
+        "unit": "Gvoxel/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(build_ms, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic: seeded scene rasterised to a float32 depth map (no dataset involved)",
+        "config": {"workload": f"{args.config}: {wl['desc']}", "map_side": n, "voxels_per_dag": int(voxels),
+                   "dag_words": dag_words, "lookups_per_batch": nq,
+                   "l2": "inputs larger than L2 (256 MiB map + 171 MiB pyramid per step)" if n >= 8192 else
+                         "map smaller than L2: later steps may hit L2",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "e2e": {"value": round(world * voxels / (e2e_build_ms * 1e-3) / 1e9, 1), "unit": "Gvoxel/s",
+                "h2d_bytes_per_step": int(depth.nbytes), "d2h_bytes_per_step": int(dag_bytes),
+                "ms_per_step": round(e2e_build_ms, 3),
+                "path": "cpvs_shadow_create_from_depth (pinned host map) + cpvs_shadow_dag_words"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": traffic,
+                     "alg_bytes_per_launch": int(dom_bytes), "ms_per_launch": round(dom_ms_launch, 4),
+                     "build_pipeline": {"alg_bytes": int(build_alg),
+                                        "achieved": round(build_alg / (build_ms * 1e-3) / 1e9, 1),
+                                        "frac": round(build_alg / (build_ms * 1e-3) / 1e9 / peak, 4)}},
+        "lookup": {"value": round(world * nq / (lookup_ms * 1e-3) / 1e9, 2), "unit": "Glookups/s",
+                   "ms_per_batch": round(lookup_ms, 4),
+                   "roofline": {"bound": "hbm", "achieved": round(lookup_alg / (lk_ms_launch * 1e-3) / 1e9, 1),
+                                "peak": peak, "unit": "GB/s",
+                                "frac": round(lookup_alg / (lk_ms_launch * 1e-3) / 1e9 / peak, 4),
+                                "alg_bytes_per_launch": int(lookup_alg)},
+                   "e2e": {"value": round(world * nq / (e2e_lookup_ms * 1e-3) / 1e9, 2), "unit": "Glookups/s",
+                           "h2d_bytes_per_step": int(q_host.nbytes), "d2h_bytes_per_step": int(bits_host.numel() * 4),
+                           "ms_per_step": round(e2e_lookup_ms, 3)}},
+        "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in build_kernels.items()},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(depth, q_host, args.config, sample_queries=1 << 22)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(depth, q, config, sample_queries, threads=None):
+    """The CPU restatement of the reference's build (pyramid on 4 threads as
+    the reference splits it, create on one thread as the reference runs it)
+    and its lookups on every host core."""
+    from oracle.oracle import Oracle
+    O = Oracle()
+    threads = threads or os.cpu_count() or 1
+    n = depth.shape[0]
+    t0 = time.perf_counter()
+    b = O.build(depth, threads=4)
+    build_s = time.perf_counter() - t0
+    qs = np.ascontiguousarray(q[:sample_queries])
+    t0 = time.perf_counter()
+    O.lookup_ndc(b.dag, b.num_levels, b.leafmasks, qs, threads=threads)
+    look_s = time.perf_counter() - t0
+    return {"value": round(float(n) ** 3 / build_s / 1e9, 3), "unit": "Gvoxel/s", "cores": 4, "kind": "port",
+            "sample": f"one full {config} build ({n}^2 map, pyramid on 4 threads, SVO/merge/compress on 1 thread, "
+                      f"{build_s:.2f} s); hash-indexed first-occurrence merge (the reference's linear scan gives "
+                      f"the same DAG more slowly)",
+            "lookup": {"value": round(qs.shape[0] / look_s / 1e9, 4), "unit": "Glookups/s", "cores": threads,
+                       "sample": f"{qs.shape[0]} of the {config} queries"}}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    wl = WORKLOADS[args.config]
+    sc = scene.config_scene(args.config)
+    n = sc.n
+    depth = scene.rasterise(sc)
+    q = scene.ndc_queries_mixed(depth, wl["queries"], 1)
+    from oracle.oracle import Oracle
+    O = Oracle()
+    threads = os.cpu_count() or 1
+    # each step: one full build (the reference builds one DAG per thread) plus
+    # one bounded lookup sample over all host cores
+    steps = max(1, min(args.steps, 5))
+    warm = min(args.warmup, 1)
+    sample = min(wl["queries"], 1 << 23)
+    for _ in range(warm):
+        O.build(depth, threads=4)
+    tb, tl = [], []
+    b = None
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        b = O.build(depth, threads=4)
+        tb.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        O.lookup_ndc(b.dag, b.num_levels, b.leafmasks, q[:sample], threads=threads)
+        tl.append(time.perf_counter() - t0)
+    build_s = statistics.mean(tb)
+    v = float(n) ** 3 / build_s / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "Gvoxel/s", "n_gpus": world,
+        "steps": steps, "warmup": warm, "ms_per_step": round(build_s * 1e3, 2), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded scene rasterised to a float32 depth map (no dataset involved)",
+        "config": {"workload": f"{args.config}: {wl['desc']}", "map_side": n, "dag_words": int(b.dag.size),
+                   "note": f"steps capped at {steps} (bounded CPU sample)"},
+        "cpu_baseline": {"value": round(v, 3), "unit": "Gvoxel/s", "cores": 4, "kind": "port",
+                         "sample": f"full {n}^2 build per step: pyramid on 4 threads, SVO/merge/compress on 1 thread "
+                                   f"(the reference's threading); hash-indexed first-occurrence merge"},
+        "e2e": {"value": round(v, 3), "unit": "Gvoxel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "lookup": {"value": round(sample / statistics.mean(tl) / 1e9, 4), "unit": "Glookups/s", "cores": threads,
+                   "sample": f"{sample} queries per step"},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--config", choices=tuple(WORKLOADS), default="c1")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        ap.error("--warmup must be at least 3")
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

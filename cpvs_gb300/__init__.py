@@ -23,6 +23,7 @@ LIB_PATH = os.path.join(HERE, "libcpvs_gb300.so")
 SHADOW, VISIBLE, PARTIAL = 0, 1, 2
 FLAG_LEAFMASKS = 0x1
 IO_DEVICE = 0x100
+FLAG_BORROW_INPUT = 0x200
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "device wait timed out",
           4: "CUDA device error", 5: "unimplemented", 6: "memory budget exceeded", 7: "cancelled",
@@ -120,6 +121,16 @@ def _is_device(a) -> bool:
     return not isinstance(a, np.ndarray) and getattr(a, "is_cuda", False)
 
 
+def _host_array(a, dtype):
+    """A C-contiguous host buffer for `a` without copying when it already is
+    one (numpy array or CPU tensor, pinned or not)."""
+    if isinstance(a, np.ndarray):
+        return np.ascontiguousarray(a, dtype)
+    if a.is_contiguous() and str(a.dtype).endswith(np.dtype(dtype).name):
+        return a  # torch CPU tensor: passed by its data pointer
+    return np.ascontiguousarray(a.numpy(), dtype)
+
+
 def _stream(stream) -> int:
     if stream is None:
         return 0
@@ -181,17 +192,23 @@ class MinMaxHierarchy:
     (src/MinMaxHierarchy.h:12-92).  `depth` is an (n, n) float32 numpy array
     or CUDA tensor."""
 
-    def __init__(self, depth, ctx: Optional[Context] = None, stream=None):
+    def __init__(self, depth, ctx: Optional[Context] = None, stream=None, borrow: bool = False):
+        """`borrow` (CUDA tensor input only): read the map in place instead of
+        copying it; the tensor is kept referenced for the hierarchy's life and
+        must not be modified meanwhile."""
         self.ctx = ctx or Context.default()
         n = int(depth.shape[0])
-        if depth.shape != (n, n):
+        if tuple(depth.shape) != (n, n):
             raise ValueError("depth map must be square")
         dev = _is_device(depth)
         if not dev:
-            depth = np.ascontiguousarray(depth, np.float32)
+            depth = _host_array(depth, np.float32)
+        elif not depth.is_contiguous():
+            raise ValueError("device depth map must be contiguous")
+        flags = (IO_DEVICE | (FLAG_BORROW_INPUT if borrow else 0)) if dev else 0
+        self._borrowed = depth if (dev and borrow) else None
         h = _vp()
-        _check(_lib.cpvs_hierarchy_create(self.ctx.handle, _ptr(depth), n, IO_DEVICE if dev else 0,
-                                          _stream(stream), C.byref(h)))
+        _check(_lib.cpvs_hierarchy_create(self.ctx.handle, _ptr(depth), n, flags, _stream(stream), C.byref(h)))
         self.handle = h.value
         self.n = n
         self._levels = {}
@@ -252,7 +269,7 @@ class CompressedShadow:
         n = int(depth.shape[0])
         dev = _is_device(depth)
         if not dev:
-            depth = np.ascontiguousarray(depth, np.float32)
+            depth = _host_array(depth, np.float32)
         flags = (FLAG_LEAFMASKS if leafmasks else 0) | (IO_DEVICE if dev else 0)
         h = _vp()
         _check(_lib.cpvs_shadow_create_from_depth(ctx.handle, _ptr(depth), n, z_tile_index, z_tile_num, flags,
@@ -314,6 +331,16 @@ class CompressedShadow:
         words = np.zeros(max((n + 31) // 32, 1), np.uint32)
         _check(fn(self.handle, pts.ctypes.data, n, words.ctypes.data, 0, _stream(stream)))
         return unpack_bits(words, n)
+
+    def lookup_ndc_packed(self, points, words_out, stream=None):
+        """Host-buffer lookup: (n, 3) float32 host points (numpy or CPU
+        tensor, pinned for asynchronous copies) -> bit-packed words written to
+        the host buffer `words_out` (ceil(n/32) 32-bit words).  The copies in
+        and out happen inside the call."""
+        n = int(points.shape[0])
+        pts = _host_array(points, np.float32)
+        _check(_lib.cpvs_shadow_lookup_ndc(self.handle, _ptr(pts), n, _ptr(words_out), 0, _stream(stream)))
+        return words_out
 
     def traverse(self, position, try_leafmasks: bool = True) -> int:
         """CompressedShadow::traverse(ndc, tryLeafmasks) for one point (a

@@ -547,8 +547,15 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
     BoundJob* bj_dev = nullptr;
     std::vector<BoundJob> bj(njobs);
     for (uint32_t j = 0; j < njobs; ++j) bj[j] = BoundJob{jobs[j].z_idx, jobs[j].z_num, j};
-    CPVS_CUDA(cudaMallocAsync((void**)&bounds_dev, bounds_bytes, st));
-    CPVS_CUDA(cudaMallocAsync((void**)&bj_dev, njobs * sizeof(BoundJob), st));
+    {
+        cpvs_status r = ctx.alloc((void**)&bounds_dev, bounds_bytes, false, st);
+        if (r != CPVS_OK) return r;
+        r = ctx.alloc((void**)&bj_dev, njobs * sizeof(BoundJob), false, st);
+        if (r != CPVS_OK) {
+            ctx.release(bounds_dev, bounds_bytes, false, st);
+            return r;
+        }
+    }
     CPVS_CUDA(cudaMemsetAsync(bounds_dev, 0, bounds_bytes, st));
     {
         // jobs grouped by source (jobs of one source need not be adjacent)
@@ -572,8 +579,8 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
     std::vector<unsigned long long> bounds((size_t)njobs * CPVS_MAX_LEVELS);
     CPVS_CUDA(cudaMemcpyAsync(bounds.data(), bounds_dev, bounds_bytes, cudaMemcpyDeviceToHost, st));
     CPVS_CUDA(cudaStreamSynchronize(st));
-    cudaFreeAsync(bounds_dev, st);
-    cudaFreeAsync(bj_dev, st);
+    ctx.release(bounds_dev, bounds_bytes, false, st);
+    ctx.release(bj_dev, njobs * sizeof(BoundJob), false, st);
 
     // capacity per level: bounded children + roots entering there
     std::vector<uint64_t> cap(CPVS_MAX_LEVELS, 0), ninj(CPVS_MAX_LEVELS, 0);

@@ -28,8 +28,8 @@ cpvs_status Ctx::alloc(void** p, uint64_t bytes, bool persistent, cudaStream_t s
     *p = nullptr;
     if (budget && in_use + scratch + bytes > budget)
         return fail(CPVS_ERR_BUDGET, "allocation of " + std::to_string(bytes) + " bytes exceeds the context budget");
-    cudaError_t e = persistent ? cudaMalloc(p, bytes) : cudaMallocAsync(p, bytes, st);
-    if (e != cudaSuccess) return cuda_fail(e, persistent ? "cudaMalloc" : "cudaMallocAsync");
+    cudaError_t e = cudaMallocFromPoolAsync(p, bytes, pool, st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocFromPoolAsync");
     if (persistent)
         in_use += bytes;
     else
@@ -37,9 +37,12 @@ cpvs_status Ctx::alloc(void** p, uint64_t bytes, bool persistent, cudaStream_t s
     return CPVS_OK;
 }
 
-void Ctx::release(void* p, uint64_t bytes, bool persistent, cudaStream_t st) {
+void Ctx::release(void* p, uint64_t bytes, bool persistent, cudaStream_t st, cudaEvent_t last_use) {
     if (persistent) {
-        if (p) cudaFree(p);
+        if (p) {
+            if (last_use) cudaStreamWaitEvent(free_stream, last_use, 0);
+            cudaFreeAsync(p, free_stream);
+        }
         in_use -= std::min(in_use, bytes);
     } else {
         if (p) cudaFreeAsync(p, st);
@@ -55,15 +58,27 @@ struct cpvs_ctx {
     cpvs::Ctx c;
 };
 
-struct cpvs_hierarchy {
+// Every object with device memory records `last_use` on the stream of each
+// call that enqueues work on it; its memory is freed after that event.
+struct DeviceObject {
+    cudaEvent_t last_use = nullptr;
+    DeviceObject() { cudaEventCreateWithFlags(&last_use, cudaEventDisableTiming); }
+    ~DeviceObject() {
+        if (last_use) cudaEventDestroy(last_use);
+    }
+    void touch(cudaStream_t st) const { cudaEventRecord(last_use, st); }
+};
+
+struct cpvs_hierarchy : DeviceObject {
     cpvs_ctx* ctx = nullptr;
     uint32_t n = 0;
     float* depth = nullptr;    // device n*n
+    bool owns_depth = true;    // false when borrowed from the caller
     float2* levels = nullptr;  // device pyramid
     uint64_t bytes = 0;
 };
 
-struct cpvs_shadow {
+struct cpvs_shadow : DeviceObject {
     cpvs_ctx* ctx = nullptr;
     uint32_t* dag = nullptr;
     uint64_t words = 0;
@@ -74,7 +89,7 @@ struct cpvs_shadow {
     std::vector<uint64_t> tree, uniq;
 };
 
-struct cpvs_grid {
+struct cpvs_grid : DeviceObject {
     cpvs_ctx* ctx = nullptr;
     uint32_t length = 0;
     std::vector<cpvs_shadow*> cells;
@@ -188,14 +203,38 @@ cpvs_status cpvs_ctx_create(int device, cpvs_ctx** out) {
     }
     if (device < 0 || device >= count) return fail(CPVS_ERR_INVALID_ARG, "ctx_create: bad device index");
     CPVS_CUDA(cudaSetDevice(device));
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    cudaMemPool_t pool = nullptr;
+    CPVS_CUDA(cudaMemPoolCreate(&pool, &props));
+    uint64_t keep = ~0ull;  // never hand freed blocks back to the driver
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    cudaStream_t fs = nullptr;
+    cudaError_t e2 = cudaStreamCreateWithFlags(&fs, cudaStreamNonBlocking);
+    if (e2 != cudaSuccess) {
+        cudaMemPoolDestroy(pool);
+        return cpvs::cuda_fail(e2, "cudaStreamCreateWithFlags");
+    }
     auto* c = new cpvs_ctx;
     c->c.device = device;
+    c->c.pool = pool;
+    c->c.free_stream = fs;
     cudaDeviceGetAttribute(&c->c.num_sms, cudaDevAttrMultiProcessorCount, device);
     *out = c;
     return CPVS_OK;
 }
 
-void cpvs_ctx_destroy(cpvs_ctx* ctx) { delete ctx; }
+// Objects created from the context must be destroyed first.
+void cpvs_ctx_destroy(cpvs_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->c.device);
+    cudaDeviceSynchronize();
+    cudaStreamDestroy(ctx->c.free_stream);
+    cudaMemPoolDestroy(ctx->c.pool);
+    delete ctx;
+}
 
 cpvs_status cpvs_ctx_set_budget(cpvs_ctx* ctx, uint64_t bytes) {
     if (!ctx) return fail(CPVS_ERR_INVALID_ARG, "null ctx");
@@ -244,18 +283,25 @@ cpvs_status cpvs_hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n,
     auto* h = new cpvs_hierarchy;
     h->ctx = ctx;
     h->n = n;
-    r = c.alloc((void**)&h->depth, dbytes, true, st);
+    const bool borrow = (flags & CPVS_IO_DEVICE) && (flags & CPVS_FLAG_BORROW_INPUT);
+    if (borrow) {
+        h->depth = const_cast<float*>(depth);
+        h->owns_depth = false;
+    } else {
+        r = c.alloc((void**)&h->depth, dbytes, true, st);
+        if (r == CPVS_OK) h->bytes += dbytes;
+    }
     if (r == CPVS_OK) {
-        h->bytes += dbytes;
         r = c.alloc((void**)&h->levels, lbytes, true, st);
         if (r == CPVS_OK) h->bytes += lbytes;
     }
-    if (r == CPVS_OK) {
+    if (r == CPVS_OK && !borrow) {
         cudaError_t e = cudaMemcpyAsync(h->depth, depth, dbytes,
                                         (flags & CPVS_IO_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) r = cpvs::cuda_fail(e, "hierarchy upload");
     }
     if (r == CPVS_OK) r = cpvs::launch_pyramid(h->depth, n, h->levels, st, &c.timing);
+    h->touch(st);
     if (r != CPVS_OK) {
         cpvs_hierarchy_destroy(h);
         return r;
@@ -268,8 +314,8 @@ void cpvs_hierarchy_destroy(cpvs_hierarchy* h) {
     if (!h) return;
     cpvs::Ctx& c = h->ctx->c;
     cudaSetDevice(c.device);
-    if (h->depth) c.release(h->depth, (uint64_t)h->n * h->n * 4, true, nullptr);
-    if (h->levels) c.release(h->levels, cpvs::pyramid_texels(h->n) * 8, true, nullptr);
+    if (h->depth && h->owns_depth) c.release(h->depth, (uint64_t)h->n * h->n * 4, true, nullptr, h->last_use);
+    if (h->levels) c.release(h->levels, cpvs::pyramid_texels(h->n) * 8, true, nullptr, h->last_use);
     delete h;
 }
 
@@ -288,6 +334,7 @@ cpvs_status cpvs_hierarchy_level(const cpvs_hierarchy* h, uint32_t level, float*
     cudaStream_t st = (cudaStream_t)stream;
     CPVS_CUDA(cudaMemcpyAsync(host_out, h->levels + cpvs::pyramid_level_offset(h->n, (int)level), 2 * s * s * 4,
                               cudaMemcpyDeviceToHost, st));
+    h->touch(st);
     CPVS_CUDA(cudaStreamSynchronize(st));
     return CPVS_OK;
 }
@@ -313,11 +360,16 @@ cpvs_status cpvs_shadow_create(cpvs_ctx* ctx, const cpvs_hierarchy* h, uint32_t 
     std::vector<cpvs::JobSpec> jobs{{0, z_tile_index, z_tile_num}};
     cpvs::BuildOutput bo;
     r = cpvs::build_dags(ctx->c, src, jobs, leaf, (cudaStream_t)stream, bo);
+    h->touch((cudaStream_t)stream);
     if (r != CPVS_OK) {
-        if (bo.dag) ctx->c.release(bo.dag, std::max<uint64_t>(bo.dag_words, 1) * 4, true, nullptr);
+        if (bo.dag) {
+            cudaStreamSynchronize((cudaStream_t)stream);
+            ctx->c.release(bo.dag, std::max<uint64_t>(bo.dag_words, 1) * 4, true, nullptr);
+        }
         return r;
     }
     auto* s = new cpvs_shadow;
+    s->touch((cudaStream_t)stream);
     s->ctx = ctx;
     s->dag = bo.dag;
     s->words = bo.dag_words;
@@ -336,11 +388,12 @@ cpvs_status cpvs_shadow_create_from_depth(cpvs_ctx* ctx, const float* depth, uin
     if (out) *out = nullptr;
     cpvs_status r = check_map_size(n, 8);
     if (r != CPVS_OK) return r;
+    // The temporary hierarchy is gone before this call returns, so a device
+    // map can be read in place.
     cpvs_hierarchy* h = nullptr;
-    r = cpvs_hierarchy_create(ctx, depth, n, flags, stream, &h);
+    r = cpvs_hierarchy_create(ctx, depth, n, flags | CPVS_FLAG_BORROW_INPUT, stream, &h);
     if (r != CPVS_OK) return r;
     r = cpvs_shadow_create(ctx, h, z_tile_index, z_tile_num, flags, stream, out);
-    cudaStreamSynchronize((cudaStream_t)stream);
     cpvs_hierarchy_destroy(h);
     return r;
 }
@@ -348,7 +401,7 @@ cpvs_status cpvs_shadow_create_from_depth(cpvs_ctx* ctx, const float* depth, uin
 void cpvs_shadow_destroy(cpvs_shadow* s) {
     if (!s) return;
     cudaSetDevice(s->ctx->c.device);
-    s->ctx->c.release(s->dag, s->bytes, true, nullptr);
+    s->ctx->c.release(s->dag, s->bytes, true, nullptr, s->last_use);
     delete s;
 }
 
@@ -375,6 +428,7 @@ cpvs_status cpvs_shadow_dag_words(const cpvs_shadow* s, uint32_t* host_out, uint
     if (r != CPVS_OK) return r;
     cudaStream_t st = (cudaStream_t)stream;
     CPVS_CUDA(cudaMemcpyAsync(host_out, s->dag, s->words * 4, cudaMemcpyDeviceToHost, st));
+    s->touch(st);
     CPVS_CUDA(cudaStreamSynchronize(st));
     return CPVS_OK;
 }
@@ -394,7 +448,10 @@ cpvs_status cpvs_shadow_lookup_ndc(const cpvs_shadow* s, const float* xyz, uint6
     if (!s) return fail(CPVS_ERR_INVALID_ARG, "lookup_ndc: null shadow");
     cudaStream_t st = (cudaStream_t)stream;
     return lookup_common(s->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
-        return cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, q, true, n, bits, st, &s->ctx->c.timing);
+        cpvs_status r = cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, q, true, n, bits, st,
+                                            &s->ctx->c.timing);
+        s->touch(st);
+        return r;
     });
 }
 
@@ -403,7 +460,10 @@ cpvs_status cpvs_shadow_lookup_voxel(const cpvs_shadow* s, const int32_t* xyz, u
     if (!s) return fail(CPVS_ERR_INVALID_ARG, "lookup_voxel: null shadow");
     cudaStream_t st = (cudaStream_t)stream;
     return lookup_common(s->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
-        return cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, q, false, n, bits, st, &s->ctx->c.timing);
+        cpvs_status r = cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, q, false, n, bits, st,
+                                            &s->ctx->c.timing);
+        s->touch(st);
+        return r;
     });
 }
 
@@ -422,8 +482,8 @@ cpvs_status cpvs_grid_create(cpvs_ctx* ctx, uint32_t length, cpvs_grid** out) {
 
 static void grid_release_device(cpvs_grid* g) {
     cpvs::Ctx& c = g->ctx->c;
-    if (g->dag) c.release(g->dag, std::max<uint64_t>(g->words, 1) * 4, true, nullptr);
-    if (g->cell_words) c.release(g->cell_words, g->cells.size() * 4, true, nullptr);
+    if (g->dag) c.release(g->dag, std::max<uint64_t>(g->words, 1) * 4, true, nullptr, g->last_use);
+    if (g->cell_words) c.release(g->cell_words, g->cells.size() * 4, true, nullptr, g->last_use);
     g->dag = nullptr;
     g->cell_words = nullptr;
     g->finalized = false;
@@ -494,9 +554,11 @@ cpvs_status cpvs_grid_finalize(cpvs_grid* g, int release_cells, void* stream) {
     uint64_t off = 0;
     for (const cpvs_shadow* s : g->cells) {
         CPVS_CUDA(cudaMemcpyAsync(g->dag + off, s->dag, s->words * 4, cudaMemcpyDeviceToDevice, st));
+        s->touch(st);
         off += s->words;
     }
     CPVS_CUDA(cudaMemcpyAsync(g->cell_words, cellw.data(), cellw.size() * 4, cudaMemcpyHostToDevice, st));
+    g->touch(st);
     CPVS_CUDA(cudaStreamSynchronize(st));
     g->words = total;
     g->dag_levels = nl;
@@ -527,6 +589,7 @@ cpvs_status cpvs_grid_words(const cpvs_grid* g, uint32_t* dag_out, uint64_t dag_
         if (cells_capacity < g->cells.size()) return fail(CPVS_ERR_CAPACITY, "grid_words: cell buffer too small");
         CPVS_CUDA(cudaMemcpyAsync(cells_out, g->cell_words, g->cells.size() * 4, cudaMemcpyDeviceToHost, st));
     }
+    g->touch(st);
     CPVS_CUDA(cudaStreamSynchronize(st));
     return CPVS_OK;
 }
@@ -536,8 +599,11 @@ cpvs_status cpvs_grid_lookup_ndc(const cpvs_grid* g, const float* xyz, uint64_t 
     if (!g || !g->finalized) return fail(CPVS_ERR_INVALID_ARG, "grid_lookup_ndc: grid not finalized");
     cudaStream_t st = (cudaStream_t)stream;
     return lookup_common(g->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
-        return cpvs::launch_grid_lookup(g->dag, g->words, g->cell_words, g->length, g->dag_levels, g->leafmasks,
-                                        static_cast<const float*>(q), n, bits, st, &g->ctx->c.timing);
+        cpvs_status r = cpvs::launch_grid_lookup(g->dag, g->words, g->cell_words, g->length, g->dag_levels,
+                                                 g->leafmasks, static_cast<const float*>(q), n, bits, st,
+                                                 &g->ctx->c.timing);
+        g->touch(st);
+        return r;
     });
 }
 

@@ -146,10 +146,16 @@ struct Ctx {
     uint64_t budget = 0;   // 0 = unlimited
     uint64_t in_use = 0;   // persistent bytes (hierarchies, DAGs, grids)
     uint64_t scratch = 0;  // stream-ordered build / staging scratch
-    // Device allocation with budget accounting: persistent blocks come from
-    // cudaMalloc, scratch from the stream-ordered pool on `st`.
+    // All device memory comes from this context's stream-ordered pool, which
+    // keeps freed blocks for reuse (no cudaMalloc / cudaFree in steady state).
+    cudaMemPool_t pool = nullptr;
+    // Stream on which persistent blocks are freed, after their last use.
+    cudaStream_t free_stream = nullptr;
+    // Allocation on stream `st`, with budget accounting.
     cpvs_status alloc(void** p, uint64_t bytes, bool persistent, cudaStream_t st);
-    void release(void* p, uint64_t bytes, bool persistent, cudaStream_t st);
+    // Scratch: freed in the order of `st`.  Persistent: freed once
+    // `last_use` (the last event recorded after work on the block) is reached.
+    void release(void* p, uint64_t bytes, bool persistent, cudaStream_t st, cudaEvent_t last_use = nullptr);
 };
 
 }  // namespace cpvs

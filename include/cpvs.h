@@ -62,6 +62,10 @@ typedef enum cpvs_visibility {
                                         src/CompressedShadow.cpp:16-27); used only
                                         when numLevels-3 >= 2, as there */
 #define CPVS_IO_DEVICE 0x100u        /* input/output pointers are device memory */
+#define CPVS_FLAG_BORROW_INPUT 0x200u  /* with CPVS_IO_DEVICE: a hierarchy reads the
+                                          caller's depth map in place instead of
+                                          copying it; the caller keeps it alive and
+                                          unchanged until the hierarchy is destroyed */
 
 typedef struct cpvs_ctx cpvs_ctx;
 typedef struct cpvs_hierarchy cpvs_hierarchy;
