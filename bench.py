@@ -167,6 +167,18 @@ def run_ours(args, rank, world, local_rank):
             torch.distributed.barrier()
         torch.cuda.synchronize(dev)
 
+    if args.part != "all":
+        # profiling aid: the build steps or the lookup batches alone
+        sh = build_step()
+        for _ in range(args.warmup + args.steps):
+            if args.part == "build":
+                build_step()
+            else:
+                sh.lookup_ndc(q_dev, bits_dev, stream=stream)
+        torch.cuda.synchronize(dev)
+        print(json.dumps({"part": args.part, "steps": args.warmup + args.steps}), flush=True)
+        return
+
     clocks = ClockSampler(local_rank)
     clocks.start()
     for _ in range(args.warmup):
@@ -377,6 +389,8 @@ def main():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--config", choices=tuple(WORKLOADS), default="c1")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--part", choices=("all", "build", "lookup"), default="all",
+                    help="profiling aid: run only the build steps or only the lookup batches (no JSON line)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         ap.error("--warmup must be at least 3")

@@ -228,58 +228,99 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // Leaf level (level 2 with leafmasks): createChildmask1x1x8 + createLeafmask
-// (src/CompressedShadowUtil.cpp:59-99).  One warp per leaf: lane l holds the
-// voxel columns (x,y) = (l&7, l>>3) and (l&7, 4+(l>>3)) of the 8x8 footprint,
-// so slice s's 64-bit mask is ballot(lit(row<4)) | ballot(lit(row>=4)) << 32,
-// bit x+8y exactly as the reference.  Also the leaf's mask, signature hash
-// and job-range bookkeeping.
+// (src/CompressedShadowUtil.cpp:59-99).  The leaf at level-2 coordinate c
+// covers voxels x in [4c.x, 4c.x+8), y likewise, z in [bz, bz+8) with
+// bz = 4c.z; slice s gets bit x+8y when the voxel centre lies at or above the
+// depth: mid(bz+s) <= d*H0, with mid(z) = (z + (z+1)) * 0.5 in float32
+// (cs::absoluteVisible).  For z < 2^23 that midpoint is exactly z + 0.5, so
+// a texel is lit in the slices s < k, k = clamp(Z - bz + 1, 0, 8), where
+// Z = floor(d*H0 - 0.5) is the highest lit voxel of that texel column: the
+// same comparisons the reference makes, taken eight at a time.
+//
+// One thread per leaf: 16 independent 16-byte loads cover the 8x8 depth
+// footprint; the four bits of each texel's k are packed into four 64-bit
+// planes, from which the eight slice masks follow by bit logic
+// (slice s = {t : k_t > s}).
+__device__ __forceinline__ uint32_t lit_count(float d_scaled, int32_t bz) {
+    // Z = floor(x - 0.5) for x = d*H0, as floor(x) - (frac(x) < 0.5); x is
+    // clamped to +-2^30 first (NaN lands on -2^30: never lit, as
+    // mid <= NaN is false).
+    const float x = fminf(fmaxf(d_scaled, -1073741824.0f), 1073741824.0f);
+    const float f = floorf(x);
+    const int32_t z = (int32_t)f - ((x - f) < 0.5f ? 1 : 0);
+    const int32_t k = z - bz + 1;
+    return (uint32_t)(k < 0 ? 0 : (k > 8 ? 8 : k));
+}
+
 __global__ void __launch_bounds__(kThreads)
     k_leaf_masks(LevelDev lv, const uint32_t* __restrict__ counts, const JobDev* __restrict__ jobs, uint32_t njobs,
                  int L, SegDev seg, uint32_t* err) {
     const uint32_t n = counts[L];
-    const int lane = threadIdx.x & 31;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nw) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint64_t c = lv.coord[i];
         const uint32_t j = lv.job[i];
         const uint32_t bx = unpack_x(c) * 4u, by = unpack_y(c) * 4u, bz = unpack_z(c) * 4u;
-        if (j >= njobs || bx + 8u > jobs[j].n || by + 8u > jobs[j].n) {
+        if (j >= njobs || bx + 8u > __ldg(&jobs[j].n) || by + 8u > __ldg(&jobs[j].n)) {
             // stale slot (an internal check already failed): inert leaf
-            if (lane < 8) lv.slices[(size_t)i * 8 + lane] = 0;
-            if (lane == 0) {
-                atomicOr(err, 4u);
-                lv.mask[i] = 0;
-                lv.job[i] = 0;
-                lv.hash[i] = 0;
-            }
+            ulonglong2* o = reinterpret_cast<ulonglong2*>(lv.slices + (size_t)i * 8);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) o[q] = make_ulonglong2(0ull, 0ull);
+            atomicOr(err, 4u);
+            lv.mask[i] = 0;
+            lv.job[i] = 0;
+            lv.hash[i] = 0;
             continue;
         }
-        const JobDev J = jobs[j];
-        const float H = __uint2float_rn(J.n * J.z_num);
-        const uint32_t col = bx + (uint32_t)(lane & 7), row = by + (uint32_t)(lane >> 3);
-        const float d0 = __fmul_rn(J.depth[(size_t)row * J.n + col], H);
-        const float d1 = __fmul_rn(J.depth[(size_t)(row + 4) * J.n + col], H);
-        uint64_t mine = 0;
+        const uint32_t nmap = __ldg(&jobs[j].n);
+        const float H = __uint2float_rn(nmap * __ldg(&jobs[j].z_num));
+        const float* row0 = jobs[j].depth + (size_t)by * nmap + bx;
+        float4 a[8], b[8];
 #pragma unroll
-        for (uint32_t s = 0; s < 8; ++s) {
-            const uint32_t lo = __ballot_sync(0xffffffffu, voxel_lit(bz + s, d0));
-            const uint32_t hi = __ballot_sync(0xffffffffu, voxel_lit(bz + s, d1));
-            if ((uint32_t)lane == s) mine = (uint64_t)lo | ((uint64_t)hi << 32);
+        for (int y = 0; y < 8; ++y) {
+            a[y] = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap));
+            b[y] = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap + 4));
         }
-        const bool full = mine == ~0ull, empty = mine == 0ull;
-        const uint32_t vis = __ballot_sync(0xffffffffu, lane < 8 && full) & 0xFFu;
-        const uint32_t part = __ballot_sync(0xffffffffu, lane < 8 && !full && !empty) & 0xFFu;
-        const uint32_t mask = spread8(vis) | (spread8(part) << 1);
-        uint64_t h = (lane < 8) ? fmix64(mine + (uint64_t)(lane + 1) * kGolden) : 0ull;
+        uint32_t p0[2] = {0u, 0u}, p1[2] = {0u, 0u}, p2[2] = {0u, 0u}, p3[2] = {0u, 0u};
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) h ^= __shfl_xor_sync(0xffffffffu, h, o);
-        if (lane < 8) lv.slices[(size_t)i * 8 + lane] = mine;
-        if (lane == 0) {
-            lv.mask[i] = mask;
-            lv.hash[i] = fmix64(h ^ ((uint64_t)(j + 1) * kGolden));
-            if (i == 0 || lv.job[i - 1] != j) seg.nstart[seg_index(j, L)] = i;
-            if (i == n - 1 || lv.job[i + 1] != j) seg.nend[seg_index(j, L)] = i + 1;
+        for (int y = 0; y < 8; ++y) {
+            const float v[8] = {a[y].x, a[y].y, a[y].z, a[y].w, b[y].x, b[y].y, b[y].z, b[y].w};
+#pragma unroll
+            for (int x = 0; x < 8; ++x) {
+                const uint32_t k = lit_count(__fmul_rn(v[x], H), (int32_t)bz);
+                const int t = 8 * y + x, w = t >> 5, sh = t & 31;
+                p0[w] |= (k & 1u) << sh;
+                p1[w] |= ((k >> 1) & 1u) << sh;
+                p2[w] |= ((k >> 2) & 1u) << sh;
+                p3[w] |= ((k >> 3) & 1u) << sh;
+            }
         }
+        const uint64_t P0 = p0[0] | ((uint64_t)p0[1] << 32), P1 = p1[0] | ((uint64_t)p1[1] << 32);
+        const uint64_t P2 = p2[0] | ((uint64_t)p2[1] << 32), P3 = p3[0] | ((uint64_t)p3[1] << 32);
+        // slice s = {t : k_t >= s+1}, k_t in [0, 8]
+        uint64_t M[8];
+        M[0] = P0 | P1 | P2 | P3;
+        M[1] = P1 | P2 | P3;
+        M[2] = P3 | P2 | (P1 & P0);
+        M[3] = P3 | P2;
+        M[4] = P3 | (P2 & (P1 | P0));
+        M[5] = P3 | (P2 & P1);
+        M[6] = P3 | (P2 & P1 & P0);
+        M[7] = P3;
+        uint32_t mask = 0;
+        uint64_t hx = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const uint32_t cls = (M[q] == ~0ull) ? kVisible : (M[q] == 0ull ? kShadow : kPartial);
+            mask |= cls << (2 * q);
+            hx ^= fmix64(M[q] + (uint64_t)(q + 1) * kGolden);
+        }
+        ulonglong2* o = reinterpret_cast<ulonglong2*>(lv.slices + (size_t)i * 8);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) o[q] = make_ulonglong2(M[2 * q], M[2 * q + 1]);
+        lv.mask[i] = mask;
+        lv.hash[i] = fmix64(hx ^ ((uint64_t)(j + 1) * kGolden));
+        if (i == 0 || lv.job[i - 1] != j) seg.nstart[seg_index(j, L)] = i;
+        if (i == n - 1 || lv.job[i + 1] != j) seg.nend[seg_index(j, L)] = i + 1;
     }
 }
 
@@ -340,7 +381,9 @@ __global__ void __launch_bounds__(kThreads)
                 cur_e = prev;
             }
             if ((cur_e >> 32) == (key >> 32) && same_node<LEAF>(cur, child, i, (uint32_t)cur_e)) {
-                atomicMin(&table[s], key);
+                // the slot only ever decreases: nothing to do when it already
+                // holds an earlier occurrence
+                if ((uint32_t)cur_e > i) atomicMin(&table[s], key);
                 break;
             }
             s = (s + 1) & cap_mask;
@@ -686,7 +729,8 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
     CPVS_CUDA(cudaMemcpyAsync(inj_dev, inj.data(), inj.size() * sizeof(Injected), cudaMemcpyHostToDevice, st));
     CPVS_CUDA(cudaMemcpyAsync(root_dev, root_level.data(), njobs * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
 
-    // top level: its roots only
+    // top level: its roots only (pageable copies are staged before the call
+    // returns, so the host vectors may go out of scope)
     {
         const uint32_t c = (uint32_t)ninj[maxR];
         std::vector<uint64_t> coords(c);
@@ -698,7 +742,6 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         CPVS_CUDA(cudaMemcpyAsync(lv[maxR].coord, coords.data(), c * 8, cudaMemcpyHostToDevice, st));
         CPVS_CUDA(cudaMemcpyAsync(lv[maxR].job, js.data(), c * 4, cudaMemcpyHostToDevice, st));
         CPVS_CUDA(cudaMemcpyAsync(counts + maxR, &c, 4, cudaMemcpyHostToDevice, st));
-        CPVS_CUDA(cudaStreamSynchronize(st));  // `c` and the vectors leave scope
     }
 
     // ---- top-down
@@ -712,7 +755,7 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
     }
     if (leafmasks) {
         KernelTimer kt(tm, K_LEAF_MASKS, st);
-        k_leaf_masks<<<grid_for(cap[2] * 32, kThreads), kThreads, 0, st>>>(lv[2], counts, jobs_dev, njobs, 2, seg, err);
+        k_leaf_masks<<<grid_for(cap[2], kThreads), kThreads, 0, st>>>(lv[2], counts, jobs_dev, njobs, 2, seg, err);
     } else {
         KernelTimer kt(tm, K_CLASSIFY_BOTTOM, st);
         k_classify_bottom<<<grid_for(cap[0], kThreads), kThreads, 0, st>>>(lv[0], counts, jobs_dev, njobs, 0, seg, err);

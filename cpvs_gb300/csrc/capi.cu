@@ -348,10 +348,11 @@ cpvs_status cpvs_shadow_create(cpvs_ctx* ctx, const cpvs_hierarchy* h, uint32_t 
     if (r0 != CPVS_OK) return r0;
     if (z_tile_num == 0 || z_tile_index >= z_tile_num)
         return fail(CPVS_ERR_INVALID_ARG, "shadow_create: need z_tile_index < z_tile_num");
-    // every z-cell index must be exact in float32, as the classification
-    // converts it (src/CompressedShadowUtil.cpp:36-40)
-    if ((uint64_t)h->n * z_tile_num > (1ull << 24))
-        return fail(CPVS_ERR_INVALID_ARG, "shadow_create: n * z_tile_num must not exceed 2^24");
+    // every voxel's z and its centre z+0.5 must be exact in float32, as the
+    // classification computes them (src/CompressedShadowUtil.cpp:36-40,
+    // src/CompressedShadowUtil.h:51-57)
+    if ((uint64_t)h->n * z_tile_num > (1ull << 23))
+        return fail(CPVS_ERR_INVALID_ARG, "shadow_create: n * z_tile_num must not exceed 2^23");
     cpvs_status r = set_device(ctx);
     if (r != CPVS_OK) return r;
     const uint32_t nl = (uint32_t)cpvs::log2_u32(h->n) + 1;
