@@ -75,6 +75,7 @@ _SIGS = {
     "cpvs_grid_dag_size": (_u64, [_vp]),
     "cpvs_grid_words": (C.c_int, [_vp, _vp, _u64, _vp, _u64, _vp]),
     "cpvs_grid_lookup_ndc": (C.c_int, [_vp, _vp, _u64, _vp, _u32, _vp]),
+    "cpvs_shadow_build_noalloc": (C.c_int, [_vp, _u32, _u32, _u32, _u32, _vp, _u64, C.POINTER(_u64), _vp]),
 }
 
 _lib: Optional[C.CDLL] = None

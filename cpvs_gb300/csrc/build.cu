@@ -35,6 +35,7 @@
 // another, so nothing can hang.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "common.cuh"
@@ -857,3 +858,202 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
 }
 
 }  // namespace cpvs
+
+// ---------------------------------------------------------------------------
+// Allocation-free build for small maps.
+//
+// Some callers may not allocate device memory at all: a render loop that must
+// not stall on cudaMalloc / cudaFree (both can synchronise the device and take
+// unpredictable time), or a plugin running inside a host application that
+// owns and pre-reserves all GPU memory.  For them, cpvs_shadow_build_noalloc
+// builds a DAG with every scratch buffer (pyramid, per-level node arrays,
+// hash table) carved out of the fixed array below, which each GPU that loads
+// this library keeps until the process exits.  It runs the same kernels as
+// build_dags; the caller passes the depth map and the output buffer.
+// ---------------------------------------------------------------------------
+namespace cpvs {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;  // 8 MiB per device
+constexpr uint32_t kNoAllocMaxSide = 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of g_noalloc_scratch on each device (host code cannot use
+// the symbol itself as a device pointer).  Looked up on a device's first call.
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[256] = {nullptr};
+
+cpvs_status noalloc_scratch_address(void** out) {
+    int dev = 0;
+    CPVS_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return fail(CPVS_ERR_DEVICE, "noalloc: device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return CPVS_OK;
+}
+
+}  // namespace
+}  // namespace cpvs
+
+extern "C" CPVS_API cpvs_status cpvs_shadow_build_noalloc(const float* depth, uint32_t n, uint32_t z_tile_index,
+                                                          uint32_t z_tile_num, uint32_t flags, uint32_t* dag_out,
+                                                          uint64_t dag_capacity, uint64_t* dag_words,
+                                                          void* stream) {
+    using namespace cpvs;
+    if (dag_words) *dag_words = 0;
+    if (!depth) return fail(CPVS_ERR_INVALID_ARG, "noalloc: null depth map");
+    if (n < 8 || n > kNoAllocMaxSide || (n & (n - 1)))
+        return fail(CPVS_ERR_INVALID_ARG, "noalloc: map side must be a power of two in [8, " +
+                                              std::to_string(kNoAllocMaxSide) + "], got " + std::to_string(n) +
+                                              " (larger maps: cpvs_shadow_create_from_depth)");
+    if (z_tile_num == 0 || z_tile_index >= z_tile_num)
+        return fail(CPVS_ERR_INVALID_ARG, "noalloc: need z_tile_index < z_tile_num");
+    if ((uint64_t)n * z_tile_num > (1ull << 23))
+        return fail(CPVS_ERR_INVALID_ARG, "noalloc: n * z_tile_num must not exceed 2^23");
+    cudaStream_t st = (cudaStream_t)stream;
+    const int nl = log2_u32(n) + 1, R = nl - 2;
+    const bool leafmasks = (flags & CPVS_FLAG_LEAFMASKS) && (nl - 3 >= 2);
+    const int bottom = leafmasks ? 2 : 0;
+
+    // full-octree capacity of every level: 8^(R-L) nodes
+    uint64_t cap[CPVS_MAX_LEVELS] = {0};
+    uint64_t maxcap = 1;
+    for (int L = bottom; L <= R; ++L) {
+        cap[L] = 1ull << (3 * (R - L));
+        maxcap = std::max(maxcap, cap[L]);
+    }
+    uint64_t tcap = 1024;
+    while (tcap < 2 * maxcap) tcap <<= 1;
+    int dev = 0, sms = 0;
+    CPVS_CUDA(cudaGetDevice(&dev));
+    CPVS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const uint32_t max_grid = (uint32_t)std::max(sms, 1) * 8;
+    auto grid_for = [&](uint64_t items, uint64_t per_block) -> uint32_t {
+        uint64_t g = (items + per_block - 1) / per_block;
+        return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, max_grid));
+    };
+
+    // carve the scratch
+    void* base = nullptr;
+    cpvs_status r = noalloc_scratch_address(&base);
+    if (r != CPVS_OK) return r;
+    Arena A;
+    A.base = static_cast<char*>(base);
+    A.size = kNoAllocScratchBytes;
+    float2* pyr = A.take<float2>(pyramid_texels(n));
+    LevelDev lv[CPVS_MAX_LEVELS];
+    std::memset(lv, 0, sizeof(lv));
+    for (int L = bottom; L <= R; ++L) {
+        const uint64_t c = cap[L];
+        lv[L].coord = A.take<uint64_t>(c);
+        lv[L].job = A.take<uint32_t>(c);
+        lv[L].mask = A.take<uint32_t>(c);
+        lv[L].first = A.take<uint32_t>(c);
+        lv[L].uid = A.take<uint32_t>(c);
+        lv[L].slot = A.take<uint32_t>(c);
+        lv[L].uniq = A.take<uint32_t>(c);
+        lv[L].woff = A.take<uint32_t>(c);
+        if (leafmasks && L == 2) {
+            lv[L].slices = A.take<uint64_t>(c * 8);
+            lv[L].hash = A.take<uint64_t>(c);
+        }
+    }
+    unsigned long long* table = A.take<unsigned long long>(tcap);
+    uint2* partials = A.take<uint2>(max_grid);
+    uint32_t* counts = A.take<uint32_t>(CPVS_MAX_LEVELS);
+    uint32_t* level_u = A.take<uint32_t>(2 * CPVS_MAX_LEVELS);
+    uint32_t* err = A.take<uint32_t>(1);
+    const size_t segn = CPVS_MAX_LEVELS;
+    uint32_t* segbuf = A.take<uint32_t>(segn * 7);
+    uint64_t* job_off = A.take<uint64_t>(2);
+    uint32_t* root_dev = A.take<uint32_t>(1);
+    JobDev* job_dev = A.take<JobDev>(1);
+    if (A.used > A.size)
+        return fail(CPVS_ERR_INVALID_ARG, "noalloc: this map needs " + std::to_string(A.used) +
+                                              " scratch bytes, above the fixed " +
+                                              std::to_string(kNoAllocScratchBytes) + " (use leafmasks or a smaller map)");
+    SegDev seg{segbuf, segbuf + segn, segbuf + 2 * segn, segbuf + 3 * segn, segbuf + 4 * segn, segbuf + 5 * segn};
+    JobLayout lay{job_off, segbuf + 6 * segn};
+
+    // the array keeps the previous call's contents: reset what starts at zero
+    CPVS_CUDA(cudaMemsetAsync(segbuf, 0, segn * 7 * sizeof(uint32_t), st));
+    CPVS_CUDA(cudaMemsetAsync(counts, 0, CPVS_MAX_LEVELS * sizeof(uint32_t), st));
+    CPVS_CUDA(cudaMemsetAsync(level_u, 0, 2 * CPVS_MAX_LEVELS * sizeof(uint32_t), st));
+    CPVS_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
+    r = launch_pyramid(depth, n, pyr, st);
+    if (r != CPVS_OK) return r;
+    const JobDev jd{pyr, depth, n, (uint32_t)nl, z_tile_index, z_tile_num};
+    const uint32_t root = (uint32_t)R, one = 1;
+    const uint64_t root_coord = pack_xyz(0, 0, 2 * z_tile_index);
+    const uint32_t zero = 0;
+    CPVS_CUDA(cudaMemcpyAsync(job_dev, &jd, sizeof(jd), cudaMemcpyHostToDevice, st));
+    CPVS_CUDA(cudaMemcpyAsync(root_dev, &root, 4, cudaMemcpyHostToDevice, st));
+    CPVS_CUDA(cudaMemcpyAsync(lv[R].coord, &root_coord, 8, cudaMemcpyHostToDevice, st));
+    CPVS_CUDA(cudaMemcpyAsync(lv[R].job, &zero, 4, cudaMemcpyHostToDevice, st));
+    CPVS_CUDA(cudaMemcpyAsync(counts + R, &one, 4, cudaMemcpyHostToDevice, st));
+
+    for (int L = R; L > bottom; --L) {
+        const uint32_t g = grid_for(cap[L], kThreads * 4);
+        k_expand_count<<<g, kThreads, 0, st>>>(lv[L], counts, job_dev, 1, L, partials, err);
+        k_expand_write<<<g, kThreads, 0, st>>>(lv[L], lv[L - 1], counts, L, partials, nullptr, 0, seg,
+                                               (uint32_t)cap[L - 1], err);
+    }
+    if (leafmasks)
+        k_leaf_masks<<<grid_for(cap[2], kThreads), kThreads, 0, st>>>(lv[2], counts, job_dev, 1, 2, seg, err);
+    else
+        k_classify_bottom<<<grid_for(cap[0], kThreads), kThreads, 0, st>>>(lv[0], counts, job_dev, 1, 0, seg, err);
+    for (int L = bottom; L <= R; ++L) {
+        uint64_t tc = 1024;
+        while (tc < 2 * cap[L]) tc <<= 1;
+        const bool leaf = leafmasks && L == 2;
+        const uint32_t gs = grid_for(cap[L], kThreads * 4), gi = grid_for(cap[L], kThreads);
+        const LevelDev child = (L > bottom) ? lv[L - 1] : lv[L];
+        CPVS_CUDA(cudaMemsetAsync(table, 0xFF, tc * sizeof(unsigned long long), st));
+        if (leaf) {
+            k_dedup_insert<true><<<gi, kThreads, 0, st>>>(lv[L], child, counts, L, table, tc - 1);
+            k_dedup_resolve<true><<<gs, kThreads, 0, st>>>(lv[L], counts, L, table, partials);
+            k_dedup_scan<true><<<gs, kThreads, 0, st>>>(lv[L], counts, level_u, L, table, partials, seg);
+        } else {
+            k_dedup_insert<false><<<gi, kThreads, 0, st>>>(lv[L], child, counts, L, table, tc - 1);
+            k_dedup_resolve<false><<<gs, kThreads, 0, st>>>(lv[L], counts, L, table, partials);
+            k_dedup_scan<false><<<gs, kThreads, 0, st>>>(lv[L], counts, level_u, L, table, partials, seg);
+        }
+        k_dedup_remap<<<gi, kThreads, 0, st>>>(lv[L], counts, L, table);
+    }
+    k_layout<<<1, 1024, 0, st>>>(seg, lay, root_dev, 1, bottom);
+    CPVS_CUDA(cudaGetLastError());
+    uint64_t hoff[2] = {0, 0};
+    uint32_t hlu[2 * CPVS_MAX_LEVELS] = {0};
+    uint32_t herr = 0;
+    CPVS_CUDA(cudaMemcpyAsync(hoff, job_off, sizeof(hoff), cudaMemcpyDeviceToHost, st));
+    CPVS_CUDA(cudaMemcpyAsync(hlu, level_u, sizeof(hlu), cudaMemcpyDeviceToHost, st));
+    CPVS_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+    CPVS_CUDA(cudaStreamSynchronize(st));
+    if (herr) return fail(CPVS_ERR_DEVICE, "noalloc: internal check " + std::to_string(herr));
+    const uint64_t total = hoff[1];
+    if (dag_words) *dag_words = total;
+    if (!dag_out || dag_capacity < total)
+        return fail(CPVS_ERR_CAPACITY, "noalloc: the DAG has " + std::to_string(total) + " words, the output holds " +
+                                           std::to_string(dag_capacity));
+    for (int L = R; L >= bottom; --L) {
+        if (!hlu[2 * L]) continue;
+        const LevelDev child = (L > bottom) ? lv[L - 1] : lv[L];
+        const uint32_t g = grid_for(hlu[2 * L], kThreads);
+        if (leafmasks && L == 2)
+            k_emit<true><<<g, kThreads, 0, st>>>(lv[L], child, level_u, L, seg, lay, dag_out, total, err);
+        else
+            k_emit<false><<<g, kThreads, 0, st>>>(lv[L], child, level_u, L, seg, lay, dag_out, total, err);
+    }
+    CPVS_CUDA(cudaGetLastError());
+    CPVS_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
+    CPVS_CUDA(cudaStreamSynchronize(st));
+    if (herr) return fail(CPVS_ERR_DEVICE, "noalloc: internal check " + std::to_string(herr));
+    return CPVS_OK;
+}

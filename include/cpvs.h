@@ -166,6 +166,29 @@ CPVS_API cpvs_status cpvs_shadow_lookup_ndc(const cpvs_shadow* s, const float* x
 CPVS_API cpvs_status cpvs_shadow_lookup_voxel(const cpvs_shadow* s, const int32_t* xyz, uint64_t n, uint32_t* bits_out,
                                      uint32_t flags, void* stream);
 
+/* ---- allocation-free build ------------------------------------------- */
+
+/* Builds one shadow DAG without allocating any device memory.  No
+ * counterpart in the reference: it exists for callers that may not allocate,
+ * e.g. a render loop that must not stall on cudaMalloc/cudaFree (both can
+ * synchronise the device) or a plugin inside a host application that owns
+ * all GPU memory.  All scratch lives in a fixed 8 MiB array compiled into
+ * this library, which every GPU that loads the library holds until the
+ * process exits; maps are limited to n <= 256 (power of two, >= 8;
+ * without leafmasks only sizes whose full octree fits the array).
+ * `depth` is a device n*n float32 map; the DAG (the same words
+ * cpvs_shadow_create_from_depth builds) is written to the device buffer
+ * `dag_out` of `dag_capacity` words, and `*dag_words` receives its size
+ * (also when the buffer is too small: CPVS_ERR_CAPACITY).  The calling
+ * thread's current device is used; the first call on each device looks up
+ * the array's device address (no allocation), so make that first call
+ * before any stream capture.  All calls share the one array: calls whose
+ * work overlaps on the GPU (other streams or host threads) race and must be
+ * serialised by the caller.  Returns after the build has finished. */
+CPVS_API cpvs_status cpvs_shadow_build_noalloc(const float* depth, uint32_t n, uint32_t z_tile_index,
+                                               uint32_t z_tile_num, uint32_t flags, uint32_t* dag_out,
+                                               uint64_t dag_capacity, uint64_t* dag_words, void* stream);
+
 /* ---- top-level grid (container) -------------------------------------- */
 
 /* A cubic length^3 grid of DAGs (length a power of two).  Replaces
