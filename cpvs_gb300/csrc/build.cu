@@ -166,8 +166,11 @@ __global__ void __launch_bounds__(kThreads)
     block_chunk(n, b, e);
     uint32_t run = ninj + block_prefix_of_partials(partials, blockIdx.x, sm).x;
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
-        // total children = prefix of the last block + its own partial
-        counts[L - 1] = run + partials[blockIdx.x].x;
+        // total children = prefix of the last block + its own partial; a
+        // level never counts more nodes than it can hold
+        const uint32_t total = run + partials[blockIdx.x].x;
+        if (total > cap_next) atomicOr(err, 1u);
+        counts[L - 1] = total < cap_next ? total : cap_next;
     }
     if (blockIdx.x == 0)
         for (uint32_t r = threadIdx.x; r < ninj; r += blockDim.x) {
@@ -368,27 +371,33 @@ __device__ __forceinline__ bool same_node(const LevelDev& cur, const LevelDev& c
 template <bool LEAF>
 __global__ void __launch_bounds__(kThreads)
     k_dedup_insert(LevelDev cur, LevelDev child, const uint32_t* __restrict__ counts, int L,
-                   unsigned long long* table, uint64_t cap_mask) {
+                   unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
     const uint32_t n = counts[L];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint64_t h = LEAF ? cur.hash[i] : inner_hash(cur, child, i);
         const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | i;
         uint64_t s = h & cap_mask;
+        bool placed = false;
         for (uint64_t probe = 0; probe <= cap_mask; ++probe) {
             unsigned long long cur_e = __ldcg(&table[s]);
             if (cur_e == kEmptySlot) {
                 const unsigned long long prev = atomicCAS(&table[s], kEmptySlot, key);
-                if (prev == kEmptySlot) break;
+                if (prev == kEmptySlot) {
+                    placed = true;
+                    break;
+                }
                 cur_e = prev;
             }
             if ((cur_e >> 32) == (key >> 32) && same_node<LEAF>(cur, child, i, (uint32_t)cur_e)) {
                 // the slot only ever decreases: nothing to do when it already
                 // holds an earlier occurrence
                 if ((uint32_t)cur_e > i) atomicMin(&table[s], key);
+                placed = true;
                 break;
             }
             s = (s + 1) & cap_mask;
         }
+        if (!placed) atomicOr(err, 16u);  // table full: the result is void, reported
         cur.slot[i] = (uint32_t)s;
     }
 }
@@ -542,6 +551,115 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// Per-job bounds inside a build plan: one block per (job, level, 256
+// texels); the job's pyramid is read through the device job table, so a
+// captured plan serves any map of the same size.
+struct BoundSeg {
+    uint32_t job;
+    int32_t level;
+    uint32_t first_block;
+};
+
+__global__ void __launch_bounds__(kThreads)
+    k_plan_bounds(const JobDev* __restrict__ jobs, const BoundSeg* __restrict__ segs, uint32_t nsegs,
+                  unsigned long long* bounds) {
+    __shared__ uint64_t red[32];
+    // segment of this block: last seg with first_block <= blockIdx.x
+    uint32_t lo = 0, hi = nsegs;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) / 2;
+        if (segs[mid].first_block <= blockIdx.x) lo = mid; else hi = mid;
+    }
+    const BoundSeg sg = segs[lo];
+    const JobDev J = jobs[sg.job];
+    const int L = sg.level, R = (int)J.num_levels - 2;
+    const uint32_t W = J.n >> L;
+    const uint64_t t = (uint64_t)(blockIdx.x - sg.first_block) * blockDim.x + threadIdx.x;
+    uint64_t c = 0;
+    if (t < (uint64_t)W * W) {
+        const float2 mm = J.pyr[pyramid_level_offset_dev(J.n, L) + t];
+        const float H = __uint2float_rn((J.n >> L) * J.z_num);
+        const uint64_t span = 2ull << (R - L);
+        const float a = __fmul_rn(mm.x, H), b = __fmul_rn(mm.y, H);
+        const uint64_t zlo = J.z_idx * span, zhi = (J.z_idx + 1) * span;
+        double s0 = (a != a) ? (double)zlo : floor((double)a);
+        double e0 = (b != b) ? (double)zhi : ceil((double)b);
+        if (s0 < (double)zlo) s0 = (double)zlo;
+        if (e0 > (double)zhi) e0 = (double)zhi;
+        c = (e0 > s0) ? (uint64_t)(e0 - s0) : 0ull;
+    }
+    c = block_sum_u64(c, red);
+    if (threadIdx.x == 0 && c) atomicAdd(&bounds[(size_t)sg.job * CPVS_MAX_LEVELS + (L - 1)], (unsigned long long)c);
+}
+
+// The top level of a batch: the roots of the jobs whose root lies there.
+__global__ void k_init_top(LevelDev top, uint32_t* counts, int L, const Injected* __restrict__ inj, uint32_t ninj) {
+    for (uint32_t r = threadIdx.x; r < ninj; r += blockDim.x) {
+        top.coord[r] = inj[r].coord;
+        top.job[r] = inj[r].job;
+    }
+    if (threadIdx.x == 0) counts[L] = ninj;
+}
+
+// Root mask of every job (the first word of its DAG).
+__global__ void k_root_masks(const LevelDev* __restrict__ lvt, SegDev seg, const uint32_t* __restrict__ root_level,
+                             uint32_t njobs, uint32_t* out) {
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < njobs; j += gridDim.x * blockDim.x) {
+        const int L = (int)root_level[j];
+        out[j] = lvt[L].mask[seg.nstart[seg_index(j, L)]];
+    }
+}
+
+// Emission of every level in one launch: global kept-node index g maps to
+// level L through the per-level prefix `ustart` (levels bottom..top).
+struct EmitLevels {
+    uint32_t ustart[CPVS_MAX_LEVELS + 1];
+};
+
+__global__ void __launch_bounds__(kThreads)
+    k_emit_all(const LevelDev* __restrict__ lvt, EmitLevels el, int bottom, int top, bool leafmasks, SegDev seg,
+               JobLayout lay, uint32_t* __restrict__ out, uint64_t total_words, uint32_t* err) {
+    const uint32_t U = el.ustart[top + 1];
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < U; g += gridDim.x * blockDim.x) {
+        int L = bottom;
+        while (L < top && g >= el.ustart[L + 1]) ++L;
+        const uint32_t u = g - el.ustart[L];
+        const LevelDev& cur = lvt[L];
+        const bool leaf = leafmasks && L == 2;
+        const uint32_t i = cur.uniq[u];
+        const uint32_t j = cur.job[i];
+        const uint32_t sj = seg_index(j, L);
+        const uint32_t m = cur.mask[i];
+        const uint64_t at = lay.job_off[j] + lay.base[sj] + (cur.woff[u] - seg.wstart[sj]);
+        if (at + node_words(m, leaf) > total_words) {
+            atomicOr(err, 2u);
+            continue;
+        }
+        uint32_t* dst = out + at;
+        dst[0] = m;
+        if (leaf) {
+            uint32_t r = 0;
+#pragma unroll
+            for (uint32_t q = 0; q < 8; ++q)
+                if (((m >> (2u * q)) & 3u) == kPartial) {
+                    const uint64_t v = cur.slices[(size_t)i * 8 + q];
+                    dst[1 + 2 * r] = (uint32_t)v;
+                    dst[2 + 2 * r] = (uint32_t)(v >> 32);
+                    ++r;
+                }
+        } else {
+            const uint32_t k = partial_children(m);
+            if (k && L > 0) {
+                const LevelDev& child = lvt[L - 1];
+                const uint32_t f = cur.first[i];
+                const uint32_t sc = seg_index(j, L - 1);
+                const uint32_t cb = lay.base[sc] - seg.wstart[sc];
+                for (uint32_t r = 0; r < k; ++r) dst[1 + r] = cb + child.woff[child.uid[f + r]];
+            }
+        }
+    }
+}
+
 // --------------------------------------------------------------- host side
 inline uint64_t next_pow2(uint64_t v) {
     uint64_t p = 1;
@@ -563,297 +681,526 @@ struct Arena {
     }
 };
 
+// Host-visible results of one build, copied in one piece at its end.
+struct ResultView {
+    uint64_t* job_off;  // njobs + 1
+    uint32_t* seg;      // 6 * segn: nstart, nend, ustart, uend, wstart, wend
+    uint32_t* level_u;  // 2 * L_MAX
+    uint32_t* err;      // 1
+    unsigned long long* bounds;  // njobs * L_MAX
+    uint32_t* root_mask;         // njobs
+};
+
+inline size_t result_bytes(uint32_t njobs) {
+    const size_t segn = (size_t)njobs * CPVS_MAX_LEVELS;
+    return align256(8 * (njobs + 1)) + align256(4 * 6 * segn) + align256(4 * 2 * CPVS_MAX_LEVELS) + align256(4) +
+           align256(8 * segn) + align256(4 * (size_t)njobs);
+}
+
+inline ResultView result_view(char* base, uint32_t njobs) {
+    const size_t segn = (size_t)njobs * CPVS_MAX_LEVELS;
+    ResultView v;
+    size_t o = 0;
+    v.job_off = reinterpret_cast<uint64_t*>(base + o); o += align256(8 * (njobs + 1));
+    v.seg = reinterpret_cast<uint32_t*>(base + o); o += align256(4 * 6 * segn);
+    v.level_u = reinterpret_cast<uint32_t*>(base + o); o += align256(4 * 2 * CPVS_MAX_LEVELS);
+    v.err = reinterpret_cast<uint32_t*>(base + o); o += align256(4);
+    v.bounds = reinterpret_cast<unsigned long long*>(base + o); o += align256(8 * segn);
+    v.root_mask = reinterpret_cast<uint32_t*>(base + o);
+    return v;
+}
+
 }  // namespace
+
+// A build plan: capacities, scratch and the captured launch sequence for
+// one shape of batch (leafmask mode + the map side of every job).  Reused as
+// long as the data fit its capacities; otherwise rebuilt larger.
+struct BuildPlan {
+    bool leafmasks = false;
+    int bottom = 0, maxR = 0;
+    uint32_t njobs = 0;
+    std::vector<uint32_t> job_n, root_level;
+    uint64_t cap[CPVS_MAX_LEVELS] = {0}, tcap[CPVS_MAX_LEVELS] = {0}, ninj[CPVS_MAX_LEVELS] = {0};
+    uint64_t inj_off[CPVS_MAX_LEVELS + 1] = {0};
+    uint32_t max_grid = 0;
+    std::vector<BoundSeg> bsegs;
+    uint32_t bound_blocks = 0;
+    // device memory
+    char* arena = nullptr;
+    size_t arena_bytes = 0;
+    unsigned long long* table = nullptr;
+    uint64_t table_slots = 0;
+    LevelDev lv[CPVS_MAX_LEVELS];
+    LevelDev* lvt = nullptr;
+    uint2* partials = nullptr;
+    uint32_t* counts = nullptr;
+    uint32_t* segbuf = nullptr;  // 7 * segn: the six SegDev arrays + JobLayout::base
+    SegDev seg{};
+    JobLayout lay{};
+    char* res = nullptr;  // device results region (ResultView layout)
+    ResultView resv{};
+    uint32_t* root_dev = nullptr;
+    JobDev* jobs_dev = nullptr;
+    Injected* inj_dev = nullptr;
+    BoundSeg* bsegs_dev = nullptr;
+    // pinned host staging
+    char* hin = nullptr;
+    size_t hin_bytes = 0;
+    char* hout = nullptr;
+    size_t hout_bytes = 0;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t done = nullptr;  // recorded after the emission that last read the scratch
+    bool tables_tuned = false;
+};
+
+struct PlanCache {
+    std::vector<BuildPlan*> plans;
+};
+
+namespace {
+
+void plan_release(Ctx& ctx, BuildPlan* P) {
+    if (P->done) cudaEventSynchronize(P->done);
+    if (P->exec) cudaGraphExecDestroy(P->exec);
+    P->exec = nullptr;
+    if (P->arena) ctx.release(P->arena, P->arena_bytes, true, nullptr);
+    if (P->table) ctx.release(P->table, P->table_slots * 8, true, nullptr);
+    P->arena = nullptr;
+    P->table = nullptr;
+    if (P->hin) cudaFreeHost(P->hin);
+    if (P->hout) cudaFreeHost(P->hout);
+    P->hin = P->hout = nullptr;
+}
+
+// Capacities -> scratch layout, pinned staging, level table.
+cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
+    const uint32_t njobs = P->njobs;
+    const size_t segn = (size_t)njobs * CPVS_MAX_LEVELS;
+    size_t bytes = 0;
+    auto add = [&](size_t count, size_t elem) { bytes += align256(count * elem); };
+    for (int L = P->bottom; L <= P->maxR; ++L) {
+        const uint64_t c = std::max<uint64_t>(P->cap[L], 1);
+        for (int a = 0; a < 8; ++a) add(c, a == 0 ? 8 : 4);
+        if (P->leafmasks && L == 2) {
+            add(c * 8, 8);
+            add(c, 8);
+        }
+    }
+    add(CPVS_MAX_LEVELS, sizeof(LevelDev));
+    add(P->max_grid, sizeof(uint2));
+    add(CPVS_MAX_LEVELS, 4);
+    add(segn * 7, 4);
+    bytes += result_bytes(njobs);
+    add(njobs, 4);
+    add(njobs, sizeof(JobDev));
+    add(njobs, sizeof(Injected));
+    add(P->bsegs.size(), sizeof(BoundSeg));
+    P->arena_bytes = bytes;
+    cpvs_status r = ctx.alloc((void**)&P->arena, bytes, true, st);
+    if (r != CPVS_OK) return r;
+    P->table_slots = 1024;
+    for (int L = P->bottom; L <= P->maxR; ++L) P->table_slots = std::max(P->table_slots, P->tcap[L]);
+    r = ctx.alloc((void**)&P->table, P->table_slots * 8, true, st);
+    if (r != CPVS_OK) return r;
+    Arena A;
+    A.base = P->arena;
+    A.size = bytes;
+    std::memset(P->lv, 0, sizeof(P->lv));
+    for (int L = P->bottom; L <= P->maxR; ++L) {
+        const uint64_t c = std::max<uint64_t>(P->cap[L], 1);
+        LevelDev& l = P->lv[L];
+        l.coord = A.take<uint64_t>(c);
+        l.job = A.take<uint32_t>(c);
+        l.mask = A.take<uint32_t>(c);
+        l.first = A.take<uint32_t>(c);
+        l.uid = A.take<uint32_t>(c);
+        l.slot = A.take<uint32_t>(c);
+        l.uniq = A.take<uint32_t>(c);
+        l.woff = A.take<uint32_t>(c);
+        if (P->leafmasks && L == 2) {
+            l.slices = A.take<uint64_t>(c * 8);
+            l.hash = A.take<uint64_t>(c);
+        }
+    }
+    P->lvt = A.take<LevelDev>(CPVS_MAX_LEVELS);
+    P->partials = A.take<uint2>(P->max_grid);
+    P->counts = A.take<uint32_t>(CPVS_MAX_LEVELS);
+    P->segbuf = A.take<uint32_t>(segn * 7);
+    P->res = A.base + A.used;
+    A.used += result_bytes(njobs);
+    P->resv = result_view(P->res, njobs);
+    P->root_dev = A.take<uint32_t>(njobs);
+    P->jobs_dev = A.take<JobDev>(njobs);
+    P->inj_dev = A.take<Injected>(njobs);
+    P->bsegs_dev = A.take<BoundSeg>(P->bsegs.size());
+    // the device results region carries SegDev's arrays, so the six segment
+    // arrays live there (copied to the host with the rest) and segbuf keeps
+    // only JobLayout::base
+    uint32_t* sg = P->resv.seg;
+    P->seg = SegDev{sg, sg + segn, sg + 2 * segn, sg + 3 * segn, sg + 4 * segn, sg + 5 * segn};
+    P->lay = JobLayout{P->resv.job_off, P->segbuf + 6 * segn};
+    // pinned staging
+    P->hin_bytes = njobs * (sizeof(JobDev) + sizeof(Injected)) + 256;
+    P->hout_bytes = result_bytes(njobs);
+    CPVS_CUDA(cudaMallocHost((void**)&P->hin, P->hin_bytes));
+    CPVS_CUDA(cudaMallocHost((void**)&P->hout, P->hout_bytes));
+    // constant per plan: level table, root levels, bound segments
+    CPVS_CUDA(cudaMemcpyAsync(P->lvt, P->lv, sizeof(P->lv), cudaMemcpyHostToDevice, st));
+    CPVS_CUDA(cudaMemcpyAsync(P->root_dev, P->root_level.data(), njobs * 4, cudaMemcpyHostToDevice, st));
+    CPVS_CUDA(cudaMemcpyAsync(P->bsegs_dev, P->bsegs.data(), P->bsegs.size() * sizeof(BoundSeg),
+                              cudaMemcpyHostToDevice, st));
+    CPVS_CUDA(cudaStreamSynchronize(st));
+    return CPVS_OK;
+}
+
+uint32_t plan_grid(const BuildPlan* P, uint64_t items, uint64_t per_block) {
+    uint64_t g = (items + per_block - 1) / per_block;
+    return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, P->max_grid));
+}
+
+// The whole device-side build after the inputs are staged: bounds, top-down
+// expansion, leaves, bottom-up merge, layout, root masks, and the copy of
+// the results region to pinned host memory.  Stream-ordered; capturable.
+cpvs_status plan_enqueue(const BuildPlan* P, cudaStream_t st, Timing* tm) {
+    const uint32_t njobs = P->njobs;
+    const size_t segn = (size_t)njobs * CPVS_MAX_LEVELS;
+    const ResultView& rv = P->resv;
+    uint32_t* err = rv.err;
+    CPVS_CUDA(cudaMemsetAsync(P->res, 0, result_bytes(njobs), st));
+    CPVS_CUDA(cudaMemsetAsync(P->counts, 0, CPVS_MAX_LEVELS * 4, st));
+    CPVS_CUDA(cudaMemsetAsync(P->segbuf + 6 * segn, 0, segn * 4, st));
+    {
+        KernelTimer kt(tm, K_LEVEL_BOUNDS, st);
+        if (P->bound_blocks)
+            k_plan_bounds<<<P->bound_blocks, kThreads, 0, st>>>(P->jobs_dev, P->bsegs_dev, (uint32_t)P->bsegs.size(),
+                                                                 rv.bounds);
+    }
+    // the top level holds only roots
+    k_init_top<<<1, 256, 0, st>>>(P->lv[P->maxR], P->counts, P->maxR, P->inj_dev + P->inj_off[P->maxR],
+                                  (uint32_t)P->ninj[P->maxR]);
+    for (int L = P->maxR; L > P->bottom; --L) {
+        const uint32_t g = plan_grid(P, P->cap[L], kThreads * 4);
+        {
+            KernelTimer kt(tm, K_EXPAND_COUNT, st);
+            k_expand_count<<<g, kThreads, 0, st>>>(P->lv[L], P->counts, P->jobs_dev, njobs, L, P->partials, err);
+        }
+        {
+            KernelTimer kt(tm, K_EXPAND_WRITE, st);
+            k_expand_write<<<g, kThreads, 0, st>>>(P->lv[L], P->lv[L - 1], P->counts, L, P->partials,
+                                                   P->inj_dev + P->inj_off[L - 1], (uint32_t)P->ninj[L - 1], P->seg,
+                                                   (uint32_t)P->cap[L - 1], err);
+        }
+    }
+    if (P->leafmasks) {
+        KernelTimer kt(tm, K_LEAF_MASKS, st);
+        k_leaf_masks<<<plan_grid(P, P->cap[2], kThreads), kThreads, 0, st>>>(P->lv[2], P->counts, P->jobs_dev, njobs,
+                                                                            2, P->seg, err);
+    } else {
+        KernelTimer kt(tm, K_CLASSIFY_BOTTOM, st);
+        k_classify_bottom<<<plan_grid(P, P->cap[0], kThreads), kThreads, 0, st>>>(P->lv[0], P->counts, P->jobs_dev,
+                                                                                 njobs, 0, P->seg, err);
+    }
+    CPVS_CUDA(cudaGetLastError());
+    for (int L = P->bottom; L <= P->maxR; ++L) {
+        const uint64_t tc = P->tcap[L];
+        const bool leaf = P->leafmasks && L == 2;
+        const uint32_t gs = plan_grid(P, P->cap[L], kThreads * 4), gi = plan_grid(P, P->cap[L], kThreads);
+        const LevelDev child = (L > P->bottom) ? P->lv[L - 1] : P->lv[L];
+        {
+            KernelTimer kt(tm, K_TABLE_CLEAR, st);
+            CPVS_CUDA(cudaMemsetAsync(P->table, 0xFF, tc * 8, st));
+        }
+        if (leaf) {
+            { KernelTimer kt(tm, K_INSERT_LEAF, st);
+              k_dedup_insert<true><<<gi, kThreads, 0, st>>>(P->lv[L], child, P->counts, L, P->table, tc - 1, err); }
+            { KernelTimer kt(tm, K_RESOLVE, st);
+              k_dedup_resolve<true><<<gs, kThreads, 0, st>>>(P->lv[L], P->counts, L, P->table, P->partials); }
+            { KernelTimer kt(tm, K_SCAN, st);
+              k_dedup_scan<true><<<gs, kThreads, 0, st>>>(P->lv[L], P->counts, rv.level_u, L, P->table, P->partials,
+                                                          P->seg); }
+        } else {
+            { KernelTimer kt(tm, K_INSERT_INNER, st);
+              k_dedup_insert<false><<<gi, kThreads, 0, st>>>(P->lv[L], child, P->counts, L, P->table, tc - 1, err); }
+            { KernelTimer kt(tm, K_RESOLVE, st);
+              k_dedup_resolve<false><<<gs, kThreads, 0, st>>>(P->lv[L], P->counts, L, P->table, P->partials); }
+            { KernelTimer kt(tm, K_SCAN, st);
+              k_dedup_scan<false><<<gs, kThreads, 0, st>>>(P->lv[L], P->counts, rv.level_u, L, P->table, P->partials,
+                                                           P->seg); }
+        }
+        { KernelTimer kt(tm, K_REMAP, st);
+          k_dedup_remap<<<gi, kThreads, 0, st>>>(P->lv[L], P->counts, L, P->table); }
+    }
+    {
+        KernelTimer kt(tm, K_LAYOUT, st);
+        k_layout<<<1, 1024, 0, st>>>(P->seg, P->lay, P->root_dev, njobs, P->bottom);
+        k_root_masks<<<(njobs + 255) / 256, 256, 0, st>>>(P->lvt, P->seg, P->root_dev, njobs, rv.root_mask);
+    }
+    CPVS_CUDA(cudaGetLastError());
+    CPVS_CUDA(cudaMemcpyAsync(P->hout, P->res, result_bytes(njobs), cudaMemcpyDeviceToHost, st));
+    return CPVS_OK;
+}
+
+bool same_shape(const BuildPlan* P, bool leafmasks, const std::vector<uint32_t>& job_n) {
+    return P->leafmasks == leafmasks && P->job_n == job_n;
+}
+
+// Capacities from per-job level bounds (+25% slack) and table sizes.
+void plan_set_capacities(BuildPlan* P, const std::vector<unsigned long long>& bounds, bool exact_tables) {
+    std::fill(std::begin(P->cap), std::end(P->cap), 0);
+    for (uint32_t j = 0; j < P->njobs; ++j)
+        for (int L = P->bottom; L < (int)P->root_level[j]; ++L) P->cap[L] += bounds[(size_t)j * CPVS_MAX_LEVELS + L];
+    for (int L = 0; L < CPVS_MAX_LEVELS; ++L) {
+        if (P->cap[L]) P->cap[L] = P->cap[L] + P->cap[L] / 4 + 256;
+        P->cap[L] += P->ninj[L];
+        if (exact_tables || !P->tcap[L] || P->tcap[L] < 1024) P->tcap[L] = next_pow2(std::max<uint64_t>(2 * P->cap[L], 1024));
+    }
+}
+
+cpvs_status plan_create(Ctx& ctx, const std::vector<JobSpec>& jobs, const std::vector<SourceSpec>& sources,
+                        bool leafmasks, const std::vector<uint32_t>& job_n,
+                        const std::vector<unsigned long long>& bounds, cudaStream_t st, BuildPlan** out) {
+    auto* P = new BuildPlan;
+    P->leafmasks = leafmasks;
+    P->bottom = leafmasks ? 2 : 0;
+    P->njobs = (uint32_t)jobs.size();
+    P->job_n = job_n;
+    P->root_level.resize(P->njobs);
+    P->max_grid = (uint32_t)std::max(ctx.num_sms, 1) * 8;
+    for (uint32_t j = 0; j < P->njobs; ++j) {
+        P->root_level[j] = (uint32_t)(log2_u32(job_n[j]) - 1);
+        P->maxR = std::max(P->maxR, (int)P->root_level[j]);
+        P->ninj[P->root_level[j]] += 1;
+    }
+    uint64_t o = 0;
+    for (int L = 0; L < CPVS_MAX_LEVELS; ++L) {
+        P->inj_off[L] = o;
+        o += P->ninj[L];
+    }
+    P->inj_off[CPVS_MAX_LEVELS] = o;
+    const int lmin = P->bottom + 1;
+    for (uint32_t j = 0; j < P->njobs; ++j)
+        for (int L = lmin; L <= (int)P->root_level[j]; ++L) {
+            const uint64_t tex = (uint64_t)(job_n[j] >> L) * (job_n[j] >> L);
+            P->bsegs.push_back(BoundSeg{j, L, P->bound_blocks});
+            P->bound_blocks += (uint32_t)((tex + kThreads - 1) / kThreads);
+        }
+    plan_set_capacities(P, bounds, true);
+    for (int L = 0; L < CPVS_MAX_LEVELS; ++L)
+        if (P->cap[L] >= (1ull << 31)) {
+            delete P;
+            return fail(CPVS_ERR_BUDGET, "build: a level exceeds 2^31 nodes");
+        }
+    cpvs_status r = plan_allocate(ctx, P, st);
+    if (r != CPVS_OK) {
+        plan_release(ctx, P);
+        delete P;
+        return r;
+    }
+    *out = P;
+    return CPVS_OK;
+}
+
+// Level bounds of a batch straight from its pyramids (one sync).
+cpvs_status prepass_bounds(Ctx& ctx, const std::vector<SourceSpec>& sources, const std::vector<JobSpec>& jobs,
+                           int lmin, cudaStream_t st, std::vector<unsigned long long>& bounds) {
+    const uint32_t njobs = (uint32_t)jobs.size();
+    const size_t bounds_bytes = (size_t)njobs * CPVS_MAX_LEVELS * sizeof(unsigned long long);
+    unsigned long long* bounds_dev = nullptr;
+    BoundJob* bj_dev = nullptr;
+    cpvs_status r = ctx.alloc((void**)&bounds_dev, bounds_bytes, false, st);
+    if (r != CPVS_OK) return r;
+    r = ctx.alloc((void**)&bj_dev, njobs * sizeof(BoundJob), false, st);
+    if (r != CPVS_OK) {
+        ctx.release(bounds_dev, bounds_bytes, false, st);
+        return r;
+    }
+    std::vector<std::vector<uint32_t>> by_src(sources.size());
+    for (uint32_t j = 0; j < njobs; ++j) by_src[jobs[j].source].push_back(j);
+    std::vector<BoundJob> grouped;
+    std::vector<std::pair<size_t, size_t>> ranges(sources.size());
+    for (size_t s = 0; s < sources.size(); ++s) {
+        ranges[s] = {grouped.size(), by_src[s].size()};
+        for (uint32_t j : by_src[s]) grouped.push_back(BoundJob{jobs[j].z_idx, jobs[j].z_num, j});
+    }
+    cudaError_t e = cudaMemsetAsync(bounds_dev, 0, bounds_bytes, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(bj_dev, grouped.data(), njobs * sizeof(BoundJob), cudaMemcpyHostToDevice, st);
+    for (size_t s = 0; s < sources.size() && e == cudaSuccess && r == CPVS_OK; ++s) {
+        if (!ranges[s].second) continue;
+        KernelTimer kt(&ctx.timing, K_LEVEL_BOUNDS, st);
+        r = launch_level_bounds(sources[s].levels, sources[s].n, lmin, bj_dev + ranges[s].first,
+                                (int)ranges[s].second, bounds_dev, st);
+    }
+    bounds.assign((size_t)njobs * CPVS_MAX_LEVELS, 0);
+    if (e == cudaSuccess && r == CPVS_OK)
+        e = cudaMemcpyAsync(bounds.data(), bounds_dev, bounds_bytes, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    ctx.release(bounds_dev, bounds_bytes, false, st);
+    ctx.release(bj_dev, njobs * sizeof(BoundJob), false, st);
+    if (e != cudaSuccess) return cuda_fail(e, "build bounds pre-pass");
+    return r;
+}
+
+}  // namespace
+
+void destroy_plans(Ctx& ctx) {
+    if (!ctx.plans) return;
+    for (BuildPlan* P : ctx.plans->plans) {
+        plan_release(ctx, P);
+        if (P->done) cudaEventDestroy(P->done);
+        delete P;
+    }
+    delete ctx.plans;
+    ctx.plans = nullptr;
+}
 
 cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const std::vector<JobSpec>& jobs,
                        bool leafmasks, cudaStream_t st, BuildOutput& out) {
     const uint32_t njobs = (uint32_t)jobs.size();
     if (njobs == 0) return fail(CPVS_ERR_INVALID_ARG, "build_dags: no jobs");
-    const int bottom = leafmasks ? 2 : 0;
-    const int lmin = bottom + 1;  // pyramid level whose cells become bottom nodes
-
-    // ---- per-job geometry
-    std::vector<uint32_t> root_level(njobs);
-    int maxR = 0;
+    std::vector<uint32_t> job_n(njobs);
     for (uint32_t j = 0; j < njobs; ++j) {
         const SourceSpec& S = sources[jobs[j].source];
         const int nl = log2_u32(S.n) + 1;
-        root_level[j] = (uint32_t)(nl - 2);
-        maxR = std::max(maxR, nl - 2);
         // leafmasks need numLevels-3 >= 2 (src/CompressedShadow.cpp:20-27)
         if (leafmasks && nl - 3 < 2) return fail(CPVS_ERR_INVALID_ARG, "build_dags: map too small for leafmasks");
+        job_n[j] = S.n;
+    }
+    if (!ctx.plans) ctx.plans = new PlanCache;
+    BuildPlan* P = nullptr;
+    for (BuildPlan* q : ctx.plans->plans)
+        if (same_shape(q, leafmasks, job_n)) P = q;
+    if (!P) {
+        std::vector<unsigned long long> bounds;
+        cpvs_status r = prepass_bounds(ctx, sources, jobs, (leafmasks ? 2 : 0) + 1, st, bounds);
+        if (r != CPVS_OK) return r;
+        r = plan_create(ctx, jobs, sources, leafmasks, job_n, bounds, st, &P);
+        if (r != CPVS_OK) return r;
+        // keep a few shapes; drop the oldest
+        if (ctx.plans->plans.size() >= 8) {
+            plan_release(ctx, ctx.plans->plans.front());
+            if (ctx.plans->plans.front()->done) cudaEventDestroy(ctx.plans->plans.front()->done);
+            delete ctx.plans->plans.front();
+            ctx.plans->plans.erase(ctx.plans->plans.begin());
+        }
+        ctx.plans->plans.push_back(P);
     }
 
-    Timing* tm = &ctx.timing;
-    // ---- level bounds (one pass over each source's pyramid), one sync
-    const size_t bounds_bytes = (size_t)njobs * CPVS_MAX_LEVELS * sizeof(unsigned long long);
-    unsigned long long* bounds_dev = nullptr;
-    BoundJob* bj_dev = nullptr;
-    std::vector<BoundJob> bj(njobs);
-    for (uint32_t j = 0; j < njobs; ++j) bj[j] = BoundJob{jobs[j].z_idx, jobs[j].z_num, j};
-    {
-        cpvs_status r = ctx.alloc((void**)&bounds_dev, bounds_bytes, false, st);
-        if (r != CPVS_OK) return r;
-        r = ctx.alloc((void**)&bj_dev, njobs * sizeof(BoundJob), false, st);
-        if (r != CPVS_OK) {
-            ctx.release(bounds_dev, bounds_bytes, false, st);
-            return r;
+    if (!P->done) CPVS_CUDA(cudaEventCreateWithFlags(&P->done, cudaEventDisableTiming));
+    // the previous build with this plan may still be emitting from its
+    // scratch on another stream
+    CPVS_CUDA(cudaStreamWaitEvent(st, P->done, 0));
+    ResultView hv{};
+    for (int attempt = 0;; ++attempt) {
+        // stage this batch's inputs: job table (pyramid and map pointers,
+        // z-tile), and roots in root-level order
+        JobDev* hj = reinterpret_cast<JobDev*>(P->hin);
+        Injected* hi = reinterpret_cast<Injected*>(P->hin + njobs * sizeof(JobDev));
+        std::vector<uint64_t> fill(CPVS_MAX_LEVELS, 0);
+        for (uint32_t j = 0; j < njobs; ++j) {
+            const SourceSpec& S = sources[jobs[j].source];
+            hj[j] = JobDev{S.levels, S.depth, S.n, P->root_level[j] + 2, jobs[j].z_idx, jobs[j].z_num};
+            const int R = (int)P->root_level[j];
+            hi[P->inj_off[R] + fill[R]++] = Injected{pack_xyz(0, 0, 2 * jobs[j].z_idx), j, 0};
         }
-    }
-    CPVS_CUDA(cudaMemsetAsync(bounds_dev, 0, bounds_bytes, st));
-    {
-        // jobs grouped by source (jobs of one source need not be adjacent)
-        std::vector<std::vector<uint32_t>> by_src(sources.size());
-        for (uint32_t j = 0; j < njobs; ++j) by_src[jobs[j].source].push_back(j);
-        std::vector<BoundJob> grouped;
-        std::vector<std::pair<size_t, size_t>> ranges(sources.size());
-        for (size_t s = 0; s < sources.size(); ++s) {
-            ranges[s] = {grouped.size(), by_src[s].size()};
-            for (uint32_t j : by_src[s]) grouped.push_back(bj[j]);
-        }
-        CPVS_CUDA(cudaMemcpyAsync(bj_dev, grouped.data(), njobs * sizeof(BoundJob), cudaMemcpyHostToDevice, st));
-        for (size_t s = 0; s < sources.size(); ++s) {
-            if (!ranges[s].second) continue;
-            KernelTimer kt(tm, K_LEVEL_BOUNDS, st);
-            cpvs_status r = launch_level_bounds(sources[s].levels, sources[s].n, lmin, bj_dev + ranges[s].first,
-                                                (int)ranges[s].second, bounds_dev, st);
+        CPVS_CUDA(cudaMemcpyAsync(P->jobs_dev, hj, njobs * sizeof(JobDev), cudaMemcpyHostToDevice, st));
+        CPVS_CUDA(cudaMemcpyAsync(P->inj_dev, hi, njobs * sizeof(Injected), cudaMemcpyHostToDevice, st));
+        if (ctx.timing.on) {
+            cpvs_status r = plan_enqueue(P, st, &ctx.timing);
             if (r != CPVS_OK) return r;
+        } else {
+            if (!P->exec) {
+                if (!ctx.capture_stream) CPVS_CUDA(cudaStreamCreateWithFlags(&ctx.capture_stream, cudaStreamNonBlocking));
+                cudaGraph_t graph = nullptr;
+                CPVS_CUDA(cudaStreamBeginCapture(ctx.capture_stream, cudaStreamCaptureModeThreadLocal));
+                cpvs_status r = plan_enqueue(P, ctx.capture_stream, nullptr);
+                cudaError_t ec = cudaStreamEndCapture(ctx.capture_stream, &graph);
+                if (r != CPVS_OK) {
+                    if (graph) cudaGraphDestroy(graph);
+                    return r;
+                }
+                if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture");
+                ec = cudaGraphInstantiate(&P->exec, graph, 0);
+                cudaGraphDestroy(graph);
+                if (ec != cudaSuccess) return cuda_fail(ec, "cudaGraphInstantiate");
+            }
+            CPVS_CUDA(cudaGraphLaunch(P->exec, st));
         }
-    }
-    std::vector<unsigned long long> bounds((size_t)njobs * CPVS_MAX_LEVELS);
-    CPVS_CUDA(cudaMemcpyAsync(bounds.data(), bounds_dev, bounds_bytes, cudaMemcpyDeviceToHost, st));
-    CPVS_CUDA(cudaStreamSynchronize(st));
-    ctx.release(bounds_dev, bounds_bytes, false, st);
-    ctx.release(bj_dev, njobs * sizeof(BoundJob), false, st);
-
-    // capacity per level: bounded children + roots entering there
-    std::vector<uint64_t> cap(CPVS_MAX_LEVELS, 0), ninj(CPVS_MAX_LEVELS, 0);
-    for (uint32_t j = 0; j < njobs; ++j) {
-        ninj[root_level[j]] += 1;
-        for (int L = bottom; L < (int)root_level[j]; ++L) cap[L] += bounds[(size_t)j * CPVS_MAX_LEVELS + L];
-    }
-    uint64_t maxcap = 0;
-    for (int L = 0; L < CPVS_MAX_LEVELS; ++L) {
-        cap[L] += ninj[L];
-        if (cap[L] >= (1ull << 31)) return fail(CPVS_ERR_BUDGET, "build_dags: a level exceeds 2^31 nodes");
-        maxcap = std::max(maxcap, cap[L]);
-    }
-    const uint64_t table_cap = next_pow2(std::max<uint64_t>(2 * maxcap, 1024));
-
-    // ---- launch shapes
-    const uint32_t max_grid = (uint32_t)std::max(ctx.num_sms, 1) * 8;
-    auto grid_for = [&](uint64_t items, uint64_t per_block) -> uint32_t {
-        uint64_t g = (items + per_block - 1) / per_block;
-        return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, max_grid));
-    };
-
-    // ---- scratch arena
-    size_t bytes = 0;
-    auto add = [&](size_t count, size_t elem) { bytes += align256(count * elem); };
-    for (int L = bottom; L <= maxR; ++L) {
-        const uint64_t c = std::max<uint64_t>(cap[L], 1);
-        add(c, 8); add(c, 4); add(c, 4); add(c, 4); add(c, 4); add(c, 4); add(c, 4); add(c, 4);
-        if (leafmasks && L == 2) { add(c * 8, 8); add(c, 8); }
-    }
-    add(table_cap, 8);
-    add(max_grid, sizeof(uint2));
-    add(CPVS_MAX_LEVELS, 4);       // counts
-    add(2 * CPVS_MAX_LEVELS, 4);   // level (U, W)
-    add(1, 4);                     // error word
-    add((size_t)njobs * CPVS_MAX_LEVELS * 7, 4);  // seg arrays + base
-    add(njobs + 1, 8);             // job_off
-    add(njobs, 4);                 // root levels
-    add(njobs, sizeof(JobDev));
-    add(njobs, sizeof(Injected));
-    Arena A;
-    A.size = bytes;
-    {
-        cpvs_status r = ctx.alloc((void**)&A.base, bytes, false, st);
+        CPVS_CUDA(cudaStreamSynchronize(st));
+        hv = result_view(P->hout, njobs);
+        const uint32_t herr = *hv.err;
+        if (herr == 0) break;
+        // bit 1 (a level outgrew the plan) or 16 (a hash table did): re-plan
+        // from this run's bounds and retry; the rejected stale slots that an
+        // overflow leaves behind (bits 4, 8) go with it.  Anything else is an
+        // internal fault.
+        const bool overflow = (herr & (1u | 16u)) != 0;
+        if (!overflow || (herr & 2u) || attempt >= 2)
+            return fail(CPVS_ERR_DEVICE, "build_dags: internal check " + std::to_string(herr));
+        std::vector<unsigned long long> bounds(hv.bounds, hv.bounds + (size_t)njobs * CPVS_MAX_LEVELS);
+        plan_release(ctx, P);
+        plan_set_capacities(P, bounds, true);
+        cpvs_status r = plan_allocate(ctx, P, st);
         if (r != CPVS_OK) return r;
     }
-    struct Free {
-        Ctx& c; Arena& a; cudaStream_t s;
-        ~Free() {
-            if (a.base) c.release(a.base, a.size, false, s);
-        }
-    } free_guard{ctx, A, st};
 
-    LevelDev lv[CPVS_MAX_LEVELS];
-    std::memset(lv, 0, sizeof(lv));
-    for (int L = bottom; L <= maxR; ++L) {
-        const uint64_t c = std::max<uint64_t>(cap[L], 1);
-        lv[L].coord = A.take<uint64_t>(c);
-        lv[L].job = A.take<uint32_t>(c);
-        lv[L].mask = A.take<uint32_t>(c);
-        lv[L].first = A.take<uint32_t>(c);
-        lv[L].uid = A.take<uint32_t>(c);
-        lv[L].slot = A.take<uint32_t>(c);
-        lv[L].uniq = A.take<uint32_t>(c);
-        lv[L].woff = A.take<uint32_t>(c);
-        if (leafmasks && L == 2) {
-            lv[L].slices = A.take<uint64_t>(c * 8);
-            lv[L].hash = A.take<uint64_t>(c);
-        }
-    }
-    unsigned long long* table = A.take<unsigned long long>(table_cap);
-    uint2* partials = A.take<uint2>(max_grid);
-    uint32_t* counts = A.take<uint32_t>(CPVS_MAX_LEVELS);
-    uint32_t* level_u = A.take<uint32_t>(2 * CPVS_MAX_LEVELS);
-    uint32_t* err = A.take<uint32_t>(1);
     const size_t segn = (size_t)njobs * CPVS_MAX_LEVELS;
-    uint32_t* segbuf = A.take<uint32_t>(segn * 7);
-    SegDev seg{segbuf, segbuf + segn, segbuf + 2 * segn, segbuf + 3 * segn, segbuf + 4 * segn, segbuf + 5 * segn};
-    JobLayout lay{A.take<uint64_t>(njobs + 1), segbuf + 6 * segn};
-    uint32_t* root_dev = A.take<uint32_t>(njobs);
-    JobDev* jobs_dev = A.take<JobDev>(njobs);
-    Injected* inj_dev = A.take<Injected>(njobs);
-
-    // ---- job table and roots (grouped by root level, in job order)
-    std::vector<JobDev> jd(njobs);
-    std::vector<Injected> inj;
-    std::vector<uint64_t> inj_off(CPVS_MAX_LEVELS + 1, 0);
-    for (uint32_t j = 0; j < njobs; ++j) {
-        const SourceSpec& S = sources[jobs[j].source];
-        jd[j] = JobDev{S.levels, S.depth, S.n, root_level[j] + 2, jobs[j].z_idx, jobs[j].z_num};
-    }
-    for (int L = 0; L < CPVS_MAX_LEVELS; ++L) {
-        inj_off[L] = inj.size();
-        for (uint32_t j = 0; j < njobs; ++j)
-            if ((int)root_level[j] == L) inj.push_back(Injected{pack_xyz(0, 0, 2 * jobs[j].z_idx), j, 0});
-    }
-    inj_off[CPVS_MAX_LEVELS] = inj.size();
-    CPVS_CUDA(cudaMemsetAsync(segbuf, 0, segn * 7 * sizeof(uint32_t), st));
-    CPVS_CUDA(cudaMemsetAsync(counts, 0, CPVS_MAX_LEVELS * sizeof(uint32_t), st));
-    CPVS_CUDA(cudaMemsetAsync(level_u, 0, 2 * CPVS_MAX_LEVELS * sizeof(uint32_t), st));
-    CPVS_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
-    CPVS_CUDA(cudaMemcpyAsync(jobs_dev, jd.data(), njobs * sizeof(JobDev), cudaMemcpyHostToDevice, st));
-    CPVS_CUDA(cudaMemcpyAsync(inj_dev, inj.data(), inj.size() * sizeof(Injected), cudaMemcpyHostToDevice, st));
-    CPVS_CUDA(cudaMemcpyAsync(root_dev, root_level.data(), njobs * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-
-    // top level: its roots only (pageable copies are staged before the call
-    // returns, so the host vectors may go out of scope)
-    {
-        const uint32_t c = (uint32_t)ninj[maxR];
-        std::vector<uint64_t> coords(c);
-        std::vector<uint32_t> js(c);
-        for (uint32_t r = 0; r < c; ++r) {
-            coords[r] = inj[inj_off[maxR] + r].coord;
-            js[r] = inj[inj_off[maxR] + r].job;
-        }
-        CPVS_CUDA(cudaMemcpyAsync(lv[maxR].coord, coords.data(), c * 8, cudaMemcpyHostToDevice, st));
-        CPVS_CUDA(cudaMemcpyAsync(lv[maxR].job, js.data(), c * 4, cudaMemcpyHostToDevice, st));
-        CPVS_CUDA(cudaMemcpyAsync(counts + maxR, &c, 4, cudaMemcpyHostToDevice, st));
-    }
-
-    // ---- top-down
-    for (int L = maxR; L > bottom; --L) {
-        const uint32_t g = grid_for(cap[L], kThreads * 4);
-        { KernelTimer kt(tm, K_EXPAND_COUNT, st);
-        k_expand_count<<<g, kThreads, 0, st>>>(lv[L], counts, jobs_dev, njobs, L, partials, err); }
-        { KernelTimer kt(tm, K_EXPAND_WRITE, st);
-        k_expand_write<<<g, kThreads, 0, st>>>(lv[L], lv[L - 1], counts, L, partials, inj_dev + inj_off[L - 1],
-                                               (uint32_t)ninj[L - 1], seg, (uint32_t)cap[L - 1], err); }
-    }
-    if (leafmasks) {
-        KernelTimer kt(tm, K_LEAF_MASKS, st);
-        k_leaf_masks<<<grid_for(cap[2], kThreads), kThreads, 0, st>>>(lv[2], counts, jobs_dev, njobs, 2, seg, err);
-    } else {
-        KernelTimer kt(tm, K_CLASSIFY_BOTTOM, st);
-        k_classify_bottom<<<grid_for(cap[0], kThreads), kThreads, 0, st>>>(lv[0], counts, jobs_dev, njobs, 0, seg, err);
-    }
-    CPVS_CUDA(cudaGetLastError());
-
-    // ---- bottom-up merge
-    for (int L = bottom; L <= maxR; ++L) {
-        const uint64_t tcap = next_pow2(std::max<uint64_t>(2 * cap[L], 1024));
-        const uint64_t cmask = tcap - 1;
-        const bool leaf = leafmasks && L == 2;
-        const uint32_t gs = grid_for(cap[L], kThreads * 4);
-        const uint32_t gi = grid_for(cap[L], kThreads);
-        const LevelDev child = (L > bottom) ? lv[L - 1] : lv[L];
-        {
-            KernelTimer kt(tm, K_TABLE_CLEAR, st);
-            CPVS_CUDA(cudaMemsetAsync(table, 0xFF, tcap * sizeof(unsigned long long), st));
-        }
-        if (leaf) {
-            { KernelTimer kt(tm, K_INSERT_LEAF, st);
-              k_dedup_insert<true><<<gi, kThreads, 0, st>>>(lv[L], child, counts, L, table, cmask); }
-            { KernelTimer kt(tm, K_RESOLVE, st);
-              k_dedup_resolve<true><<<gs, kThreads, 0, st>>>(lv[L], counts, L, table, partials); }
-            { KernelTimer kt(tm, K_SCAN, st);
-              k_dedup_scan<true><<<gs, kThreads, 0, st>>>(lv[L], counts, level_u, L, table, partials, seg); }
-        } else {
-            { KernelTimer kt(tm, K_INSERT_INNER, st);
-              k_dedup_insert<false><<<gi, kThreads, 0, st>>>(lv[L], child, counts, L, table, cmask); }
-            { KernelTimer kt(tm, K_RESOLVE, st);
-              k_dedup_resolve<false><<<gs, kThreads, 0, st>>>(lv[L], counts, L, table, partials); }
-            { KernelTimer kt(tm, K_SCAN, st);
-              k_dedup_scan<false><<<gs, kThreads, 0, st>>>(lv[L], counts, level_u, L, table, partials, seg); }
-        }
-        { KernelTimer kt(tm, K_REMAP, st);
-          k_dedup_remap<<<gi, kThreads, 0, st>>>(lv[L], counts, L, table); }
-        CPVS_CUDA(cudaGetLastError());
-    }
-
-    // ---- layout, one sync for the sizes
-    {
-        KernelTimer kt(tm, K_LAYOUT, st);
-        k_layout<<<1, 1024, 0, st>>>(seg, lay, root_dev, njobs, bottom);
-    }
-    CPVS_CUDA(cudaGetLastError());
-    std::vector<uint64_t> job_off(njobs + 1);
-    std::vector<uint32_t> hseg(segn * 6);
-    std::vector<uint32_t> hcounts(CPVS_MAX_LEVELS), hlu(2 * CPVS_MAX_LEVELS);
-    CPVS_CUDA(cudaMemcpyAsync(job_off.data(), lay.job_off, (njobs + 1) * 8, cudaMemcpyDeviceToHost, st));
-    CPVS_CUDA(cudaMemcpyAsync(hseg.data(), segbuf, segn * 6 * 4, cudaMemcpyDeviceToHost, st));
-    CPVS_CUDA(cudaMemcpyAsync(hlu.data(), level_u, 2 * CPVS_MAX_LEVELS * 4, cudaMemcpyDeviceToHost, st));
-    uint32_t herr = 0;
-    CPVS_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
-    CPVS_CUDA(cudaStreamSynchronize(st));
-    if (herr) return fail(CPVS_ERR_DEVICE, "build_dags: a level outgrew its bound (internal check " + std::to_string(herr) + ")");
-    const uint64_t total = job_off[njobs];
-
+    const uint32_t* hseg = hv.seg;
+    const uint64_t total = hv.job_off[njobs];
     out.leafmasks = leafmasks;
     out.dag_words = total;
-    out.job_offset.assign(job_off.begin(), job_off.begin() + njobs);
+    out.job_offset.assign(hv.job_off, hv.job_off + njobs);
     out.job_words.resize(njobs);
+    out.root_mask.assign(hv.root_mask, hv.root_mask + njobs);
     out.tree_nodes.assign(njobs, std::vector<uint64_t>());
     out.unique_nodes.assign(njobs, std::vector<uint64_t>());
+    uint64_t level_unique[CPVS_MAX_LEVELS] = {0};
     for (uint32_t j = 0; j < njobs; ++j) {
-        out.job_words[j] = job_off[j + 1] - job_off[j];
+        out.job_words[j] = hv.job_off[j + 1] - hv.job_off[j];
         if (out.job_words[j] >= (1ull << 32)) return fail(CPVS_ERR_BUDGET, "build_dags: DAG exceeds 2^32 words");
-        const int nl = (int)root_level[j] + 2;
+        const int nl = (int)P->root_level[j] + 2;
         out.tree_nodes[j].assign(nl, 0);
         out.unique_nodes[j].assign(nl, 0);
-        for (int L = bottom; L <= (int)root_level[j]; ++L) {
+        for (int L = P->bottom; L <= (int)P->root_level[j]; ++L) {
             const size_t s = (size_t)j * CPVS_MAX_LEVELS + L;
             out.tree_nodes[j][L] = hseg[1 * segn + s] - hseg[0 * segn + s];
             out.unique_nodes[j][L] = hseg[3 * segn + s] - hseg[2 * segn + s];
         }
     }
+    EmitLevels el{};
+    for (int L = P->bottom; L <= P->maxR; ++L) {
+        level_unique[L] = hv.level_u[2 * L];
+        el.ustart[L + 1] = el.ustart[L] + hv.level_u[2 * L];
+    }
     {
         cpvs_status r = ctx.alloc((void**)&out.dag, std::max<uint64_t>(total, 1) * 4, true, st);
         if (r != CPVS_OK) return r;
     }
-    for (int L = maxR; L >= bottom; --L) {
-        const uint32_t U = hlu[2 * L];
-        if (!U) continue;
-        const uint32_t g = grid_for(U, kThreads);
-        const LevelDev child = (L > bottom) ? lv[L - 1] : lv[L];
-        KernelTimer kt(tm, K_EMIT, st);
-        if (leafmasks && L == 2)
-            k_emit<true><<<g, kThreads, 0, st>>>(lv[L], child, level_u, L, seg, lay, out.dag, total, err);
-        else
-            k_emit<false><<<g, kThreads, 0, st>>>(lv[L], child, level_u, L, seg, lay, out.dag, total, err);
+    {
+        KernelTimer kt(&ctx.timing, K_EMIT, st);
+        const uint32_t U = el.ustart[P->maxR + 1];
+        if (U)
+            k_emit_all<<<plan_grid(P, U, kThreads), kThreads, 0, st>>>(P->lvt, el, P->bottom, P->maxR, P->leafmasks,
+                                                                       P->seg, P->lay, out.dag, total, P->resv.err);
+        CPVS_CUDA(cudaGetLastError());
+        CPVS_CUDA(cudaEventRecord(P->done, st));
     }
-    CPVS_CUDA(cudaGetLastError());
-    // root masks of every job (the first word of each DAG)
-    out.root_mask.resize(njobs);
-    for (uint32_t j = 0; j < njobs; ++j)
-        CPVS_CUDA(cudaMemcpyAsync(&out.root_mask[j], out.dag + job_off[j], 4, cudaMemcpyDeviceToHost, st));
-    CPVS_CUDA(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st));
-    CPVS_CUDA(cudaStreamSynchronize(st));
-    if (herr) return fail(CPVS_ERR_DEVICE, "build_dags: DAG layout out of range (internal check " + std::to_string(herr) + ")");
+    // size the hash tables to the unique counts seen (1.5x, load <= 2/3);
+    // a later build that needs more grows them back
+    if (!P->tables_tuned) {
+        bool changed = false;
+        for (int L = P->bottom; L <= P->maxR; ++L) {
+            const uint64_t t = next_pow2(std::max<uint64_t>(3 * level_unique[L], 1024));
+            const uint64_t tc = std::min<uint64_t>(t, next_pow2(std::max<uint64_t>(2 * P->cap[L], 1024)));
+            if (tc != P->tcap[L]) changed = true;
+            P->tcap[L] = tc;
+        }
+        P->tables_tuned = true;
+        if (changed && P->exec) {
+            cudaGraphExecDestroy(P->exec);
+            P->exec = nullptr;
+        }
+    }
     return CPVS_OK;
 }
 
@@ -1017,11 +1364,11 @@ extern "C" CPVS_API cpvs_status cpvs_shadow_build_noalloc(const float* depth, ui
         const LevelDev child = (L > bottom) ? lv[L - 1] : lv[L];
         CPVS_CUDA(cudaMemsetAsync(table, 0xFF, tc * sizeof(unsigned long long), st));
         if (leaf) {
-            k_dedup_insert<true><<<gi, kThreads, 0, st>>>(lv[L], child, counts, L, table, tc - 1);
+            k_dedup_insert<true><<<gi, kThreads, 0, st>>>(lv[L], child, counts, L, table, tc - 1, err);
             k_dedup_resolve<true><<<gs, kThreads, 0, st>>>(lv[L], counts, L, table, partials);
             k_dedup_scan<true><<<gs, kThreads, 0, st>>>(lv[L], counts, level_u, L, table, partials, seg);
         } else {
-            k_dedup_insert<false><<<gi, kThreads, 0, st>>>(lv[L], child, counts, L, table, tc - 1);
+            k_dedup_insert<false><<<gi, kThreads, 0, st>>>(lv[L], child, counts, L, table, tc - 1, err);
             k_dedup_resolve<false><<<gs, kThreads, 0, st>>>(lv[L], counts, L, table, partials);
             k_dedup_scan<false><<<gs, kThreads, 0, st>>>(lv[L], counts, level_u, L, table, partials, seg);
         }

@@ -231,6 +231,9 @@ void cpvs_ctx_destroy(cpvs_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->c.device);
     cudaDeviceSynchronize();
+    cpvs::destroy_plans(ctx->c);
+    cudaDeviceSynchronize();
+    if (ctx->c.capture_stream) cudaStreamDestroy(ctx->c.capture_stream);
     cudaStreamDestroy(ctx->c.free_stream);
     cudaMemPoolDestroy(ctx->c.pool);
     delete ctx;

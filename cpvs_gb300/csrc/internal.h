@@ -80,6 +80,7 @@ struct Ctx;
 // Builds the DAGs of `jobs` (all with the same leafmask mode).
 cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const std::vector<JobSpec>& jobs,
                        bool leafmasks, cudaStream_t st, BuildOutput& out);
+void destroy_plans(Ctx& ctx);
 
 // -------------------------------------------------------------- lookup
 cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks, const void* xyz,
@@ -156,6 +157,10 @@ struct Ctx {
     // Scratch: freed in the order of `st`.  Persistent: freed once
     // `last_use` (the last event recorded after work on the block) is reached.
     void release(void* p, uint64_t bytes, bool persistent, cudaStream_t st, cudaEvent_t last_use = nullptr);
+    // Cached build plans (scratch + captured launch sequence per batch shape)
+    // and the stream their launch sequences are captured on.
+    struct PlanCache* plans = nullptr;
+    cudaStream_t capture_stream = nullptr;
 };
 
 }  // namespace cpvs
