@@ -216,6 +216,18 @@ def run_ours(args, rank, world, local_rank):
     lookup_ms = e0.elapsed_time(e1) / args.steps
     lk = ctx.kernel_times()["lookup"]
     ctx.enable_timing(False)
+    # the tuner's alternatives (queries carried per thread), for the record
+    variants = {}
+    for qpt in (1, 2, 4):
+        ctx.set_option(ctx.OPT_LOOKUP_QUERIES_PER_THREAD, qpt)
+        sh.lookup_ndc(q_dev, bits_dev, stream=stream)
+        e0.record(stream)
+        for _ in range(3):
+            sh.lookup_ndc(q_dev, bits_dev, stream=stream)
+        e1.record(stream)
+        barrier()
+        variants[str(qpt)] = round(e0.elapsed_time(e1) / 3, 4)
+    ctx.set_option(ctx.OPT_LOOKUP_QUERIES_PER_THREAD, 0)
 
     # end to end through the public API with host buffers
     def e2e_build():
@@ -298,7 +310,7 @@ def run_ours(args, rank, world, local_rank):
                                         "achieved": round(build_alg / (build_ms * 1e-3) / 1e9, 1),
                                         "frac": round(build_alg / (build_ms * 1e-3) / 1e9 / peak, 4)}},
         "lookup": {"value": round(world * nq / (lookup_ms * 1e-3) / 1e9, 2), "unit": "Glookups/s",
-                   "ms_per_batch": round(lookup_ms, 4),
+                   "ms_per_batch": round(lookup_ms, 4), "ms_by_queries_per_thread": variants,
                    "roofline": {"bound": "hbm", "achieved": round(lookup_alg / (lk_ms_launch * 1e-3) / 1e9, 1),
                                 "peak": peak, "unit": "GB/s",
                                 "frac": round(lookup_alg / (lk_ms_launch * 1e-3) / 1e9 / peak, 4),

@@ -46,6 +46,8 @@ _SIGS = {
     "cpvs_ctx_destroy": (None, [_vp]),
     "cpvs_ctx_set_budget": (C.c_int, [_vp, _u64]),
     "cpvs_ctx_bytes_in_use": (_u64, [_vp]),
+    "cpvs_ctx_set_option": (C.c_int, [_vp, C.c_int, C.c_int64]),
+    "cpvs_ctx_get_option": (C.c_int64, [_vp, C.c_int]),
     "cpvs_ctx_enable_timing": (C.c_int, [_vp, C.c_int]),
     "cpvs_ctx_kernel_times": (C.c_int, [_vp, _vp, _vp, _u32, C.POINTER(_u32)]),
     "cpvs_kernel_name": (C.c_char_p, [_u32]),
@@ -163,6 +165,14 @@ class Context:
 
     def bytes_in_use(self) -> int:
         return int(_lib.cpvs_ctx_bytes_in_use(self.handle))
+
+    OPT_LOOKUP_QUERIES_PER_THREAD = 1
+
+    def set_option(self, key: int, value: int):
+        _check(_lib.cpvs_ctx_set_option(self.handle, key, int(value)))
+
+    def get_option(self, key: int) -> int:
+        return int(_lib.cpvs_ctx_get_option(self.handle, key))
 
     def enable_timing(self, on: bool = True):
         _check(_lib.cpvs_ctx_enable_timing(self.handle, int(on)))

@@ -1157,7 +1157,7 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
     uint64_t level_unique[CPVS_MAX_LEVELS] = {0};
     for (uint32_t j = 0; j < njobs; ++j) {
         out.job_words[j] = hv.job_off[j + 1] - hv.job_off[j];
-        if (out.job_words[j] >= (1ull << 32)) return fail(CPVS_ERR_BUDGET, "build_dags: DAG exceeds 2^32 words");
+        if (out.job_words[j] >= 0xFFFFFFFEull) return fail(CPVS_ERR_BUDGET, "build_dags: DAG exceeds 2^32-2 words");
         const int nl = (int)P->root_level[j] + 2;
         out.tree_nodes[j].assign(nl, 0);
         out.unique_nodes[j].assign(nl, 0);
@@ -1173,8 +1173,9 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         el.ustart[L + 1] = el.ustart[L] + hv.level_u[2 * L];
     }
     {
-        cpvs_status r = ctx.alloc((void**)&out.dag, std::max<uint64_t>(total, 1) * 4, true, st);
+        cpvs_status r = ctx.alloc((void**)&out.dag, (total + kDagPad) * 4, true, st);
         if (r != CPVS_OK) return r;
+        CPVS_CUDA(cudaMemsetAsync(out.dag + total, 0, kDagPad * 4, st));
     }
     {
         KernelTimer kt(&ctx.timing, K_EMIT, st);

@@ -80,9 +80,11 @@ struct cpvs_hierarchy : DeviceObject {
 
 struct cpvs_shadow : DeviceObject {
     cpvs_ctx* ctx = nullptr;
-    uint32_t* dag = nullptr;
+    uint32_t* dag = nullptr;   // words + kDagPad zeroed words
     uint64_t words = 0;
     uint64_t bytes = 0;
+    uint32_t* top = nullptr;   // dense top index for lookups (may be null)
+    uint64_t top_bytes = 0;
     uint32_t num_levels = 0;
     bool leafmasks = false;
     uint32_t root_mask = 0;
@@ -120,11 +122,31 @@ cpvs_status check_map_size(uint32_t n, uint32_t min_n) {
     return CPVS_OK;
 }
 
-// Device copy of a host or device input; `owned` tells whether to free it.
+// The address under which the GPU reads host memory `p` in place, or null:
+// pinned / registered memory through its mapped address, and, where the GPU
+// walks the host page tables (Grace-class hosts), any host pointer.
+void* host_accessible(const cpvs::Ctx& c, const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+    if (a.type == cudaMemoryTypeUnregistered && c.pageable_access) return const_cast<void*>(p);
+    return nullptr;
+}
+
+// Device view of a host or device input: used in place when the GPU can read
+// it, else copied to scratch (`owned` then tells to free it).
 cpvs_status stage_in(cpvs::Ctx& c, const void* src, uint64_t bytes, uint32_t flags, cudaStream_t st, void** dev,
                      bool* owned) {
     if (flags & CPVS_IO_DEVICE) {
         *dev = const_cast<void*>(src);
+        *owned = false;
+        return CPVS_OK;
+    }
+    if (void* in_place = host_accessible(c, src)) {
+        *dev = in_place;
         *owned = false;
         return CPVS_OK;
     }
@@ -150,24 +172,38 @@ cpvs_status lookup_common(cpvs_ctx* ctx, const void* xyz, uint64_t n, uint32_t* 
     r = stage_in(c, xyz, qbytes, flags, st, &q, &qowned);
     if (r != CPVS_OK) return r;
     uint32_t* bits = bits_out;
-    bool bowned = false;
+    bool bowned = false, host_out = false;
     if (!(flags & CPVS_IO_DEVICE)) {
-        r = c.alloc((void**)&bits, bbytes, false, st);
-        if (r != CPVS_OK) {
-            if (qowned) c.release(q, qbytes, false, st);
-            return r;
+        host_out = true;
+        bits = static_cast<uint32_t*>(host_accessible(c, bits_out));
+        if (!bits) {
+            r = c.alloc((void**)&bits, bbytes, false, st);
+            if (r != CPVS_OK) {
+                if (qowned) c.release(q, qbytes, false, st);
+                return r;
+            }
+            bowned = true;
         }
-        bowned = true;
     }
     r = run(q, bits);
-    if (r == CPVS_OK && bowned) {
-        cudaError_t e = cudaMemcpyAsync(bits_out, bits, bbytes, cudaMemcpyDeviceToHost, st);
+    if (r == CPVS_OK && host_out) {
+        cudaError_t e = bowned ? cudaMemcpyAsync(bits_out, bits, bbytes, cudaMemcpyDeviceToHost, st) : cudaSuccess;
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) r = cpvs::cuda_fail(e, "lookup read-back");
     }
     if (qowned) c.release(q, std::max<uint64_t>(qbytes, 4), false, st);
     if (bowned) c.release(bits, bbytes, false, st);
     return r;
+}
+
+// Queries per thread for a lookup on `s`: the context's fixed choice, or the
+// tuned one for this DAG depth (tuned on the first batch that needs it).
+int lookup_qpt(const cpvs_shadow* s, const void* q, bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st) {
+    cpvs::Ctx& c = s->ctx->c;
+    if (c.lookup_qpt) return c.lookup_qpt;
+    int& t = c.lookup_qpt_tuned[s->num_levels % CPVS_MAX_LEVELS][ndc ? 1 : 0];
+    if (!t) t = cpvs::tune_lookup(s->dag, s->words, s->num_levels, s->leafmasks, s->top, q, ndc, n, bits, st);
+    return t;
 }
 
 }  // namespace
@@ -222,6 +258,9 @@ cpvs_status cpvs_ctx_create(int device, cpvs_ctx** out) {
     c->c.pool = pool;
     c->c.free_stream = fs;
     cudaDeviceGetAttribute(&c->c.num_sms, cudaDevAttrMultiProcessorCount, device);
+    int pageable = 0;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device);
+    c->c.pageable_access = pageable != 0;
     *out = c;
     return CPVS_OK;
 }
@@ -246,6 +285,26 @@ cpvs_status cpvs_ctx_set_budget(cpvs_ctx* ctx, uint64_t bytes) {
 }
 
 uint64_t cpvs_ctx_bytes_in_use(const cpvs_ctx* ctx) { return ctx ? ctx->c.in_use + ctx->c.scratch : 0; }
+
+cpvs_status cpvs_ctx_set_option(cpvs_ctx* ctx, cpvs_option key, int64_t value) {
+    if (!ctx) return fail(CPVS_ERR_INVALID_ARG, "null ctx");
+    switch (key) {
+        case CPVS_OPT_LOOKUP_QUERIES_PER_THREAD:
+            if (value != 0 && value != 1 && value != 2 && value != 4)
+                return fail(CPVS_ERR_INVALID_ARG, "lookup queries per thread must be 0 (tuned), 1, 2 or 4");
+            ctx->c.lookup_qpt = (int)value;
+            return CPVS_OK;
+    }
+    return fail(CPVS_ERR_INVALID_ARG, "unknown option");
+}
+
+int64_t cpvs_ctx_get_option(const cpvs_ctx* ctx, cpvs_option key) {
+    if (!ctx) return -1;
+    switch (key) {
+        case CPVS_OPT_LOOKUP_QUERIES_PER_THREAD: return ctx->c.lookup_qpt;
+    }
+    return -1;
+}
 
 cpvs_status cpvs_ctx_enable_timing(cpvs_ctx* ctx, int on) {
     if (!ctx) return fail(CPVS_ERR_INVALID_ARG, "null ctx");
@@ -368,16 +427,27 @@ cpvs_status cpvs_shadow_create(cpvs_ctx* ctx, const cpvs_hierarchy* h, uint32_t 
     if (r != CPVS_OK) {
         if (bo.dag) {
             cudaStreamSynchronize((cudaStream_t)stream);
-            ctx->c.release(bo.dag, std::max<uint64_t>(bo.dag_words, 1) * 4, true, nullptr);
+            ctx->c.release(bo.dag, (bo.dag_words + cpvs::kDagPad) * 4, true, nullptr);
         }
         return r;
     }
     auto* s = new cpvs_shadow;
-    s->touch((cudaStream_t)stream);
     s->ctx = ctx;
     s->dag = bo.dag;
     s->words = bo.dag_words;
-    s->bytes = std::max<uint64_t>(bo.dag_words, 1) * 4;
+    s->bytes = (bo.dag_words + cpvs::kDagPad) * 4;
+    const int depth = cpvs::top_index_depth(nl, leaf);
+    if (depth > 0) {
+        s->top_bytes = uint64_t(4) << (3 * depth);
+        r = ctx->c.alloc((void**)&s->top, s->top_bytes, true, (cudaStream_t)stream);
+        if (r == CPVS_OK) r = cpvs::launch_top_index(s->dag, s->words, nl, leaf, s->top, (cudaStream_t)stream);
+        if (r != CPVS_OK) {
+            s->touch((cudaStream_t)stream);
+            cpvs_shadow_destroy(s);
+            return r;
+        }
+    }
+    s->touch((cudaStream_t)stream);
     s->num_levels = nl;
     s->leafmasks = leaf;
     s->root_mask = bo.root_mask[0];
@@ -406,6 +476,7 @@ void cpvs_shadow_destroy(cpvs_shadow* s) {
     if (!s) return;
     cudaSetDevice(s->ctx->c.device);
     s->ctx->c.release(s->dag, s->bytes, true, nullptr, s->last_use);
+    if (s->top) s->ctx->c.release(s->top, s->top_bytes, true, nullptr, s->last_use);
     delete s;
 }
 
@@ -452,8 +523,8 @@ cpvs_status cpvs_shadow_lookup_ndc(const cpvs_shadow* s, const float* xyz, uint6
     if (!s) return fail(CPVS_ERR_INVALID_ARG, "lookup_ndc: null shadow");
     cudaStream_t st = (cudaStream_t)stream;
     return lookup_common(s->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
-        cpvs_status r = cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, q, true, n, bits, st,
-                                            &s->ctx->c.timing);
+        cpvs_status r = cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, s->top, q, true, n, bits,
+                                            st, &s->ctx->c.timing, lookup_qpt(s, q, true, n, bits, st));
         s->touch(st);
         return r;
     });
@@ -464,8 +535,8 @@ cpvs_status cpvs_shadow_lookup_voxel(const cpvs_shadow* s, const int32_t* xyz, u
     if (!s) return fail(CPVS_ERR_INVALID_ARG, "lookup_voxel: null shadow");
     cudaStream_t st = (cudaStream_t)stream;
     return lookup_common(s->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
-        cpvs_status r = cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, q, false, n, bits, st,
-                                            &s->ctx->c.timing);
+        cpvs_status r = cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, s->top, q, false, n,
+                                            bits, st, &s->ctx->c.timing, lookup_qpt(s, q, false, n, bits, st));
         s->touch(st);
         return r;
     });
@@ -486,7 +557,7 @@ cpvs_status cpvs_grid_create(cpvs_ctx* ctx, uint32_t length, cpvs_grid** out) {
 
 static void grid_release_device(cpvs_grid* g) {
     cpvs::Ctx& c = g->ctx->c;
-    if (g->dag) c.release(g->dag, std::max<uint64_t>(g->words, 1) * 4, true, nullptr, g->last_use);
+    if (g->dag) c.release(g->dag, (g->words + cpvs::kDagPad) * 4, true, nullptr, g->last_use);
     if (g->cell_words) c.release(g->cell_words, g->cells.size() * 4, true, nullptr, g->last_use);
     g->dag = nullptr;
     g->cell_words = nullptr;
@@ -548,8 +619,10 @@ cpvs_status cpvs_grid_finalize(cpvs_grid* g, int release_cells, void* stream) {
     }
     grid_release_device(g);
     cpvs::Ctx& c = g->ctx->c;
-    r = c.alloc((void**)&g->dag, std::max<uint64_t>(total, 1) * 4, true, st);
+    r = c.alloc((void**)&g->dag, (total + cpvs::kDagPad) * 4, true, st);
     if (r != CPVS_OK) return r;
+    g->words = total;
+    CPVS_CUDA(cudaMemsetAsync(g->dag + total, 0, cpvs::kDagPad * 4, st));
     r = c.alloc((void**)&g->cell_words, g->cells.size() * 4, true, st);
     if (r != CPVS_OK) {
         grid_release_device(g);

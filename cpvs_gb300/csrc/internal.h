@@ -12,6 +12,15 @@
 #define CPVS_MAX_LEVELS 18
 
 namespace cpvs {
+// Every resident DAG buffer carries this many zeroed words past its last
+// word, so a node's mask and child slots can be read once its offset is
+// known to lie inside the DAG.
+constexpr uint64_t kDagPad = 16;
+// Levels below the root replaced by the dense top index in lookups.
+constexpr int kTopIndexDepth = 4;
+}  // namespace cpvs
+
+namespace cpvs {
 
 // Records `msg` as this thread's last error and returns `s`.
 cpvs_status fail(cpvs_status s, const std::string& msg);
@@ -83,8 +92,19 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
 void destroy_plans(Ctx& ctx);
 
 // -------------------------------------------------------------- lookup
-cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks, const void* xyz,
-                          bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st, Timing* timing = nullptr);
+// Depth of the top index of a DAG (0: none) and its build: 8^depth words.
+int top_index_depth(uint32_t num_levels, bool leafmasks);
+cpvs_status launch_top_index(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks,
+                             uint32_t* out, cudaStream_t st);
+// `top` may be null (no top index).
+// Times queries_per_thread = 1, 2, 4 on the first 2^20 queries (writing
+// their bits) and returns the fastest.
+int tune_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks, const uint32_t* top,
+                const void* xyz, bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st);
+// `queries_per_thread` (1, 2 or 4): independent descents each thread carries.
+cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks,
+                          const uint32_t* top, const void* xyz, bool ndc, uint64_t n, uint32_t* bits,
+                          cudaStream_t st, Timing* timing = nullptr, int queries_per_thread = 4);
 cpvs_status launch_grid_lookup(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
                                uint32_t dag_levels, bool leafmasks, const float* xyz, uint64_t n, uint32_t* bits,
                                cudaStream_t st, Timing* timing = nullptr);
@@ -144,6 +164,11 @@ struct Ctx {
     Timing timing;
     int device = 0;
     int num_sms = 0;
+    bool pageable_access = false;  // the GPU reads pageable host memory in place
+    // lookup queries per thread: fixed by cpvs_ctx_set_option, else tuned
+    // once per (DAG levels, NDC or voxel input)
+    int lookup_qpt = 0;
+    int lookup_qpt_tuned[CPVS_MAX_LEVELS][2] = {{0}};
     uint64_t budget = 0;   // 0 = unlimited
     uint64_t in_use = 0;   // persistent bytes (hierarchies, DAGs, grids)
     uint64_t scratch = 0;  // stream-ordered build / staging scratch

@@ -8,81 +8,256 @@
 // stop at a lit or shadowed child, and finish in the 64-bit leafmask.  The
 // answer of 32 consecutive queries is packed by one ballot into one word.
 //
-// The DAG (9.4 MB for an 8192^2 map) stays in L2; the hops are dependent
-// 4-byte loads, so the kernel is latency- and L2-bound rather than HBM-bound.
-// Every query issues its loads through the read-only path (__ldg).
+// The descent is a chain of dependent L1/L2 hits (an 8192^2 map's DAG is
+// 9.4 MB), so every hop is kept short -- 32-bit offsets, one bounds check
+// per node (DAG buffers carry a zeroed tail of kDagPad words, so both reads
+// of a node stay inside the buffer once its offset is), and the child's
+// 2-bit class and rank from one shift and one popcount.  The first levels
+// below the root are replaced by a dense "top index" (8^depth words: the
+// node offset reached after `depth` hops, or a lit/shadow sentinel) staged
+// in shared memory by every CTA -- and each thread carries Q independent
+// queries (Q picked per DAG depth by timing Q = 1, 2, 4 on the first batch).
 #include "common.cuh"
 
 namespace cpvs {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr uint32_t kCellShadow = 0xFFFFFFFFu, kCellLit = 0xFFFFFFFEu;
 
 __device__ __forceinline__ int32_t quantise(float v, float scale) {
     const float t = __fmul_rn(__fadd_rn(v, 1.0f), 0.5f);
     return __float2int_rz(__fmul_rn(t, scale));
 }
 
-// Descent from word `base` (the DAG's root) with pointers relative to
-// `base`.  Returns true when the voxel is lit.  Every read is checked
-// against `words` (the buffer's size), so a malformed DAG cannot make the
-// kernel read outside it; such a query answers "shadow".
-__device__ __forceinline__ bool descend(const uint32_t* __restrict__ dag, uint64_t words, uint32_t base,
-                                        int num_levels, bool leafmasks, int32_t px, int32_t py, int32_t pz) {
-    uint64_t off = base;
-    const int min_level = leafmasks ? 3 : 0;
-    for (int level = num_levels - 2; level >= min_level; --level) {
-        const int32_t bit = 1 << level;
-        const uint32_t c = ((px & bit) ? 1u : 0u) | ((py & bit) ? 2u : 0u) | ((pz & bit) ? 4u : 0u);
+// 2 * child index at `level`: bit `level` of x, y, z at weights 2, 4, 8.
+__device__ __forceinline__ uint32_t child2(int32_t px, int32_t py, int32_t pz, int level) {
+    return (((uint32_t)px >> level) & 1u) * 2u + (((uint32_t)py >> level) & 1u) * 4u +
+           (((uint32_t)pz >> level) & 1u) * 8u;
+}
+
+// Descent from node `off` at `level` down to the leafmask, pointers relative
+// to `base` (the DAG's first word).  Returns true when the voxel is lit.  A
+// node offset outside the DAG (a malformed buffer) answers "shadow".
+__device__ __forceinline__ bool descend(const uint32_t* __restrict__ dag, uint32_t words, uint32_t base,
+                                        uint32_t off, int level, int min_level, bool leafmasks, int32_t px,
+                                        int32_t py, int32_t pz) {
+    for (; level >= min_level; --level) {
         if (off >= words) return false;
+        const uint32_t c2 = child2(px, py, pz, level);
         const uint32_t m = __ldg(dag + off);
-        const uint32_t v = (m >> (2u * c)) & 3u;
+        const uint32_t v = (m >> c2) & 3u;
         if (v != kPartial) return v == kVisible;
-        const uint64_t slot = off + 1u + child_rank(m, c);
-        if (slot >= words) return false;
-        off = (uint64_t)base + __ldg(dag + slot);
+        // rank among partial children = popcount of the partial bits below c2
+        const uint32_t rank = __popc(m & 0xAAAAu & ((1u << c2) - 1u));
+        off = base + __ldg(dag + off + 1u + rank);
     }
     if (!leafmasks) return true;  // unreachable: level 0 has no partial children
     if (off >= words) return false;
-    const uint32_t c = (uint32_t)(pz & 7);
+    const uint32_t c2 = ((uint32_t)pz & 7u) * 2u;
     const uint32_t m = __ldg(dag + off);
-    const uint32_t v = (m >> (2u * c)) & 3u;
+    const uint32_t v = (m >> c2) & 3u;
     if (v != kPartial) return v == kVisible;
-    const uint32_t b = (uint32_t)((px & 7) + 8 * (py & 7));
-    const uint64_t idx = off + child_rank(m, c) * 2u + 1u + (b >> 5);
-    if (idx >= words) return false;
-    const uint32_t w = __ldg(dag + idx);
+    const uint32_t rank = __popc(m & 0xAAAAu & ((1u << c2) - 1u));
+    const uint32_t b = ((uint32_t)px & 7u) + 8u * ((uint32_t)py & 7u);
+    const uint32_t w = __ldg(dag + off + 1u + 2u * rank + (b >> 5));
     return (w >> (b & 31u)) & 1u;
 }
 
-template <bool NDC>
+// Top index: entry for the `depth` child indices taken below the root
+// (most significant first) = the node offset reached, or a sentinel when the
+// descent ended in a lit or shadowed child on the way.
+__global__ void k_top_index(const uint32_t* __restrict__ dag, uint32_t words, int depth, uint32_t* __restrict__ out) {
+    const uint32_t cells = 1u << (3 * depth);
+    for (uint32_t cell = blockIdx.x * blockDim.x + threadIdx.x; cell < cells; cell += gridDim.x * blockDim.x) {
+        uint32_t off = 0, entry = 0;
+        bool done = false;
+        for (int d = 0; d < depth; ++d) {
+            const uint32_t c = (cell >> (3 * (depth - 1 - d))) & 7u;
+            if (off >= words) {
+                entry = kCellShadow;
+                done = true;
+                break;
+            }
+            const uint32_t m = dag[off];
+            const uint32_t v = (m >> (2u * c)) & 3u;
+            if (v != kPartial) {
+                entry = (v == kVisible) ? kCellLit : kCellShadow;
+                done = true;
+                break;
+            }
+            off = dag[off + 1u + __popc(m & 0xAAAAu & ((1u << (2u * c)) - 1u))];
+        }
+        out[cell] = done ? entry : off;
+    }
+}
+
+// Q queries per thread, carried through the levels in lockstep so that each
+// level issues Q independent loads (the descent is a chain of dependent
+// L1/L2 hits, so memory-level parallelism per thread sets the rate).  Query
+// q of a thread is i = (w*Q + q)*32 + lane: each of the Q ballots packs 32
+// consecutive queries into one output word.
+template <bool NDC, int Q>
 __global__ void __launch_bounds__(kThreads)
-    k_lookup(const uint32_t* __restrict__ dag, uint64_t words, int num_levels, bool leafmasks,
-             const void* __restrict__ q, uint64_t n, uint32_t* __restrict__ bits) {
+    k_lookup(const uint32_t* __restrict__ dag, uint32_t words, int num_levels, bool leafmasks,
+             const uint32_t* __restrict__ top, int depth, const void* __restrict__ q, uint64_t n,
+             uint32_t* __restrict__ bits) {
+    extern __shared__ uint32_t s_top[];
+    const uint32_t cells = depth > 0 ? (1u << (3 * depth)) : 0u;
+    for (uint32_t i = threadIdx.x; i < cells; i += blockDim.x) s_top[i] = __ldg(top + i);
+    __syncthreads();
     const int lane = threadIdx.x & 31;
+    const int root = num_levels - 2, min_level = leafmasks ? 3 : 0;
     const uint64_t nwords = (n + 31) / 32;
+    const uint64_t ngroups = (nwords + Q - 1) / Q;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const float scale = (float)((1u << (num_levels - 1)) - 1u);
-    for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwords; w += nw) {
-        const uint64_t i = w * 32 + (uint64_t)lane;
-        bool lit = false;
-        if (i < n) {
-            int32_t px, py, pz;
-            if (NDC) {
-                const float* p = static_cast<const float*>(q) + 3 * i;
-                px = quantise(p[0], scale);
-                py = quantise(p[1], scale);
-                pz = quantise(p[2], scale);
-            } else {
-                const int32_t* p = static_cast<const int32_t*>(q) + 3 * i;
-                px = p[0];
-                py = p[1];
-                pz = p[2];
+    if (Q == 1) {
+        // one query per thread, each descending on its own
+        for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwords; w += nw) {
+            const uint64_t i = w * 32 + (uint64_t)lane;
+            bool lit = false;
+            if (i < n) {
+                int32_t px, py, pz;
+                if (NDC) {
+                    const float* p = static_cast<const float*>(q) + 3 * i;
+                    px = quantise(p[0], scale);
+                    py = quantise(p[1], scale);
+                    pz = quantise(p[2], scale);
+                } else {
+                    const int32_t* p = static_cast<const int32_t*>(q) + 3 * i;
+                    px = p[0];
+                    py = p[1];
+                    pz = p[2];
+                }
+                uint32_t off = 0;
+                int level = root;
+                bool done = false;
+                if (depth > 0) {
+                    uint32_t cell = 0;
+                    for (int d = 0; d < depth; ++d) cell = (cell << 3) | (child2(px, py, pz, root - d) >> 1);
+                    const uint32_t e = s_top[cell];
+                    if (e >= kCellLit) {
+                        lit = (e == kCellLit);
+                        done = true;
+                    } else {
+                        off = e;
+                        level = root - depth;
+                    }
+                }
+                if (!done) lit = descend(dag, words, 0u, off, level, min_level, leafmasks, px, py, pz);
             }
-            lit = descend(dag, words, 0u, num_levels, leafmasks, px, py, pz);
+            const uint32_t word = __ballot_sync(0xffffffffu, lit);
+            if (lane == 0) bits[w] = word;
         }
-        const uint32_t word = __ballot_sync(0xffffffffu, lit);
-        if (lane == 0) bits[w] = word;
+        return;
+    }
+    for (uint64_t gidx = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; gidx < ngroups; gidx += nw) {
+        int32_t px[Q], py[Q], pz[Q];
+        uint32_t off[Q];
+        bool done[Q], lit[Q];
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            const uint64_t i = (gidx * Q + k) * 32 + (uint64_t)lane;
+            done[k] = true;
+            lit[k] = false;
+            off[k] = 0;
+            px[k] = py[k] = pz[k] = 0;
+            if (i < n) {
+                if (NDC) {
+                    const float* p = static_cast<const float*>(q) + 3 * i;
+                    px[k] = quantise(p[0], scale);
+                    py[k] = quantise(p[1], scale);
+                    pz[k] = quantise(p[2], scale);
+                } else {
+                    const int32_t* p = static_cast<const int32_t*>(q) + 3 * i;
+                    px[k] = p[0];
+                    py[k] = p[1];
+                    pz[k] = p[2];
+                }
+                done[k] = false;
+            }
+        }
+        int level = root;
+        if (depth > 0) {
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                if (done[k]) continue;
+                uint32_t cell = 0;
+                for (int d = 0; d < depth; ++d) cell = (cell << 3) | (child2(px[k], py[k], pz[k], root - d) >> 1);
+                const uint32_t e = s_top[cell];
+                if (e >= kCellLit) {
+                    lit[k] = (e == kCellLit);
+                    done[k] = true;
+                } else {
+                    off[k] = e;
+                }
+            }
+            level = root - depth;
+        }
+        for (; level >= min_level; --level) {
+            uint32_t m[Q];
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                if (!done[k] && off[k] >= words) {
+                    done[k] = true;  // malformed DAG: shadow
+                    lit[k] = false;
+                }
+                m[k] = done[k] ? 0u : __ldg(dag + off[k]);
+            }
+            uint32_t slot[Q];
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                slot[k] = 0;
+                if (done[k]) continue;
+                const uint32_t c2 = child2(px[k], py[k], pz[k], level);
+                const uint32_t v = (m[k] >> c2) & 3u;
+                if (v != kPartial) {
+                    lit[k] = (v == kVisible);
+                    done[k] = true;
+                } else {
+                    slot[k] = off[k] + 1u + __popc(m[k] & 0xAAAAu & ((1u << c2) - 1u));
+                }
+            }
+            bool any = false;
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                if (!done[k]) off[k] = __ldg(dag + slot[k]);
+                any |= !done[k];
+            }
+            if (!__any_sync(0xffffffffu, any)) break;
+        }
+        if (leafmasks) {
+            uint32_t m[Q];
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                if (!done[k] && off[k] >= words) {
+                    done[k] = true;
+                    lit[k] = false;
+                }
+                m[k] = done[k] ? 0u : __ldg(dag + off[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                if (done[k]) continue;
+                const uint32_t c2 = ((uint32_t)pz[k] & 7u) * 2u;
+                const uint32_t v = (m[k] >> c2) & 3u;
+                if (v != kPartial) {
+                    lit[k] = (v == kVisible);
+                } else {
+                    const uint32_t rank = __popc(m[k] & 0xAAAAu & ((1u << c2) - 1u));
+                    const uint32_t b = ((uint32_t)px[k] & 7u) + 8u * ((uint32_t)py[k] & 7u);
+                    const uint32_t w = __ldg(dag + off[k] + 1u + 2u * rank + (b >> 5));
+                    lit[k] = (w >> (b & 31u)) & 1u;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            const uint32_t word = __ballot_sync(0xffffffffu, lit[k]);
+            const uint64_t wi = gidx * Q + k;
+            if (lane == 0 && wi < nwords) bits[wi] = word;
+        }
     }
 }
 
@@ -90,10 +265,11 @@ __global__ void __launch_bounds__(kThreads)
 // 2^(dag_levels+grid_levels-1), its top bits select the cell, the cell word
 // holds the DAG offset or a uniform-cell sentinel.
 __global__ void __launch_bounds__(kThreads)
-    k_grid_lookup(const uint32_t* __restrict__ dag, uint64_t words, const uint32_t* __restrict__ cells, uint32_t length,
-                  int dag_levels, int grid_levels, bool leafmasks, const float* __restrict__ q, uint64_t n,
-                  uint32_t* __restrict__ bits) {
+    k_grid_lookup(const uint32_t* __restrict__ dag, uint32_t words, const uint32_t* __restrict__ cells,
+                  uint32_t length, int dag_levels, int grid_levels, bool leafmasks, const float* __restrict__ q,
+                  uint64_t n, uint32_t* __restrict__ bits) {
     const int lane = threadIdx.x & 31;
+    const int root = dag_levels - 2, min_level = leafmasks ? 3 : 0;
     const uint64_t nwords = (n + 31) / 32;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const float scale = (float)((1u << (dag_levels + grid_levels - 1)) - 1u);
@@ -108,12 +284,12 @@ __global__ void __launch_bounds__(kThreads)
                 lit = true;
             } else {
                 const uint32_t cell = __ldg(cells + ((size_t)gz * length + gy) * length + gx);
-                if (cell == 0xFFFFFFFFu)
+                if (cell == kCellShadow)
                     lit = false;
-                else if (cell == 0xFFFFFFFEu)
+                else if (cell == kCellLit)
                     lit = true;
                 else
-                    lit = descend(dag, words, cell, dag_levels, leafmasks, px, py, pz);
+                    lit = descend(dag, words, cell, cell, root, min_level, leafmasks, px, py, pz);
             }
         }
         const uint32_t word = __ballot_sync(0xffffffffu, lit);
@@ -124,26 +300,93 @@ __global__ void __launch_bounds__(kThreads)
 uint32_t lookup_grid(int num_sms, uint64_t n) {
     const uint64_t warps = (n + 31) / 32;
     const uint64_t blocks = (warps * 32 + kThreads - 1) / kThreads;
-    const uint64_t cap = (uint64_t)(num_sms > 0 ? num_sms : 152) * 16;
+    const uint64_t cap = (uint64_t)(num_sms > 0 ? num_sms : 152) * 8;
     return (uint32_t)(blocks < 1 ? 1 : (blocks < cap ? blocks : cap));
+}
+
+int device_sms() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
 }
 
 }  // namespace
 
-cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks, const void* xyz,
-                          bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st, Timing* timing) {
-    if (n == 0) return CPVS_OK;
-    KernelTimer kt(timing, K_LOOKUP, st);
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const uint32_t g = lookup_grid(sms, n);
-    if (ndc)
-        k_lookup<true><<<g, kThreads, 0, st>>>(dag, words, (int)num_levels, leafmasks, xyz, n, bits);
-    else
-        k_lookup<false><<<g, kThreads, 0, st>>>(dag, words, (int)num_levels, leafmasks, xyz, n, bits);
+int top_index_depth(uint32_t num_levels, bool leafmasks) {
+    const int root = (int)num_levels - 2, min_level = leafmasks ? 3 : 0;
+    const int d = root - min_level + 1;
+    return d < 0 ? 0 : (d > kTopIndexDepth ? kTopIndexDepth : d);
+}
+
+cpvs_status launch_top_index(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks,
+                             uint32_t* out, cudaStream_t st) {
+    const int depth = top_index_depth(num_levels, leafmasks);
+    if (depth == 0) return CPVS_OK;
+    const uint32_t cells = 1u << (3 * depth);
+    k_top_index<<<(cells + 255) / 256, 256, 0, st>>>(dag, (uint32_t)words, depth, out);
     CPVS_CUDA(cudaGetLastError());
     return CPVS_OK;
+}
+
+template <bool NDC, int Q>
+void launch_lookup_q(uint32_t g, size_t smem, cudaStream_t st, const uint32_t* dag, uint64_t words,
+                     uint32_t num_levels, bool leafmasks, const uint32_t* top, int depth, const void* xyz, uint64_t n,
+                     uint32_t* bits) {
+    k_lookup<NDC, Q><<<g, kThreads, smem, st>>>(dag, (uint32_t)words, (int)num_levels, leafmasks, top, depth, xyz, n,
+                                                bits);
+}
+
+cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks,
+                          const uint32_t* top, const void* xyz, bool ndc, uint64_t n, uint32_t* bits,
+                          cudaStream_t st, Timing* timing, int queries_per_thread) {
+    if (n == 0) return CPVS_OK;
+    KernelTimer kt(timing, K_LOOKUP, st);
+    const int Q = (queries_per_thread == 1 || queries_per_thread == 2) ? queries_per_thread : 4;
+    const uint32_t g = lookup_grid(device_sms(), (n + Q - 1) / Q);
+    const int depth = top ? top_index_depth(num_levels, leafmasks) : 0;
+    const size_t smem = depth ? (size_t(4) << (3 * depth)) : 0;
+    if (ndc) {
+        if (Q == 1) launch_lookup_q<true, 1>(g, smem, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
+        else if (Q == 2) launch_lookup_q<true, 2>(g, smem, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
+        else launch_lookup_q<true, 4>(g, smem, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
+    } else {
+        if (Q == 1) launch_lookup_q<false, 1>(g, smem, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
+        else if (Q == 2) launch_lookup_q<false, 2>(g, smem, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
+        else launch_lookup_q<false, 4>(g, smem, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
+    }
+    CPVS_CUDA(cudaGetLastError());
+    return CPVS_OK;
+}
+
+int tune_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks, const uint32_t* top,
+                const void* xyz, bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st) {
+    const uint64_t sample = n < (1ull << 20) ? n : (1ull << 20);
+    cudaEvent_t a = nullptr, b = nullptr;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+        cudaGetLastError();
+        return 4;
+    }
+    int best = 4;
+    float best_ms = 1e30f;
+    for (int q : {1, 2, 4}) {
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; ++rep) {  // the first run warms the caches
+            cudaEventRecord(a, st);
+            launch_lookup(dag, words, num_levels, leafmasks, top, xyz, ndc, sample, bits, st, nullptr, q);
+            cudaEventRecord(b, st);
+            cudaEventSynchronize(b);
+            cudaEventElapsedTime(&ms, a, b);
+        }
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = q;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaGetLastError();
+    return best;
 }
 
 cpvs_status launch_grid_lookup(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
@@ -151,12 +394,9 @@ cpvs_status launch_grid_lookup(const uint32_t* dag, uint64_t words, const uint32
                                cudaStream_t st, Timing* timing) {
     if (n == 0) return CPVS_OK;
     KernelTimer kt(timing, K_GRID_LOOKUP, st);
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const uint32_t g = lookup_grid(sms, n);
-    k_grid_lookup<<<g, kThreads, 0, st>>>(dag, words, cells, length, (int)dag_levels, log2_u32(length), leafmasks, xyz, n,
-                                          bits);
+    const uint32_t g = lookup_grid(device_sms(), n);
+    k_grid_lookup<<<g, kThreads, 0, st>>>(dag, (uint32_t)words, cells, length, (int)dag_levels, log2_u32(length),
+                                          leafmasks, xyz, n, bits);
     CPVS_CUDA(cudaGetLastError());
     return CPVS_OK;
 }

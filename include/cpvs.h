@@ -83,6 +83,15 @@ CPVS_API void cpvs_ctx_destroy(cpvs_ctx* ctx);
  * CPVS_ERR_BUDGET. */
 CPVS_API cpvs_status cpvs_ctx_set_budget(cpvs_ctx* ctx, uint64_t bytes);
 CPVS_API uint64_t cpvs_ctx_bytes_in_use(const cpvs_ctx* ctx);
+/* Tunable launch shapes.  CPVS_OPT_LOOKUP_QUERIES_PER_THREAD: independent
+ * descents each lookup thread carries (1, 2 or 4); 0 (default) = tuned per
+ * DAG depth by timing the three on the first lookup batch of that depth. */
+typedef enum cpvs_option {
+    CPVS_OPT_LOOKUP_QUERIES_PER_THREAD = 1
+} cpvs_option;
+CPVS_API cpvs_status cpvs_ctx_set_option(cpvs_ctx* ctx, cpvs_option key, int64_t value);
+CPVS_API int64_t cpvs_ctx_get_option(const cpvs_ctx* ctx, cpvs_option key);
+
 /* Per-kernel CUDA-event timing (off by default).  When on, every kernel the
  * context launches is bracketed by an event pair on its stream;
  * cpvs_ctx_kernel_times waits for those events and returns, per kernel id

@@ -147,6 +147,25 @@ def test_c1_config_matches_oracle(cp, oracle):
     assert np.array_equal(sh.lookup_ndc(q), oracle.lookup_ndc(want.dag, want.num_levels, True, q, threads=8))
 
 
+def test_lookup_variants_agree(cp, oracle):
+    """Every queries-per-thread variant of the lookup kernel (and the tuned
+    choice) answers exactly like the oracle, for NDC and voxel input."""
+    d = scene.rasterise(scene.config_scene("c0"))
+    want = oracle.build(d)
+    ctx = cp.Context(0)
+    sh = cp.CompressedShadow.from_depth(d, ctx=ctx)
+    q = scene.ndc_queries_mixed(d, 300_001, 9)
+    v = scene.voxel_queries(200_003, 1024, 9)
+    ref_q = oracle.lookup_ndc(want.dag, want.num_levels, True, q, threads=8)
+    ref_v = oracle.lookup_voxel(want.dag, want.num_levels, True, v, threads=8)
+    for qpt in (0, 1, 2, 4):
+        ctx.set_option(ctx.OPT_LOOKUP_QUERIES_PER_THREAD, qpt)
+        assert np.array_equal(sh.lookup_ndc(q), ref_q), qpt
+        assert np.array_equal(sh.lookup_voxel(v), ref_v), qpt
+    with pytest.raises(cp.CpvsError):
+        ctx.set_option(ctx.OPT_LOOKUP_QUERIES_PER_THREAD, 3)
+
+
 def test_repeated_builds_are_identical(cp):
     d = scene.rasterise(scene.config_scene("c0", n=512))
     a = cp.CompressedShadow.from_depth(d).get_dag()
