@@ -59,6 +59,8 @@ _SIGS = {
     "cpvs_shadow_create": (C.c_int, [_vp, _vp, _u32, _u32, _u32, _vp, C.POINTER(_vp)]),
     "cpvs_shadow_create_from_depth": (C.c_int, [_vp, _vp, _u32, _u32, _u32, _u32, _vp, C.POINTER(_vp)]),
     "cpvs_shadow_destroy": (None, [_vp]),
+    "cpvs_shadow_create_batch": (C.c_int, [_vp, _vp, _u32, _vp, _u32, _u32, _vp, _vp]),
+    "cpvs_grid_build": (C.c_int, [_vp, _vp, _u32, _vp]),
     "cpvs_shadow_num_levels": (_u32, [_vp]),
     "cpvs_shadow_uses_leafmasks": (C.c_int, [_vp]),
     "cpvs_shadow_total_visibility": (C.c_int, [_vp]),
@@ -252,6 +254,10 @@ class MinMaxHierarchy:
             self.handle = None
 
 
+class _BuildJob(C.Structure):
+    _fields_ = [("source", C.c_uint32), ("z_tile_index", C.c_uint32), ("z_tile_num", C.c_uint32)]
+
+
 class CompressedShadow:
     """A resident shadow DAG (src/CompressedShadow.h:20-125)."""
 
@@ -286,6 +292,19 @@ class CompressedShadow:
         _check(_lib.cpvs_shadow_create_from_depth(ctx.handle, _ptr(depth), n, z_tile_index, z_tile_num, flags,
                                                   _stream(stream), C.byref(h)))
         return CompressedShadow(h.value, ctx)
+
+    @staticmethod
+    def create_batch(sources, jobs, leafmasks: bool = True, stream=None) -> list:
+        """Many DAGs in one batch.  `sources`: MinMaxHierarchy list; `jobs`:
+        (source index, z_tile_index, z_tile_num) per DAG.  Returns one
+        CompressedShadow per job."""
+        ctx = sources[0].ctx
+        hs = (_vp * len(sources))(*[m.handle for m in sources])
+        jb = (_BuildJob * len(jobs))(*[_BuildJob(*j) for j in jobs])
+        out = (_vp * len(jobs))()
+        _check(_lib.cpvs_shadow_create_batch(ctx.handle, hs, len(sources), jb, len(jobs),
+                                             FLAG_LEAFMASKS if leafmasks else 0, _stream(stream), out))
+        return [CompressedShadow(out[j], ctx) for j in range(len(jobs))]
 
     def get_num_levels(self) -> int:
         return int(_lib.cpvs_shadow_num_levels(self.handle))
@@ -395,6 +414,13 @@ class CompressedShadowContainer:
 
     def get(self, x: int, y: int, z: int) -> Optional[CompressedShadow]:
         return self._cells.get((x, y, z))
+
+    def build(self, xy_tiles, leafmasks: bool = True, stream=None):
+        """Builds every cell in one batch: cell (x,y,z) = z-tile z of
+        xy_tiles[y*length+x] (MinMaxHierarchy objects of one size)."""
+        hs = (_vp * len(xy_tiles))(*[m.handle for m in xy_tiles])
+        _check(_lib.cpvs_grid_build(self.handle, hs, FLAG_LEAFMASKS if leafmasks else 0, _stream(stream)))
+        self._cells.clear()
 
     def copy_to_gpu(self, stream=None):
         _check(_lib.cpvs_grid_finalize(self.handle, 0, _stream(stream)))

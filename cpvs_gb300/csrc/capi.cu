@@ -78,12 +78,33 @@ struct cpvs_hierarchy : DeviceObject {
     uint64_t bytes = 0;
 };
 
+// Device block holding the DAGs of one build (one or many jobs back to
+// back, followed by kDagPad zeroed words).  Shared by the shadows (and the
+// grid) that point into it; freed when the last of them lets go, after every
+// holder's last use.
+struct DagBlock {
+    cpvs_ctx* ctx = nullptr;
+    uint32_t* base = nullptr;
+    uint64_t bytes = 0;
+    int refs = 0;
+};
+
+void block_unref(DagBlock* b, cudaEvent_t last_use) {
+    if (!b) return;
+    cpvs::Ctx& c = b->ctx->c;
+    if (last_use) cudaStreamWaitEvent(c.free_stream, last_use, 0);  // the free waits for every holder
+    if (--b->refs == 0) {
+        c.release(b->base, b->bytes, true, nullptr, nullptr);
+        delete b;
+    }
+}
+
 struct cpvs_shadow : DeviceObject {
     cpvs_ctx* ctx = nullptr;
-    uint32_t* dag = nullptr;   // words + kDagPad zeroed words
+    DagBlock* block = nullptr;
+    uint32_t* dag = nullptr;   // inside block; at least kDagPad readable words follow it
     uint64_t words = 0;
-    uint64_t bytes = 0;
-    uint32_t* top = nullptr;   // dense top index for lookups (may be null)
+    uint32_t* top = nullptr;   // dense top index for lookups, built on the first lookup
     uint64_t top_bytes = 0;
     uint32_t num_levels = 0;
     bool leafmasks = false;
@@ -95,6 +116,7 @@ struct cpvs_grid : DeviceObject {
     cpvs_ctx* ctx = nullptr;
     uint32_t length = 0;
     std::vector<cpvs_shadow*> cells;
+    DagBlock* block = nullptr;  // the combined DAG
     uint32_t* dag = nullptr;
     uint64_t words = 0;
     uint32_t* cell_words = nullptr;
@@ -194,6 +216,59 @@ cpvs_status lookup_common(cpvs_ctx* ctx, const void* xyz, uint64_t n, uint32_t* 
     if (qowned) c.release(q, std::max<uint64_t>(qbytes, 4), false, st);
     if (bowned) c.release(bits, bbytes, false, st);
     return r;
+}
+
+// Builds `jobs` in one batch and wraps each job's DAG in a shadow; all of
+// them share one device block.  `total` receives the block's DAG words.
+cpvs_status build_into_shadows(cpvs_ctx* ctx, const std::vector<cpvs::SourceSpec>& src,
+                               const std::vector<cpvs::JobSpec>& jobs, bool leaf, cudaStream_t st, DagBlock** block_out,
+                               std::vector<cpvs_shadow*>& out, std::vector<uint64_t>* offsets = nullptr,
+                               uint64_t* total = nullptr) {
+    cpvs::BuildOutput bo;
+    cpvs_status r = cpvs::build_dags(ctx->c, src, jobs, leaf, st, bo);
+    if (r != CPVS_OK) {
+        if (bo.dag) {
+            cudaStreamSynchronize(st);
+            ctx->c.release(bo.dag, (bo.dag_words + cpvs::kDagPad) * 4, true, nullptr);
+        }
+        return r;
+    }
+    auto* b = new DagBlock{ctx, bo.dag, (bo.dag_words + cpvs::kDagPad) * 4, 0};
+    for (size_t j = 0; j < jobs.size(); ++j) {
+        auto* s = new cpvs_shadow;
+        s->ctx = ctx;
+        s->block = b;
+        b->refs++;
+        s->dag = bo.dag + bo.job_offset[j];
+        s->words = bo.job_words[j];
+        s->num_levels = (uint32_t)cpvs::log2_u32(src[jobs[j].source].n) + 1;
+        s->leafmasks = leaf;
+        s->root_mask = bo.root_mask[j];
+        s->tree = bo.tree_nodes[j];
+        s->uniq = bo.unique_nodes[j];
+        s->touch(st);
+        out.push_back(s);
+    }
+    if (offsets) *offsets = bo.job_offset;
+    if (total) *total = bo.dag_words;
+    *block_out = b;
+    return CPVS_OK;
+}
+
+// The shadow's top index, built on its first lookup (stream-ordered).
+void ensure_top(const cpvs_shadow* cs, cudaStream_t st) {
+    cpvs_shadow* s = const_cast<cpvs_shadow*>(cs);
+    if (s->top || s->top_bytes == ~0ull) return;
+    const int depth = cpvs::top_index_depth(s->num_levels, s->leafmasks);
+    if (depth <= 0 || s->ctx->c.alloc((void**)&s->top, uint64_t(4) << (3 * depth), true, st) != CPVS_OK ||
+        cpvs::launch_top_index(s->dag, s->words, s->num_levels, s->leafmasks, s->top, st) != CPVS_OK) {
+        if (s->top) s->ctx->c.release(s->top, uint64_t(4) << (3 * depth), true, st);
+        s->top = nullptr;
+        s->top_bytes = ~0ull;  // look up without it
+        cudaGetLastError();
+        return;
+    }
+    s->top_bytes = uint64_t(4) << (3 * depth);
 }
 
 // Queries per thread for a lookup on `s`: the context's fixed choice, or the
@@ -421,40 +496,60 @@ cpvs_status cpvs_shadow_create(cpvs_ctx* ctx, const cpvs_hierarchy* h, uint32_t 
     const bool leaf = (flags & CPVS_FLAG_LEAFMASKS) && (nl - 3 >= 2);
     std::vector<cpvs::SourceSpec> src{{h->depth, h->levels, h->n}};
     std::vector<cpvs::JobSpec> jobs{{0, z_tile_index, z_tile_num}};
-    cpvs::BuildOutput bo;
-    r = cpvs::build_dags(ctx->c, src, jobs, leaf, (cudaStream_t)stream, bo);
+    DagBlock* block = nullptr;
+    std::vector<cpvs_shadow*> shadows;
+    r = build_into_shadows(ctx, src, jobs, leaf, (cudaStream_t)stream, &block, shadows);
     h->touch((cudaStream_t)stream);
-    if (r != CPVS_OK) {
-        if (bo.dag) {
-            cudaStreamSynchronize((cudaStream_t)stream);
-            ctx->c.release(bo.dag, (bo.dag_words + cpvs::kDagPad) * 4, true, nullptr);
-        }
-        return r;
-    }
-    auto* s = new cpvs_shadow;
-    s->ctx = ctx;
-    s->dag = bo.dag;
-    s->words = bo.dag_words;
-    s->bytes = (bo.dag_words + cpvs::kDagPad) * 4;
-    const int depth = cpvs::top_index_depth(nl, leaf);
-    if (depth > 0) {
-        s->top_bytes = uint64_t(4) << (3 * depth);
-        r = ctx->c.alloc((void**)&s->top, s->top_bytes, true, (cudaStream_t)stream);
-        if (r == CPVS_OK) r = cpvs::launch_top_index(s->dag, s->words, nl, leaf, s->top, (cudaStream_t)stream);
-        if (r != CPVS_OK) {
-            s->touch((cudaStream_t)stream);
-            cpvs_shadow_destroy(s);
-            return r;
-        }
-    }
-    s->touch((cudaStream_t)stream);
-    s->num_levels = nl;
-    s->leafmasks = leaf;
-    s->root_mask = bo.root_mask[0];
-    s->tree = bo.tree_nodes[0];
-    s->uniq = bo.unique_nodes[0];
-    *out = s;
+    if (r != CPVS_OK) return r;
+    *out = shadows[0];
     return CPVS_OK;
+}
+
+cpvs_status cpvs_shadow_create_batch(cpvs_ctx* ctx, const cpvs_hierarchy* const* sources, uint32_t num_sources,
+                                     const cpvs_build_job* jobs, uint32_t num_jobs, uint32_t flags, void* stream,
+                                     cpvs_shadow** out) {
+    if (!ctx || !sources || !jobs || !out) return fail(CPVS_ERR_INVALID_ARG, "create_batch: null argument");
+    for (uint32_t j = 0; j < num_jobs; ++j) out[j] = nullptr;
+    if (num_jobs == 0) return CPVS_OK;
+    std::vector<cpvs::SourceSpec> src(num_sources);
+    for (uint32_t i = 0; i < num_sources; ++i) {
+        if (!sources[i]) return fail(CPVS_ERR_INVALID_ARG, "create_batch: null hierarchy");
+        cpvs_status r = check_map_size(sources[i]->n, 8);
+        if (r != CPVS_OK) return r;
+        src[i] = cpvs::SourceSpec{sources[i]->depth, sources[i]->levels, sources[i]->n};
+    }
+    // jobs grouped by leafmask mode (maps below 16^2 cannot use leafmasks)
+    std::vector<cpvs::JobSpec> group[2];
+    std::vector<uint32_t> index[2];
+    for (uint32_t j = 0; j < num_jobs; ++j) {
+        const cpvs_build_job& jb = jobs[j];
+        if (jb.source >= num_sources) return fail(CPVS_ERR_INVALID_ARG, "create_batch: job source out of range");
+        if (jb.z_tile_num == 0 || jb.z_tile_index >= jb.z_tile_num)
+            return fail(CPVS_ERR_INVALID_ARG, "create_batch: need z_tile_index < z_tile_num");
+        if ((uint64_t)src[jb.source].n * jb.z_tile_num > (1ull << 23))
+            return fail(CPVS_ERR_INVALID_ARG, "create_batch: n * z_tile_num must not exceed 2^23");
+        const uint32_t nl = (uint32_t)cpvs::log2_u32(src[jb.source].n) + 1;
+        const int g = ((flags & CPVS_FLAG_LEAFMASKS) && nl - 3 >= 2) ? 1 : 0;
+        group[g].push_back(cpvs::JobSpec{jb.source, jb.z_tile_index, jb.z_tile_num});
+        index[g].push_back(j);
+    }
+    cpvs_status r = set_device(ctx);
+    if (r != CPVS_OK) return r;
+    for (int g = 0; g < 2 && r == CPVS_OK; ++g) {
+        if (group[g].empty()) continue;
+        DagBlock* block = nullptr;
+        std::vector<cpvs_shadow*> shadows;
+        r = build_into_shadows(ctx, src, group[g], g == 1, (cudaStream_t)stream, &block, shadows);
+        for (size_t k = 0; k < shadows.size(); ++k) out[index[g][k]] = shadows[k];
+    }
+    for (uint32_t i = 0; i < num_sources; ++i) sources[i]->touch((cudaStream_t)stream);
+    if (r != CPVS_OK) {
+        for (uint32_t j = 0; j < num_jobs; ++j) {
+            cpvs_shadow_destroy(out[j]);
+            out[j] = nullptr;
+        }
+    }
+    return r;
 }
 
 cpvs_status cpvs_shadow_create_from_depth(cpvs_ctx* ctx, const float* depth, uint32_t n, uint32_t z_tile_index,
@@ -475,8 +570,8 @@ cpvs_status cpvs_shadow_create_from_depth(cpvs_ctx* ctx, const float* depth, uin
 void cpvs_shadow_destroy(cpvs_shadow* s) {
     if (!s) return;
     cudaSetDevice(s->ctx->c.device);
-    s->ctx->c.release(s->dag, s->bytes, true, nullptr, s->last_use);
     if (s->top) s->ctx->c.release(s->top, s->top_bytes, true, nullptr, s->last_use);
+    block_unref(s->block, s->last_use);
     delete s;
 }
 
@@ -523,6 +618,7 @@ cpvs_status cpvs_shadow_lookup_ndc(const cpvs_shadow* s, const float* xyz, uint6
     if (!s) return fail(CPVS_ERR_INVALID_ARG, "lookup_ndc: null shadow");
     cudaStream_t st = (cudaStream_t)stream;
     return lookup_common(s->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
+        ensure_top(s, st);
         cpvs_status r = cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, s->top, q, true, n, bits,
                                             st, &s->ctx->c.timing, lookup_qpt(s, q, true, n, bits, st));
         s->touch(st);
@@ -535,6 +631,7 @@ cpvs_status cpvs_shadow_lookup_voxel(const cpvs_shadow* s, const int32_t* xyz, u
     if (!s) return fail(CPVS_ERR_INVALID_ARG, "lookup_voxel: null shadow");
     cudaStream_t st = (cudaStream_t)stream;
     return lookup_common(s->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
+        ensure_top(s, st);
         cpvs_status r = cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, s->top, q, false, n,
                                             bits, st, &s->ctx->c.timing, lookup_qpt(s, q, false, n, bits, st));
         s->touch(st);
@@ -557,8 +654,9 @@ cpvs_status cpvs_grid_create(cpvs_ctx* ctx, uint32_t length, cpvs_grid** out) {
 
 static void grid_release_device(cpvs_grid* g) {
     cpvs::Ctx& c = g->ctx->c;
-    if (g->dag) c.release(g->dag, (g->words + cpvs::kDagPad) * 4, true, nullptr, g->last_use);
+    block_unref(g->block, g->last_use);
     if (g->cell_words) c.release(g->cell_words, g->cells.size() * 4, true, nullptr, g->last_use);
+    g->block = nullptr;
     g->dag = nullptr;
     g->cell_words = nullptr;
     g->finalized = false;
@@ -619,8 +717,11 @@ cpvs_status cpvs_grid_finalize(cpvs_grid* g, int release_cells, void* stream) {
     }
     grid_release_device(g);
     cpvs::Ctx& c = g->ctx->c;
-    r = c.alloc((void**)&g->dag, (total + cpvs::kDagPad) * 4, true, st);
+    uint32_t* dag = nullptr;
+    r = c.alloc((void**)&dag, (total + cpvs::kDagPad) * 4, true, st);
     if (r != CPVS_OK) return r;
+    g->block = new DagBlock{g->ctx, dag, (total + cpvs::kDagPad) * 4, 1};
+    g->dag = dag;
     g->words = total;
     CPVS_CUDA(cudaMemsetAsync(g->dag + total, 0, cpvs::kDagPad * 4, st));
     r = c.alloc((void**)&g->cell_words, g->cells.size() * 4, true, st);
@@ -647,6 +748,71 @@ cpvs_status cpvs_grid_finalize(cpvs_grid* g, int release_cells, void* stream) {
             s = nullptr;
         }
     }
+    return CPVS_OK;
+}
+
+cpvs_status cpvs_grid_build(cpvs_grid* g, const cpvs_hierarchy* const* xy_tiles, uint32_t flags, void* stream) {
+    if (!g || !xy_tiles) return fail(CPVS_ERR_INVALID_ARG, "grid_build: null argument");
+    const uint32_t L = g->length;
+    std::vector<cpvs::SourceSpec> src(L * L);
+    for (uint32_t i = 0; i < L * L; ++i) {
+        const cpvs_hierarchy* h = xy_tiles[i];
+        if (!h) return fail(CPVS_ERR_INVALID_ARG, "grid_build: null tile hierarchy");
+        if (h->n != xy_tiles[0]->n) return fail(CPVS_ERR_INVALID_ARG, "grid_build: tiles differ in size");
+        cpvs_status r = check_map_size(h->n, 8);
+        if (r != CPVS_OK) return r;
+        src[i] = cpvs::SourceSpec{h->depth, h->levels, h->n};
+    }
+    if ((uint64_t)src[0].n * L > (1ull << 23)) return fail(CPVS_ERR_INVALID_ARG, "grid_build: n * length must not exceed 2^23");
+    cpvs_status r = set_device(g->ctx);
+    if (r != CPVS_OK) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    // cell (x,y,z) = z-tile z of xy tile (x,y), jobs in cell order z*L^2+y*L+x
+    // (src/DeferredRenderer.cpp:150-187, src/CompressedShadowContainer.h:34-39)
+    std::vector<cpvs::JobSpec> jobs;
+    jobs.reserve((size_t)L * L * L);
+    for (uint32_t z = 0; z < L; ++z)
+        for (uint32_t y = 0; y < L; ++y)
+            for (uint32_t x = 0; x < L; ++x) jobs.push_back(cpvs::JobSpec{y * L + x, z, L});
+    const uint32_t nl = (uint32_t)cpvs::log2_u32(src[0].n) + 1;
+    const bool leaf = (flags & CPVS_FLAG_LEAFMASKS) && (nl - 3 >= 2);
+    DagBlock* block = nullptr;
+    std::vector<cpvs_shadow*> shadows;
+    std::vector<uint64_t> offsets;
+    uint64_t total = 0;
+    r = build_into_shadows(g->ctx, src, jobs, leaf, st, &block, shadows, &offsets, &total);
+    for (uint32_t i = 0; i < L * L; ++i) xy_tiles[i]->touch(st);
+    if (r != CPVS_OK) return r;
+    if (total >= 0xFFFFFFFEull) {
+        for (auto* sh : shadows) cpvs_shadow_destroy(sh);
+        return fail(CPVS_ERR_BUDGET, "grid_build: combined DAG exceeds 2^32-2 words");
+    }
+    std::vector<uint32_t> cellw(jobs.size());
+    for (size_t i = 0; i < jobs.size(); ++i) {
+        const uint32_t m = shadows[i]->root_mask;
+        cellw[i] = (m == 0u) ? 0xFFFFFFFFu : (m == 0x5555u ? 0xFFFFFFFEu : (uint32_t)offsets[i]);
+    }
+    for (auto*& c : g->cells) {
+        cpvs_shadow_destroy(c);
+        c = nullptr;
+    }
+    grid_release_device(g);
+    r = g->ctx->c.alloc((void**)&g->cell_words, g->cells.size() * 4, true, st);
+    if (r != CPVS_OK) {
+        for (auto* sh : shadows) cpvs_shadow_destroy(sh);
+        return r;
+    }
+    CPVS_CUDA(cudaMemcpyAsync(g->cell_words, cellw.data(), cellw.size() * 4, cudaMemcpyHostToDevice, st));
+    g->block = block;
+    block->refs++;
+    g->dag = block->base;
+    g->words = total;
+    for (size_t i = 0; i < jobs.size(); ++i) g->cells[i] = shadows[i];
+    g->dag_levels = nl;
+    g->leafmasks = leaf;
+    g->finalized = true;
+    g->touch(st);
+    CPVS_CUDA(cudaStreamSynchronize(st));  // the host staging above leaves scope
     return CPVS_OK;
 }
 

@@ -137,6 +137,24 @@ CPVS_API cpvs_status cpvs_hierarchy_level(const cpvs_hierarchy* h, uint32_t leve
  * reference's getDAG() whenever the reference's own build is defined. */
 CPVS_API cpvs_status cpvs_shadow_create(cpvs_ctx* ctx, const cpvs_hierarchy* h, uint32_t z_tile_index, uint32_t z_tile_num,
                                uint32_t flags, void* stream, cpvs_shadow** out);
+/* One DAG of a batch: z-tile `z_tile_index` of `z_tile_num` of hierarchy
+ * `source`. */
+typedef struct cpvs_build_job {
+    uint32_t source;
+    uint32_t z_tile_index;
+    uint32_t z_tile_num;
+} cpvs_build_job;
+
+/* Builds many DAGs in one batch: z-tiles of one map (the reference's
+ * createShadowTiles thread per z-tile, src/DeferredRenderer.cpp:150-163) or
+ * independent lights of different sizes.  All jobs run through the same
+ * device launches; each gets its own shadow handle in out[j] (the handles
+ * share one device block, freed when the last of them is destroyed).  The
+ * DAG of every job equals the one cpvs_shadow_create would build. */
+CPVS_API cpvs_status cpvs_shadow_create_batch(cpvs_ctx* ctx, const cpvs_hierarchy* const* sources,
+                                              uint32_t num_sources, const cpvs_build_job* jobs, uint32_t num_jobs,
+                                              uint32_t flags, void* stream, cpvs_shadow** out);
+
 /* Depth map straight to DAG: hierarchy + create in one call.  Replaces
  * CompressedShadow::create(const ShadowMap*, ...) (src/CompressedShadow.h:55-56),
  * whose GL read-back becomes a host or device float32 buffer. */
@@ -216,6 +234,12 @@ CPVS_API const cpvs_shadow* cpvs_grid_get(const cpvs_grid* g, uint32_t x, uint32
  * uniformly shadowed / lit cell.  All cells must be set and share numLevels.
  * With `release_cells` the per-cell DAGs are freed afterwards (moveToGPU). */
 CPVS_API cpvs_status cpvs_grid_finalize(cpvs_grid* g, int release_cells, void* stream);
+/* Builds every cell of the grid in one batch and finalizes it: cell
+ * (x,y,z) is z-tile z of length of the xy tile hierarchy xy_tiles[y*length+x]
+ * (the reference's tiled precompute, src/DeferredRenderer.cpp:150-187, and
+ * copyToGPU).  Replaces any cells set before; tiles must share one size. */
+CPVS_API cpvs_status cpvs_grid_build(cpvs_grid* g, const cpvs_hierarchy* const* xy_tiles, uint32_t flags,
+                                     void* stream);
 /* Size in words of the concatenated DAG, and its copy (after finalize). */
 CPVS_API uint64_t cpvs_grid_dag_size(const cpvs_grid* g);
 CPVS_API cpvs_status cpvs_grid_words(const cpvs_grid* g, uint32_t* dag_out, uint64_t dag_capacity, uint32_t* cells_out,

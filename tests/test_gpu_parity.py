@@ -230,3 +230,54 @@ def test_errors(cp):
     assert e.value.status == 6
     ctx.set_budget(0)
     assert cp.CompressedShadow.from_depth(d, ctx=ctx).dag_size() > 0
+
+
+# ------------------------------------------------------------ batched forms
+def test_batch_matches_single_builds(cp, oracle):
+    """Independent lights of uneven sizes plus z-tiles of one map, built in one
+    batch (including an 8x8 map, which cannot use leafmasks): every DAG equals
+    its own single build and the oracle's."""
+    rng = np.random.default_rng(21)
+    maps = [scene.rasterise(scene.make_scene(int(n), 0.9, int(rng.integers(5, 60)), 2, 100 + i))
+            for i, n in enumerate([64, 1024, 256, 8, 512, 128, 2048, 256])]
+    hs = [cp.MinMaxHierarchy(m) for m in maps]
+    jobs = [(i, 0, 1) for i in range(len(maps))] + [(2, z, 4) for z in range(4)] + [(6, 1, 3)]
+    batch = cp.CompressedShadow.create_batch(hs, jobs)
+    q = np.random.default_rng(5).uniform(-1, 1, (50_000, 3)).astype(np.float32)
+    for (src, zi, zn), sh in zip(jobs, batch):
+        want = oracle.build(maps[src], zi, zn)
+        single = cp.CompressedShadow.create(hs[src], zi, zn)
+        assert np.array_equal(sh.get_dag(), single.get_dag()), (src, zi, zn)
+        assert np.array_equal(sh.get_dag(), want.dag), (src, zi, zn)
+        assert sh.level_counts() == single.level_counts()
+        assert sh.get_total_visibility() == single.get_total_visibility()
+        assert np.array_equal(sh.lookup_ndc(q), oracle.lookup_ndc(want.dag, want.num_levels, want.leafmasks, q))
+    del batch  # handles share one device block; dropping them frees it
+
+
+def test_grid_build_matches_oracle(cp, oracle):
+    """cpvs_grid_build: 4x4 xy tiles of a 256^2 map, 4 z-tiles each (64
+    DAGs in one batch) against per-cell oracle builds and the oracle's grid
+    routing."""
+    n, L = 64, 4
+    full = scene.rasterise(scene.make_scene(n * L, 0.95, 60, 8, 55))
+    full[:n, :n] = np.float32(1.0)  # a lit tile: uniform cells
+    tiles = [np.ascontiguousarray(full[y * n:(y + 1) * n, x * n:(x + 1) * n]) for y in range(L) for x in range(L)]
+    grid = cp.CompressedShadowContainer(L)
+    grid.build([cp.MinMaxHierarchy(t) for t in tiles])
+    dag, cells = grid.words()
+    dags, offs, off = [], [], 0
+    for z in range(L):
+        for y in range(L):
+            for x in range(L):
+                b = oracle.build(tiles[y * L + x], z, L)
+                dags.append(b.dag)
+                offs.append(off)
+                off += b.dag.size
+    assert np.array_equal(dag, np.concatenate(dags))
+    uniform = [i for i in range(L ** 3) if dags[i].size == 1]
+    assert uniform and all(cells[i] in (0xFFFFFFFE, 0xFFFFFFFF) for i in uniform)
+    q = np.random.default_rng(4).uniform(-1.05, 1.05, (300_000, 3)).astype(np.float32)
+    want = oracle.grid_lookup_ndc(np.concatenate(dags).astype(np.uint32), np.asarray(offs, np.uint32), L,
+                                  int(np.log2(n)) + 1, True, q)
+    assert np.array_equal(grid.lookup_ndc(q), want)
