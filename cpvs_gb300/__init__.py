@@ -51,6 +51,8 @@ _SIGS = {
     "cpvs_ctx_enable_timing": (C.c_int, [_vp, C.c_int]),
     "cpvs_ctx_kernel_times": (C.c_int, [_vp, _vp, _vp, _u32, C.POINTER(_u32)]),
     "cpvs_kernel_name": (C.c_char_p, [_u32]),
+    "cpvs_raster_depth": (C.c_int, [_vp, _vp, _u32, _vp, _u32, C.c_float, _u32, _u32, _u32, _u32, _u32, _vp, _u32,
+                                    _vp]),
     "cpvs_hierarchy_create": (C.c_int, [_vp, _vp, _u32, _u32, _vp, C.POINTER(_vp)]),
     "cpvs_hierarchy_destroy": (None, [_vp]),
     "cpvs_hierarchy_num_levels": (_u32, [_vp]),
@@ -70,6 +72,7 @@ _SIGS = {
     "cpvs_shadow_level_counts": (C.c_int, [_vp, _vp, _vp, _u32]),
     "cpvs_shadow_lookup_ndc": (C.c_int, [_vp, _vp, _u64, _vp, _u32, _vp]),
     "cpvs_shadow_lookup_voxel": (C.c_int, [_vp, _vp, _u64, _vp, _u32, _vp]),
+    "cpvs_lookup_ndc_multi": (C.c_int, [_vp, _u32, _vp, _vp, _u64, _vp, _u32, _vp]),
     "cpvs_grid_create": (C.c_int, [_vp, _u32, C.POINTER(_vp)]),
     "cpvs_grid_destroy": (None, [_vp]),
     "cpvs_grid_length": (_u32, [_vp]),
@@ -198,6 +201,27 @@ def unpack_bits(words: np.ndarray, n: int) -> np.ndarray:
     """Bit-packed lookup result -> uint8 class per point (1 lit, 0 shadow)."""
     b = np.unpackbits(np.ascontiguousarray(words, np.uint32).view(np.uint8), bitorder="little")
     return b[:n].astype(np.uint8)
+
+
+def raster_depth(sc, x0: int = 0, y0: int = 0, w: Optional[int] = None, h: Optional[int] = None,
+                 out=None, ctx: Optional[Context] = None, stream=None):
+    """Depth map of a `cpvs_gb300.scene.Scene` (or its window) rasterised on
+    the GPU, into a new (h, w) float32 CUDA tensor or `out`."""
+    import torch
+    ctx = ctx or Context.default()
+    w = sc.n if w is None else w
+    h = sc.n if h is None else h
+    dev = torch.device("cuda", ctx.device)
+    boxes = torch.from_numpy(np.ascontiguousarray(sc.boxes, np.float32)).to(dev)
+    spheres = torch.from_numpy(np.ascontiguousarray(sc.spheres, np.float32)).to(dev)
+    if out is None:
+        out = torch.empty((h, w), dtype=torch.float32, device=dev)
+    nb, ns = int(sc.boxes.shape[0]), int(sc.spheres.shape[0])
+    _check(_lib.cpvs_raster_depth(ctx.handle, _ptr(boxes) if nb else None, nb, _ptr(spheres) if ns else None, ns,
+                                  float(sc.plane), sc.n, x0, y0, w, h, _ptr(out), IO_DEVICE, _stream(stream)))
+    if stream is None:
+        torch.cuda.synchronize(dev)
+    return out
 
 
 class MinMaxHierarchy:
@@ -387,6 +411,26 @@ class CompressedShadow:
 
     def __del__(self):
         self.release()
+
+
+def lookup_ndc_multi(shadows, dag_index, points, out=None, stream=None):
+    """Point i looked up in shadows[dag_index[i]] in one launch.  numpy in ->
+    uint8 classes out; CUDA tensors in -> bit-packed int32 CUDA tensor out."""
+    n = int(points.shape[0])
+    tab = (_vp * len(shadows))(*[s.handle for s in shadows])
+    if _is_device(points):
+        import torch
+        if out is None:
+            out = torch.empty((n + 31) // 32, dtype=torch.int32, device=points.device)
+        _check(_lib.cpvs_lookup_ndc_multi(tab, len(shadows), _ptr(dag_index), _ptr(points), n, _ptr(out), IO_DEVICE,
+                                          _stream(stream)))
+        return out
+    pts = _host_array(points, np.float32)
+    ids = _host_array(dag_index, np.uint32)
+    words = np.zeros(max((n + 31) // 32, 1), np.uint32)
+    _check(_lib.cpvs_lookup_ndc_multi(tab, len(shadows), _ptr(ids), _ptr(pts), n, words.ctypes.data, 0,
+                                      _stream(stream)))
+    return unpack_bits(words, n)
 
 
 class CompressedShadowContainer:

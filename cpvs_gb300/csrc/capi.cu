@@ -476,6 +476,47 @@ cpvs_status cpvs_hierarchy_level(const cpvs_hierarchy* h, uint32_t level, float*
     return CPVS_OK;
 }
 
+// ---------------------------------------------------------------- raster
+cpvs_status cpvs_raster_depth(cpvs_ctx* ctx, const float* boxes, uint32_t num_boxes, const float* spheres,
+                              uint32_t num_spheres, float plane, uint32_t n, uint32_t x0, uint32_t y0, uint32_t w,
+                              uint32_t h, float* depth_out, uint32_t flags, void* stream) {
+    if (!ctx || !depth_out || (num_boxes && !boxes) || (num_spheres && !spheres))
+        return fail(CPVS_ERR_INVALID_ARG, "raster_depth: null argument");
+    if (!is_pow2(n) || n > 65536 || (uint64_t)x0 + w > n || (uint64_t)y0 + h > n)
+        return fail(CPVS_ERR_INVALID_ARG, "raster_depth: window must lie inside a power-of-two map of side <= 65536");
+    cpvs_status r = set_device(ctx);
+    if (r != CPVS_OK) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    cpvs::Ctx& c = ctx->c;
+    const uint64_t bb = (uint64_t)num_boxes * 5 * 4, sb = (uint64_t)num_spheres * 4 * 4;
+    const uint64_t ob = (uint64_t)w * h * 4;
+    void *db = nullptr, *ds = nullptr;
+    bool ob_own = false, os_own = false;
+    r = stage_in(c, boxes, bb, flags, st, &db, &ob_own);
+    if (r == CPVS_OK) r = stage_in(c, spheres, sb, flags, st, &ds, &os_own);
+    float* out = depth_out;
+    bool out_own = false;
+    if (r == CPVS_OK && !(flags & CPVS_IO_DEVICE)) {
+        out = static_cast<float*>(host_accessible(c, depth_out));
+        if (!out) {
+            r = c.alloc((void**)&out, std::max<uint64_t>(ob, 4), false, st);
+            out_own = r == CPVS_OK;
+        }
+    }
+    if (r == CPVS_OK)
+        r = cpvs::launch_raster(static_cast<const float*>(db), num_boxes, static_cast<const float*>(ds), num_spheres,
+                                plane, n, x0, y0, w, h, out, st, &c.timing);
+    if (r == CPVS_OK && !(flags & CPVS_IO_DEVICE)) {
+        cudaError_t e = out_own ? cudaMemcpyAsync(depth_out, out, ob, cudaMemcpyDeviceToHost, st) : cudaSuccess;
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) r = cpvs::cuda_fail(e, "raster read-back");
+    }
+    if (ob_own) c.release(db, std::max<uint64_t>(bb, 4), false, st);
+    if (os_own) c.release(ds, std::max<uint64_t>(sb, 4), false, st);
+    if (out_own) c.release(out, std::max<uint64_t>(ob, 4), false, st);
+    return r;
+}
+
 // ---------------------------------------------------------------- shadow
 cpvs_status cpvs_shadow_create(cpvs_ctx* ctx, const cpvs_hierarchy* h, uint32_t z_tile_index, uint32_t z_tile_num,
                                uint32_t flags, void* stream, cpvs_shadow** out) {
@@ -637,6 +678,40 @@ cpvs_status cpvs_shadow_lookup_voxel(const cpvs_shadow* s, const int32_t* xyz, u
         s->touch(st);
         return r;
     });
+}
+
+cpvs_status cpvs_lookup_ndc_multi(const cpvs_shadow* const* shadows, uint32_t num_shadows, const uint32_t* dag_index,
+                                  const float* xyz, uint64_t n, uint32_t* bits_out, uint32_t flags, void* stream) {
+    if (!shadows || num_shadows == 0) return fail(CPVS_ERR_INVALID_ARG, "lookup_multi: no shadows");
+    if (n && !dag_index) return fail(CPVS_ERR_INVALID_ARG, "lookup_multi: null dag_index");
+    cpvs_ctx* ctx = shadows[0] ? shadows[0]->ctx : nullptr;
+    std::vector<cpvs::MultiDag> table(num_shadows);
+    for (uint32_t i = 0; i < num_shadows; ++i) {
+        const cpvs_shadow* sh = shadows[i];
+        if (!sh || sh->ctx != ctx) return fail(CPVS_ERR_INVALID_ARG, "lookup_multi: shadows must share one context");
+        table[i] = cpvs::MultiDag{sh->dag, (uint32_t)sh->words, sh->num_levels, sh->leafmasks ? 1u : 0u, 0u};
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    cpvs_status r = set_device(ctx);
+    if (r != CPVS_OK) return r;
+    cpvs::Ctx& c = ctx->c;
+    cpvs::MultiDag* dtab = nullptr;
+    const uint64_t tb = num_shadows * sizeof(cpvs::MultiDag);
+    r = c.alloc((void**)&dtab, tb, false, st);
+    if (r != CPVS_OK) return r;
+    CPVS_CUDA(cudaMemcpyAsync(dtab, table.data(), tb, cudaMemcpyHostToDevice, st));
+    void* ids = nullptr;
+    bool ids_own = false;
+    r = stage_in(c, dag_index, n * 4, flags, st, &ids, &ids_own);
+    if (r == CPVS_OK)
+        r = lookup_common(ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
+            return cpvs::launch_multi_lookup(dtab, num_shadows, static_cast<const uint32_t*>(ids),
+                                             static_cast<const float*>(q), n, bits, st, &c.timing);
+        });
+    for (uint32_t i = 0; i < num_shadows; ++i) shadows[i]->touch(st);
+    if (ids_own) c.release(ids, std::max<uint64_t>(n * 4, 4), false, st);
+    c.release(dtab, tb, false, st);
+    return r;
 }
 
 // ------------------------------------------------------------------ grid

@@ -66,6 +66,13 @@ struct BoundJob {
 cpvs_status launch_level_bounds(const float2* levels, uint32_t n, int lmin, const BoundJob* jobs_dev, int njobs,
                                 unsigned long long* bounds, cudaStream_t st);
 
+// Depth map of a plane plus boxes (cx,cy,hx,hy,top) and spheres
+// (cx,cy,r,depth), window [x0,x0+w) x [y0,y0+h) of an n x n map (device
+// pointers).
+cpvs_status launch_raster(const float* boxes, uint32_t nb, const float* spheres, uint32_t ns, float plane, uint32_t n,
+                          uint32_t x0, uint32_t y0, uint32_t w, uint32_t h, float* out, cudaStream_t st,
+                          Timing* timing = nullptr);
+
 // --------------------------------------------------------------- build
 struct SourceSpec {
     const float* depth;    // device, n*n
@@ -97,6 +104,16 @@ int top_index_depth(uint32_t num_levels, bool leafmasks);
 cpvs_status launch_top_index(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks,
                              uint32_t* out, cudaStream_t st);
 // `top` may be null (no top index).
+// One resident DAG in a multi-DAG lookup table.
+struct MultiDag {
+    const uint32_t* dag;
+    uint32_t words;
+    uint32_t num_levels;
+    uint32_t leafmasks;
+    uint32_t pad;
+};
+cpvs_status launch_multi_lookup(const MultiDag* dags, uint32_t ndags, const uint32_t* ids, const float* xyz, uint64_t n,
+                                uint32_t* bits, cudaStream_t st, Timing* timing = nullptr);
 // Times queries_per_thread = 1, 2, 4 on the first 2^20 queries (writing
 // their bits) and returns the fastest.
 int tune_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks, const uint32_t* top,
@@ -129,6 +146,8 @@ enum KernelId : int {
     K_EMIT,
     K_LOOKUP,
     K_GRID_LOOKUP,
+    K_RASTER,
+    K_MULTI_LOOKUP,
     K_COUNT
 };
 const char* kernel_name(int id);

@@ -297,6 +297,33 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// Many resident DAGs at once: query i descends DAG dags[ids[i]] (its own
+// depth and leafmask mode); ids outside the table answer "shadow".
+__global__ void __launch_bounds__(kThreads)
+    k_multi_lookup(const MultiDag* __restrict__ dags, uint32_t ndags, const uint32_t* __restrict__ ids,
+                   const float* __restrict__ q, uint64_t n, uint32_t* __restrict__ bits) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t nwords = (n + 31) / 32;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwords; w += nw) {
+        const uint64_t i = w * 32 + (uint64_t)lane;
+        bool lit = false;
+        if (i < n) {
+            const uint32_t id = ids[i];
+            if (id < ndags) {
+                const MultiDag D = dags[id];
+                const float scale = (float)((1u << (D.num_levels - 1)) - 1u);
+                const float* p = q + 3 * i;
+                const int32_t px = quantise(p[0], scale), py = quantise(p[1], scale), pz = quantise(p[2], scale);
+                lit = descend(D.dag, D.words, 0u, 0u, (int)D.num_levels - 2, D.leafmasks ? 3 : 0, D.leafmasks != 0,
+                              px, py, pz);
+            }
+        }
+        const uint32_t word = __ballot_sync(0xffffffffu, lit);
+        if (lane == 0) bits[w] = word;
+    }
+}
+
 uint32_t lookup_grid(int num_sms, uint64_t n) {
     const uint64_t warps = (n + 31) / 32;
     const uint64_t blocks = (warps * 32 + kThreads - 1) / kThreads;
@@ -387,6 +414,15 @@ int tune_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool l
     cudaEventDestroy(b);
     cudaGetLastError();
     return best;
+}
+
+cpvs_status launch_multi_lookup(const MultiDag* dags, uint32_t ndags, const uint32_t* ids, const float* xyz, uint64_t n,
+                                uint32_t* bits, cudaStream_t st, Timing* timing) {
+    if (n == 0) return CPVS_OK;
+    KernelTimer kt(timing, K_MULTI_LOOKUP, st);
+    k_multi_lookup<<<lookup_grid(device_sms(), n), kThreads, 0, st>>>(dags, ndags, ids, xyz, n, bits);
+    CPVS_CUDA(cudaGetLastError());
+    return CPVS_OK;
 }
 
 cpvs_status launch_grid_lookup(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,

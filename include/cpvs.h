@@ -127,6 +127,23 @@ CPVS_API uint32_t cpvs_hierarchy_size(const cpvs_hierarchy* h);
 CPVS_API cpvs_status cpvs_hierarchy_level(const cpvs_hierarchy* h, uint32_t level, float* host_out, uint64_t capacity,
                                  void* stream);
 
+/* ---- depth-map producer ----------------------------------------------- */
+
+/* Rasterises the window [x0,x0+w) x [y0,y0+h) of an n x n depth map (n a
+ * power of two): a ground plane at depth `plane`, min-combined with
+ * axis-aligned boxes (num_boxes x {cx, cy, half-width, half-height, top
+ * depth}) and spheres (num_spheres x {cx, cy, radius, centre depth}), in map
+ * coordinates [0,1].  Pixel (x,y) samples its centre ((x+0.5)/n, (y+0.5)/n);
+ * a box covers the centres in [c-h, c+h]; a sphere contributes
+ * depth - sqrt(r^2 - rho^2) where rho^2 < r^2.  Writes w*h float32,
+ * row-major.  Replaces the reference's GL shadow pass and read-back
+ * (src/DeferredRenderer.cpp:110-148, src/ShadowMap.cpp:23-30) for the
+ * synthetic scenes the benchmarks use.  Primitive arrays and the output are
+ * host memory unless flags has CPVS_IO_DEVICE. */
+CPVS_API cpvs_status cpvs_raster_depth(cpvs_ctx* ctx, const float* boxes, uint32_t num_boxes, const float* spheres,
+                                       uint32_t num_spheres, float plane, uint32_t n, uint32_t x0, uint32_t y0,
+                                       uint32_t w, uint32_t h, float* depth_out, uint32_t flags, void* stream);
+
 /* ---- compressed shadow (one DAG) ------------------------------------- */
 
 /* Builds the DAG of z-tile `z_tile_index` of `z_tile_num` from a hierarchy.
@@ -215,6 +232,15 @@ CPVS_API cpvs_status cpvs_shadow_lookup_voxel(const cpvs_shadow* s, const int32_
 CPVS_API cpvs_status cpvs_shadow_build_noalloc(const float* depth, uint32_t n, uint32_t z_tile_index,
                                                uint32_t z_tile_num, uint32_t flags, uint32_t* dag_out,
                                                uint64_t dag_capacity, uint64_t* dag_words, void* stream);
+
+/* Visibility of n NDC points against many resident DAGs at once: point i
+ * descends shadows[dag_index[i]] (an index outside the table answers
+ * shadow).  One launch serves lookups spread over many lights or requests;
+ * each answer equals cpvs_shadow_lookup_ndc on that shadow alone.  All
+ * shadows must come from one context. */
+CPVS_API cpvs_status cpvs_lookup_ndc_multi(const cpvs_shadow* const* shadows, uint32_t num_shadows,
+                                           const uint32_t* dag_index, const float* xyz, uint64_t n,
+                                           uint32_t* bits_out, uint32_t flags, void* stream);
 
 /* ---- top-level grid (container) -------------------------------------- */
 

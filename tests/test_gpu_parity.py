@@ -281,3 +281,40 @@ def test_grid_build_matches_oracle(cp, oracle):
     want = oracle.grid_lookup_ndc(np.concatenate(dags).astype(np.uint32), np.asarray(offs, np.uint32), L,
                                   int(np.log2(n)) + 1, True, q)
     assert np.array_equal(grid.lookup_ndc(q), want)
+
+
+def test_raster_matches_host_rasteriser(cp):
+    """The CUDA depth producer equals the host rasteriser bit for bit, for
+    whole maps and windows, boxes and spheres."""
+    for n, nb, ns, seed in ((64, 10, 4, 1), (512, 120, 30, 2), (1024, 40, 0, 0), (2048, 500, 64, 3)):
+        sc = scene.make_scene(n, 0.95, nb, ns, seed)
+        want = scene.rasterise(sc)
+        got = cp.raster_depth(sc).cpu().numpy()
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), n
+    sc = scene.make_scene(1024, 0.9, 200, 40, 7)
+    full = scene.rasterise(sc)
+    for x0, y0, w, h in ((0, 0, 256, 256), (256, 512, 256, 128), (1000, 3, 24, 100)):
+        got = cp.raster_depth(sc, x0, y0, w, h).cpu().numpy()
+        assert np.array_equal(got, full[y0:y0 + h, x0:x0 + w]), (x0, y0, w, h)
+
+
+def test_multi_dag_lookup_matches_single_lookups(cp, oracle):
+    """Queries spread over many resident DAGs in one launch answer exactly as
+    each DAG's own lookup (and the oracle)."""
+    import torch
+    rng = np.random.default_rng(31)
+    sizes = [64, 256, 1024, 128, 512, 16, 2048, 256]
+    maps = [scene.rasterise(scene.make_scene(n, 0.9, 30, 3, 300 + i)) for i, n in enumerate(sizes)]
+    hs = [cp.MinMaxHierarchy(m) for m in maps]
+    shadows = cp.CompressedShadow.create_batch(hs, [(i, 0, 1) for i in range(len(maps))])
+    nq = 400_000
+    ids = rng.integers(0, len(maps) + 1, nq).astype(np.uint32)  # the last id is outside the table
+    q = rng.uniform(-1, 1, (nq, 3)).astype(np.float32)
+    got = cp.lookup_ndc_multi(shadows, ids, q)
+    for i, sh in enumerate(shadows):
+        sel = ids == i
+        assert np.array_equal(got[sel], sh.lookup_ndc(q[sel])), i
+    assert (got[ids == len(maps)] == 0).all()
+    dev = cp.lookup_ndc_multi(shadows, torch.from_numpy(ids).cuda(), torch.from_numpy(q).cuda())
+    torch.cuda.synchronize()
+    assert np.array_equal(cp.unpack_bits(dev.cpu().numpy().view(np.uint32), nq), got)
