@@ -42,6 +42,11 @@ WORKLOADS = {
                                       "the depth surface +-0.5 voxel, half uniform"),
     "c0": dict(queries=1 << 20, desc="1024^2 float32 depth map (plane 0.9, 40 boxes; seed 0) -> 1024^3-voxel DAG "
                                      "with 64-bit leafmasks; 2^20 NDC lookups"),
+    "c2": dict(queries=1 << 27, desc="32768^2 float32 depth map (plane 0.95, 4000 boxes, 512 spheres; seed 2) in 8x8 "
+                                      "xy tiles of 4096^2, 8 z-tiles each: 512 DAGs of 4096^3 in one grid build; 2^27 "
+                                      "NDC lookups routed through the 8^3 grid"),
+    "c3": dict(queries=1 << 24, desc="64 independent lights (seeds 100..163, 10..2000 boxes, sides 2^round(U[8,13])) "
+                                      "built in one batch; 2^24 NDC lookups spread over the 64 DAGs"),
 }
 METRIC = "DAG-build Gvoxel/s (shadow DAG from a depth map, bit-exact with the reference)"
 CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -400,6 +405,180 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def c3_scenes():
+    """64 lights: side 2^round(8 + 5u), 10 + floor(1991u) boxes, plane 0.9."""
+    meta = scene.SplitMix64(3)
+    out = []
+    for i in range(64):
+        side = 1 << int(round(8 + 5 * meta.uniform()))
+        nb = 10 + int(1991 * meta.uniform())
+        out.append(scene.make_scene(side, 0.9, nb, 0, 100 + i))
+    return out
+
+
+def surface_queries_device(torch, maps, n_total, count, gen, tile_of=None):
+    """`count` NDC points on the depth surfaces of `maps` (device tensors),
+    offset by up to half a voxel in z, at path resolution `n_total`."""
+    k = len(maps)
+    which = torch.randint(0, k, (count,), generator=gen, device=maps[0].device)
+    out = torch.empty((count, 3), dtype=torch.float32, device=maps[0].device)
+    scale = 2.0 / (n_total - 1)
+    for i, m in enumerate(maps):
+        sel = (which == i).nonzero().squeeze(1)
+        if sel.numel() == 0:
+            continue
+        h, w = m.shape
+        px = torch.randint(0, w, (sel.numel(),), generator=gen, device=m.device)
+        py = torch.randint(0, h, (sel.numel(),), generator=gen, device=m.device)
+        ox, oy, oz, nz = tile_of(i) if tile_of else (0, 0, 0, w)
+        vz = m[py, px].double() * nz + (torch.rand(sel.numel(), generator=gen, device=m.device, dtype=torch.float64) - 0.5)
+        out[sel, 0] = ((px + ox + 0.5) * scale - 1.0).float()
+        out[sel, 1] = ((py + oy + 0.5) * scale - 1.0).float()
+        out[sel, 2] = ((vz + oz) * scale - 1.0).float()
+    return out, which
+
+
+def run_batched(args):
+    """c2 / c3: many DAGs per step in one batched build (one plan, one graph
+    launch) against the plain path (one build call per DAG)."""
+    import torch
+    import cpvs_gb300 as cp
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    wl = WORKLOADS[args.config]
+    ctx = cp.Context(0)
+    stream = torch.cuda.current_stream(dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(7)
+    nq = wl["queries"]
+    if args.config == "c2":
+        sc = scene.config_scene("c2")
+        T, L = 4096, 8
+        maps = [cp.raster_depth(sc, x * T, y * T, T, T, ctx=ctx) for y in range(L) for x in range(L)]
+        voxels = float(T) ** 3 * L ** 3
+        half = nq // 2
+        qs, _ = surface_queries_device(torch, maps, T * L, half, gen,
+                                       tile_of=lambda i: ((i % L) * T, (i // L) * T, 0, T * L))
+        qu = torch.rand((nq - half, 3), generator=gen, device=dev) * 2 - 1
+        q = torch.cat([qs, qu]).contiguous()
+
+        def batched():
+            hs = [cp.MinMaxHierarchy(m, ctx=ctx, stream=stream, borrow=True) for m in maps]
+            grid = cp.CompressedShadowContainer(L, ctx=ctx)
+            grid.build(hs, stream=stream)
+            return grid
+
+        def plain():
+            hs = [cp.MinMaxHierarchy(m, ctx=ctx, stream=stream, borrow=True) for m in maps]
+            grid = cp.CompressedShadowContainer(L, ctx=ctx)
+            for z in range(L):
+                for y in range(L):
+                    for x in range(L):
+                        grid.set(cp.CompressedShadow.create(hs[y * L + x], z, L, stream=stream), x, y, z)
+            grid.copy_to_gpu(stream=stream)
+            return grid
+
+        def look(g, out):
+            return g.lookup_ndc(q, out, stream=stream)
+        ndags = L ** 3
+    else:
+        scs = c3_scenes()
+        maps = [cp.raster_depth(s, ctx=ctx) for s in scs]
+        voxels = float(sum(s.n ** 3 for s in scs))
+        half = nq // 2
+        # surface points of each light at its own resolution, half uniform
+        ids = torch.randint(0, len(maps), (nq,), generator=gen, device=dev, dtype=torch.int64)
+        q = torch.rand((nq, 3), generator=gen, device=dev) * 2 - 1
+        for i, m in enumerate(maps):
+            sel = (ids[:half] == i).nonzero().squeeze(1)
+            if sel.numel() == 0:
+                continue
+            nmap = m.shape[0]
+            px = torch.randint(0, nmap, (sel.numel(),), generator=gen, device=dev)
+            py = torch.randint(0, nmap, (sel.numel(),), generator=gen, device=dev)
+            vz = m[py, px].double() * nmap + (torch.rand(sel.numel(), generator=gen, device=dev, dtype=torch.float64) - 0.5)
+            sc2 = 2.0 / (nmap - 1)
+            q[sel, 0] = ((px + 0.5) * sc2 - 1).float()
+            q[sel, 1] = ((py + 0.5) * sc2 - 1).float()
+            q[sel, 2] = (vz * sc2 - 1).float()
+        ids32 = ids.to(torch.int32).contiguous()
+        q = q.contiguous()
+
+        def batched():
+            hs = [cp.MinMaxHierarchy(m, ctx=ctx, stream=stream, borrow=True) for m in maps]
+            return cp.CompressedShadow.create_batch(hs, [(i, 0, 1) for i in range(len(hs))], stream=stream)
+
+        def plain():
+            out = []
+            for m in maps:
+                h = cp.MinMaxHierarchy(m, ctx=ctx, stream=stream, borrow=True)
+                out.append(cp.CompressedShadow.create(h, stream=stream))
+            return out
+
+        def look(shs, out):
+            return cp.lookup_ndc_multi(shs, ids32, q, out, stream=stream)
+        ndags = len(maps)
+    out = torch.empty((nq + 31) // 32, dtype=torch.int32, device=dev)
+
+    def timed(fn, steps, warm):
+        keep = None
+        for _ in range(warm):
+            keep = fn()
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            keep = fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        return keep, times
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    res_b, tb = timed(batched, args.steps, args.warmup)
+    res_p, tp = timed(plain, max(2, args.steps // 4), 1)
+    # correctness of the batched form against the plain one on the same maps
+    same = None
+    if args.config == "c3":
+        same = all(np.array_equal(a.get_dag(), b.get_dag()) for a, b in zip(res_b, res_p))
+    else:
+        da, _ = res_b.words()
+        db, _ = res_p.words()
+        same = bool(np.array_equal(da, db))
+    for _ in range(3):
+        look(res_b, out)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        look(res_b, out)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    look_ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()
+    ms_b = statistics.median(tb)
+    ms_p = statistics.median(tp)
+    line = {
+        "metric": METRIC + (" -- batched grid build" if args.config == "c2" else " -- batched multi-light build"),
+        "value": round(voxels / (ms_b * 1e-3) / 1e9, 1), "unit": "Gvoxel/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_b, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded scenes rasterised on the GPU (no dataset)",
+        "config": {"workload": f"{args.config}: {wl['desc']}", "dags_per_step": ndags, "voxels_per_step": voxels},
+        "plain": {"value": round(voxels / (ms_p * 1e-3) / 1e9, 1), "unit": "Gvoxel/s", "ms_per_step": round(ms_p, 3),
+                  "path": "one cpvs_shadow_create per DAG" + (" + grid finalize" if args.config == "c2" else "")},
+        "batched_over_plain": round(ms_p / ms_b, 2),
+        "p50_ms": {"batched": round(ms_b, 3), "plain": round(ms_p, 3)},
+        "p99_ms": {"batched": round(float(np.percentile(tb, 99)), 3), "plain": round(float(np.percentile(tp, 99)), 3)},
+        "dags_identical_to_plain": same,
+        "lookup": {"value": round(nq / (look_ms * 1e-3) / 1e9, 2), "unit": "Glookups/s", "ms_per_batch": round(look_ms, 4),
+                   "path": "cpvs_grid_lookup_ndc" if args.config == "c2" else "cpvs_lookup_ndc_multi"},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -418,6 +597,8 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.config in ("c2", "c3"):
+        run_batched(args)
     else:
         run_ours(args, rank, world, local_rank)
 

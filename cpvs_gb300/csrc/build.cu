@@ -944,14 +944,17 @@ bool same_shape(const BuildPlan* P, bool leafmasks, const std::vector<uint32_t>&
     return P->leafmasks == leafmasks && P->job_n == job_n;
 }
 
-// Capacities from per-job level bounds (+25% slack) and table sizes.
+// Capacities from per-job level bounds (+25% slack) and table sizes.  A
+// plan only grows: re-planning keeps every level at least as large as before,
+// so batches of different maps settle on one plan.
 void plan_set_capacities(BuildPlan* P, const std::vector<unsigned long long>& bounds, bool exact_tables) {
-    std::fill(std::begin(P->cap), std::end(P->cap), 0);
+    uint64_t cap[CPVS_MAX_LEVELS] = {0};
     for (uint32_t j = 0; j < P->njobs; ++j)
-        for (int L = P->bottom; L < (int)P->root_level[j]; ++L) P->cap[L] += bounds[(size_t)j * CPVS_MAX_LEVELS + L];
+        for (int L = P->bottom; L < (int)P->root_level[j]; ++L) cap[L] += bounds[(size_t)j * CPVS_MAX_LEVELS + L];
     for (int L = 0; L < CPVS_MAX_LEVELS; ++L) {
-        if (P->cap[L]) P->cap[L] = P->cap[L] + P->cap[L] / 4 + 256;
-        P->cap[L] += P->ninj[L];
+        if (cap[L]) cap[L] = cap[L] + cap[L] / 4 + 256;
+        cap[L] += P->ninj[L];
+        P->cap[L] = std::max(P->cap[L], cap[L]);
         if (exact_tables || !P->tcap[L] || P->tcap[L] < 1024) P->tcap[L] = next_pow2(std::max<uint64_t>(2 * P->cap[L], 1024));
     }
 }
