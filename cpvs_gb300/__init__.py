@@ -73,6 +73,13 @@ _SIGS = {
     "cpvs_shadow_lookup_ndc": (C.c_int, [_vp, _vp, _u64, _vp, _u32, _vp]),
     "cpvs_shadow_lookup_voxel": (C.c_int, [_vp, _vp, _u64, _vp, _u32, _vp]),
     "cpvs_lookup_ndc_multi": (C.c_int, [_vp, _u32, _vp, _vp, _u64, _vp, _u32, _vp]),
+    "cpvs_server_create": (C.c_int, [_vp, _vp, C.POINTER(_vp)]),
+    "cpvs_server_destroy": (None, [_vp]),
+    "cpvs_server_submit_build": (C.c_int, [_vp, _u64, _vp, _u32, C.POINTER(_u64)]),
+    "cpvs_server_submit_lookup": (C.c_int, [_vp, _u64, _vp, _u64, _vp, C.POINTER(_u64)]),
+    "cpvs_server_wait": (C.c_int, [_vp, _u64, C.c_int64, C.POINTER(C.c_double)]),
+    "cpvs_server_cancel": (C.c_int, [_vp, _u64]),
+    "cpvs_server_get_stats": (C.c_int, [_vp, _vp]),
     "cpvs_grid_create": (C.c_int, [_vp, _u32, C.POINTER(_vp)]),
     "cpvs_grid_destroy": (None, [_vp]),
     "cpvs_grid_length": (_u32, [_vp]),
@@ -502,3 +509,71 @@ class CompressedShadowContainer:
         if getattr(self, "handle", None) and _lib is not None:
             _lib.cpvs_grid_destroy(self.handle)
             self.handle = None
+
+
+class _ServerConfig(C.Structure):
+    _fields_ = [("budget_bytes", C.c_uint64), ("max_batch_builds", C.c_uint32), ("max_batch_lookups", C.c_uint32),
+                ("flags", C.c_uint32)]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("builds_done", "lookups_done", "failed", "cancelled", "evictions",
+                                           "resident_dags", "resident_bytes", "queued")] + \
+               [(k, C.c_double) for k in ("build_p50_ms", "build_p99_ms", "lookup_p50_ms", "lookup_p99_ms")]
+
+
+class Server:
+    """The serving loop (cpvs_server): submit builds and lookups from any
+    thread, wait on tickets.  The server takes over its context."""
+
+    def __init__(self, ctx: Optional[Context] = None, budget_bytes: int = 0, max_batch_builds: int = 0,
+                 max_batch_lookups: int = 0, leafmasks: bool = True):
+        self.ctx = ctx or Context(0)
+        cfg = _ServerConfig(budget_bytes, max_batch_builds, max_batch_lookups, FLAG_LEAFMASKS if leafmasks else 0)
+        h = _vp()
+        _check(_lib.cpvs_server_create(self.ctx.handle, C.byref(cfg), C.byref(h)))
+        self.handle = h.value
+        self._keep = {}  # ticket -> buffers that must outlive it
+
+    def submit_build(self, key: int, depth) -> int:
+        d = _host_array(depth, np.float32)
+        t = C.c_uint64()
+        _check(_lib.cpvs_server_submit_build(self.handle, key, _ptr(d), int(depth.shape[0]), C.byref(t)))
+        self._keep[t.value] = (d,)
+        return t.value
+
+    def submit_lookup(self, key: int, points, out=None) -> int:
+        pts = _host_array(points, np.float32)
+        n = int(points.shape[0])
+        words = out if out is not None else np.zeros(max((n + 31) // 32, 1), np.uint32)
+        t = C.c_uint64()
+        _check(_lib.cpvs_server_submit_lookup(self.handle, key, _ptr(pts), n, _ptr(words), C.byref(t)))
+        self._keep[t.value] = (pts, words, n)
+        return t.value
+
+    def wait(self, ticket: int, timeout_us: int = -1):
+        """Returns (latency_ms, result): result is the uint8 classes for a
+        lookup ticket, None for a build.  Raises CpvsError on failure."""
+        lat = C.c_double()
+        st = _lib.cpvs_server_wait(self.handle, ticket, timeout_us, C.byref(lat))
+        keep = self._keep.pop(ticket, None) if st != 3 else self._keep.get(ticket)
+        _check(st)
+        if keep is not None and len(keep) == 3:
+            return lat.value, unpack_bits(np.asarray(keep[1]).view(np.uint32), keep[2])
+        return lat.value, None
+
+    def cancel(self, ticket: int):
+        _check(_lib.cpvs_server_cancel(self.handle, ticket))
+
+    def stats(self) -> dict:
+        st = _ServerStats()
+        _check(_lib.cpvs_server_get_stats(self.handle, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def close(self):
+        if getattr(self, "handle", None) and _lib is not None:
+            _lib.cpvs_server_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        self.close()

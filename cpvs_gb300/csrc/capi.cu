@@ -54,76 +54,25 @@ void Ctx::release(void* p, uint64_t bytes, bool persistent, cudaStream_t st, cud
 
 using cpvs::fail;
 
-struct cpvs_ctx {
-    cpvs::Ctx c;
-};
-
-// Every object with device memory records `last_use` on the stream of each
-// call that enqueues work on it; its memory is freed after that event.
-struct DeviceObject {
-    cudaEvent_t last_use = nullptr;
-    DeviceObject() { cudaEventCreateWithFlags(&last_use, cudaEventDisableTiming); }
-    ~DeviceObject() {
-        if (last_use) cudaEventDestroy(last_use);
+namespace cpvs {
+// The address under which the GPU reads host memory `p` in place, or null:
+// pinned / registered memory through its mapped address, and, where the GPU
+// walks the host page tables (Grace-class hosts), any host pointer.
+void* host_accessible(const Ctx& c, const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
     }
-    void touch(cudaStream_t st) const { cudaEventRecord(last_use, st); }
-};
-
-struct cpvs_hierarchy : DeviceObject {
-    cpvs_ctx* ctx = nullptr;
-    uint32_t n = 0;
-    float* depth = nullptr;    // device n*n
-    bool owns_depth = true;    // false when borrowed from the caller
-    float2* levels = nullptr;  // device pyramid
-    uint64_t bytes = 0;
-};
-
-// Device block holding the DAGs of one build (one or many jobs back to
-// back, followed by kDagPad zeroed words).  Shared by the shadows (and the
-// grid) that point into it; freed when the last of them lets go, after every
-// holder's last use.
-struct DagBlock {
-    cpvs_ctx* ctx = nullptr;
-    uint32_t* base = nullptr;
-    uint64_t bytes = 0;
-    int refs = 0;
-};
-
-void block_unref(DagBlock* b, cudaEvent_t last_use) {
-    if (!b) return;
-    cpvs::Ctx& c = b->ctx->c;
-    if (last_use) cudaStreamWaitEvent(c.free_stream, last_use, 0);  // the free waits for every holder
-    if (--b->refs == 0) {
-        c.release(b->base, b->bytes, true, nullptr, nullptr);
-        delete b;
-    }
+    if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+    if (a.type == cudaMemoryTypeUnregistered && c.pageable_access) return const_cast<void*>(p);
+    return nullptr;
 }
 
-struct cpvs_shadow : DeviceObject {
-    cpvs_ctx* ctx = nullptr;
-    DagBlock* block = nullptr;
-    uint32_t* dag = nullptr;   // inside block; at least kDagPad readable words follow it
-    uint64_t words = 0;
-    uint32_t* top = nullptr;   // dense top index for lookups, built on the first lookup
-    uint64_t top_bytes = 0;
-    uint32_t num_levels = 0;
-    bool leafmasks = false;
-    uint32_t root_mask = 0;
-    std::vector<uint64_t> tree, uniq;
-};
+}  // namespace cpvs
+using cpvs::host_accessible;
 
-struct cpvs_grid : DeviceObject {
-    cpvs_ctx* ctx = nullptr;
-    uint32_t length = 0;
-    std::vector<cpvs_shadow*> cells;
-    DagBlock* block = nullptr;  // the combined DAG
-    uint32_t* dag = nullptr;
-    uint64_t words = 0;
-    uint32_t* cell_words = nullptr;
-    uint32_t dag_levels = 0;
-    bool leafmasks = false;
-    bool finalized = false;
-};
+#include "objects.h"
 
 namespace {
 
@@ -142,20 +91,6 @@ cpvs_status check_map_size(uint32_t n, uint32_t min_n) {
         return fail(CPVS_ERR_INVALID_ARG, "map side must be a power of two in [" + std::to_string(min_n) +
                                               ", 65536], got " + std::to_string(n));
     return CPVS_OK;
-}
-
-// The address under which the GPU reads host memory `p` in place, or null:
-// pinned / registered memory through its mapped address, and, where the GPU
-// walks the host page tables (Grace-class hosts), any host pointer.
-void* host_accessible(const cpvs::Ctx& c, const void* p) {
-    cudaPointerAttributes a{};
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-        cudaGetLastError();
-        return nullptr;
-    }
-    if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
-    if (a.type == cudaMemoryTypeUnregistered && c.pageable_access) return const_cast<void*>(p);
-    return nullptr;
 }
 
 // Device view of a host or device input: used in place when the GPU can read

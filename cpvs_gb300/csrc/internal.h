@@ -114,6 +114,18 @@ struct MultiDag {
 };
 cpvs_status launch_multi_lookup(const MultiDag* dags, uint32_t ndags, const uint32_t* ids, const float* xyz, uint64_t n,
                                 uint32_t* bits, cudaStream_t st, Timing* timing = nullptr);
+// One request of a segmented lookup: n points at xyz, ceil(n/32) words of
+// bits, output words [word_start, ...) of the launch, against dags[dag].
+struct LookupSegment {
+    const float* xyz;
+    uint32_t* bits;
+    uint64_t word_start;
+    uint64_t n;
+    uint32_t dag;
+    uint32_t pad;
+};
+cpvs_status launch_segment_lookup(const MultiDag* dags, uint32_t ndags, const LookupSegment* segs, uint32_t nsegs,
+                                  uint64_t total_words, cudaStream_t st, Timing* timing = nullptr);
 // Times queries_per_thread = 1, 2, 4 on the first 2^20 queries (writing
 // their bits) and returns the fastest.
 int tune_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks, const uint32_t* top,

@@ -324,6 +324,39 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// Segmented multi-DAG lookup: many independent requests in one launch.
+// Segment s owns output words [word_start, word_start + ceil(n/32)); warp w
+// finds its segment by binary search and answers 32 of its queries, reading
+// the request's points and writing its bits where they lie (device memory,
+// or host memory the GPU reads in place).
+__global__ void __launch_bounds__(kThreads)
+    k_segment_lookup(const MultiDag* __restrict__ dags, uint32_t ndags, const LookupSegment* __restrict__ segs,
+                     uint32_t nsegs, uint64_t total_words) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total_words; w += nw) {
+        uint32_t lo = 0, hi = nsegs;
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) / 2;
+            if (segs[mid].word_start <= w) lo = mid; else hi = mid;
+        }
+        const LookupSegment sg = segs[lo];
+        const uint64_t lw = w - sg.word_start;
+        const uint64_t i = lw * 32 + (uint64_t)lane;
+        bool lit = false;
+        if (i < sg.n && sg.dag < ndags) {
+            const MultiDag D = dags[sg.dag];
+            const float scale = (float)((1u << (D.num_levels - 1)) - 1u);
+            const float* p = sg.xyz + 3 * i;
+            const int32_t px = quantise(p[0], scale), py = quantise(p[1], scale), pz = quantise(p[2], scale);
+            lit = descend(D.dag, D.words, 0u, 0u, (int)D.num_levels - 2, D.leafmasks ? 3 : 0, D.leafmasks != 0, px, py,
+                          pz);
+        }
+        const uint32_t word = __ballot_sync(0xffffffffu, lit);
+        if (lane == 0) sg.bits[lw] = word;
+    }
+}
+
 uint32_t lookup_grid(int num_sms, uint64_t n) {
     const uint64_t warps = (n + 31) / 32;
     const uint64_t blocks = (warps * 32 + kThreads - 1) / kThreads;
@@ -421,6 +454,16 @@ cpvs_status launch_multi_lookup(const MultiDag* dags, uint32_t ndags, const uint
     if (n == 0) return CPVS_OK;
     KernelTimer kt(timing, K_MULTI_LOOKUP, st);
     k_multi_lookup<<<lookup_grid(device_sms(), n), kThreads, 0, st>>>(dags, ndags, ids, xyz, n, bits);
+    CPVS_CUDA(cudaGetLastError());
+    return CPVS_OK;
+}
+
+cpvs_status launch_segment_lookup(const MultiDag* dags, uint32_t ndags, const LookupSegment* segs, uint32_t nsegs,
+                                  uint64_t total_words, cudaStream_t st, Timing* timing) {
+    if (total_words == 0 || nsegs == 0) return CPVS_OK;
+    KernelTimer kt(timing, K_MULTI_LOOKUP, st);
+    k_segment_lookup<<<lookup_grid(device_sms(), total_words * 32), kThreads, 0, st>>>(dags, ndags, segs, nsegs,
+                                                                                     total_words);
     CPVS_CUDA(cudaGetLastError());
     return CPVS_OK;
 }

@@ -276,6 +276,57 @@ CPVS_API cpvs_status cpvs_grid_words(const cpvs_grid* g, uint32_t* dag_out, uint
 CPVS_API cpvs_status cpvs_grid_lookup_ndc(const cpvs_grid* g, const float* xyz, uint64_t n, uint32_t* bits_out,
                                  uint32_t flags, void* stream);
 
+/* ---- serving ---------------------------------------------------------- */
+
+/* A request loop that takes builds and lookup batches of any size from any
+ * host thread, keeps the built DAGs resident in HBM under a byte budget
+ * (least recently used first out), and batches continuously: all lookups
+ * whose DAG is resident go out as one multi-DAG launch on a lookup stream,
+ * pending builds as one batch on a build stream, so the two overlap on the
+ * device and requests that arrive meanwhile join the next launch.  Every
+ * answer equals what the plain calls give for that request alone.  The
+ * reference has no serving layer; its app builds once and evaluates every
+ * frame (src/main.cpp:236-268).  The server takes over `ctx`: do not use the
+ * context elsewhere while the server lives. */
+typedef struct cpvs_server cpvs_server;
+
+typedef struct cpvs_server_config {
+    uint64_t budget_bytes;       /* resident DAG bytes; 0 = unlimited */
+    uint32_t max_batch_builds;   /* builds per batch; 0 = 16 */
+    uint32_t max_batch_lookups;  /* lookup requests per launch; 0 = 256 */
+    uint32_t flags;              /* build flags (CPVS_FLAG_LEAFMASKS) */
+} cpvs_server_config;
+
+typedef struct cpvs_server_stats {
+    uint64_t builds_done, lookups_done, failed, cancelled, evictions;
+    uint64_t resident_dags, resident_bytes, queued;
+    double build_p50_ms, build_p99_ms;   /* submit -> done */
+    double lookup_p50_ms, lookup_p99_ms;
+} cpvs_server_stats;
+
+CPVS_API cpvs_status cpvs_server_create(cpvs_ctx* ctx, const cpvs_server_config* cfg, cpvs_server** out);
+/* Cancels queued requests, finishes running ones, frees the resident DAGs. */
+CPVS_API void cpvs_server_destroy(cpvs_server* s);
+/* Builds the n x n host depth map into the resident DAG `key` (replacing any
+ * DAG of that key).  `depth` must stay valid until the ticket completes. */
+CPVS_API cpvs_status cpvs_server_submit_build(cpvs_server* s, uint64_t key, const float* depth, uint32_t n,
+                                              uint64_t* ticket);
+/* Looks up n NDC points (xyz interleaved) in the resident DAG `key`; waits
+ * while a build of `key` is pending; fails if `key` is neither resident nor
+ * being built.  Bits are written to `bits_out` (ceil(n/32) words).  Both
+ * buffers must stay valid until the ticket completes and be readable by the
+ * GPU in place (pinned memory; any host memory on hosts where the GPU reads
+ * pageable memory). */
+CPVS_API cpvs_status cpvs_server_submit_lookup(cpvs_server* s, uint64_t key, const float* xyz, uint64_t n,
+                                               uint32_t* bits_out, uint64_t* ticket);
+/* Waits up to timeout_us (< 0: forever) for a ticket; returns its result
+ * (CPVS_ERR_TIMEOUT if it is not done yet) and its submit-to-done latency.
+ * A ticket is reported once. */
+CPVS_API cpvs_status cpvs_server_wait(cpvs_server* s, uint64_t ticket, int64_t timeout_us, double* latency_ms);
+/* Cancels a ticket that has not started (CPVS_ERR_CANCELLED is then its result). */
+CPVS_API cpvs_status cpvs_server_cancel(cpvs_server* s, uint64_t ticket);
+CPVS_API cpvs_status cpvs_server_get_stats(cpvs_server* s, cpvs_server_stats* out);
+
 #ifdef __cplusplus
 }
 #endif
