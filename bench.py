@@ -45,6 +45,10 @@ WORKLOADS = {
     "c2": dict(queries=1 << 27, desc="32768^2 float32 depth map (plane 0.95, 4000 boxes, 512 spheres; seed 2) in 8x8 "
                                       "xy tiles of 4096^2, 8 z-tiles each: 512 DAGs of 4096^3 in one grid build; 2^27 "
                                       "NDC lookups routed through the 8^3 grid"),
+    "c4": dict(queries=0, desc="serving: Poisson arrivals, 1 build per 20 lookup batches; builds of config-0-style "
+                                 "scenes (plane 0.9, 40 boxes) with sides 2^round(U[9,13]); lookup batches of "
+                                 "2^round(U[12,22]) NDC points against a uniformly chosen resident DAG; 120 GB budget, "
+                                 "LRU eviction; offered load 0.8 of the serial plain path's capacity"),
     "c3": dict(queries=1 << 24, desc="64 independent lights (seeds 100..163, 10..2000 boxes, sides 2^round(U[8,13])) "
                                       "built in one batch; 2^24 NDC lookups spread over the 64 DAGs"),
 }
@@ -579,6 +583,111 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
+def run_served(args):
+    """c4: the same request trace through the server (continuous batching)
+    and through serial plain-path handling on the same GPU."""
+    import threading
+    import torch
+    import cpvs_gb300 as cp
+    torch.cuda.set_device(0)
+    ctx = cp.Context(0)
+    sides = [512, 1024, 2048, 4096, 8192]
+    pool = {}
+    for si, side in enumerate(sides):
+        for v in range(2):
+            sc = scene.make_scene(side, 0.9, 40, 0, 400 + 10 * si + v)
+            pool[(side, v)] = cp.raster_depth(sc, ctx=ctx).cpu().pin_memory()
+    g = np.random.Generator(np.random.PCG64(44))
+    pts_pool = torch.from_numpy((g.random((1 << 22, 3)) * 2 - 1).astype(np.float32)).pin_memory()
+    meta = np.random.Generator(np.random.PCG64(45))
+    nreq = 1200
+
+    def make_trace(rate):
+        t, trace, built = 0.0, [], []
+        for i in range(nreq):
+            t += meta.exponential(1.0 / rate)
+            if not built or meta.random() < 1.0 / 21.0:
+                side = 1 << int(round(9 + 4 * meta.random()))
+                trace.append(("build", t, i, pool[(side, int(meta.integers(0, 2)))]))
+                built.append(i)
+            else:
+                cnt = 1 << int(round(12 + 10 * meta.random()))
+                off = int(meta.integers(0, pts_pool.shape[0] - cnt + 1))
+                trace.append(("lookup", t, built[int(meta.integers(0, len(built)))], pts_pool[off:off + cnt]))
+        return trace
+
+    def plain_run(trace):
+        shadows, lat = {}, {"build": [], "lookup": []}
+        t0 = time.perf_counter()
+        for kind, at, key, data in trace:
+            now = time.perf_counter() - t0
+            if now < at:
+                time.sleep(at - now)
+            if kind == "build":
+                shadows[key] = cp.CompressedShadow.from_depth(data, ctx=ctx)
+            else:
+                out = np.empty((data.shape[0] + 31) // 32, np.uint32)
+                shadows[key].lookup_ndc_packed(data, out)
+            lat[kind].append((time.perf_counter() - t0 - at) * 1e3)
+        return lat, time.perf_counter() - t0
+
+    # calibrate: the plain path's service time over a back-to-back trace
+    calib = make_trace(1e9)
+    _, busy = plain_run(calib[:300])
+    rate = 0.8 * 300 / busy
+    trace = make_trace(rate)
+    lat_p, wall_p = plain_run(trace)
+
+    srv = cp.Server(cp.Context(0), budget_bytes=120 << 30)
+    tickets = []
+    t0 = time.perf_counter()
+
+    def submitter():
+        for kind, at, key, data in trace:
+            now = time.perf_counter() - t0
+            if now < at:
+                time.sleep(at - now)
+            if kind == "build":
+                tickets.append((kind, srv.submit_build(key, data)))
+            else:
+                tickets.append((kind, srv.submit_lookup(key, data)))
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    lat_s = {"build": [], "lookup": []}
+    got = 0
+    while got < len(trace):
+        while got >= len(tickets):
+            time.sleep(0.0001)
+        kind, t = tickets[got]
+        ms, _ = srv.wait(t)
+        lat_s[kind].append(ms)
+        got += 1
+    wall_s = time.perf_counter() - t0
+    th.join()
+    stats = srv.stats()
+    srv.close()
+
+    def summ(lat, wall):
+        allv = lat["build"] + lat["lookup"]
+        return {"p50_ms": round(float(np.percentile(allv, 50)), 3), "p99_ms": round(float(np.percentile(allv, 99)), 3),
+                "lookup_p50_ms": round(float(np.percentile(lat["lookup"], 50)), 3),
+                "lookup_p99_ms": round(float(np.percentile(lat["lookup"], 99)), 3),
+                "build_p50_ms": round(float(np.percentile(lat["build"], 50)), 3),
+                "build_p99_ms": round(float(np.percentile(lat["build"], 99)), 3),
+                "throughput_req_s": round(len(allv) / wall, 1), "wall_s": round(wall, 3)}
+    served, plain = summ(lat_s, wall_s), summ(lat_p, wall_p)
+    line = {"metric": "served p99 latency ms (c4)", "value": served["p99_ms"], "unit": "ms", "n_gpus": 1,
+            "steps": len(trace), "warmup": 300, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic: seeded scenes and Poisson request trace (no dataset)",
+            "config": {"workload": "c4: " + WORKLOADS["c4"]["desc"], "requests": len(trace),
+                       "builds": sum(1 for r in trace if r[0] == "build"), "offered_req_s": round(rate, 1)},
+            "served": served, "plain_serial": plain,
+            "p99_plain_over_served": round(plain["p99_ms"] / max(served["p99_ms"], 1e-9), 2),
+            "server_stats": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in stats.items()}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -599,6 +708,8 @@ def main():
         run_reference(args, rank, world)
     elif args.config in ("c2", "c3"):
         run_batched(args)
+    elif args.config == "c4":
+        run_served(args)
     else:
         run_ours(args, rank, world, local_rank)
 
