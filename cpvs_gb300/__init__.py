@@ -551,14 +551,17 @@ class Server:
         self._keep[t.value] = (pts, words, n)
         return t.value
 
-    def wait(self, ticket: int, timeout_us: int = -1):
+    def wait(self, ticket: int, timeout_us: int = -1, packed: bool = False):
         """Returns (latency_ms, result): result is the uint8 classes for a
-        lookup ticket, None for a build.  Raises CpvsError on failure."""
+        lookup ticket (with `packed`, the uint32 bit words as written), None
+        for a build.  Raises CpvsError on failure."""
         lat = C.c_double()
         st = _lib.cpvs_server_wait(self.handle, ticket, timeout_us, C.byref(lat))
         keep = self._keep.pop(ticket, None) if st != 3 else self._keep.get(ticket)
         _check(st)
         if keep is not None and len(keep) == 3:
+            if packed:
+                return lat.value, keep[1]
             return lat.value, unpack_bits(np.asarray(keep[1]).view(np.uint32), keep[2])
         return lat.value, None
 

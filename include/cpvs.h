@@ -280,10 +280,11 @@ CPVS_API cpvs_status cpvs_grid_lookup_ndc(const cpvs_grid* g, const float* xyz, 
 
 /* A request loop that takes builds and lookup batches of any size from any
  * host thread, keeps the built DAGs resident in HBM under a byte budget
- * (least recently used first out), and batches continuously: all lookups
- * whose DAG is resident go out as one multi-DAG launch on a lookup stream,
- * pending builds as one batch on a build stream, so the two overlap on the
- * device and requests that arrive meanwhile join the next launch.  Every
+ * (least recently used first out), and batches continuously: a dispatcher
+ * thread sends all lookups whose DAG is resident as one multi-DAG launch on
+ * a lookup stream and never waits for a build; a builder thread builds the
+ * pending maps of one side as one batch on a build stream.  The two overlap
+ * on the device, and requests that arrive meanwhile join the next launch.  Every
  * answer equals what the plain calls give for that request alone.  The
  * reference has no serving layer; its app builds once and evaluates every
  * frame (src/main.cpp:236-268).  The server takes over `ctx`: do not use the
@@ -311,9 +312,10 @@ CPVS_API void cpvs_server_destroy(cpvs_server* s);
  * DAG of that key).  `depth` must stay valid until the ticket completes. */
 CPVS_API cpvs_status cpvs_server_submit_build(cpvs_server* s, uint64_t key, const float* depth, uint32_t n,
                                               uint64_t* ticket);
-/* Looks up n NDC points (xyz interleaved) in the resident DAG `key`; waits
- * while a build of `key` is pending; fails if `key` is neither resident nor
- * being built.  Bits are written to `bits_out` (ceil(n/32) words).  Both
+/* Looks up n NDC points (xyz interleaved) in the DAG of `key` built by the
+ * latest build of `key` submitted before this call (or a later one): waits
+ * while that build is pending; fails with CPVS_ERR_INVALID_ARG if it failed,
+ * was cancelled or its DAG was evicted, or if `key` was never built.  Bits are written to `bits_out` (ceil(n/32) words).  Both
  * buffers must stay valid until the ticket completes and be readable by the
  * GPU in place (pinned memory; any host memory on hosts where the GPU reads
  * pageable memory). */

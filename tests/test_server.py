@@ -107,3 +107,40 @@ def test_cancel_a_waiting_lookup(cp):
         srv.wait(tl)
     srv.wait(tb)
     srv.close()
+
+
+def test_rebuild_orders_lookups_by_generation(cp):
+    a, b = maps_for([1024, 1024], 1000)
+    pts = np.random.default_rng(2).uniform(-1, 1, (20000, 3)).astype(np.float32)
+    want_a = cp.CompressedShadow.from_depth(a).lookup_ndc(pts)
+    want_b = cp.CompressedShadow.from_depth(b).lookup_ndc(pts)
+    assert not np.array_equal(want_a, want_b)
+    srv = cp.Server(cp.Context(0))
+    srv.wait(srv.submit_build(5, a))
+    t_old = srv.submit_lookup(5, pts)   # needs the first build (or a later one)
+    t_build = srv.submit_build(5, b)
+    t_new = srv.submit_lookup(5, pts)   # needs the second build
+    _, bits_new = srv.wait(t_new)
+    _, bits_old = srv.wait(t_old)
+    srv.wait(t_build)
+    assert np.array_equal(bits_new, want_b)
+    assert np.array_equal(bits_old, want_a) or np.array_equal(bits_old, want_b)
+    with pytest.raises(cp.CpvsError) as e:
+        srv.wait(srv.submit_lookup(6, pts))  # never built
+    assert e.value.status == 1
+    srv.close()
+
+
+def test_lookup_after_a_failed_build_fails(cp):
+    m = maps_for([2048], 1100)[0]
+    dag_bytes = cp.CompressedShadow.from_depth(m).dag_size() * 4
+    srv = cp.Server(cp.Context(0), budget_bytes=dag_bytes // 2)
+    tb = srv.submit_build(3, m)
+    tl = srv.submit_lookup(3, np.zeros((100, 3), np.float32))
+    with pytest.raises(cp.CpvsError) as e:
+        srv.wait(tb)
+    assert e.value.status == 6  # CPVS_ERR_BUDGET
+    with pytest.raises(cp.CpvsError) as e:
+        srv.wait(tl)
+    assert e.value.status == 1
+    srv.close()
