@@ -24,6 +24,7 @@ SHADOW, VISIBLE, PARTIAL = 0, 1, 2
 FLAG_LEAFMASKS = 0x1
 IO_DEVICE = 0x100
 FLAG_BORROW_INPUT = 0x200
+EVAL_U8 = 0x400
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "device wait timed out",
           4: "CUDA device error", 5: "unimplemented", 6: "memory budget exceeded", 7: "cancelled",
@@ -89,6 +90,12 @@ _SIGS = {
     "cpvs_grid_dag_size": (_u64, [_vp]),
     "cpvs_grid_words": (C.c_int, [_vp, _vp, _u64, _vp, _u64, _vp]),
     "cpvs_grid_lookup_ndc": (C.c_int, [_vp, _vp, _u64, _vp, _u32, _vp]),
+    "cpvs_grid_set_filter_size": (C.c_int, [_vp, _u32]),
+    "cpvs_shadow_serialize": (C.c_int, [_vp, _vp, _u64, _vp, _vp]),
+    "cpvs_shadow_deserialize": (C.c_int, [_vp, _vp, _u64, _vp, _vp]),
+    "cpvs_grid_serialize": (C.c_int, [_vp, _vp, _u64, _vp, _vp]),
+    "cpvs_grid_deserialize": (C.c_int, [_vp, _vp, _u64, _vp, _vp]),
+    "cpvs_grid_evaluate": (C.c_int, [_vp, _vp, _u32, _u32, _u32, _vp, _u32, _vp, _vp]),
     "cpvs_shadow_build_noalloc": (C.c_int, [_vp, _u32, _u32, _u32, _u32, _vp, _u64, C.POINTER(_u64), _vp]),
 }
 
@@ -324,6 +331,31 @@ class CompressedShadow:
                                                   _stream(stream), C.byref(h)))
         return CompressedShadow(h.value, ctx)
 
+    def to_bytes(self, stream=None) -> bytes:
+        """The saved form (cpvs_shadow_serialize): header, level counts, DAG."""
+        size = C.c_uint64()
+        _check(_lib.cpvs_shadow_serialize(self.handle, None, 0, C.byref(size), _stream(stream)))
+        buf = np.zeros(size.value, np.uint8)
+        _check(_lib.cpvs_shadow_serialize(self.handle, buf.ctypes.data, buf.size, C.byref(size), _stream(stream)))
+        return buf.tobytes()
+
+    @staticmethod
+    def from_bytes(data, ctx: Optional[Context] = None, stream=None) -> "CompressedShadow":
+        ctx = ctx or Context.default()
+        buf = np.frombuffer(data, np.uint8)
+        h = _vp()
+        _check(_lib.cpvs_shadow_deserialize(ctx.handle, buf.ctypes.data, buf.size, _stream(stream), C.byref(h)))
+        return CompressedShadow(h.value, ctx)
+
+    def save(self, path: str):
+        with open(path, "wb") as f:
+            f.write(self.to_bytes())
+
+    @staticmethod
+    def load(path: str, ctx: Optional[Context] = None) -> "CompressedShadow":
+        with open(path, "rb") as f:
+            return CompressedShadow.from_bytes(f.read(), ctx)
+
     @staticmethod
     def create_batch(sources, jobs, leafmasks: bool = True, stream=None) -> list:
         """Many DAGs in one batch.  `sources`: MinMaxHierarchy list; `jobs`:
@@ -504,6 +536,70 @@ class CompressedShadowContainer:
         words = np.zeros(max((n + 31) // 32, 1), np.uint32)
         _check(_lib.cpvs_grid_lookup_ndc(self.handle, pts.ctypes.data, n, words.ctypes.data, 0, _stream(stream)))
         return unpack_bits(words, n)
+
+    def to_bytes(self, stream=None) -> bytes:
+        """The saved form (cpvs_grid_serialize): header, cell words, combined DAG."""
+        size = C.c_uint64()
+        _check(_lib.cpvs_grid_serialize(self.handle, None, 0, C.byref(size), _stream(stream)))
+        buf = np.zeros(size.value, np.uint8)
+        _check(_lib.cpvs_grid_serialize(self.handle, buf.ctypes.data, buf.size, C.byref(size), _stream(stream)))
+        return buf.tobytes()
+
+    @classmethod
+    def from_bytes(cls, data, ctx: Optional[Context] = None, stream=None) -> "CompressedShadowContainer":
+        """A finalized container (no cell shadows) from its saved form."""
+        ctx = ctx or Context.default()
+        buf = np.frombuffer(data, np.uint8)
+        h = _vp()
+        _check(_lib.cpvs_grid_deserialize(ctx.handle, buf.ctypes.data, buf.size, _stream(stream), C.byref(h)))
+        c = cls.__new__(cls)
+        c.ctx, c.handle, c._cells = ctx, h.value, {}
+        c.length = int(_lib.cpvs_grid_length(c.handle))
+        return c
+
+    def save(self, path: str):
+        with open(path, "wb") as f:
+            f.write(self.to_bytes())
+
+    @classmethod
+    def load(cls, path: str, ctx: Optional[Context] = None) -> "CompressedShadowContainer":
+        with open(path, "rb") as f:
+            return cls.from_bytes(f.read(), ctx)
+
+    def set_filter_size(self, size: int):
+        """Width (= height) of the percentage-closer filter of evaluate."""
+        _check(_lib.cpvs_grid_set_filter_size(self.handle, size))
+        self.filter_size = size
+
+    setFilterSize = set_filter_size
+
+    def evaluate(self, positions, light_view_proj, out=None, packed: bool = False, stream=None):
+        """Visibility of every world-space position of an (H, W, C>=3)
+        float32 image under `light_view_proj` (4x4, M[row, col] acting on
+        column vectors; a flat 16-vector is read column-major, as
+        glm::value_ptr gives it).  Returns an (H, W) uint8 image (255 lit,
+        0 shadowed, or the PCF fraction * 255), or with `packed` the bit
+        words (filter size 1 only).  Device tensors in, device tensor out."""
+        M = np.asarray(light_view_proj, np.float32)
+        colmajor = np.ascontiguousarray(M.T.ravel() if M.shape == (4, 4) else M.ravel(), np.float32)
+        if colmajor.size != 16:
+            raise ValueError("light_view_proj must be 4x4 or 16 floats")
+        h, w, fpp = (int(v) for v in positions.shape)
+        n = h * w
+        flags = 0 if packed else EVAL_U8
+        if _is_device(positions):
+            import torch
+            if out is None:
+                out = (torch.empty((n + 31) // 32, dtype=torch.int32, device=positions.device) if packed
+                       else torch.empty((h, w), dtype=torch.uint8, device=positions.device))
+            _check(_lib.cpvs_grid_evaluate(self.handle, _ptr(positions), w, h, fpp, colmajor.ctypes.data,
+                                           flags | IO_DEVICE, _ptr(out), _stream(stream)))
+            return out
+        pos = np.ascontiguousarray(positions, np.float32)
+        res = np.zeros(max((n + 31) // 32, 1), np.uint32) if packed else np.zeros((h, w), np.uint8)
+        _check(_lib.cpvs_grid_evaluate(self.handle, pos.ctypes.data, w, h, fpp, colmajor.ctypes.data, flags,
+                                       res.ctypes.data, _stream(stream)))
+        return res
 
     def __del__(self):
         if getattr(self, "handle", None) and _lib is not None:

@@ -114,43 +114,52 @@ cpvs_status stage_in(cpvs::Ctx& c, const void* src, uint64_t bytes, uint32_t fla
     return CPVS_OK;
 }
 
+// Host or device input of `qbytes` and output of `obytes` around one launch:
+// host buffers are read / written in place where the GPU can reach them,
+// else staged through stream-ordered scratch.  Host output is complete on
+// return.
+cpvs_status io_common(cpvs_ctx* ctx, const void* in, uint64_t qbytes, void* out, uint64_t obytes, uint32_t flags,
+                      cudaStream_t st, const std::function<cpvs_status(const void*, void*)>& run) {
+    cpvs_status r = set_device(ctx);
+    if (r != CPVS_OK) return r;
+    cpvs::Ctx& c = ctx->c;
+    void* q = nullptr;
+    bool qowned = false;
+    r = stage_in(c, in, qbytes, flags, st, &q, &qowned);
+    if (r != CPVS_OK) return r;
+    void* o = out;
+    bool oowned = false, host_out = false;
+    if (!(flags & CPVS_IO_DEVICE)) {
+        host_out = true;
+        o = host_accessible(c, out);
+        if (!o) {
+            r = c.alloc(&o, obytes, false, st);
+            if (r != CPVS_OK) {
+                if (qowned) c.release(q, qbytes, false, st);
+                return r;
+            }
+            oowned = true;
+        }
+    }
+    r = run(q, o);
+    if (r == CPVS_OK && host_out) {
+        cudaError_t e = oowned ? cudaMemcpyAsync(out, o, obytes, cudaMemcpyDeviceToHost, st) : cudaSuccess;
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) r = cpvs::cuda_fail(e, "lookup read-back");
+    }
+    if (qowned) c.release(q, std::max<uint64_t>(qbytes, 4), false, st);
+    if (oowned) c.release(o, obytes, false, st);
+    return r;
+}
+
 cpvs_status lookup_common(cpvs_ctx* ctx, const void* xyz, uint64_t n, uint32_t* bits_out, uint32_t flags,
                           cudaStream_t st, const std::function<cpvs_status(const void*, uint32_t*)>& run) {
     if (!xyz && n) return fail(CPVS_ERR_INVALID_ARG, "lookup: null input");
     if (!bits_out && n) return fail(CPVS_ERR_INVALID_ARG, "lookup: null output");
     if (n == 0) return CPVS_OK;
     if (n >= (1ull << 40)) return fail(CPVS_ERR_INVALID_ARG, "lookup: batch too large");
-    cpvs_status r = set_device(ctx);
-    if (r != CPVS_OK) return r;
-    cpvs::Ctx& c = ctx->c;
-    const uint64_t qbytes = n * 12, bbytes = (n + 31) / 32 * 4;
-    void* q = nullptr;
-    bool qowned = false;
-    r = stage_in(c, xyz, qbytes, flags, st, &q, &qowned);
-    if (r != CPVS_OK) return r;
-    uint32_t* bits = bits_out;
-    bool bowned = false, host_out = false;
-    if (!(flags & CPVS_IO_DEVICE)) {
-        host_out = true;
-        bits = static_cast<uint32_t*>(host_accessible(c, bits_out));
-        if (!bits) {
-            r = c.alloc((void**)&bits, bbytes, false, st);
-            if (r != CPVS_OK) {
-                if (qowned) c.release(q, qbytes, false, st);
-                return r;
-            }
-            bowned = true;
-        }
-    }
-    r = run(q, bits);
-    if (r == CPVS_OK && host_out) {
-        cudaError_t e = bowned ? cudaMemcpyAsync(bits_out, bits, bbytes, cudaMemcpyDeviceToHost, st) : cudaSuccess;
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) r = cpvs::cuda_fail(e, "lookup read-back");
-    }
-    if (qowned) c.release(q, std::max<uint64_t>(qbytes, 4), false, st);
-    if (bowned) c.release(bits, bbytes, false, st);
-    return r;
+    return io_common(ctx, xyz, n * 12, bits_out, (n + 31) / 32 * 4, flags, st,
+                     [&](const void* q, void* o) { return run(q, static_cast<uint32_t*>(o)); });
 }
 
 // Builds `jobs` in one batch and wraps each job's DAG in a shadow; all of
@@ -858,6 +867,39 @@ cpvs_status cpvs_grid_lookup_ndc(const cpvs_grid* g, const float* xyz, uint64_t 
         g->touch(st);
         return r;
     });
+}
+
+cpvs_status cpvs_grid_set_filter_size(cpvs_grid* g, uint32_t filter_size) {
+    if (!g) return fail(CPVS_ERR_INVALID_ARG, "grid_set_filter_size: null grid");
+    if (filter_size > 32) return fail(CPVS_ERR_INVALID_ARG, "grid_set_filter_size: filter size above 32");
+    g->filter_size = filter_size ? filter_size : 1;
+    return CPVS_OK;
+}
+
+cpvs_status cpvs_grid_evaluate(const cpvs_grid* g, const float* positions, uint32_t width, uint32_t height,
+                               uint32_t floats_per_pixel, const float* light_view_proj, uint32_t flags, void* out,
+                               void* stream) {
+    if (!g || !g->finalized) return fail(CPVS_ERR_INVALID_ARG, "grid_evaluate: grid not finalized");
+    if (!light_view_proj) return fail(CPVS_ERR_INVALID_ARG, "grid_evaluate: null matrix");
+    if (floats_per_pixel < 3) return fail(CPVS_ERR_INVALID_ARG, "grid_evaluate: fewer than 3 floats per pixel");
+    const uint64_t n = (uint64_t)width * height;
+    if (n == 0) return CPVS_OK;
+    if (!positions || !out) return fail(CPVS_ERR_INVALID_ARG, "grid_evaluate: null buffer");
+    if (n >= (1ull << 40)) return fail(CPVS_ERR_INVALID_ARG, "grid_evaluate: image too large");
+    const bool u8 = (flags & CPVS_EVAL_U8) != 0;
+    if (!u8 && g->filter_size > 1)
+        return fail(CPVS_ERR_INVALID_ARG, "grid_evaluate: a filter size above 1 needs CPVS_EVAL_U8 output");
+    cudaStream_t st = (cudaStream_t)stream;
+    const uint64_t obytes = u8 ? n : (n + 31) / 32 * 4;
+    return io_common(g->ctx, positions, n * floats_per_pixel * 4, out, obytes, flags, st,
+                     [&](const void* q, void* o) {
+                         cpvs_status r = cpvs::launch_grid_evaluate(
+                             g->dag, g->words, g->cell_words, g->length, g->dag_levels, g->leafmasks,
+                             static_cast<const float*>(q), floats_per_pixel, n, light_view_proj, g->filter_size, u8, o,
+                             st, &g->ctx->c.timing);
+                         g->touch(st);
+                         return r;
+                     });
 }
 
 }  // extern "C"

@@ -134,6 +134,13 @@ int tune_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool l
 cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks,
                           const uint32_t* top, const void* xyz, bool ndc, uint64_t n, uint32_t* bits,
                           cudaStream_t st, Timing* timing = nullptr, int queries_per_thread = 4);
+// World-space evaluation over a grid: n pixels of `fpp` floats (xyz first),
+// column-major 4x4 light view-projection, PCF footprint `filter`; output one
+// byte per pixel (u8) or one bit per pixel.
+cpvs_status launch_grid_evaluate(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
+                                 uint32_t dag_levels, bool leafmasks, const float* positions, uint32_t fpp, uint64_t n,
+                                 const float* light_view_proj, uint32_t filter, bool u8, void* out, cudaStream_t st,
+                                 Timing* timing = nullptr);
 cpvs_status launch_grid_lookup(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
                                uint32_t dag_levels, bool leafmasks, const float* xyz, uint64_t n, uint32_t* bits,
                                cudaStream_t st, Timing* timing = nullptr);
@@ -160,6 +167,7 @@ enum KernelId : int {
     K_GRID_LOOKUP,
     K_RASTER,
     K_MULTI_LOOKUP,
+    K_EVALUATE,
     K_COUNT
 };
 const char* kernel_name(int id);

@@ -297,6 +297,85 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// One grid sample at an integer path (shader/traverse.cs:75-88 routing):
+// outside the grid answers lit, a uniform cell its class, else the descent
+// of the cell's DAG with pointers relative to its first word.
+__device__ __forceinline__ bool grid_sample(const uint32_t* __restrict__ dag, uint32_t words,
+                                            const uint32_t* __restrict__ cells, uint32_t length, int dag_levels,
+                                            bool leafmasks, int64_t px, int64_t py, int64_t pz) {
+    const int sh = dag_levels - 1;
+    const int64_t lim = (int64_t)length << sh;
+    if (px < 0 || py < 0 || pz < 0 || px >= lim || py >= lim || pz >= lim) return true;
+    const uint32_t cell = __ldg(cells + ((size_t)(pz >> sh) * length + (size_t)(py >> sh)) * length + (size_t)(px >> sh));
+    if (cell == kCellShadow) return false;
+    if (cell == kCellLit) return true;
+    return descend(dag, words, cell, cell, dag_levels - 2, leafmasks ? 3 : 0, leafmasks, (int32_t)px, (int32_t)py,
+                   (int32_t)pz);
+}
+
+// World-space evaluation (src/CompressedShadowContainer.cpp:93-124,
+// shader/traverse.cs:134-148): pixel i's position p (the first three of its
+// `fpp` floats) goes through the column-major light view-projection m as
+// c_r = ((m[r]*x + m[4+r]*y) + m[8+r]*z) + m[12+r] (the shader's
+// lightViewProj * vec4(p, 1), no contraction), ndc = c.xyz / c.w, then the
+// grid lookup.  With filter f > 1, the f x f texel footprint around the
+// path (offsets -(f-1)/2 .. f/2 in x and y, same depth voxel) is sampled and
+// the lit fraction written as round(255 * lit / f^2) -- percentage-closer
+// filtering, which the reference declares (setFilterSize) but never
+// implements.  U8: one byte per pixel (0 / 255 when f <= 1, as an r8 image
+// stores 0.0 / 1.0); else one bit per pixel, 32 per word.
+struct EvalMatrix {
+    float m[16];
+};
+
+template <bool U8>
+__global__ void __launch_bounds__(kThreads)
+    k_grid_evaluate(const uint32_t* __restrict__ dag, uint32_t words, const uint32_t* __restrict__ cells,
+                    uint32_t length, int dag_levels, int grid_levels, bool leafmasks, const float* __restrict__ pos,
+                    uint32_t fpp, uint64_t n, EvalMatrix M, int filter, void* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t nwords = (n + 31) / 32;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const float scale = (float)((1u << (dag_levels + grid_levels - 1)) - 1u);
+    const int lo = -((filter - 1) / 2), hi = filter / 2;
+    const uint32_t f2 = (uint32_t)(filter * filter);
+    for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwords; w += nw) {
+        const uint64_t i = w * 32 + (uint64_t)lane;
+        bool lit = false;
+        uint32_t cnt = 0;
+        if (i < n) {
+            const float* p = pos + (size_t)fpp * i;
+            const float x = p[0], y = p[1], z = p[2];
+            float c[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+                c[r] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(M.m[r], x), __fmul_rn(M.m[4 + r], y)),
+                                           __fmul_rn(M.m[8 + r], z)),
+                                 M.m[12 + r]);
+            const int64_t px = quantise(__fdiv_rn(c[0], c[3]), scale);
+            const int64_t py = quantise(__fdiv_rn(c[1], c[3]), scale);
+            const int64_t pz = quantise(__fdiv_rn(c[2], c[3]), scale);
+            if (filter <= 1) {
+                lit = grid_sample(dag, words, cells, length, dag_levels, leafmasks, px, py, pz);
+                cnt = lit ? 1u : 0u;
+            } else {
+                for (int dy = lo; dy <= hi; ++dy)
+                    for (int dx = lo; dx <= hi; ++dx)
+                        cnt += grid_sample(dag, words, cells, length, dag_levels, leafmasks, px + dx, py + dy, pz) ? 1u
+                                                                                                                 : 0u;
+            }
+        }
+        if (U8) {
+            if (i < n)
+                static_cast<uint8_t*>(out)[i] =
+                    filter <= 1 ? (uint8_t)(cnt ? 255u : 0u) : (uint8_t)((255u * cnt + f2 / 2u) / f2);
+        } else {
+            const uint32_t word = __ballot_sync(0xffffffffu, lit);
+            if (lane == 0) static_cast<uint32_t*>(out)[w] = word;
+        }
+    }
+}
+
 // Many resident DAGs at once: query i descends DAG dags[ids[i]] (its own
 // depth and leafmask mode); ids outside the table answer "shadow".
 __global__ void __launch_bounds__(kThreads)
@@ -464,6 +543,27 @@ cpvs_status launch_segment_lookup(const MultiDag* dags, uint32_t ndags, const Lo
     KernelTimer kt(timing, K_MULTI_LOOKUP, st);
     k_segment_lookup<<<lookup_grid(device_sms(), total_words * 32), kThreads, 0, st>>>(dags, ndags, segs, nsegs,
                                                                                      total_words);
+    CPVS_CUDA(cudaGetLastError());
+    return CPVS_OK;
+}
+
+cpvs_status launch_grid_evaluate(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
+                                 uint32_t dag_levels, bool leafmasks, const float* positions, uint32_t fpp, uint64_t n,
+                                 const float* light_view_proj, uint32_t filter, bool u8, void* out, cudaStream_t st,
+                                 Timing* timing) {
+    if (n == 0) return CPVS_OK;
+    KernelTimer kt(timing, K_EVALUATE, st);
+    EvalMatrix M;
+    for (int k = 0; k < 16; ++k) M.m[k] = light_view_proj[k];
+    const uint32_t g = lookup_grid(device_sms(), n);
+    if (u8)
+        k_grid_evaluate<true><<<g, kThreads, 0, st>>>(dag, (uint32_t)words, cells, length, (int)dag_levels,
+                                                      log2_u32(length), leafmasks, positions, fpp, n, M, (int)filter,
+                                                      out);
+    else
+        k_grid_evaluate<false><<<g, kThreads, 0, st>>>(dag, (uint32_t)words, cells, length, (int)dag_levels,
+                                                       log2_u32(length), leafmasks, positions, fpp, n, M, (int)filter,
+                                                       out);
     CPVS_CUDA(cudaGetLastError());
     return CPVS_OK;
 }

@@ -75,6 +75,7 @@ struct cpvs_grid : DeviceObject {
     uint32_t dag_levels = 0;
     bool leafmasks = false;
     bool finalized = false;
+    uint32_t filter_size = 1;  // PCF footprint of evaluate
 };
 
 

@@ -278,6 +278,55 @@ CPVS_API cpvs_status cpvs_grid_lookup_ndc(const cpvs_grid* g, const float* xyz, 
 
 /* ---- serving ---------------------------------------------------------- */
 
+/* Saving and loading built DAGs (no reference counterpart: the reference
+ * keeps DAGs in memory only, getDAG() in src/CompressedShadow.h:71-77).
+ * The format, little-endian: a 48-byte header -- magic "CPVSDAG\0", u32
+ * version 1, u32 kind (0 shadow, 1 grid), u32 numLevels, u32 flags (bit 0
+ * leafmasks), u32 grid length (1 for a shadow), u32 0, u64 DAG words, u64
+ * FNV-1a-64 checksum of all bytes after the header -- then for a shadow its
+ * per-level tree and unique node counts (2 x numLevels u64) and the DAG
+ * words, for a grid its length^3 cell words and the combined DAG words.
+ * serialize: with buf == NULL only *size is set; else the image is written
+ * to the host buffer (CPVS_ERR_CAPACITY when capacity < *size).
+ * deserialize: checks magic, version, sizes, checksum and cell offsets
+ * (CPVS_ERR_INVALID_ARG) and uploads the DAG; a loaded grid is finalized and
+ * has no cell shadows (cpvs_grid_get returns NULL). */
+CPVS_API cpvs_status cpvs_shadow_serialize(const cpvs_shadow* s, void* buf, uint64_t capacity, uint64_t* size,
+                                           void* stream);
+CPVS_API cpvs_status cpvs_shadow_deserialize(cpvs_ctx* ctx, const void* buf, uint64_t size, void* stream,
+                                             cpvs_shadow** out);
+CPVS_API cpvs_status cpvs_grid_serialize(const cpvs_grid* g, void* buf, uint64_t capacity, uint64_t* size,
+                                         void* stream);
+CPVS_API cpvs_status cpvs_grid_deserialize(cpvs_ctx* ctx, const void* buf, uint64_t size, void* stream,
+                                           cpvs_grid** out);
+
+/* Output of cpvs_grid_evaluate: one byte per pixel instead of one bit. */
+#define CPVS_EVAL_U8 0x400u
+
+/* CompressedShadowContainer::setFilterSize (src/CompressedShadowContainer.h:70-73):
+ * the width (= height) of the percentage-closer filter footprint of
+ * cpvs_grid_evaluate, 1 (default) .. 32.  The reference passes it to its
+ * shader but never uses it (shader/traverse.cs:16-17); here it filters. */
+CPVS_API cpvs_status cpvs_grid_set_filter_size(cpvs_grid* g, uint32_t filter_size);
+/* CompressedShadowContainer::evaluate (src/CompressedShadowContainer.cpp:93-124,
+ * shader/traverse.cs:134-148) on buffers instead of textures: `positions`
+ * is a row-major width x height image of `floats_per_pixel` (>= 3) floats
+ * per pixel whose first three are the world-space position (an rgba32f
+ * G-buffer has 4; the 4th is ignored, as the shader reads .xyz).  Each
+ * position goes through `light_view_proj` (16 floats, column-major as
+ * glm::value_ptr gives them) as c = M * (x, y, z, 1) in float32 without
+ * contraction, in the order ((m[r]*x + m[4+r]*y) + m[8+r]*z) + m[12+r];
+ * ndc = c.xyz / c.w; then the grid lookup of cpvs_grid_lookup_ndc.  Output:
+ * with CPVS_EVAL_U8 one byte per pixel -- 255 lit / 0 shadowed (what the
+ * shader's r8 image stores), or with a filter size f > 1 round(255 * lit / f^2)
+ * over the f x f texel footprint (offsets -(f-1)/2 .. f/2 in x and y around
+ * the quantised path, same depth voxel) -- else one bit per pixel
+ * (ceil(width*height/32) words; filter size 1 only).  Host or device
+ * buffers as for lookups (CPVS_IO_DEVICE). */
+CPVS_API cpvs_status cpvs_grid_evaluate(const cpvs_grid* g, const float* positions, uint32_t width, uint32_t height,
+                                        uint32_t floats_per_pixel, const float* light_view_proj, uint32_t flags,
+                                        void* out, void* stream);
+
 /* A request loop that takes builds and lookup batches of any size from any
  * host thread, keeps the built DAGs resident in HBM under a byte budget
  * (least recently used first out), and batches continuously: a dispatcher

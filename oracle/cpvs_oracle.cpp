@@ -530,6 +530,53 @@ void oracle_grid_lookup_ndc(const uint32_t* dag, const uint32_t* cell_offset, ui
     });
 }
 
+/* CompressedShadowContainer::evaluate (src/CompressedShadowContainer.cpp:93-124)
+ * with the shader's per-pixel body (shader/traverse.cs:134-148): pixel i's
+ * position (the first three of its `fpp` floats) times the column-major
+ * light view-projection m as c_r = ((m[r]*x + m[4+r]*y) + m[8+r]*z) + m[12+r]
+ * (the shader's lightViewProj * vec4(pos, 1); float32, no contraction), the
+ * perspective divide ndc = c.xyz / c.w, the path of getPathFromNDC at the
+ * grid's resolution, then the grid lookup of oracle_grid_lookup_ndc.  Output
+ * one byte per pixel: 255 lit / 0 shadowed, or with filter f > 1 the
+ * percentage-closer fraction round(255 * lit / f^2) over the paths
+ * (px+dx, py+dy, pz), dx, dy in -(f-1)/2 .. f/2 (the reference declares the
+ * filter size, src/CompressedShadowContainer.h:70-73, but its shader never
+ * uses it; this is the definition the GPU path implements). */
+void oracle_grid_evaluate(const uint32_t* dag, const uint32_t* cell_offset, uint32_t length, uint32_t dag_levels,
+                          int leafmasks, const float* pos, uint64_t n, uint32_t fpp, const float* m, uint32_t filter,
+                          uint8_t* out, int threads) {
+    const int grid_levels = log2_exact(length);
+    const float scale = (float)((1u << (dag_levels + grid_levels - 1)) - 1u);
+    const int64_t lim = (int64_t)length << (dag_levels - 1);
+    const int f = filter < 1 ? 1 : (int)filter;
+    const int lo = -((f - 1) / 2), hi = f / 2;
+    auto sample = [&](int64_t px, int64_t py, int64_t pz) -> bool {
+        if (px < 0 || py < 0 || pz < 0 || px >= lim || py >= lim || pz >= lim) return true;
+        const int s = (int)dag_levels - 1;
+        const uint32_t base = cell_offset[((size_t)(pz >> s) * length + (size_t)(py >> s)) * length + (size_t)(px >> s)];
+        return descend(dag, base, (int)dag_levels, leafmasks != 0, (int32_t)px, (int32_t)py, (int32_t)pz) == VISIBLE;
+    };
+    run_parallel(n, threads, [&](uint64_t a, uint64_t b) {
+        for (uint64_t i = a; i < b; ++i) {
+            const float x = pos[fpp * i], y = pos[fpp * i + 1], z = pos[fpp * i + 2];
+            float c[4];
+            for (int r = 0; r < 4; ++r) {
+                float t = m[r] * x;
+                t = t + m[4 + r] * y;
+                t = t + m[8 + r] * z;
+                c[r] = t + m[12 + r];
+            }
+            const int64_t px = quantise(c[0] / c[3], scale), py = quantise(c[1] / c[3], scale),
+                          pz = quantise(c[2] / c[3], scale);
+            uint32_t cnt = 0;
+            for (int dy = lo; dy <= hi; ++dy)
+                for (int dx = lo; dx <= hi; ++dx) cnt += sample(px + dx, py + dy, pz) ? 1u : 0u;
+            const uint32_t f2 = (uint32_t)(f * f);
+            out[i] = (f == 1) ? (uint8_t)(cnt ? 255u : 0u) : (uint8_t)((255u * cnt + f2 / 2u) / f2);
+        }
+    });
+}
+
 }  // extern "C"
 
 static void run_parallel(uint64_t n, int threads, const std::function<void(uint64_t, uint64_t)>& f) {

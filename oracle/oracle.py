@@ -94,6 +94,8 @@ class Oracle:
         L.oracle_lookup_ndc.argtypes = [_u32p, C.c_uint32, C.c_int, _f32p, C.c_uint64, _u8p, C.c_int]
         L.oracle_grid_lookup_ndc.argtypes = [_u32p, _u32p, C.c_uint32, C.c_uint32, C.c_int, _f32p,
                                              C.c_uint64, _u8p, C.c_int]
+        L.oracle_grid_evaluate.argtypes = [_u32p, _u32p, C.c_uint32, C.c_uint32, C.c_int, _f32p, C.c_uint64,
+                                           C.c_uint32, _f32p, C.c_uint32, _u8p, C.c_int]
         L.oracle_merge_level.argtypes = [_u32p, C.c_uint32, C.c_uint32, _u32p, _u32p]
         L.oracle_merge_level.restype = C.c_uint32
         self.lib = L
@@ -148,6 +150,18 @@ class Oracle:
         self.lib.oracle_lookup_ndc(np.ascontiguousarray(dag, np.uint32), num_levels, int(leafmasks), q,
                                    out.size, out, threads)
         return out
+
+    def grid_evaluate(self, dag, cell_offsets, length, dag_levels, leafmasks, positions, light_view_proj_colmajor,
+                      filter_size: int = 1, threads: int = 1):
+        """(H, W) uint8 visibilities of an (H, W, C>=3) position image."""
+        h, w, fpp = positions.shape
+        pos = np.ascontiguousarray(positions, np.float32).reshape(-1)
+        m = np.ascontiguousarray(light_view_proj_colmajor, np.float32).reshape(16)
+        out = np.zeros(h * w, np.uint8)
+        self.lib.oracle_grid_evaluate(np.ascontiguousarray(dag, np.uint32),
+                                      np.ascontiguousarray(cell_offsets, np.uint32), length, dag_levels,
+                                      int(leafmasks), pos, h * w, fpp, m, filter_size, out, threads)
+        return out.reshape(h, w)
 
     def grid_lookup_ndc(self, dag, cell_offsets, length, dag_levels, leafmasks, xyz, threads: int = 1):
         q = np.ascontiguousarray(xyz, np.float32).reshape(-1)
