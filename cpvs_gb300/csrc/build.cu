@@ -245,86 +245,194 @@ __global__ void __launch_bounds__(kThreads)
 // footprint; the four bits of each texel's k are packed into four 64-bit
 // planes, from which the eight slice masks follow by bit logic
 // (slice s = {t : k_t > s}).
-__device__ __forceinline__ uint32_t lit_count(float d_scaled, int32_t bz) {
-    // Z = floor(x - 0.5) for x = d*H0, as floor(x) - (frac(x) < 0.5); x is
-    // clamped to +-2^30 first (NaN lands on -2^30: never lit, as
-    // mid <= NaN is false).
-    const float x = fminf(fmaxf(d_scaled, -1073741824.0f), 1073741824.0f);
-    const float f = floorf(x);
-    const int32_t z = (int32_t)f - ((x - f) < 0.5f ? 1 : 0);
-    const int32_t k = z - bz + 1;
-    return (uint32_t)(k < 0 ? 0 : (k > 8 ? 8 : k));
+// Lit voxels among z = bz .. bz+7 of a texel with v = fl(d * H0): voxel z is
+// lit iff z + 0.5 <= v (src/CompressedShadowUtil.h:35-57), so the count is
+// clamp(floor(t) + 1, 0, 8) with t = v - (bz + 0.5).  bz is a multiple of 8
+// below 2^23, so bz + 0.5 is exact, and the float subtraction decides every
+// case exactly: for v in [c/2, 2c] (c = bz + 0.5) it is exact (Sterbenz);
+// below c/2, t < -c/2 stays negative (count 0); above 2c, either bz = 0 and
+// v - 0.5 is exact for v < 8.5, or t > 8 (count 8).  NaN: fmaxf picks -1
+// (count 0, as z + 0.5 <= NaN is false); +inf saturates to 8.
+__device__ __forceinline__ uint32_t lit_count(float v, float c) {
+    const float t = fmaxf(__fsub_rn(v, c), -1.0f);
+    const int32_t k = __float2int_rd(t) + 1;
+    return (uint32_t)min(k, 8);
 }
 
+// The eight 64-bit slice masks of leaf i (level-2 node: the 8x8x8 voxels at
+// 4 * its coordinate), its 16-bit class mask (01 lit / 00 shadow / 10
+// partial per slice, src/CompressedShadowUtil.cpp:59-99) and its signature
+// hash.  Returns false for a stale slot (an internal check already failed):
+// the caller then treats it as an empty leaf of job 0.
+__device__ __forceinline__ bool leaf_compute(const LevelDev& lv, const JobDev* __restrict__ jobs, uint32_t njobs,
+                                             uint32_t i, uint64_t M[8], uint32_t& mask, uint64_t& hash,
+                                             uint32_t& j) {
+    const uint64_t c = lv.coord[i];
+    j = lv.job[i];
+    const uint32_t bx = unpack_x(c) * 4u, by = unpack_y(c) * 4u, bz = unpack_z(c) * 4u;
+    if (j >= njobs || bx + 8u > __ldg(&jobs[j].n) || by + 8u > __ldg(&jobs[j].n)) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) M[q] = 0ull;
+        mask = 0;
+        j = 0;
+        hash = 0;
+        return false;
+    }
+    const uint32_t nmap = __ldg(&jobs[j].n);
+    const float H = __uint2float_rn(nmap * __ldg(&jobs[j].z_num));
+    const float cz = __fadd_rn(__uint2float_rn(bz), 0.5f);
+    const float* row0 = jobs[j].depth + (size_t)by * nmap + bx;
+    float4 a[8], b[8];
+#pragma unroll
+    for (int y = 0; y < 8; ++y) {
+        a[y] = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap));
+        b[y] = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap + 4));
+    }
+    uint32_t p0[2] = {0u, 0u}, p1[2] = {0u, 0u}, p2[2] = {0u, 0u}, p3[2] = {0u, 0u};
+#pragma unroll
+    for (int y = 0; y < 8; ++y) {
+        const float v[8] = {a[y].x, a[y].y, a[y].z, a[y].w, b[y].x, b[y].y, b[y].z, b[y].w};
+#pragma unroll
+        for (int x = 0; x < 8; ++x) {
+            const uint32_t k = lit_count(__fmul_rn(v[x], H), cz);
+            const int t = 8 * y + x, w = t >> 5, sh = t & 31;
+            p0[w] |= (k & 1u) << sh;
+            p1[w] |= ((k >> 1) & 1u) << sh;
+            p2[w] |= ((k >> 2) & 1u) << sh;
+            p3[w] |= ((k >> 3) & 1u) << sh;
+        }
+    }
+    const uint64_t P0 = p0[0] | ((uint64_t)p0[1] << 32), P1 = p1[0] | ((uint64_t)p1[1] << 32);
+    const uint64_t P2 = p2[0] | ((uint64_t)p2[1] << 32), P3 = p3[0] | ((uint64_t)p3[1] << 32);
+    // slice s = {t : k_t >= s+1}, k_t in [0, 8]
+    M[0] = P0 | P1 | P2 | P3;
+    M[1] = P1 | P2 | P3;
+    M[2] = P3 | P2 | (P1 & P0);
+    M[3] = P3 | P2;
+    M[4] = P3 | (P2 & (P1 | P0));
+    M[5] = P3 | (P2 & P1);
+    M[6] = P3 | (P2 & P1 & P0);
+    M[7] = P3;
+    mask = 0;
+    uint64_t hx = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const uint32_t cls = (M[q] == ~0ull) ? kVisible : (M[q] == 0ull ? kShadow : kPartial);
+        mask |= cls << (2 * q);
+        hx ^= fmix64(M[q] + (uint64_t)(q + 1) * kGolden);
+    }
+    hash = fmix64(hx ^ ((uint64_t)(j + 1) * kGolden));
+    return true;
+}
+
+__device__ __forceinline__ void leaf_segments(const LevelDev& lv, SegDev& seg, uint32_t i, uint32_t n, uint32_t j,
+                                              int L) {
+    if (i == 0 || lv.job[i - 1] != j) seg.nstart[seg_index(j, L)] = i;
+    if (i == n - 1 || lv.job[i + 1] != j) seg.nend[seg_index(j, L)] = i + 1;
+}
+
+__device__ __forceinline__ void store_slices(const LevelDev& lv, uint32_t i, const uint64_t M[8]) {
+    ulonglong2* o = reinterpret_cast<ulonglong2*>(lv.slices + (size_t)i * 8);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) o[q] = make_ulonglong2(M[2 * q], M[2 * q + 1]);
+}
+
+// Leaf masks into per-leaf arrays (masks, class mask, hash) for a separate
+// dedup_insert pass.
 __global__ void __launch_bounds__(kThreads)
     k_leaf_masks(LevelDev lv, const uint32_t* __restrict__ counts, const JobDev* __restrict__ jobs, uint32_t njobs,
                  int L, SegDev seg, uint32_t* err) {
     const uint32_t n = counts[L];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint64_t c = lv.coord[i];
-        const uint32_t j = lv.job[i];
-        const uint32_t bx = unpack_x(c) * 4u, by = unpack_y(c) * 4u, bz = unpack_z(c) * 4u;
-        if (j >= njobs || bx + 8u > __ldg(&jobs[j].n) || by + 8u > __ldg(&jobs[j].n)) {
-            // stale slot (an internal check already failed): inert leaf
-            ulonglong2* o = reinterpret_cast<ulonglong2*>(lv.slices + (size_t)i * 8);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) o[q] = make_ulonglong2(0ull, 0ull);
+        uint64_t M[8], h;
+        uint32_t mask, j;
+        const bool ok = leaf_compute(lv, jobs, njobs, i, M, mask, h, j);
+        store_slices(lv, i, M);
+        lv.mask[i] = mask;
+        lv.hash[i] = h;
+        if (!ok) {
             atomicOr(err, 4u);
-            lv.mask[i] = 0;
             lv.job[i] = 0;
-            lv.hash[i] = 0;
             continue;
         }
-        const uint32_t nmap = __ldg(&jobs[j].n);
-        const float H = __uint2float_rn(nmap * __ldg(&jobs[j].z_num));
-        const float* row0 = jobs[j].depth + (size_t)by * nmap + bx;
-        float4 a[8], b[8];
-#pragma unroll
-        for (int y = 0; y < 8; ++y) {
-            a[y] = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap));
-            b[y] = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap + 4));
+        leaf_segments(lv, seg, i, n, j, L);
+    }
+}
+
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Leaf masks fused with the leaf level's dedup insert: each leaf keeps its
+// masks in registers and looks its class up in the (cleared) table right
+// away.  Only a leaf that becomes, even for a while, its class's
+// representative stores its masks -- before it publishes itself in the slot
+// (fence, then CAS or atomicMin), so a reader that sees its index in a slot
+// (acquire load) reads complete masks.  Every other leaf (the vast
+// majority: c. 7.9 M leaves fold into 137 k classes at 8192^2) writes only
+// its class mask and slot.  The slot rule is dedup_insert's: it ends with
+// the class's smallest index, the first occurrence.
+__global__ void __launch_bounds__(kThreads)
+    k_leaf_insert(LevelDev lv, const uint32_t* __restrict__ counts, const JobDev* __restrict__ jobs, uint32_t njobs,
+                  int L, SegDev seg, unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
+    const uint32_t n = counts[L];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint64_t M[8], h;
+        uint32_t mask, j;
+        if (!leaf_compute(lv, jobs, njobs, i, M, mask, h, j)) {
+            atomicOr(err, 4u);
+            lv.job[i] = 0;
+        } else {
+            leaf_segments(lv, seg, i, n, j, L);
         }
-        uint32_t p0[2] = {0u, 0u}, p1[2] = {0u, 0u}, p2[2] = {0u, 0u}, p3[2] = {0u, 0u};
-#pragma unroll
-        for (int y = 0; y < 8; ++y) {
-            const float v[8] = {a[y].x, a[y].y, a[y].z, a[y].w, b[y].x, b[y].y, b[y].z, b[y].w};
-#pragma unroll
-            for (int x = 0; x < 8; ++x) {
-                const uint32_t k = lit_count(__fmul_rn(v[x], H), (int32_t)bz);
-                const int t = 8 * y + x, w = t >> 5, sh = t & 31;
-                p0[w] |= (k & 1u) << sh;
-                p1[w] |= ((k >> 1) & 1u) << sh;
-                p2[w] |= ((k >> 2) & 1u) << sh;
-                p3[w] |= ((k >> 3) & 1u) << sh;
-            }
-        }
-        const uint64_t P0 = p0[0] | ((uint64_t)p0[1] << 32), P1 = p1[0] | ((uint64_t)p1[1] << 32);
-        const uint64_t P2 = p2[0] | ((uint64_t)p2[1] << 32), P3 = p3[0] | ((uint64_t)p3[1] << 32);
-        // slice s = {t : k_t >= s+1}, k_t in [0, 8]
-        uint64_t M[8];
-        M[0] = P0 | P1 | P2 | P3;
-        M[1] = P1 | P2 | P3;
-        M[2] = P3 | P2 | (P1 & P0);
-        M[3] = P3 | P2;
-        M[4] = P3 | (P2 & (P1 | P0));
-        M[5] = P3 | (P2 & P1);
-        M[6] = P3 | (P2 & P1 & P0);
-        M[7] = P3;
-        uint32_t mask = 0;
-        uint64_t hx = 0;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const uint32_t cls = (M[q] == ~0ull) ? kVisible : (M[q] == 0ull ? kShadow : kPartial);
-            mask |= cls << (2 * q);
-            hx ^= fmix64(M[q] + (uint64_t)(q + 1) * kGolden);
-        }
-        ulonglong2* o = reinterpret_cast<ulonglong2*>(lv.slices + (size_t)i * 8);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) o[q] = make_ulonglong2(M[2 * q], M[2 * q + 1]);
         lv.mask[i] = mask;
-        lv.hash[i] = fmix64(hx ^ ((uint64_t)(j + 1) * kGolden));
-        if (i == 0 || lv.job[i - 1] != j) seg.nstart[seg_index(j, L)] = i;
-        if (i == n - 1 || lv.job[i + 1] != j) seg.nend[seg_index(j, L)] = i + 1;
+        const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | i;
+        uint64_t s = h & cap_mask;
+        bool placed = false, published = false;
+        for (uint64_t probe = 0; probe <= cap_mask; ++probe) {
+            unsigned long long e = ld_acquire(&table[s]);
+            if (e == kEmptySlot) {
+                store_slices(lv, i, M);
+                __threadfence();
+                published = true;
+                const unsigned long long prev = atomicCAS(&table[s], kEmptySlot, key);
+                if (prev == kEmptySlot) {
+                    placed = true;
+                    break;
+                }
+                __threadfence();  // acquire: the winner's masks are read below
+                e = prev;
+            }
+            if ((e >> 32) == (key >> 32)) {
+                const uint32_t r = (uint32_t)e;
+                bool same = (r < n) && (__ldcg(lv.job + r) == lv.job[i]);
+                if (same) {
+                    const ulonglong2* o = reinterpret_cast<const ulonglong2*>(lv.slices + (size_t)r * 8);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const ulonglong2 x = __ldcg(o + q);
+                        same = same && x.x == M[2 * q] && x.y == M[2 * q + 1];
+                    }
+                }
+                if (same) {
+                    if (r > i) {
+                        // an earlier occurrence: publish, then lower the slot
+                        if (!published) {
+                            store_slices(lv, i, M);
+                            __threadfence();
+                        }
+                        atomicMin(&table[s], key);
+                    }
+                    placed = true;
+                    break;
+                }
+            }
+            s = (s + 1) & cap_mask;
+        }
+        if (!placed) atomicOr(err, 16u);  // table full: the result is void, reported
+        lv.slot[i] = (uint32_t)s;
     }
 }
 
@@ -892,9 +1000,13 @@ cpvs_status plan_enqueue(const BuildPlan* P, cudaStream_t st, Timing* tm) {
         }
     }
     if (P->leafmasks) {
+        {
+            KernelTimer kt(tm, K_TABLE_CLEAR, st);
+            CPVS_CUDA(cudaMemsetAsync(P->table, 0xFF, P->tcap[2] * 8, st));
+        }
         KernelTimer kt(tm, K_LEAF_MASKS, st);
-        k_leaf_masks<<<plan_grid(P, P->cap[2], kThreads), kThreads, 0, st>>>(P->lv[2], P->counts, P->jobs_dev, njobs,
-                                                                            2, P->seg, err);
+        k_leaf_insert<<<plan_grid(P, P->cap[2], kThreads), kThreads, 0, st>>>(P->lv[2], P->counts, P->jobs_dev, njobs,
+                                                                             2, P->seg, P->table, P->tcap[2] - 1, err);
     } else {
         KernelTimer kt(tm, K_CLASSIFY_BOTTOM, st);
         k_classify_bottom<<<plan_grid(P, P->cap[0], kThreads), kThreads, 0, st>>>(P->lv[0], P->counts, P->jobs_dev,
@@ -906,13 +1018,12 @@ cpvs_status plan_enqueue(const BuildPlan* P, cudaStream_t st, Timing* tm) {
         const bool leaf = P->leafmasks && L == 2;
         const uint32_t gs = plan_grid(P, P->cap[L], kThreads * 4), gi = plan_grid(P, P->cap[L], kThreads);
         const LevelDev child = (L > P->bottom) ? P->lv[L - 1] : P->lv[L];
-        {
+        if (!leaf) {
             KernelTimer kt(tm, K_TABLE_CLEAR, st);
             CPVS_CUDA(cudaMemsetAsync(P->table, 0xFF, tc * 8, st));
         }
         if (leaf) {
-            { KernelTimer kt(tm, K_INSERT_LEAF, st);
-              k_dedup_insert<true><<<gi, kThreads, 0, st>>>(P->lv[L], child, P->counts, L, P->table, tc - 1, err); }
+            // the leaves were inserted as they were built (k_leaf_insert)
             { KernelTimer kt(tm, K_RESOLVE, st);
               k_dedup_resolve<true><<<gs, kThreads, 0, st>>>(P->lv[L], P->counts, L, P->table, P->partials); }
             { KernelTimer kt(tm, K_SCAN, st);

@@ -233,7 +233,10 @@ public:
     const CompressedShadow* get(uint x, uint y, uint z) const {
         return m_data[((size_t)z * m_length + y) * m_length + x].get();
     }
-    void freeOnCPU() { m_data.clear(); }
+    /* Drops the host-side handles; get() then returns NULL. */
+    void freeOnCPU() {
+        for (auto& p : m_data) p.reset();
+    }
     void copyToGPU() { check(cpvs_grid_finalize(m_g, 0, nullptr)); }
     void moveToGPU() {
         check(cpvs_grid_finalize(m_g, 1, nullptr));

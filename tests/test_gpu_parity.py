@@ -122,6 +122,29 @@ def test_special_values_match_oracle(cp, oracle):
         check_against_oracle(cp, oracle, np.full((32, 32), v, np.float32))
 
 
+def boundary_map(rng, n, H):
+    """Depths whose d*H lands on or a few ulps beside voxel centres z + 0.5
+    (the lit test's boundary), plus tiny, denormal and negative values."""
+    z = rng.integers(-2, H + 2, (n, n))
+    d = ((z + 0.5) / H).astype(np.float32)
+    steps = rng.integers(-3, 4, (n, n))
+    for k in range(3):
+        d = np.where(steps > k, np.nextafter(d, np.float32(np.inf)), d)
+        d = np.where(steps < -k, np.nextafter(d, np.float32(-np.inf)), d)
+    special = np.array([0.5 / H, np.nextafter(np.float32(0.5 / H), np.float32(0)), 1e-40, -1e-40, 1e-30, -0.0,
+                        0.5 - 2 ** -25, np.float32(8.5 / H), 7.5 / H], np.float32)
+    pick = rng.random((n, n)) < 0.1
+    d[pick] = special[rng.integers(0, special.size, int(pick.sum()))]
+    return d.astype(np.float32)
+
+
+def test_voxel_boundary_values_match_oracle(cp, oracle):
+    rng = np.random.default_rng(77)
+    for trial, (n, zn) in enumerate([(64, 1), (64, 3), (128, 8), (32, 5), (256, 1), (64, 2)]):
+        zi = int(rng.integers(0, zn))
+        check_against_oracle(cp, oracle, boundary_map(rng, n, n * zn), zi, zn, seed=trial)
+
+
 def test_c0_config_matches_oracle(cp, oracle):
     """The 1024^2 map of 40 boxes: DAG words and 2^20 voxel lookups."""
     d = scene.rasterise(scene.config_scene("c0"))
