@@ -252,18 +252,38 @@ __global__ void __launch_bounds__(kThreads)
 // case exactly: for v in [c/2, 2c] (c = bz + 0.5) it is exact (Sterbenz);
 // below c/2, t < -c/2 stays negative (count 0); above 2c, either bz = 0 and
 // v - 0.5 is exact for v < 8.5, or t > 8 (count 8).  NaN: fmaxf picks -1
-// (count 0, as z + 0.5 <= NaN is false); +inf saturates to 8.
-__device__ __forceinline__ uint32_t lit_count(float v, float c) {
-    const float t = fmaxf(__fsub_rn(v, c), -1.0f);
-    const int32_t k = __float2int_rd(t) + 1;
-    return (uint32_t)min(k, 8);
+// (count 0, as z + 0.5 <= NaN is false); +inf clamps to 8.
+// The count is produced without a float-to-int conversion: t is clamped to
+// [-1, 7] and added, rounding down, to 1.5 * 2^23 + 1, whose unit in the last
+// place is 1 -- so the sum is 1.5 * 2^23 + 1 + floor(t) and its bit pattern
+// is 0x4B400000 + count (count in the low four bits).
+__device__ __forceinline__ uint32_t lit_count_bits(float v, float c) {
+    const float t = fminf(fmaxf(__fsub_rn(v, c), -1.0f), 7.0f);
+    return __float_as_uint(__fadd_rd(t, 12582913.0f));
+}
+constexpr uint32_t kCountBias = 0x4B400000u;
+
+// Eight counts as nibbles (texel x at bits 4x..4x+3) -> four bytes, byte b
+// holding bit b of every texel's count (texel x at bit x): the bit-index
+// rotation (x2 x1 x0 b1 b0) -> (b1 b0 x2 x1 x0) as four delta swaps.
+__device__ __forceinline__ uint32_t delta_swap(uint32_t x, uint32_t m, int d) {
+    const uint32_t t = ((x >> d) ^ x) & m;
+    return x ^ t ^ (t << d);
+}
+__device__ __forceinline__ uint32_t nibbles_to_planes(uint32_t w) {
+    w = delta_swap(w, 0x22222222u, 1);
+    w = delta_swap(w, 0x0a0a0a0au, 3);
+    w = delta_swap(w, 0x00cc00ccu, 6);
+    return delta_swap(w, 0x0000f0f0u, 12);
 }
 
 // The eight 64-bit slice masks of leaf i (level-2 node: the 8x8x8 voxels at
 // 4 * its coordinate), its 16-bit class mask (01 lit / 00 shadow / 10
 // partial per slice, src/CompressedShadowUtil.cpp:59-99) and its signature
-// hash.  Returns false for a stale slot (an internal check already failed):
-// the caller then treats it as an empty leaf of job 0.
+// hash.  Per texel row: the eight lit counts, packed as nibbles, transposed
+// into count bit-planes; slice s is then {texels with count > s}.  Returns
+// false for a stale slot (an internal check already failed): the caller
+// then treats it as an empty leaf of job 0.
 __device__ __forceinline__ bool leaf_compute(const LevelDev& lv, const JobDev* __restrict__ jobs, uint32_t njobs,
                                              uint32_t i, uint64_t M[8], uint32_t& mask, uint64_t& hash,
                                              uint32_t& j) {
@@ -282,28 +302,36 @@ __device__ __forceinline__ bool leaf_compute(const LevelDev& lv, const JobDev* _
     const float H = __uint2float_rn(nmap * __ldg(&jobs[j].z_num));
     const float cz = __fadd_rn(__uint2float_rn(bz), 0.5f);
     const float* row0 = jobs[j].depth + (size_t)by * nmap + bx;
-    float4 a[8], b[8];
+    uint32_t R[8];  // per row: byte b = count bit b of the row's 8 texels
 #pragma unroll
     for (int y = 0; y < 8; ++y) {
-        a[y] = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap));
-        b[y] = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap + 4));
-    }
-    uint32_t p0[2] = {0u, 0u}, p1[2] = {0u, 0u}, p2[2] = {0u, 0u}, p3[2] = {0u, 0u};
+        const float4 a = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap));
+        const float4 b = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap + 4));
+        const float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        uint32_t w = 0;
 #pragma unroll
-    for (int y = 0; y < 8; ++y) {
-        const float v[8] = {a[y].x, a[y].y, a[y].z, a[y].w, b[y].x, b[y].y, b[y].z, b[y].w};
-#pragma unroll
-        for (int x = 0; x < 8; ++x) {
-            const uint32_t k = lit_count(__fmul_rn(v[x], H), cz);
-            const int t = 8 * y + x, w = t >> 5, sh = t & 31;
-            p0[w] |= (k & 1u) << sh;
-            p1[w] |= ((k >> 1) & 1u) << sh;
-            p2[w] |= ((k >> 2) & 1u) << sh;
-            p3[w] |= ((k >> 3) & 1u) << sh;
-        }
+        for (int x = 0; x < 8; ++x) w += lit_count_bits(__fmul_rn(v[x], H), cz) << (4 * x);
+        // every term carried kCountBias above its nibble: remove them all
+        constexpr uint32_t bias = kCountBias + (kCountBias << 4) + (kCountBias << 8) + (kCountBias << 12) +
+                                  (kCountBias << 16) + (kCountBias << 20) + (kCountBias << 24) + (kCountBias << 28);
+        R[y] = nibbles_to_planes(w - bias);
     }
-    const uint64_t P0 = p0[0] | ((uint64_t)p0[1] << 32), P1 = p1[0] | ((uint64_t)p1[1] << 32);
-    const uint64_t P2 = p2[0] | ((uint64_t)p2[1] << 32), P3 = p3[0] | ((uint64_t)p3[1] << 32);
+    // gather byte b of rows 0..7 into plane b (row y at byte y): 4x4 byte
+    // transposes of rows 0..3 and 4..7
+    uint32_t plo[4], phi[4];
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        const uint32_t r0 = R[4 * half], r1 = R[4 * half + 1], r2 = R[4 * half + 2], r3 = R[4 * half + 3];
+        const uint32_t A = __byte_perm(r0, r1, 0x5140), B = __byte_perm(r0, r1, 0x7362);
+        const uint32_t C = __byte_perm(r2, r3, 0x5140), D = __byte_perm(r2, r3, 0x7362);
+        uint32_t* dst = half ? phi : plo;
+        dst[0] = __byte_perm(A, C, 0x5410);
+        dst[1] = __byte_perm(A, C, 0x7632);
+        dst[2] = __byte_perm(B, D, 0x5410);
+        dst[3] = __byte_perm(B, D, 0x7632);
+    }
+    const uint64_t P0 = plo[0] | ((uint64_t)phi[0] << 32), P1 = plo[1] | ((uint64_t)phi[1] << 32);
+    const uint64_t P2 = plo[2] | ((uint64_t)phi[2] << 32), P3 = plo[3] | ((uint64_t)phi[3] << 32);
     // slice s = {t : k_t >= s+1}, k_t in [0, 8]
     M[0] = P0 | P1 | P2 | P3;
     M[1] = P1 | P2 | P3;
@@ -314,14 +342,15 @@ __device__ __forceinline__ bool leaf_compute(const LevelDev& lv, const JobDev* _
     M[6] = P3 | (P2 & P1 & P0);
     M[7] = P3;
     mask = 0;
-    uint64_t hx = 0;
+    uint64_t h = (uint64_t)(j + 1) * kGolden;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const uint32_t cls = (M[q] == ~0ull) ? kVisible : (M[q] == 0ull ? kShadow : kPartial);
         mask |= cls << (2 * q);
-        hx ^= fmix64(M[q] + (uint64_t)(q + 1) * kGolden);
+        h = (h ^ M[q]) * 0xD6E8FEB86659FD93ull;
+        h ^= h >> 32;
     }
-    hash = fmix64(hx ^ ((uint64_t)(j + 1) * kGolden));
+    hash = fmix64(h);
     return true;
 }
 
@@ -374,7 +403,7 @@ __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long lon
 // majority: c. 7.9 M leaves fold into 137 k classes at 8192^2) writes only
 // its class mask and slot.  The slot rule is dedup_insert's: it ends with
 // the class's smallest index, the first occurrence.
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 5)
     k_leaf_insert(LevelDev lv, const uint32_t* __restrict__ counts, const JobDev* __restrict__ jobs, uint32_t njobs,
                   int L, SegDev seg, unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
     const uint32_t n = counts[L];
