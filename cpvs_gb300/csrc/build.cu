@@ -63,6 +63,9 @@ struct LevelDev {
     uint32_t* woff;    // rank -> word offset (running over the level)
     uint64_t* slices;  // leaf level: 8 leafmasks per node
     uint64_t* hash;    // leaf level: signature hash per node
+    unsigned long long* table;  // this level's hash slots (build plans): after
+                                // the merge, (rank << 32 | representative)
+    uint64_t table_mask;        // slots - 1
 };
 
 // Per-job, per-level bookkeeping of segment boundaries (jobs are contiguous
@@ -110,6 +113,47 @@ __device__ __forceinline__ uint32_t node_mask(const JobDev& J, int L, uint64_t c
         const float2* P = J.pyr + pyramid_level_offset_dev(J.n, L);
         const float4 r0 = *reinterpret_cast<const float4*>(P + (size_t)y * W + x);
         const float4 r1 = *reinterpret_cast<const float4*>(P + (size_t)(y + 1) * W + x);
+        mn[0] = r0.x; mx[0] = r0.y;
+        mn[1] = r0.z; mx[1] = r0.w;
+        mn[2] = r1.x; mx[2] = r1.y;
+        mn[3] = r1.z; mx[3] = r1.w;
+    }
+    uint32_t m = 0;
+#pragma unroll
+    for (uint32_t ch = 0; ch < 8; ++ch) {
+        const uint32_t t = ch & 3u, zc = z + (ch >> 2);
+        uint32_t v;
+        if (L > 0)
+            v = classify_cell(zc, __fmul_rn(mn[t], H), __fmul_rn(mx[t], H));
+        else
+            v = voxel_lit(zc, __fmul_rn(mn[t], H)) ? kVisible : kShadow;
+        m |= v << (2u * ch);
+    }
+    return m;
+}
+
+// node_mask without side effects: a node whose 2x2 texels fall outside its
+// level sets `bad` (the caller reports error bit 4) and yields mask 0.
+__device__ __forceinline__ uint32_t node_mask_nf(const JobDev& J, int L, uint64_t c, bool& bad) {
+    const uint32_t x = unpack_x(c), y = unpack_y(c), z = unpack_z(c);
+    const uint32_t W = J.n >> L;
+    if (x + 1u >= W || y + 1u >= W) {
+        bad = true;
+        return 0u;
+    }
+    const float H = __uint2float_rn((J.n >> L) * J.z_num);
+    float mn[4], mx[4];
+    if (L == 0) {
+        const float2 r0 = *reinterpret_cast<const float2*>(J.depth + (size_t)y * J.n + x);
+        const float2 r1 = *reinterpret_cast<const float2*>(J.depth + (size_t)(y + 1) * J.n + x);
+        mn[0] = mx[0] = r0.x;
+        mn[1] = mx[1] = r0.y;
+        mn[2] = mx[2] = r1.x;
+        mn[3] = mx[3] = r1.y;
+    } else {
+        const float2* P = J.pyr + pyramid_level_offset_dev(J.n, L);
+        const float4 r0 = __ldg(reinterpret_cast<const float4*>(P + (size_t)y * W + x));
+        const float4 r1 = __ldg(reinterpret_cast<const float4*>(P + (size_t)(y + 1) * W + x));
         mn[0] = r0.x; mx[0] = r0.y;
         mn[1] = r0.z; mx[1] = r0.w;
         mn[2] = r1.x; mx[2] = r1.y;
@@ -616,6 +660,534 @@ __global__ void __launch_bounds__(kThreads)
         cur.uid[i] = (uint32_t)table[cur.slot[i]];
 }
 
+// ------------------------------------------------------- single-pass levels
+// Build plans run each level in as few launches as possible: the top-down
+// expansion of a level is one kernel (classify, count, scan, write the
+// children); its merge is the insert plus one kernel that finds the kept
+// nodes (first occurrences), ranks them and assigns their word offsets.  The
+// prefix across blocks is a decoupled look-back: a block takes the next tile
+// by ticket, publishes its tile's aggregate, then walks back over its
+// predecessors' flags until one carries an inclusive prefix.  Tiles are
+// taken in order, so a block only waits on blocks that already run, and
+// every wait is bounded in time (a timeout sets error bit 32).  A kept
+// node's rank goes into the upper half of its hash slot (the lower half
+// keeps the class representative), so the level above and the emission read
+// a node's rank as table[slot] >> 32 and no remap pass runs.  The topmost
+// levels, which hold few nodes, run in one single-block launch for the
+// expansion and one for the merge.
+
+constexpr unsigned long long kFlagAgg = 1ull << 62, kFlagInc = 2ull << 62, kFlagState = 3ull << 62;
+constexpr uint64_t kLookbackTimeoutNs = 200000000ull;  // 0.2 s
+constexpr int kExpItems = 4;
+constexpr uint32_t kExpTile = kThreads * kExpItems;
+constexpr int kScanItems = 8;
+constexpr uint32_t kScanTile = kThreads * kScanItems;
+constexpr int kSmallThreads = 1024;
+
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// A tile's flag: state (bits 63..62: aggregate / inclusive), then two
+// 31-bit sums (bits 61..31 and 30..0).  Every level's sums stay below 2^31
+// (node counts are bounded by the plan, word counts by the DAG size check);
+// a sum that does not fit sets error bit 64.
+__device__ __forceinline__ unsigned long long pack_flag(unsigned long long state, uint2 v) {
+    return state | ((unsigned long long)(v.x & 0x7FFFFFFFu) << 31) | (v.y & 0x7FFFFFFFu);
+}
+__device__ __forceinline__ uint2 flag_values(unsigned long long f) {
+    return make_uint2((uint32_t)(f >> 31) & 0x7FFFFFFFu, (uint32_t)f & 0x7FFFFFFFu);
+}
+
+// Exclusive prefix of `agg` over tiles 0..tile-1; called by all 32 lanes of
+// one warp, which read 32 predecessors' flags per step: the nearest
+// inclusive flag ends the walk, aggregates before it are summed.
+__device__ uint2 lookback(unsigned long long* flags, uint32_t tile, uint2 agg, uint32_t* err) {
+    const int lane = threadIdx.x & 31;
+    if (agg.x > 0x7FFFFFFFu || agg.y > 0x7FFFFFFFu) atomicOr(err, 64u);
+    if (tile == 0) {
+        if (lane == 0) atomicExch(&flags[0], pack_flag(kFlagInc, agg));
+        return make_uint2(0u, 0u);
+    }
+    if (lane == 0) atomicExch(&flags[tile], pack_flag(kFlagAgg, agg));
+    uint2 excl = make_uint2(0u, 0u);
+    int64_t p = (int64_t)tile - 1;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        const int64_t q = p - lane;
+        // before tile 0: an inclusive zero
+        unsigned long long f = q >= 0 ? ld_relaxed(&flags[q]) : kFlagInc;
+        bool timed_out = false;
+        while (__any_sync(0xffffffffu, (f & kFlagState) == 0ull)) {
+            timed_out = __shfl_sync(0xffffffffu, global_ns() - t0 > kLookbackTimeoutNs, 0);
+            if (timed_out) break;
+            __nanosleep(32);
+            if ((f & kFlagState) == 0ull) f = ld_relaxed(&flags[q]);
+        }
+        if (timed_out) {
+            if (lane == 0) atomicOr(err, 32u);  // a predecessor never published: the result is void, reported
+            break;
+        }
+        const unsigned inc = __ballot_sync(0xffffffffu, (f & kFlagState) == kFlagInc);
+        const int stop = inc ? __ffs(inc) - 1 : 31;
+        uint2 v = lane <= stop ? flag_values(f) : make_uint2(0u, 0u);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+            v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        }
+        excl.x += v.x;
+        excl.y += v.y;
+        if (inc) break;
+        p -= 32;
+    }
+    const uint2 incl = make_uint2(excl.x + agg.x, excl.y + agg.y);
+    if (incl.x > 0x7FFFFFFFu || incl.y > 0x7FFFFFFFu) atomicOr(err, 64u);
+    if (lane == 0) atomicExch(&flags[tile], pack_flag(kFlagInc, incl));
+    return excl;
+}
+
+// Rank (merged identity) of node x of a merged level: upper half of its slot.
+__device__ __forceinline__ uint32_t rank_of(const LevelDev& lv, uint32_t x) {
+    return (uint32_t)(__ldcg(lv.table + lv.slot[x]) >> 32);
+}
+
+// Classifies node i of level L, writing its mask; false and mask 0 for a
+// node whose job is out of range (only after an internal check failed).
+__device__ __forceinline__ uint32_t classify_node(LevelDev& cur, const JobDev* __restrict__ jobs, uint32_t njobs,
+                                                  int L, uint32_t i, uint32_t* err) {
+    const uint32_t j = cur.job[i];
+    uint32_t m = 0;
+    if (j < njobs) {
+        m = node_mask(jobs[j], L, cur.coord[i], err);
+    } else {
+        atomicOr(err, 8u);
+        cur.job[i] = 0;  // keep later passes' job lookups in range
+    }
+    cur.mask[i] = m;
+    return m;
+}
+
+// Writes the children of node i (mask m, first child at f) into level L-1,
+// or drops them when they would exceed the level's capacity; records job
+// boundaries at level L.
+__device__ __forceinline__ void write_children(LevelDev& cur, LevelDev& nxt, SegDev& seg, int L, uint32_t n,
+                                               uint32_t i, uint32_t m, uint32_t f, uint32_t cap_next,
+                                               uint32_t* err) {
+    const uint32_t k = partial_children(m);
+    if (f + k > cap_next) {
+        // more children than the level bound: drop them (the count already
+        // includes them; their slots keep stale coordinates, which
+        // node_mask rejects) and report
+        atomicOr(err, 1u);
+        cur.mask[i] = m & 0x5555u;
+        cur.first[i] = 0;
+        return;
+    }
+    cur.first[i] = f;
+    const uint64_t c = cur.coord[i];
+    const uint32_t x = unpack_x(c), y = unpack_y(c), z = unpack_z(c), j = cur.job[i];
+    uint32_t r = 0;
+#pragma unroll
+    for (uint32_t ch = 0; ch < 8; ++ch)
+        if (m & (2u << (2u * ch))) {
+            // cs::getChildCoordinates (src/CompressedShadowUtil.cpp:101-117)
+            nxt.coord[f + r] = pack_xyz((x + (ch & 1u)) * 2u, (y + ((ch >> 1) & 1u)) * 2u, (z + (ch >> 2)) * 2u);
+            nxt.job[f + r] = j;
+            ++r;
+        }
+    if (i == 0 || cur.job[i - 1] != j) seg.nstart[seg_index(j, L)] = i;
+    if (i == n - 1 || cur.job[i + 1] != j) seg.nend[seg_index(j, L)] = i + 1;
+}
+
+// 8-bit set of the partial children (bit ch) of a 16-bit class mask.
+__device__ __forceinline__ uint32_t partial_set(uint32_t m) {
+    uint32_t pb = 0;
+#pragma unroll
+    for (uint32_t ch = 0; ch < 8; ++ch) pb |= ((m >> (2u * ch + 1u)) & 1u) << ch;
+    return pb;
+}
+
+// Expansion of level L into L-1 in one pass, tiles of kExpTile nodes.  Each
+// thread classifies four consecutive nodes (their inputs loaded before any
+// store, so the loads overlap); after the tile's scan and look-back, the
+// tile's children are written cooperatively -- thread t writes children
+// t, t + 256, ... of the tile, finding its parent by binary search over the
+// tile's child offsets in shared memory -- so the child arrays are written
+// in coalesced runs.
+__global__ void __launch_bounds__(kThreads)
+    k_expand_lb(LevelDev cur, LevelDev nxt, uint32_t* counts, const JobDev* __restrict__ jobs, uint32_t njobs,
+                int L, const Injected* __restrict__ inj, uint32_t ninj, SegDev seg, uint32_t cap_next,
+                unsigned int* ticket, unsigned long long* flags, uint32_t* err) {
+    __shared__ uint32_t sm[64];
+    __shared__ uint32_t s_tile, s_excl;
+    __shared__ uint32_t s_off[kExpTile + 1];
+    __shared__ uint64_t s_coord[kExpTile];
+    __shared__ uint32_t s_job[kExpTile];
+    __shared__ uint8_t s_pset[kExpTile];
+    const uint32_t n = counts[L];
+    const uint32_t ntiles = n ? (n + kExpTile - 1) / kExpTile : 1u;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        if (tile >= ntiles) break;
+        if (tile == 0)
+            for (uint32_t r = threadIdx.x; r < ninj; r += blockDim.x) {
+                nxt.coord[r] = inj[r].coord;
+                nxt.job[r] = inj[r].job;
+            }
+        const uint32_t l0 = threadIdx.x * kExpItems;  // first node of this thread within the tile
+        const uint32_t b0 = tile * kExpTile + l0;
+        uint32_t jv[kExpItems];
+        uint64_t cv[kExpItems];
+        if (b0 + kExpItems <= n) {
+            const uint4 j4 = *reinterpret_cast<const uint4*>(cur.job + b0);
+            const ulonglong2 c01 = *reinterpret_cast<const ulonglong2*>(cur.coord + b0);
+            const ulonglong2 c23 = *reinterpret_cast<const ulonglong2*>(cur.coord + b0 + 2);
+            jv[0] = j4.x; jv[1] = j4.y; jv[2] = j4.z; jv[3] = j4.w;
+            cv[0] = c01.x; cv[1] = c01.y; cv[2] = c23.x; cv[3] = c23.y;
+        } else {
+#pragma unroll
+            for (int it = 0; it < kExpItems; ++it) {
+                const bool in = b0 + it < n;
+                jv[it] = in ? cur.job[b0 + it] : 0u;
+                cv[it] = in ? cur.coord[b0 + it] : 0ull;
+            }
+        }
+        uint32_t m[kExpItems], ksum = 0;
+        bool bad_job = false, bad_node = false;
+#pragma unroll
+        for (int it = 0; it < kExpItems; ++it) {
+            m[it] = 0;
+            if (b0 + it < n) {
+                if (jv[it] < njobs) {
+                    m[it] = node_mask_nf(jobs[jv[it]], L, cv[it], bad_node);
+                } else {
+                    bad_job = true;
+                    jv[it] = 0;
+                }
+            }
+            ksum += partial_children(m[it]);
+        }
+        if (bad_job) atomicOr(err, 8u);
+        if (bad_node) atomicOr(err, 4u);
+        uint2 tot;
+        const uint32_t pre = block_exclusive_scan2(make_uint2(ksum, 0u), tot, sm).x;
+        if (threadIdx.x < 32) {
+            const uint32_t e = lookback(flags, tile, make_uint2(tot.x, 0u), err).x;
+            if (threadIdx.x == 0) s_excl = e;
+        }
+        // the tile's parents and their child offsets, for the cooperative writes
+        uint32_t off = pre;
+#pragma unroll
+        for (int it = 0; it < kExpItems; ++it) {
+            s_off[l0 + it] = off;
+            s_coord[l0 + it] = cv[it];
+            s_job[l0 + it] = jv[it];
+            s_pset[l0 + it] = (uint8_t)partial_set(m[it]);
+            off += partial_children(m[it]);
+        }
+        if (threadIdx.x == 0) s_off[kExpTile] = tot.x;
+        __syncthreads();
+        const uint32_t f0 = ninj + s_excl;  // first child of the tile in level L-1
+        // per parent: first child, overflow, job boundaries
+#pragma unroll
+        for (int it = 0; it < kExpItems; ++it) {
+            const uint32_t i = b0 + it;
+            if (i >= n) break;
+            const uint32_t k = partial_children(m[it]);
+            const uint32_t f = f0 + s_off[l0 + it];
+            if (f + k > cap_next) {
+                // more children than the level bound: they are not written;
+                // reported, and the plan grows
+                atomicOr(err, 1u);
+                m[it] &= 0x5555u;
+                cur.first[i] = 0;
+            } else {
+                cur.first[i] = f;
+            }
+            cur.mask[i] = m[it];
+            if (jv[it] != cur.job[i]) cur.job[i] = jv[it];
+            const uint32_t j = jv[it];
+            if (i == 0 || cur.job[i - 1] != j) seg.nstart[seg_index(j, L)] = i;
+            if (i == n - 1 || cur.job[i + 1] != j) seg.nend[seg_index(j, L)] = i + 1;
+        }
+        // cs::getChildCoordinates (src/CompressedShadowUtil.cpp:101-117),
+        // one child per thread and step
+        const uint32_t C = tot.x;
+        for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
+            const uint32_t dst = f0 + c;
+            if (dst >= cap_next) break;
+            uint32_t lo = 0, hi = kExpTile;
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (s_off[mid] <= c) lo = mid; else hi = mid;
+            }
+            // the (c - s_off[lo])-th partial child of the parent, in child order
+            const uint32_t pb = s_pset[lo];
+            uint32_t r = c - s_off[lo], ch = 0;
+#pragma unroll
+            for (uint32_t b = 0; b < 8; ++b)
+                if ((pb >> b) & 1u) {
+                    if (r == 0u) {
+                        ch = b;
+                        r = 8u;  // found: later bits are not taken
+                    }
+                    --r;
+                }
+            const uint64_t pc = s_coord[lo];
+            const uint32_t x = unpack_x(pc), y = unpack_y(pc), z = unpack_z(pc);
+            nxt.coord[dst] = pack_xyz((x + (ch & 1u)) * 2u, (y + ((ch >> 1) & 1u)) * 2u, (z + (ch >> 2)) * 2u);
+            nxt.job[dst] = s_job[lo];
+        }
+        if (tile == ntiles - 1 && threadIdx.x == 0) {
+            const uint32_t total = f0 + tot.x;
+            if (total > cap_next) atomicOr(err, 1u);
+            counts[L - 1] = total < cap_next ? total : cap_next;
+        }
+        __syncthreads();
+    }
+}
+
+// Hash insert of inner node i into `table` (dedup_insert's rule: the slot
+// ends with the class's first occurrence); children are compared by their
+// class representatives (uid).
+__device__ __forceinline__ void insert_inner(LevelDev& cur, const LevelDev& child, uint32_t i,
+                                             unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
+    const uint64_t h = inner_hash(cur, child, i);
+    const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | i;
+    uint64_t s = h & cap_mask;
+    bool placed = false;
+    for (uint64_t probe = 0; probe <= cap_mask; ++probe) {
+        unsigned long long e = __ldcg(&table[s]);
+        if (e == kEmptySlot) {
+            const unsigned long long prev = atomicCAS(&table[s], kEmptySlot, key);
+            if (prev == kEmptySlot) {
+                placed = true;
+                break;
+            }
+            e = prev;
+        }
+        if ((e >> 32) == (key >> 32) && same_node<false>(cur, child, i, (uint32_t)e)) {
+            if ((uint32_t)e > i) atomicMin(&table[s], key);
+            placed = true;
+            break;
+        }
+        s = (s + 1) & cap_mask;
+    }
+    if (!placed) atomicOr(err, 16u);  // table full: the result is void, reported
+    cur.slot[i] = (uint32_t)s;
+}
+
+// Kept nodes of level L in node order: rank, word offset, the rank in the
+// slot's upper half, job boundaries; the level's totals from the last tile.
+// Each thread takes eight consecutive nodes; their slots, masks and jobs are
+// loaded as vectors and all eight table entries requested before any store.
+template <bool LEAF>
+__global__ void __launch_bounds__(kThreads)
+    k_merge_scan_lb(LevelDev cur, const uint32_t* __restrict__ counts, uint32_t* level_u, int L, SegDev seg,
+                    unsigned int* ticket, unsigned long long* flags, uint32_t* err) {
+    __shared__ uint32_t sm[64];
+    __shared__ uint32_t s_tile;
+    __shared__ uint2 s_excl;
+    const uint32_t n = counts[L];
+    const uint32_t ntiles = n ? (n + kScanTile - 1) / kScanTile : 1u;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        if (tile >= ntiles) break;
+        const uint32_t b0 = tile * kScanTile + threadIdx.x * kScanItems;
+        const bool full = b0 + kScanItems <= n;
+        uint32_t sl[kScanItems], mk[kScanItems], jb[kScanItems];
+        if (full) {
+#pragma unroll
+            for (int h = 0; h < kScanItems; h += 4) {
+                const uint4 a4 = *reinterpret_cast<const uint4*>(cur.slot + b0 + h);
+                const uint4 m4 = *reinterpret_cast<const uint4*>(cur.mask + b0 + h);
+                const uint4 j4 = *reinterpret_cast<const uint4*>(cur.job + b0 + h);
+                sl[h] = a4.x; sl[h + 1] = a4.y; sl[h + 2] = a4.z; sl[h + 3] = a4.w;
+                mk[h] = m4.x; mk[h + 1] = m4.y; mk[h + 2] = m4.z; mk[h + 3] = m4.w;
+                jb[h] = j4.x; jb[h + 1] = j4.y; jb[h + 2] = j4.z; jb[h + 3] = j4.w;
+            }
+        } else {
+#pragma unroll
+            for (int it = 0; it < kScanItems; ++it) {
+                const bool in = b0 + it < n;
+                sl[it] = in ? cur.slot[b0 + it] : 0u;
+                mk[it] = in ? cur.mask[b0 + it] : 0u;
+                jb[it] = in ? cur.job[b0 + it] : 0u;
+            }
+        }
+        const uint32_t jprev = (b0 > 0 && b0 <= n) ? cur.job[b0 - 1] : ~0u;
+        const uint32_t jnext = (b0 + kScanItems < n) ? cur.job[b0 + kScanItems] : ~0u;
+        uint32_t rep[kScanItems];
+#pragma unroll
+        for (int it = 0; it < kScanItems; ++it)
+            rep[it] = b0 + it < n ? (uint32_t)__ldcg(cur.table + sl[it]) : ~0u;
+        // the class representative (lower half of the slot) is the node's
+        // merged identity for the level above
+        if (full) {
+#pragma unroll
+            for (int h = 0; h < kScanItems; h += 4)
+                *reinterpret_cast<uint4*>(cur.uid + b0 + h) = make_uint4(rep[h], rep[h + 1], rep[h + 2], rep[h + 3]);
+        } else {
+#pragma unroll
+            for (int it = 0; it < kScanItems; ++it)
+                if (b0 + it < n) cur.uid[b0 + it] = rep[it];
+        }
+        uint32_t kept = 0, cnt = 0, words = 0;
+#pragma unroll
+        for (int it = 0; it < kScanItems; ++it)
+            if (rep[it] == b0 + it) {
+                kept |= 1u << it;
+                ++cnt;
+                words += node_words(mk[it], LEAF);
+            }
+        uint2 tot;
+        const uint2 pre = block_exclusive_scan2(make_uint2(cnt, words), tot, sm);
+        if (threadIdx.x < 32) {
+            const uint2 e = lookback(flags, tile, tot, err);
+            if (threadIdx.x == 0) s_excl = e;
+        }
+        __syncthreads();
+        uint32_t qx = s_excl.x + pre.x, qy = s_excl.y + pre.y;
+#pragma unroll
+        for (int it = 0; it < kScanItems; ++it) {
+            const uint32_t i = b0 + it;
+            if (i >= n) break;
+            const uint32_t j = jb[it];
+            const uint32_t jl = it == 0 ? jprev : jb[it - 1];
+            const uint32_t jr = it == kScanItems - 1 ? jnext : jb[it + 1];
+            if (i == 0 || jl != j) {
+                seg.ustart[seg_index(j, L)] = qx;
+                seg.wstart[seg_index(j, L)] = qy;
+            }
+            if (kept & (1u << it)) {
+                cur.uniq[qx] = i;
+                cur.woff[qx] = qy;
+                reinterpret_cast<uint32_t*>(cur.table + sl[it])[1] = qx;  // upper half: the rank
+                ++qx;
+                qy += node_words(mk[it], LEAF);
+            }
+            if (i == n - 1 || jr != j) {
+                seg.uend[seg_index(j, L)] = qx;
+                seg.wend[seg_index(j, L)] = qy;
+            }
+        }
+        if (tile == ntiles - 1 && threadIdx.x == 0) {
+            level_u[2 * L] = s_excl.x + tot.x;
+            level_u[2 * L + 1] = s_excl.y + tot.y;
+        }
+        __syncthreads();
+    }
+}
+
+// The topmost levels in one block.
+struct SmallLevels {
+    uint32_t inj_off[CPVS_MAX_LEVELS];
+    uint32_t ninj[CPVS_MAX_LEVELS];
+    uint32_t cap[CPVS_MAX_LEVELS];
+};
+
+// Expansion of levels Lhi down to Llo (each into the level below it).
+__global__ void __launch_bounds__(kSmallThreads)
+    k_expand_small(const LevelDev* __restrict__ lvt, uint32_t* counts, const JobDev* __restrict__ jobs,
+                   uint32_t njobs, int Lhi, int Llo, const Injected* __restrict__ inj_all, SmallLevels sl, SegDev seg,
+                   uint32_t* err) {
+    __shared__ uint32_t sm[64];
+    for (int L = Lhi; L >= Llo; --L) {
+        LevelDev cur = lvt[L], nxt = lvt[L - 1];
+        const uint32_t n = counts[L];
+        const uint32_t ninj = sl.ninj[L - 1], cap_next = sl.cap[L - 1];
+        const Injected* inj = inj_all + sl.inj_off[L - 1];
+        for (uint32_t r = threadIdx.x; r < ninj; r += blockDim.x) {
+            nxt.coord[r] = inj[r].coord;
+            nxt.job[r] = inj[r].job;
+        }
+        uint32_t run = ninj;
+        for (uint32_t t0 = 0; t0 < n; t0 += blockDim.x) {
+            const uint32_t i = t0 + threadIdx.x;
+            const uint32_t m = i < n ? classify_node(cur, jobs, njobs, L, i, err) : 0u;
+            uint2 tot;
+            const uint32_t p = block_exclusive_scan2(make_uint2(partial_children(m), 0u), tot, sm).x;
+            if (i < n) write_children(cur, nxt, seg, L, n, i, m, run + p, cap_next, err);
+            run += tot.x;
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            if (run > cap_next) atomicOr(err, 1u);
+            counts[L - 1] = run < cap_next ? run : cap_next;
+        }
+        __syncthreads();
+    }
+}
+
+// Merge of levels Llo..Lhi (insert, then ranks and offsets); the leaf level
+// (leaf_level, or -1) was inserted by k_leaf_insert.
+__global__ void __launch_bounds__(kSmallThreads)
+    k_merge_small(const LevelDev* __restrict__ lvt, const uint32_t* __restrict__ counts, uint32_t* level_u,
+                  int Llo, int Lhi, int bottom, int leaf_level, SegDev seg, uint32_t* err) {
+    __shared__ uint32_t sm[64];
+    for (int L = Llo; L <= Lhi; ++L) {
+        LevelDev cur = lvt[L];
+        const LevelDev child = L > bottom ? lvt[L - 1] : lvt[L];
+        const bool leaf = L == leaf_level;
+        const uint32_t n = counts[L];
+        if (!leaf)
+            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+                insert_inner(cur, child, i, cur.table, cur.table_mask, err);
+        __syncthreads();
+        uint32_t rx = 0, ry = 0;
+        for (uint32_t t0 = 0; t0 < n; t0 += blockDim.x) {
+            const uint32_t i = t0 + threadIdx.x;
+            bool kept = false;
+            if (i < n) {
+                const uint32_t rep = (uint32_t)__ldcg(cur.table + cur.slot[i]);
+                cur.uid[i] = rep;
+                kept = rep == i;
+            }
+            const uint32_t w = kept ? node_words(cur.mask[i], leaf) : 0u;
+            uint2 tot;
+            const uint2 p = block_exclusive_scan2(make_uint2(kept ? 1u : 0u, w), tot, sm);
+            if (i < n) {
+                const uint32_t qx = rx + p.x, qy = ry + p.y;
+                const uint32_t j = cur.job[i];
+                if (i == 0 || cur.job[i - 1] != j) {
+                    seg.ustart[seg_index(j, L)] = qx;
+                    seg.wstart[seg_index(j, L)] = qy;
+                }
+                if (kept) {
+                    cur.uniq[qx] = i;
+                    cur.woff[qx] = qy;
+                    reinterpret_cast<uint32_t*>(cur.table + cur.slot[i])[1] = qx;
+                }
+                if (i == n - 1 || cur.job[i + 1] != j) {
+                    seg.uend[seg_index(j, L)] = qx + (kept ? 1u : 0u);
+                    seg.wend[seg_index(j, L)] = qy + w;
+                }
+            }
+            rx += tot.x;
+            ry += tot.y;
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            level_u[2 * L] = rx;
+            level_u[2 * L + 1] = ry;
+        }
+        __syncthreads();
+    }
+}
+
 // ------------------------------------------------------------------ layout
 // Per job: level bases top-down and the DAG size; then job offsets.
 struct JobLayout {
@@ -791,7 +1363,7 @@ __global__ void __launch_bounds__(kThreads)
                 const uint32_t f = cur.first[i];
                 const uint32_t sc = seg_index(j, L - 1);
                 const uint32_t cb = lay.base[sc] - seg.wstart[sc];
-                for (uint32_t r = 0; r < k; ++r) dst[1 + r] = cb + child.woff[child.uid[f + r]];
+                for (uint32_t r = 0; r < k; ++r) dst[1 + r] = cb + child.woff[rank_of(child, f + r)];
             }
         }
     }
@@ -888,6 +1460,14 @@ struct BuildPlan {
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t done = nullptr;  // recorded after the emission that last read the scratch
     bool tables_tuned = false;
+    // single-pass levels: the levels >= small_lo run in the single-block
+    // kernels; look-back tickets and flags (zeroed by every build)
+    int small_lo = CPVS_MAX_LEVELS;
+    unsigned int* tickets = nullptr;     // [2 * L_MAX]
+    unsigned long long* flags = nullptr;
+    uint64_t flags_count = 0;
+    uint64_t exp_flag_off[CPVS_MAX_LEVELS] = {0}, scan_flag_off[CPVS_MAX_LEVELS] = {0};
+    uint64_t scan_tiles_cap[CPVS_MAX_LEVELS] = {0};
 };
 
 struct PlanCache {
@@ -907,6 +1487,28 @@ void plan_release(Ctx& ctx, BuildPlan* P) {
     if (P->hin) cudaFreeHost(P->hin);
     if (P->hout) cudaFreeHost(P->hout);
     P->hin = P->hout = nullptr;
+}
+
+// Per-level table regions (consecutive, tcap[L] slots each) and the split
+// between the multi-block levels and the topmost ones that run in single
+// blocks (a level is small when it and every level above it hold at most
+// kSmallLevelCap nodes).
+constexpr uint64_t kSmallLevelCap = 2048;
+void plan_bind_tables(BuildPlan* P) {
+    uint64_t off = 0;
+    for (int L = P->bottom; L <= P->maxR; ++L) {
+        P->lv[L].table = P->table + off;
+        P->lv[L].table_mask = P->tcap[L] - 1;
+        off += P->tcap[L];
+    }
+    P->small_lo = P->maxR + 1;
+    while (P->small_lo > P->bottom && P->cap[P->small_lo - 1] <= kSmallLevelCap) --P->small_lo;
+}
+
+uint64_t plan_table_slots(const BuildPlan* P) {
+    uint64_t t = 0;
+    for (int L = P->bottom; L <= P->maxR; ++L) t += P->tcap[L];
+    return t;
 }
 
 // Capacities -> scratch layout, pinned staging, level table.
@@ -932,11 +1534,25 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
     add(njobs, sizeof(JobDev));
     add(njobs, sizeof(Injected));
     add(P->bsegs.size(), sizeof(BoundSeg));
+    // look-back flags: per level, expansion tiles and 2 x merge tiles
+    P->flags_count = 0;
+    for (int L = P->bottom; L <= P->maxR; ++L) {
+        const uint64_t c = std::max<uint64_t>(P->cap[L], 1);
+        P->exp_flag_off[L] = P->flags_count;
+        P->flags_count += (c + kExpTile - 1) / kExpTile + 1;
+        P->scan_tiles_cap[L] = (c + kScanTile - 1) / kScanTile + 1;
+        P->scan_flag_off[L] = P->flags_count;
+        P->flags_count += P->scan_tiles_cap[L];
+    }
+    add(2 * CPVS_MAX_LEVELS, 4);
+    add(P->flags_count, 8);
     P->arena_bytes = bytes;
     cpvs_status r = ctx.alloc((void**)&P->arena, bytes, true, st);
     if (r != CPVS_OK) return r;
-    P->table_slots = 1024;
-    for (int L = P->bottom; L <= P->maxR; ++L) P->table_slots = std::max(P->table_slots, P->tcap[L]);
+    // one region of per-level hash tables (sized for the untuned tables;
+    // tuning only shrinks them)
+    P->table_slots = 0;
+    for (int L = P->bottom; L <= P->maxR; ++L) P->table_slots += P->tcap[L];
     r = ctx.alloc((void**)&P->table, P->table_slots * 8, true, st);
     if (r != CPVS_OK) return r;
     Arena A;
@@ -970,6 +1586,9 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
     P->jobs_dev = A.take<JobDev>(njobs);
     P->inj_dev = A.take<Injected>(njobs);
     P->bsegs_dev = A.take<BoundSeg>(P->bsegs.size());
+    P->tickets = A.take<unsigned int>(2 * CPVS_MAX_LEVELS);
+    P->flags = A.take<unsigned long long>(P->flags_count);
+    plan_bind_tables(P);
     // the device results region carries SegDev's arrays, so the six segment
     // arrays live there (copied to the host with the rest) and segbuf keeps
     // only JobLayout::base
@@ -1006,6 +1625,16 @@ cpvs_status plan_enqueue(const BuildPlan* P, cudaStream_t st, Timing* tm) {
     CPVS_CUDA(cudaMemsetAsync(P->res, 0, result_bytes(njobs), st));
     CPVS_CUDA(cudaMemsetAsync(P->counts, 0, CPVS_MAX_LEVELS * 4, st));
     CPVS_CUDA(cudaMemsetAsync(P->segbuf + 6 * segn, 0, segn * 4, st));
+    // look-back tickets and flags (adjacent in the arena), then every
+    // level's hash table
+    CPVS_CUDA(cudaMemsetAsync(P->tickets, 0,
+                              reinterpret_cast<const char*>(P->flags + P->flags_count) -
+                                  reinterpret_cast<const char*>(P->tickets),
+                              st));
+    {
+        KernelTimer kt(tm, K_TABLE_CLEAR, st);
+        CPVS_CUDA(cudaMemsetAsync(P->table, 0xFF, plan_table_slots(P) * 8, st));
+    }
     {
         KernelTimer kt(tm, K_LEVEL_BOUNDS, st);
         if (P->bound_blocks)
@@ -1015,60 +1644,62 @@ cpvs_status plan_enqueue(const BuildPlan* P, cudaStream_t st, Timing* tm) {
     // the top level holds only roots
     k_init_top<<<1, 256, 0, st>>>(P->lv[P->maxR], P->counts, P->maxR, P->inj_dev + P->inj_off[P->maxR],
                                   (uint32_t)P->ninj[P->maxR]);
-    for (int L = P->maxR; L > P->bottom; --L) {
-        const uint32_t g = plan_grid(P, P->cap[L], kThreads * 4);
-        {
-            KernelTimer kt(tm, K_EXPAND_COUNT, st);
-            k_expand_count<<<g, kThreads, 0, st>>>(P->lv[L], P->counts, P->jobs_dev, njobs, L, P->partials, err);
+    // top-down: the small top levels in one block, then one pass per level
+    const int Ls = P->small_lo;
+    const int exp_lo = std::max(Ls, P->bottom + 1);
+    if (P->maxR >= exp_lo) {
+        KernelTimer kt(tm, K_EXPAND_WRITE, st);
+        SmallLevels sl{};
+        for (int L = 0; L < CPVS_MAX_LEVELS; ++L) {
+            sl.inj_off[L] = (uint32_t)P->inj_off[L];
+            sl.ninj[L] = (uint32_t)P->ninj[L];
+            sl.cap[L] = (uint32_t)P->cap[L];
         }
-        {
-            KernelTimer kt(tm, K_EXPAND_WRITE, st);
-            k_expand_write<<<g, kThreads, 0, st>>>(P->lv[L], P->lv[L - 1], P->counts, L, P->partials,
-                                                   P->inj_dev + P->inj_off[L - 1], (uint32_t)P->ninj[L - 1], P->seg,
-                                                   (uint32_t)P->cap[L - 1], err);
-        }
+        k_expand_small<<<1, kSmallThreads, 0, st>>>(P->lvt, P->counts, P->jobs_dev, njobs, P->maxR, exp_lo,
+                                                    P->inj_dev, sl, P->seg, err);
+    }
+    for (int L = std::min(exp_lo - 1, P->maxR); L > P->bottom; --L) {
+        KernelTimer kt(tm, K_EXPAND_WRITE, st);
+        k_expand_lb<<<plan_grid(P, P->cap[L], kExpTile), kThreads, 0, st>>>(
+            P->lv[L], P->lv[L - 1], P->counts, P->jobs_dev, njobs, L, P->inj_dev + P->inj_off[L - 1],
+            (uint32_t)P->ninj[L - 1], P->seg, (uint32_t)P->cap[L - 1], P->tickets + L, P->flags + P->exp_flag_off[L],
+            err);
     }
     if (P->leafmasks) {
-        {
-            KernelTimer kt(tm, K_TABLE_CLEAR, st);
-            CPVS_CUDA(cudaMemsetAsync(P->table, 0xFF, P->tcap[2] * 8, st));
-        }
         KernelTimer kt(tm, K_LEAF_MASKS, st);
-        k_leaf_insert<<<plan_grid(P, P->cap[2], kThreads), kThreads, 0, st>>>(P->lv[2], P->counts, P->jobs_dev, njobs,
-                                                                             2, P->seg, P->table, P->tcap[2] - 1, err);
+        k_leaf_insert<<<plan_grid(P, P->cap[2], kThreads), kThreads, 0, st>>>(
+            P->lv[2], P->counts, P->jobs_dev, njobs, 2, P->seg, P->lv[2].table, P->lv[2].table_mask, err);
     } else {
         KernelTimer kt(tm, K_CLASSIFY_BOTTOM, st);
         k_classify_bottom<<<plan_grid(P, P->cap[0], kThreads), kThreads, 0, st>>>(P->lv[0], P->counts, P->jobs_dev,
                                                                                  njobs, 0, P->seg, err);
     }
     CPVS_CUDA(cudaGetLastError());
-    for (int L = P->bottom; L <= P->maxR; ++L) {
-        const uint64_t tc = P->tcap[L];
+    // bottom-up: one insert and one ranking pass per level, then the small
+    // top levels in one block
+    const int merge_hi = std::min(Ls - 1, P->maxR);
+    for (int L = P->bottom; L <= merge_hi; ++L) {
         const bool leaf = P->leafmasks && L == 2;
-        const uint32_t gs = plan_grid(P, P->cap[L], kThreads * 4), gi = plan_grid(P, P->cap[L], kThreads);
         const LevelDev child = (L > P->bottom) ? P->lv[L - 1] : P->lv[L];
         if (!leaf) {
-            KernelTimer kt(tm, K_TABLE_CLEAR, st);
-            CPVS_CUDA(cudaMemsetAsync(P->table, 0xFF, tc * 8, st));
+            KernelTimer kt(tm, K_INSERT_INNER, st);
+            k_dedup_insert<false><<<plan_grid(P, P->cap[L], kThreads), kThreads, 0, st>>>(
+                P->lv[L], child, P->counts, L, P->lv[L].table, P->lv[L].table_mask, err);
         }
-        if (leaf) {
-            // the leaves were inserted as they were built (k_leaf_insert)
-            { KernelTimer kt(tm, K_RESOLVE, st);
-              k_dedup_resolve<true><<<gs, kThreads, 0, st>>>(P->lv[L], P->counts, L, P->table, P->partials); }
-            { KernelTimer kt(tm, K_SCAN, st);
-              k_dedup_scan<true><<<gs, kThreads, 0, st>>>(P->lv[L], P->counts, rv.level_u, L, P->table, P->partials,
-                                                          P->seg); }
-        } else {
-            { KernelTimer kt(tm, K_INSERT_INNER, st);
-              k_dedup_insert<false><<<gi, kThreads, 0, st>>>(P->lv[L], child, P->counts, L, P->table, tc - 1, err); }
-            { KernelTimer kt(tm, K_RESOLVE, st);
-              k_dedup_resolve<false><<<gs, kThreads, 0, st>>>(P->lv[L], P->counts, L, P->table, P->partials); }
-            { KernelTimer kt(tm, K_SCAN, st);
-              k_dedup_scan<false><<<gs, kThreads, 0, st>>>(P->lv[L], P->counts, rv.level_u, L, P->table, P->partials,
-                                                           P->seg); }
-        }
-        { KernelTimer kt(tm, K_REMAP, st);
-          k_dedup_remap<<<gi, kThreads, 0, st>>>(P->lv[L], P->counts, L, P->table); }
+        KernelTimer kt(tm, K_SCAN, st);
+        const uint32_t g = plan_grid(P, P->cap[L], kScanTile);
+        unsigned long long* fl = P->flags + P->scan_flag_off[L];
+        unsigned int* ticket = P->tickets + CPVS_MAX_LEVELS + L;
+        if (leaf)
+            k_merge_scan_lb<true><<<g, kThreads, 0, st>>>(P->lv[L], P->counts, rv.level_u, L, P->seg, ticket, fl, err);
+        else
+            k_merge_scan_lb<false><<<g, kThreads, 0, st>>>(P->lv[L], P->counts, rv.level_u, L, P->seg, ticket, fl,
+                                                           err);
+    }
+    if (merge_hi < P->maxR) {
+        KernelTimer kt(tm, K_SCAN, st);
+        k_merge_small<<<1, kSmallThreads, 0, st>>>(P->lvt, P->counts, rv.level_u, std::max(merge_hi + 1, P->bottom),
+                                                   P->maxR, P->bottom, P->leafmasks ? 2 : -1, P->seg, err);
     }
     {
         KernelTimer kt(tm, K_LAYOUT, st);
@@ -1340,9 +1971,15 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
             P->tcap[L] = tc;
         }
         P->tables_tuned = true;
-        if (changed && P->exec) {
-            cudaGraphExecDestroy(P->exec);
-            P->exec = nullptr;
+        if (changed) {
+            if (P->exec) {
+                cudaGraphExecDestroy(P->exec);
+                P->exec = nullptr;
+            }
+            // after this build's emission (stream order), which reads the
+            // level table
+            plan_bind_tables(P);
+            CPVS_CUDA(cudaMemcpyAsync(P->lvt, P->lv, sizeof(P->lv), cudaMemcpyHostToDevice, st));
         }
     }
     return CPVS_OK;
