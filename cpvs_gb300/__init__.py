@@ -381,13 +381,22 @@ class CompressedShadow:
     def dag_size(self) -> int:
         return int(_lib.cpvs_shadow_dag_size(self.handle))
 
-    def get_dag(self) -> np.ndarray:
-        """CompressedShadow::getDAG(): the DAG words, copied to the host."""
+    def get_dag(self, out=None, stream=None):
+        """CompressedShadow::getDAG(): the DAG words, copied to the host (and
+        cached).  With `out` (a host uint32 array or tensor of at least
+        dag_size() words, e.g. reused pinned memory) the words are written
+        there and a view of it is returned, uncached."""
+        if out is not None:
+            n = self.dag_size()
+            if int(out.numel() if hasattr(out, "numel") else out.size) < n:
+                raise ValueError("get_dag: output buffer too small")
+            _check(_lib.cpvs_shadow_dag_words(self.handle, _ptr(out), n, None, _stream(stream)))
+            return out[:n]
         if self._dag is None:
             n = self.dag_size()
-            out = np.zeros(max(n, 1), np.uint32)
-            _check(_lib.cpvs_shadow_dag_words(self.handle, out.ctypes.data, out.size, None, 0))
-            self._dag = out[:n]
+            buf = np.zeros(max(n, 1), np.uint32)
+            _check(_lib.cpvs_shadow_dag_words(self.handle, buf.ctypes.data, buf.size, None, _stream(stream)))
+            self._dag = buf[:n]
         return self._dag
 
     getNumLevels, getTotalVisibility, getDAG = get_num_levels, get_total_visibility, get_dag

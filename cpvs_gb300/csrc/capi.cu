@@ -376,12 +376,23 @@ cpvs_status cpvs_hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n,
         r = c.alloc((void**)&h->levels, lbytes, true, st);
         if (r == CPVS_OK) h->bytes += lbytes;
     }
-    if (r == CPVS_OK && !borrow) {
+    // a host map the GPU reads in place is copied by the pyramid kernel as
+    // it reduces it (one pass over the host link); any other host map is
+    // uploaded first
+    const float* in_place = (!(flags & CPVS_IO_DEVICE) && r == CPVS_OK)
+                                ? static_cast<const float*>(cpvs::host_accessible(c, depth))
+                                : nullptr;
+    if (r == CPVS_OK && !borrow && !in_place) {
         cudaError_t e = cudaMemcpyAsync(h->depth, depth, dbytes,
                                         (flags & CPVS_IO_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) r = cpvs::cuda_fail(e, "hierarchy upload");
     }
-    if (r == CPVS_OK) r = cpvs::launch_pyramid(h->depth, n, h->levels, st, &c.timing);
+    if (r == CPVS_OK) {
+        if (in_place)
+            r = cpvs::launch_pyramid(in_place, n, h->levels, st, &c.timing, h->depth);
+        else
+            r = cpvs::launch_pyramid(h->depth, n, h->levels, st, &c.timing);
+    }
     h->touch(st);
     if (r != CPVS_OK) {
         cpvs_hierarchy_destroy(h);

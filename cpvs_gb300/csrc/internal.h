@@ -53,7 +53,9 @@ inline int log2_u32(uint32_t n) {
 
 // Builds levels 1..log2(n) of the min-max pyramid of `depth` into `levels`.
 struct Timing;
-cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaStream_t st, Timing* timing = nullptr);
+// `depth_copy` (optional): the map is also copied there while it is read.
+cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaStream_t st, Timing* timing = nullptr,
+                           float* depth_copy = nullptr);
 
 // One z-tile of a source map whose per-level node bounds are wanted.
 struct BoundJob {

@@ -25,10 +25,13 @@ constexpr int kTile = 64;
 constexpr int kThreads = 256;
 
 // in: level `L0-1` of side S (the depth map when FROM_DEPTH), out: pyramid
-// level array; writes levels L0 .. L0+log2(T)-1 of this CTA's tile.
+// level array; writes levels L0 .. L0+log2(T)-1 of this CTA's tile.  With
+// `copy` (FROM_DEPTH only) the depth map is also written there as it is
+// read: a map in host memory that the GPU reads in place crosses the host
+// link once, while it is reduced, instead of in a separate copy first.
 template <bool FROM_DEPTH>
 __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ in, uint32_t S, float2* __restrict__ out,
-                                                      uint32_t n, int L0, uint32_t T) {
+                                                      uint32_t n, int L0, uint32_t T, float* __restrict__ copy) {
     __shared__ float2 buf0[(kTile / 2) * (kTile / 2)];
     __shared__ float2 buf1[(kTile / 4) * (kTile / 4)];
     const uint32_t tiles_x = S / T;
@@ -47,6 +50,10 @@ __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ i
                 const float* d = static_cast<const float*>(in);
                 const float2 r0 = *reinterpret_cast<const float2*>(d + (size_t)iy * S + ix);
                 const float2 r1 = *reinterpret_cast<const float2*>(d + (size_t)(iy + 1) * S + ix);
+                if (copy) {
+                    *reinterpret_cast<float2*>(copy + (size_t)iy * S + ix) = r0;
+                    *reinterpret_cast<float2*>(copy + (size_t)(iy + 1) * S + ix) = r1;
+                }
                 lo = pmin(pmin(r0.x, r0.y), pmin(r1.x, r1.y));
                 hi = pmax(pmax(r0.x, r0.y), pmax(r1.x, r1.y));
             } else {
@@ -135,7 +142,8 @@ __global__ void __launch_bounds__(kBoundThreads)
 
 }  // namespace
 
-cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaStream_t st, Timing* timing) {
+cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaStream_t st, Timing* timing,
+                           float* depth_copy) {
     KernelTimer kt(timing, K_PYRAMID, st);
     uint32_t S = n;
     int L0 = 1;
@@ -144,9 +152,10 @@ cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaS
         const uint32_t T = S < (uint32_t)kTile ? S : (uint32_t)kTile;
         const uint32_t tiles = (S / T) * (S / T);
         if (first)
-            k_pyramid<true><<<tiles, kThreads, 0, st>>>(depth, S, levels, n, L0, T);
+            k_pyramid<true><<<tiles, kThreads, 0, st>>>(depth, S, levels, n, L0, T, depth_copy);
         else
-            k_pyramid<false><<<tiles, kThreads, 0, st>>>(levels + pyramid_level_offset(n, L0 - 1), S, levels, n, L0, T);
+            k_pyramid<false><<<tiles, kThreads, 0, st>>>(levels + pyramid_level_offset(n, L0 - 1), S, levels, n, L0, T,
+                                                          nullptr);
         CPVS_CUDA(cudaGetLastError());
         first = false;
         L0 += log2_u32(T);
