@@ -11,8 +11,10 @@ is required: importing the API without it raises, there is no fallback.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import os
+import weakref
 from typing import Optional
 
 import numpy as np
@@ -100,6 +102,23 @@ _SIGS = {
 }
 
 _lib: Optional[C.CDLL] = None
+_exiting = False
+_servers = weakref.WeakSet()
+
+
+@atexit.register
+def _at_exit():
+    """Servers are stopped (their threads joined) while the library is intact;
+    after that, native objects still alive at interpreter exit are left to the
+    process teardown instead of being destroyed in an arbitrary order."""
+    global _exiting
+    for srv in list(_servers):
+        srv.close()
+    _exiting = True
+
+
+def _live() -> bool:
+    return _lib is not None and not _exiting
 
 
 def library_path() -> str:
@@ -206,7 +225,7 @@ class Context:
         return {_lib.cpvs_kernel_name(i).decode(): (float(ms[i]), int(ln[i])) for i in range(cnt.value)}
 
     def __del__(self):
-        if getattr(self, "handle", None) and _lib is not None:
+        if getattr(self, "handle", None) and _live():
             _lib.cpvs_ctx_destroy(self.handle)
             self.handle = None
 
@@ -287,7 +306,7 @@ class MinMaxHierarchy:
     getMin, getMax = get_min, get_max
 
     def __del__(self):
-        if getattr(self, "handle", None) and _lib is not None:
+        if getattr(self, "handle", None) and _live():
             _lib.cpvs_hierarchy_destroy(self.handle)
             self.handle = None
 
@@ -453,7 +472,7 @@ class CompressedShadow:
         return int(self.lookup_ndc(np.asarray(position, np.float32).reshape(1, 3))[0])
 
     def release(self):
-        if getattr(self, "handle", None) and self._owned and _lib is not None:
+        if getattr(self, "handle", None) and self._owned and _live():
             _lib.cpvs_shadow_destroy(self.handle)
         self.handle = None
 
@@ -611,7 +630,7 @@ class CompressedShadowContainer:
         return res
 
     def __del__(self):
-        if getattr(self, "handle", None) and _lib is not None:
+        if getattr(self, "handle", None) and _live():
             _lib.cpvs_grid_destroy(self.handle)
             self.handle = None
 
@@ -638,6 +657,7 @@ class Server:
         h = _vp()
         _check(_lib.cpvs_server_create(self.ctx.handle, C.byref(cfg), C.byref(h)))
         self.handle = h.value
+        _servers.add(self)
         self._keep = {}  # ticket -> buffers that must outlive it
 
     def submit_build(self, key: int, depth) -> int:
@@ -679,7 +699,7 @@ class Server:
         return {k: getattr(st, k) for k, _ in st._fields_}
 
     def close(self):
-        if getattr(self, "handle", None) and _lib is not None:
+        if getattr(self, "handle", None) and _live():
             _lib.cpvs_server_destroy(self.handle)
         self.handle = None
 

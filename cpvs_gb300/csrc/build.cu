@@ -818,21 +818,20 @@ __device__ __forceinline__ uint32_t partial_set(uint32_t m) {
 
 // Expansion of level L into L-1 in one pass, tiles of kExpTile nodes.  Each
 // thread classifies four consecutive nodes (their inputs loaded before any
-// store, so the loads overlap); after the tile's scan and look-back, the
-// tile's children are written cooperatively -- thread t writes children
-// t, t + 256, ... of the tile, finding its parent by binary search over the
-// tile's child offsets in shared memory -- so the child arrays are written
-// in coalesced runs.
+// store, so the loads overlap) and records, for each of their children, the
+// (parent, child slot) pair at the child's position in a shared-memory map;
+// after the tile's scan and look-back, thread t writes children t, t + 256,
+// ... of the tile from that map, so the child arrays are written in
+// coalesced runs.
 __global__ void __launch_bounds__(kThreads)
     k_expand_lb(LevelDev cur, LevelDev nxt, uint32_t* counts, const JobDev* __restrict__ jobs, uint32_t njobs,
                 int L, const Injected* __restrict__ inj, uint32_t ninj, SegDev seg, uint32_t cap_next,
                 unsigned int* ticket, unsigned long long* flags, uint32_t* err) {
     __shared__ uint32_t sm[64];
     __shared__ uint32_t s_tile, s_excl;
-    __shared__ uint32_t s_off[kExpTile + 1];
     __shared__ uint64_t s_coord[kExpTile];
     __shared__ uint32_t s_job[kExpTile];
-    __shared__ uint8_t s_pset[kExpTile];
+    __shared__ uint16_t s_child[8 * kExpTile];  // tile child c: parent (local index) << 3 | child slot
     const uint32_t n = counts[L];
     const uint32_t ntiles = n ? (n + kExpTile - 1) / kExpTile : 1u;
     for (;;) {
@@ -886,26 +885,31 @@ __global__ void __launch_bounds__(kThreads)
             const uint32_t e = lookback(flags, tile, make_uint2(tot.x, 0u), err).x;
             if (threadIdx.x == 0) s_excl = e;
         }
-        // the tile's parents and their child offsets, for the cooperative writes
+        // the tile's parents and, per child, its parent and slot, for the
+        // cooperative writes
         uint32_t off = pre;
 #pragma unroll
         for (int it = 0; it < kExpItems; ++it) {
-            s_off[l0 + it] = off;
             s_coord[l0 + it] = cv[it];
             s_job[l0 + it] = jv[it];
-            s_pset[l0 + it] = (uint8_t)partial_set(m[it]);
-            off += partial_children(m[it]);
+            uint32_t pb = partial_set(m[it]);
+            while (pb) {
+                const uint32_t ch = (uint32_t)__ffs((int)pb) - 1u;
+                pb &= pb - 1u;
+                s_child[off++] = (uint16_t)(((l0 + it) << 3) | ch);
+            }
         }
-        if (threadIdx.x == 0) s_off[kExpTile] = tot.x;
         __syncthreads();
         const uint32_t f0 = ninj + s_excl;  // first child of the tile in level L-1
         // per parent: first child, overflow, job boundaries
+        uint32_t poff = pre;
 #pragma unroll
         for (int it = 0; it < kExpItems; ++it) {
             const uint32_t i = b0 + it;
             if (i >= n) break;
             const uint32_t k = partial_children(m[it]);
-            const uint32_t f = f0 + s_off[l0 + it];
+            const uint32_t f = f0 + poff;
+            poff += k;
             if (f + k > cap_next) {
                 // more children than the level bound: they are not written;
                 // reported, and the plan grows
@@ -927,23 +931,8 @@ __global__ void __launch_bounds__(kThreads)
         for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
             const uint32_t dst = f0 + c;
             if (dst >= cap_next) break;
-            uint32_t lo = 0, hi = kExpTile;
-            while (hi - lo > 1) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (s_off[mid] <= c) lo = mid; else hi = mid;
-            }
-            // the (c - s_off[lo])-th partial child of the parent, in child order
-            const uint32_t pb = s_pset[lo];
-            uint32_t r = c - s_off[lo], ch = 0;
-#pragma unroll
-            for (uint32_t b = 0; b < 8; ++b)
-                if ((pb >> b) & 1u) {
-                    if (r == 0u) {
-                        ch = b;
-                        r = 8u;  // found: later bits are not taken
-                    }
-                    --r;
-                }
+            const uint32_t e = s_child[c];
+            const uint32_t lo = e >> 3, ch = e & 7u;
             const uint64_t pc = s_coord[lo];
             const uint32_t x = unpack_x(pc), y = unpack_y(pc), z = unpack_z(pc);
             nxt.coord[dst] = pack_xyz((x + (ch & 1u)) * 2u, (y + ((ch >> 1) & 1u)) * 2u, (z + (ch >> 2)) * 2u);

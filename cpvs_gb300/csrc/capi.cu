@@ -388,10 +388,16 @@ cpvs_status cpvs_hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n,
         if (e != cudaSuccess) r = cpvs::cuda_fail(e, "hierarchy upload");
     }
     if (r == CPVS_OK) {
-        if (in_place)
+        if (in_place) {
             r = cpvs::launch_pyramid(in_place, n, h->levels, st, &c.timing, h->depth);
-        else
+            // the caller may reuse its buffer on return: wait for the read
+            if (r == CPVS_OK) {
+                const cudaError_t e = cudaStreamSynchronize(st);
+                if (e != cudaSuccess) r = cpvs::cuda_fail(e, "hierarchy read of the host map");
+            }
+        } else {
             r = cpvs::launch_pyramid(h->depth, n, h->levels, st, &c.timing);
+        }
     }
     h->touch(st);
     if (r != CPVS_OK) {

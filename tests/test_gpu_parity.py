@@ -341,3 +341,18 @@ def test_multi_dag_lookup_matches_single_lookups(cp, oracle):
     dev = cp.lookup_ndc_multi(shadows, torch.from_numpy(ids).cuda(), torch.from_numpy(q).cuda())
     torch.cuda.synchronize()
     assert np.array_equal(cp.unpack_bits(dev.cpu().numpy().view(np.uint32), nq), got)
+
+
+def test_host_map_may_be_reused_on_return(cp, oracle):
+    """cpvs_hierarchy_create reads a host map in place where the GPU can: the
+    call returns only when the map has been read, so the caller may overwrite
+    or free it right away (here: overwritten immediately, many times)."""
+    rng = np.random.default_rng(21)
+    maps = [random_map(rng, 64, k % 5) for k in range(12)]
+    buf = np.empty((64, 64), np.float32)
+    for k, m in enumerate(maps):
+        buf[:] = m
+        mm = cp.MinMaxHierarchy(buf)
+        buf[:] = np.float32(np.nan)  # clobber the caller's buffer after the call
+        got = cp.CompressedShadow.create(mm).get_dag()
+        assert np.array_equal(got, oracle.build(m).dag), k
