@@ -1249,46 +1249,6 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
-// Per-job bounds inside a build plan: one block per (job, level, 256
-// texels); the job's pyramid is read through the device job table, so a
-// captured plan serves any map of the same size.
-struct BoundSeg {
-    uint32_t job;
-    int32_t level;
-    uint32_t first_block;
-};
-
-__global__ void __launch_bounds__(kThreads)
-    k_plan_bounds(const JobDev* __restrict__ jobs, const BoundSeg* __restrict__ segs, uint32_t nsegs,
-                  unsigned long long* bounds) {
-    __shared__ uint64_t red[32];
-    // segment of this block: last seg with first_block <= blockIdx.x
-    uint32_t lo = 0, hi = nsegs;
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) / 2;
-        if (segs[mid].first_block <= blockIdx.x) lo = mid; else hi = mid;
-    }
-    const BoundSeg sg = segs[lo];
-    const JobDev J = jobs[sg.job];
-    const int L = sg.level, R = (int)J.num_levels - 2;
-    const uint32_t W = J.n >> L;
-    const uint64_t t = (uint64_t)(blockIdx.x - sg.first_block) * blockDim.x + threadIdx.x;
-    uint64_t c = 0;
-    if (t < (uint64_t)W * W) {
-        const float2 mm = J.pyr[pyramid_level_offset_dev(J.n, L) + t];
-        const float H = __uint2float_rn((J.n >> L) * J.z_num);
-        const uint64_t span = 2ull << (R - L);
-        const float a = __fmul_rn(mm.x, H), b = __fmul_rn(mm.y, H);
-        const uint64_t zlo = J.z_idx * span, zhi = (J.z_idx + 1) * span;
-        double s0 = (a != a) ? (double)zlo : floor((double)a);
-        double e0 = (b != b) ? (double)zhi : ceil((double)b);
-        if (s0 < (double)zlo) s0 = (double)zlo;
-        if (e0 > (double)zhi) e0 = (double)zhi;
-        c = (e0 > s0) ? (uint64_t)(e0 - s0) : 0ull;
-    }
-    c = block_sum_u64(c, red);
-    if (threadIdx.x == 0 && c) atomicAdd(&bounds[(size_t)sg.job * CPVS_MAX_LEVELS + (L - 1)], (unsigned long long)c);
-}
 
 // The top level of a batch: the roots of the jobs whose root lies there.
 __global__ void k_init_top(LevelDev top, uint32_t* counts, int L, const Injected* __restrict__ inj, uint32_t ninj) {
@@ -1385,14 +1345,13 @@ struct ResultView {
     uint32_t* seg;      // 6 * segn: nstart, nend, ustart, uend, wstart, wend
     uint32_t* level_u;  // 2 * L_MAX
     uint32_t* err;      // 1
-    unsigned long long* bounds;  // njobs * L_MAX
-    uint32_t* root_mask;         // njobs
+    uint32_t* root_mask;  // njobs
 };
 
 inline size_t result_bytes(uint32_t njobs) {
     const size_t segn = (size_t)njobs * CPVS_MAX_LEVELS;
     return align256(8 * (njobs + 1)) + align256(4 * 6 * segn) + align256(4 * 2 * CPVS_MAX_LEVELS) + align256(4) +
-           align256(8 * segn) + align256(4 * (size_t)njobs);
+           align256(4 * (size_t)njobs);
 }
 
 inline ResultView result_view(char* base, uint32_t njobs) {
@@ -1403,7 +1362,6 @@ inline ResultView result_view(char* base, uint32_t njobs) {
     v.seg = reinterpret_cast<uint32_t*>(base + o); o += align256(4 * 6 * segn);
     v.level_u = reinterpret_cast<uint32_t*>(base + o); o += align256(4 * 2 * CPVS_MAX_LEVELS);
     v.err = reinterpret_cast<uint32_t*>(base + o); o += align256(4);
-    v.bounds = reinterpret_cast<unsigned long long*>(base + o); o += align256(8 * segn);
     v.root_mask = reinterpret_cast<uint32_t*>(base + o);
     return v;
 }
@@ -1421,8 +1379,6 @@ struct BuildPlan {
     uint64_t cap[CPVS_MAX_LEVELS] = {0}, tcap[CPVS_MAX_LEVELS] = {0}, ninj[CPVS_MAX_LEVELS] = {0};
     uint64_t inj_off[CPVS_MAX_LEVELS + 1] = {0};
     uint32_t max_grid = 0;
-    std::vector<BoundSeg> bsegs;
-    uint32_t bound_blocks = 0;
     // device memory
     char* arena = nullptr;
     size_t arena_bytes = 0;
@@ -1440,7 +1396,6 @@ struct BuildPlan {
     uint32_t* root_dev = nullptr;
     JobDev* jobs_dev = nullptr;
     Injected* inj_dev = nullptr;
-    BoundSeg* bsegs_dev = nullptr;
     // pinned host staging
     char* hin = nullptr;
     size_t hin_bytes = 0;
@@ -1522,7 +1477,6 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
     add(njobs, 4);
     add(njobs, sizeof(JobDev));
     add(njobs, sizeof(Injected));
-    add(P->bsegs.size(), sizeof(BoundSeg));
     // look-back flags: per level, expansion tiles and 2 x merge tiles
     P->flags_count = 0;
     for (int L = P->bottom; L <= P->maxR; ++L) {
@@ -1574,7 +1528,6 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
     P->root_dev = A.take<uint32_t>(njobs);
     P->jobs_dev = A.take<JobDev>(njobs);
     P->inj_dev = A.take<Injected>(njobs);
-    P->bsegs_dev = A.take<BoundSeg>(P->bsegs.size());
     P->tickets = A.take<unsigned int>(2 * CPVS_MAX_LEVELS);
     P->flags = A.take<unsigned long long>(P->flags_count);
     plan_bind_tables(P);
@@ -1592,8 +1545,6 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
     // constant per plan: level table, root levels, bound segments
     CPVS_CUDA(cudaMemcpyAsync(P->lvt, P->lv, sizeof(P->lv), cudaMemcpyHostToDevice, st));
     CPVS_CUDA(cudaMemcpyAsync(P->root_dev, P->root_level.data(), njobs * 4, cudaMemcpyHostToDevice, st));
-    CPVS_CUDA(cudaMemcpyAsync(P->bsegs_dev, P->bsegs.data(), P->bsegs.size() * sizeof(BoundSeg),
-                              cudaMemcpyHostToDevice, st));
     CPVS_CUDA(cudaStreamSynchronize(st));
     return CPVS_OK;
 }
@@ -1603,7 +1554,7 @@ uint32_t plan_grid(const BuildPlan* P, uint64_t items, uint64_t per_block) {
     return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, P->max_grid));
 }
 
-// The whole device-side build after the inputs are staged: bounds, top-down
+// The whole device-side build after the inputs are staged: top-down
 // expansion, leaves, bottom-up merge, layout, root masks, and the copy of
 // the results region to pinned host memory.  Stream-ordered; capturable.
 cpvs_status plan_enqueue(const BuildPlan* P, cudaStream_t st, Timing* tm) {
@@ -1623,12 +1574,6 @@ cpvs_status plan_enqueue(const BuildPlan* P, cudaStream_t st, Timing* tm) {
     {
         KernelTimer kt(tm, K_TABLE_CLEAR, st);
         CPVS_CUDA(cudaMemsetAsync(P->table, 0xFF, plan_table_slots(P) * 8, st));
-    }
-    {
-        KernelTimer kt(tm, K_LEVEL_BOUNDS, st);
-        if (P->bound_blocks)
-            k_plan_bounds<<<P->bound_blocks, kThreads, 0, st>>>(P->jobs_dev, P->bsegs_dev, (uint32_t)P->bsegs.size(),
-                                                                 rv.bounds);
     }
     // the top level holds only roots
     k_init_top<<<1, 256, 0, st>>>(P->lv[P->maxR], P->counts, P->maxR, P->inj_dev + P->inj_off[P->maxR],
@@ -1740,13 +1685,6 @@ cpvs_status plan_create(Ctx& ctx, const std::vector<JobSpec>& jobs, const std::v
         o += P->ninj[L];
     }
     P->inj_off[CPVS_MAX_LEVELS] = o;
-    const int lmin = P->bottom + 1;
-    for (uint32_t j = 0; j < P->njobs; ++j)
-        for (int L = lmin; L <= (int)P->root_level[j]; ++L) {
-            const uint64_t tex = (uint64_t)(job_n[j] >> L) * (job_n[j] >> L);
-            P->bsegs.push_back(BoundSeg{j, L, P->bound_blocks});
-            P->bound_blocks += (uint32_t)((tex + kThreads - 1) / kThreads);
-        }
     plan_set_capacities(P, bounds, true);
     for (int L = 0; L < CPVS_MAX_LEVELS; ++L)
         if (P->cap[L] >= (1ull << 31)) {
@@ -1894,13 +1832,17 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         const uint32_t herr = *hv.err;
         if (herr == 0) break;
         // bit 1 (a level outgrew the plan) or 16 (a hash table did): re-plan
-        // from this run's bounds and retry; the rejected stale slots that an
-        // overflow leaves behind (bits 4, 8) go with it.  Anything else is an
-        // internal fault.
+        // from these maps' level bounds and retry; the rejected stale slots
+        // that an overflow leaves behind (bits 4, 8) go with it.  Anything
+        // else is an internal fault.
         const bool overflow = (herr & (1u | 16u)) != 0;
         if (!overflow || (herr & 2u) || attempt >= 2)
             return fail(CPVS_ERR_DEVICE, "build_dags: internal check " + std::to_string(herr));
-        std::vector<unsigned long long> bounds(hv.bounds, hv.bounds + (size_t)njobs * CPVS_MAX_LEVELS);
+        std::vector<unsigned long long> bounds;
+        {
+            cpvs_status r = prepass_bounds(ctx, sources, jobs, (leafmasks ? 2 : 0) + 1, st, bounds);
+            if (r != CPVS_OK) return r;
+        }
         plan_release(ctx, P);
         plan_set_capacities(P, bounds, true);
         cpvs_status r = plan_allocate(ctx, P, st);

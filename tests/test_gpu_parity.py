@@ -356,3 +356,18 @@ def test_host_map_may_be_reused_on_return(cp, oracle):
         buf[:] = np.float32(np.nan)  # clobber the caller's buffer after the call
         got = cp.CompressedShadow.create(mm).get_dag()
         assert np.array_equal(got, oracle.build(m).dag), k
+
+
+def test_plan_grows_for_a_busier_map(cp, oracle):
+    """A plan sized by a nearly flat map overflows on a noisy map of the same
+    side: the build re-plans from the new map's level bounds and retries, and
+    every DAG still equals the oracle's (then the grown plan serves both)."""
+    ctx = cp.Context(0)
+    flat = np.full((512, 512), np.float32(0.9))
+    flat[100:140, 200:260] = np.float32(0.4)
+    noisy = np.random.default_rng(8).random((512, 512), dtype=np.float32)
+    for d in (flat, noisy, flat, noisy):
+        sh = cp.CompressedShadow.create(cp.MinMaxHierarchy(d, ctx=ctx))
+        want = oracle.build(d)
+        assert np.array_equal(sh.get_dag(), want.dag)
+        assert sh.level_counts() == (want.tree_nodes, want.unique_nodes)
