@@ -38,10 +38,14 @@
 #include <mutex>
 #include <string>
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 
 namespace cpvs {
 namespace {
+
+namespace cg = cooperative_groups;
 
 constexpr int kThreads = 256;
 
@@ -291,19 +295,20 @@ __global__ void __launch_bounds__(kThreads)
 // (slice s = {t : k_t > s}).
 // Lit voxels among z = bz .. bz+7 of a texel with v = fl(d * H0): voxel z is
 // lit iff z + 0.5 <= v (src/CompressedShadowUtil.h:35-57), so the count is
-// clamp(floor(t) + 1, 0, 8) with t = v - (bz + 0.5).  bz is a multiple of 8
-// below 2^23, so bz + 0.5 is exact, and the float subtraction decides every
-// case exactly: for v in [c/2, 2c] (c = bz + 0.5) it is exact (Sterbenz);
-// below c/2, t < -c/2 stays negative (count 0); above 2c, either bz = 0 and
-// v - 0.5 is exact for v < 8.5, or t > 8 (count 8).  NaN: fmaxf picks -1
-// (count 0, as z + 0.5 <= NaN is false); +inf clamps to 8.
-// The count is produced without a float-to-int conversion: t is clamped to
-// [-1, 7] and added, rounding down, to 1.5 * 2^23 + 1, whose unit in the last
-// place is 1 -- so the sum is 1.5 * 2^23 + 1 + floor(t) and its bit pattern
-// is 0x4B400000 + count (count in the low four bits).
-__device__ __forceinline__ uint32_t lit_count_bits(float v, float c) {
-    const float t = fminf(fmaxf(__fsub_rn(v, c), -1.0f), 7.0f);
-    return __float_as_uint(__fadd_rd(t, 12582913.0f));
+// clamp(floor(x), 0, 8) with x = v - (bz + 0.5) + 1, exactly.  Two roundings
+// toward minus infinity give it without a float-to-int conversion:
+//   w = sat(fl_down(x / 8))  -- one fused multiply-add, v * 0.125 plus the
+//       exact constant (0.5 - bz) * 0.125; scaling by 1/8 is exact, so
+//       floor(8 w) = floor(fl_down(x)) = floor(x) for x in [0, 8], the
+//       saturation clamps to [0, 1] and sends NaN to 0 (as z + 0.5 <= NaN is
+//       false);
+//   fl_down(8 w + 1.5 * 2^23): the unit in the last place there is 1, so
+//       the sum is 1.5 * 2^23 + floor(8 w) and its bit pattern is
+//       0x4B400000 + count (count in the low four bits).
+__device__ __forceinline__ uint32_t lit_count_bits(float v, float c8) {
+    float w;
+    asm("fma.rm.sat.f32 %0, %1, %2, %3;" : "=f"(w) : "f"(v), "f"(0.125f), "f"(c8));
+    return __float_as_uint(__fmaf_rd(w, 8.0f, 12582912.0f));
 }
 constexpr uint32_t kCountBias = 0x4B400000u;
 
@@ -344,7 +349,7 @@ __device__ __forceinline__ bool leaf_compute(const LevelDev& lv, const JobDev* _
     }
     const uint32_t nmap = __ldg(&jobs[j].n);
     const float H = __uint2float_rn(nmap * __ldg(&jobs[j].z_num));
-    const float cz = __fadd_rn(__uint2float_rn(bz), 0.5f);
+    const float c8 = __fmul_rn(__fsub_rn(0.5f, __uint2float_rn(bz)), 0.125f);  // exact: bz < 2^23
     const float* row0 = jobs[j].depth + (size_t)by * nmap + bx;
     uint32_t R[8];  // per row: byte b = count bit b of the row's 8 texels
 #pragma unroll
@@ -354,7 +359,7 @@ __device__ __forceinline__ bool leaf_compute(const LevelDev& lv, const JobDev* _
         const float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
         uint32_t w = 0;
 #pragma unroll
-        for (int x = 0; x < 8; ++x) w += lit_count_bits(__fmul_rn(v[x], H), cz) << (4 * x);
+        for (int x = 0; x < 8; ++x) w += lit_count_bits(__fmul_rn(v[x], H), c8) << (4 * x);
         // every term carried kCountBias above its nibble: remove them all
         constexpr uint32_t bias = kCountBias + (kCountBias << 4) + (kCountBias << 8) + (kCountBias << 12) +
                                   (kCountBias << 16) + (kCountBias << 20) + (kCountBias << 24) + (kCountBias << 28);
@@ -510,17 +515,26 @@ __global__ void __launch_bounds__(kThreads, 5)
 }
 
 // --------------------------------------------------------------- bottom-up
+// A child's merged identity; CG: written by other blocks of the same
+// launch, so read from L2.
+template <bool CG>
+__device__ __forceinline__ uint32_t child_uid(const LevelDev& child, uint32_t x) {
+    return CG ? __ldcg(child.uid + x) : child.uid[x];
+}
+
+template <bool CG = false>
 __device__ __forceinline__ uint64_t inner_hash(const LevelDev& cur, const LevelDev& child, uint32_t i) {
     const uint32_t m = cur.mask[i];
     uint64_t h = fmix64((((uint64_t)cur.job[i] + 1) << 32 | m) ^ kGolden);
     const uint32_t k = partial_children(m);
     if (!k) return h;
     const uint32_t f = cur.first[i];
-    for (uint32_t r = 0; r < k; ++r) h = fmix64(h ^ ((uint64_t)child.uid[f + r] + (uint64_t)(r + 1) * kGolden));
+    for (uint32_t r = 0; r < k; ++r)
+        h = fmix64(h ^ ((uint64_t)child_uid<CG>(child, f + r) + (uint64_t)(r + 1) * kGolden));
     return h;
 }
 
-template <bool LEAF>
+template <bool LEAF, bool CG = false>
 __device__ __forceinline__ bool same_node(const LevelDev& cur, const LevelDev& child, uint32_t a, uint32_t b) {
     if (cur.job[a] != cur.job[b]) return false;
     if (LEAF) {
@@ -539,7 +553,7 @@ __device__ __forceinline__ bool same_node(const LevelDev& cur, const LevelDev& c
         if (!k) return true;
         const uint32_t fa = cur.first[a], fb = cur.first[b];
         for (uint32_t r = 0; r < k; ++r)
-            if (child.uid[fa + r] != child.uid[fb + r]) return false;
+            if (child_uid<CG>(child, fa + r) != child_uid<CG>(child, fb + r)) return false;
         return true;
     }
 }
@@ -682,7 +696,6 @@ constexpr int kExpItems = 4;
 constexpr uint32_t kExpTile = kThreads * kExpItems;
 constexpr int kScanItems = 8;
 constexpr uint32_t kScanTile = kThreads * kScanItems;
-constexpr int kSmallThreads = 1024;
 
 __device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p) {
     unsigned long long v;
@@ -950,9 +963,10 @@ __global__ void __launch_bounds__(kThreads)
 // Hash insert of inner node i into `table` (dedup_insert's rule: the slot
 // ends with the class's first occurrence); children are compared by their
 // class representatives (uid).
+template <bool CG>
 __device__ __forceinline__ void insert_inner(LevelDev& cur, const LevelDev& child, uint32_t i,
                                              unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
-    const uint64_t h = inner_hash(cur, child, i);
+    const uint64_t h = inner_hash<CG>(cur, child, i);
     const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | i;
     uint64_t s = h & cap_mask;
     bool placed = false;
@@ -966,7 +980,7 @@ __device__ __forceinline__ void insert_inner(LevelDev& cur, const LevelDev& chil
             }
             e = prev;
         }
-        if ((e >> 32) == (key >> 32) && same_node<false>(cur, child, i, (uint32_t)e)) {
+        if ((e >> 32) == (key >> 32) && same_node<false, CG>(cur, child, i, (uint32_t)e)) {
             if ((uint32_t)e > i) atomicMin(&table[s], key);
             placed = true;
             break;
@@ -1081,99 +1095,219 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
-// The topmost levels in one block.
+// The small top levels (at most kClusterItems * 1024 nodes per block) run as
+// one thread-block cluster (up to 16 blocks of 1024 threads on one GPC) in
+// one launch for the expansion and one for the merge.  Each level is split
+// into contiguous per-block ranges; block totals cross the cluster through
+// distributed shared memory, and a cluster barrier separates the passes and
+// the levels.  Node data written by other blocks of the same launch is read
+// from L2 (ld.global.cg).
+constexpr int kClusterThreads = 1024;
+constexpr int kClusterItems = 4;
+constexpr int kClusterMaxBlocks = 16;
+
 struct SmallLevels {
     uint32_t inj_off[CPVS_MAX_LEVELS];
     uint32_t ninj[CPVS_MAX_LEVELS];
     uint32_t cap[CPVS_MAX_LEVELS];
 };
 
-// Expansion of levels Lhi down to Llo (each into the level below it).
-__global__ void __launch_bounds__(kSmallThreads)
-    k_expand_small(const LevelDev* __restrict__ lvt, uint32_t* counts, const JobDev* __restrict__ jobs,
-                   uint32_t njobs, int Lhi, int Llo, const Injected* __restrict__ inj_all, SmallLevels sl, SegDev seg,
-                   uint32_t* err) {
+// Exclusive prefix of this block's `v` over the lower-ranked blocks of the
+// cluster, and the cluster total (every thread calls it; `v` is uniform).
+__device__ __forceinline__ uint2 cluster_prefix(cg::cluster_group& cl, uint2 v, uint2* s_tot, uint2& total) {
+    const uint32_t nb = cl.num_blocks(), rank = cl.block_rank();
+    if (threadIdx.x < nb) cl.map_shared_rank(s_tot, threadIdx.x)[rank] = v;
+    cl.sync();
+    uint2 p = make_uint2(0u, 0u), t = make_uint2(0u, 0u);
+    for (uint32_t r = 0; r < nb; ++r) {
+        const uint2 x = s_tot[r];
+        if (r < rank) {
+            p.x += x.x;
+            p.y += x.y;
+        }
+        t.x += x.x;
+        t.y += x.y;
+    }
+    total = t;
+    return p;
+}
+
+// Expansion of levels Lhi (whose roots this kernel writes) down to Llo, each
+// into the level below it.
+__global__ void __launch_bounds__(kClusterThreads, 1)
+    k_expand_cluster(const LevelDev* __restrict__ lvt, uint32_t* counts, const JobDev* __restrict__ jobs,
+                     uint32_t njobs, int Lhi, int Llo, const Injected* __restrict__ inj_all, SmallLevels sl,
+                     SegDev seg, uint32_t* err) {
+    cg::cluster_group cl = cg::this_cluster();
+    const uint32_t nb = cl.num_blocks(), rank = cl.block_rank();
     __shared__ uint32_t sm[64];
+    __shared__ uint2 s_tot[kClusterMaxBlocks];
+    if (rank == 0) {
+        LevelDev top = lvt[Lhi];
+        const Injected* inj = inj_all + sl.inj_off[Lhi];
+        for (uint32_t r = threadIdx.x; r < sl.ninj[Lhi]; r += blockDim.x) {
+            top.coord[r] = inj[r].coord;
+            top.job[r] = inj[r].job;
+        }
+        if (threadIdx.x == 0) counts[Lhi] = sl.ninj[Lhi];
+    }
+    cl.sync();
     for (int L = Lhi; L >= Llo; --L) {
         LevelDev cur = lvt[L], nxt = lvt[L - 1];
-        const uint32_t n = counts[L];
+        const uint32_t n = __ldcg(counts + L);
+        const uint32_t per = (n + nb - 1) / nb;
+        const uint32_t lo = min(n, rank * per), hi = min(n, lo + per);
+        if (hi - lo > (uint32_t)(kClusterItems * kClusterThreads)) atomicOr(err, 1u);  // the plan sized this level
+        uint32_t m[kClusterItems], jv[kClusterItems], ksum = 0;
+        uint64_t cv[kClusterItems];
+        bool bad_job = false, bad_node = false;
+#pragma unroll
+        for (int it = 0; it < kClusterItems; ++it) {
+            const uint32_t i = lo + it * kClusterThreads + threadIdx.x;
+            m[it] = 0;
+            jv[it] = 0;
+            cv[it] = 0;
+            if (i < hi) {
+                jv[it] = __ldcg(cur.job + i);
+                cv[it] = __ldcg(cur.coord + i);
+                if (jv[it] < njobs) {
+                    m[it] = node_mask_nf(jobs[jv[it]], L, cv[it], bad_node);
+                } else {
+                    bad_job = true;
+                    jv[it] = 0;
+                }
+            }
+            ksum += partial_children(m[it]);
+        }
+        if (bad_job) atomicOr(err, 8u);
+        if (bad_node) atomicOr(err, 4u);
+        uint2 btot, ctot;
+        block_exclusive_scan2(make_uint2(ksum, 0u), btot, sm);
+        const uint2 bpre = cluster_prefix(cl, btot, s_tot, ctot);
         const uint32_t ninj = sl.ninj[L - 1], cap_next = sl.cap[L - 1];
-        const Injected* inj = inj_all + sl.inj_off[L - 1];
-        for (uint32_t r = threadIdx.x; r < ninj; r += blockDim.x) {
-            nxt.coord[r] = inj[r].coord;
-            nxt.job[r] = inj[r].job;
-        }
-        uint32_t run = ninj;
-        for (uint32_t t0 = 0; t0 < n; t0 += blockDim.x) {
-            const uint32_t i = t0 + threadIdx.x;
-            const uint32_t m = i < n ? classify_node(cur, jobs, njobs, L, i, err) : 0u;
+        uint32_t run = ninj + bpre.x;
+#pragma unroll
+        for (int it = 0; it < kClusterItems; ++it) {
+            const uint32_t i = lo + it * kClusterThreads + threadIdx.x;
+            const bool in = i < hi;
+            uint32_t mi = in ? m[it] : 0u;
+            const uint32_t k = partial_children(mi);
             uint2 tot;
-            const uint32_t p = block_exclusive_scan2(make_uint2(partial_children(m), 0u), tot, sm).x;
-            if (i < n) write_children(cur, nxt, seg, L, n, i, m, run + p, cap_next, err);
+            const uint32_t f = run + block_exclusive_scan2(make_uint2(k, 0u), tot, sm).x;
+            if (in) {
+                if (f + k > cap_next) {
+                    atomicOr(err, 1u);  // more children than the level holds: not written, reported
+                    mi &= 0x5555u;
+                    cur.first[i] = 0;
+                } else {
+                    cur.first[i] = f;
+                    const uint32_t x = unpack_x(cv[it]), y = unpack_y(cv[it]), z = unpack_z(cv[it]);
+                    uint32_t r = 0;
+#pragma unroll
+                    for (uint32_t ch = 0; ch < 8; ++ch)
+                        if (mi & (2u << (2u * ch))) {
+                            // cs::getChildCoordinates (src/CompressedShadowUtil.cpp:101-117)
+                            nxt.coord[f + r] =
+                                pack_xyz((x + (ch & 1u)) * 2u, (y + ((ch >> 1) & 1u)) * 2u, (z + (ch >> 2)) * 2u);
+                            nxt.job[f + r] = jv[it];
+                            ++r;
+                        }
+                }
+                cur.mask[i] = mi;
+                if (jv[it] == 0 && __ldcg(cur.job + i) != 0) cur.job[i] = 0;
+                const uint32_t j = jv[it];
+                if (i == 0 || __ldcg(cur.job + i - 1) != j) seg.nstart[seg_index(j, L)] = i;
+                if (i == n - 1 || __ldcg(cur.job + i + 1) != j) seg.nend[seg_index(j, L)] = i + 1;
+            }
             run += tot.x;
-            __syncthreads();
         }
-        if (threadIdx.x == 0) {
-            if (run > cap_next) atomicOr(err, 1u);
-            counts[L - 1] = run < cap_next ? run : cap_next;
+        if (rank == 0) {
+            const Injected* inj = inj_all + sl.inj_off[L - 1];
+            for (uint32_t r = threadIdx.x; r < ninj; r += blockDim.x) {
+                nxt.coord[r] = inj[r].coord;
+                nxt.job[r] = inj[r].job;
+            }
+            if (threadIdx.x == 0) {
+                const uint32_t total = ninj + ctot.x;
+                if (total > cap_next) atomicOr(err, 1u);
+                counts[L - 1] = total < cap_next ? total : cap_next;
+            }
         }
-        __syncthreads();
+        cl.sync();
     }
 }
 
 // Merge of levels Llo..Lhi (insert, then ranks and offsets); the leaf level
 // (leaf_level, or -1) was inserted by k_leaf_insert.
-__global__ void __launch_bounds__(kSmallThreads)
-    k_merge_small(const LevelDev* __restrict__ lvt, const uint32_t* __restrict__ counts, uint32_t* level_u,
-                  int Llo, int Lhi, int bottom, int leaf_level, SegDev seg, uint32_t* err) {
+__global__ void __launch_bounds__(kClusterThreads, 1)
+    k_merge_cluster(const LevelDev* __restrict__ lvt, const uint32_t* __restrict__ counts, uint32_t* level_u,
+                    int Llo, int Lhi, int bottom, int leaf_level, SegDev seg, uint32_t* err) {
+    cg::cluster_group cl = cg::this_cluster();
+    const uint32_t nb = cl.num_blocks(), rank = cl.block_rank();
     __shared__ uint32_t sm[64];
+    __shared__ uint2 s_tot[kClusterMaxBlocks];
     for (int L = Llo; L <= Lhi; ++L) {
         LevelDev cur = lvt[L];
         const LevelDev child = L > bottom ? lvt[L - 1] : lvt[L];
         const bool leaf = L == leaf_level;
         const uint32_t n = counts[L];
+        const uint32_t per = (n + nb - 1) / nb;
+        const uint32_t lo = min(n, rank * per), hi = min(n, lo + per);
         if (!leaf)
-            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
-                insert_inner(cur, child, i, cur.table, cur.table_mask, err);
-        __syncthreads();
-        uint32_t rx = 0, ry = 0;
-        for (uint32_t t0 = 0; t0 < n; t0 += blockDim.x) {
-            const uint32_t i = t0 + threadIdx.x;
-            bool kept = false;
-            if (i < n) {
+            for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
+                insert_inner<true>(cur, child, i, cur.table, cur.table_mask, err);
+        cl.sync();  // every slot final
+        uint32_t kept = 0, cnt = 0, words = 0, w[kClusterItems];
+#pragma unroll
+        for (int it = 0; it < kClusterItems; ++it) {
+            const uint32_t i = lo + it * kClusterThreads + threadIdx.x;
+            w[it] = 0;
+            if (i < hi) {
                 const uint32_t rep = (uint32_t)__ldcg(cur.table + cur.slot[i]);
                 cur.uid[i] = rep;
-                kept = rep == i;
+                if (rep == i) {
+                    kept |= 1u << it;
+                    w[it] = node_words(cur.mask[i], leaf);
+                    ++cnt;
+                    words += w[it];
+                }
             }
-            const uint32_t w = kept ? node_words(cur.mask[i], leaf) : 0u;
+        }
+        uint2 btot, ctot;
+        block_exclusive_scan2(make_uint2(cnt, words), btot, sm);
+        const uint2 bpre = cluster_prefix(cl, btot, s_tot, ctot);
+        uint32_t rx = bpre.x, ry = bpre.y;
+#pragma unroll
+        for (int it = 0; it < kClusterItems; ++it) {
+            const uint32_t i = lo + it * kClusterThreads + threadIdx.x;
+            const bool kp = (kept >> it) & 1u;
             uint2 tot;
-            const uint2 p = block_exclusive_scan2(make_uint2(kept ? 1u : 0u, w), tot, sm);
-            if (i < n) {
+            const uint2 p = block_exclusive_scan2(make_uint2(kp ? 1u : 0u, w[it]), tot, sm);
+            if (i < hi) {
                 const uint32_t qx = rx + p.x, qy = ry + p.y;
                 const uint32_t j = cur.job[i];
                 if (i == 0 || cur.job[i - 1] != j) {
                     seg.ustart[seg_index(j, L)] = qx;
                     seg.wstart[seg_index(j, L)] = qy;
                 }
-                if (kept) {
+                if (kp) {
                     cur.uniq[qx] = i;
                     cur.woff[qx] = qy;
                     reinterpret_cast<uint32_t*>(cur.table + cur.slot[i])[1] = qx;
                 }
                 if (i == n - 1 || cur.job[i + 1] != j) {
-                    seg.uend[seg_index(j, L)] = qx + (kept ? 1u : 0u);
-                    seg.wend[seg_index(j, L)] = qy + w;
+                    seg.uend[seg_index(j, L)] = qx + (kp ? 1u : 0u);
+                    seg.wend[seg_index(j, L)] = qy + w[it];
                 }
             }
             rx += tot.x;
             ry += tot.y;
-            __syncthreads();
         }
-        if (threadIdx.x == 0) {
-            level_u[2 * L] = rx;
-            level_u[2 * L + 1] = ry;
+        if (rank == 0 && threadIdx.x == 0) {
+            level_u[2 * L] = ctot.x;
+            level_u[2 * L + 1] = ctot.y;
         }
-        __syncthreads();
+        cl.sync();  // identities visible to the level above
     }
 }
 
@@ -1407,6 +1541,7 @@ struct BuildPlan {
     // single-pass levels: the levels >= small_lo run in the single-block
     // kernels; look-back tickets and flags (zeroed by every build)
     int small_lo = CPVS_MAX_LEVELS;
+    int cluster_blocks = 0;  // blocks of the small-level cluster kernels (0: none)
     unsigned int* tickets = nullptr;     // [2 * L_MAX]
     unsigned long long* flags = nullptr;
     uint64_t flags_count = 0;
@@ -1434,11 +1569,11 @@ void plan_release(Ctx& ctx, BuildPlan* P) {
 }
 
 // Per-level table regions (consecutive, tcap[L] slots each) and the split
-// between the multi-block levels and the topmost ones that run in single
-// blocks (a level is small when it and every level above it hold at most
-// kSmallLevelCap nodes).
-constexpr uint64_t kSmallLevelCap = 2048;
+// between the multi-block levels and the topmost ones that run in the
+// cluster kernels (a level is small when it and every level above it hold
+// at most kClusterItems * 1024 nodes per cluster block).
 void plan_bind_tables(BuildPlan* P) {
+    const uint64_t small_cap = (uint64_t)P->cluster_blocks * kClusterThreads * kClusterItems;
     uint64_t off = 0;
     for (int L = P->bottom; L <= P->maxR; ++L) {
         P->lv[L].table = P->table + off;
@@ -1446,7 +1581,7 @@ void plan_bind_tables(BuildPlan* P) {
         off += P->tcap[L];
     }
     P->small_lo = P->maxR + 1;
-    while (P->small_lo > P->bottom && P->cap[P->small_lo - 1] <= kSmallLevelCap) --P->small_lo;
+    while (P->small_lo > P->bottom && P->cap[P->small_lo - 1] <= small_cap) --P->small_lo;
 }
 
 uint64_t plan_table_slots(const BuildPlan* P) {
@@ -1554,6 +1689,50 @@ uint32_t plan_grid(const BuildPlan* P, uint64_t items, uint64_t per_block) {
     return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, P->max_grid));
 }
 
+// Cluster launch of a small-level kernel: `nb` blocks of 1024 threads, one
+// cluster.
+template <typename... Exp, typename... Act>
+cudaError_t launch_cluster(void (*kernel)(Exp...), uint32_t nb, cudaStream_t st, Act&&... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(nb);
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = nb;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Act>(args)...);
+}
+
+// The largest cluster (16, else 8 blocks of 1024 threads) that both
+// small-level kernels can have resident on this device; 0 if none.
+int probe_cluster_blocks() {
+    cudaFuncSetAttribute(k_expand_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute(k_merge_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaGetLastError();
+    for (int nb : {16, 8}) {
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(nb);
+        cfg.blockDim = dim3(kClusterThreads);
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = nb;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int a = 0, b = 0;
+        const bool ok = cudaOccupancyMaxActiveClusters(&a, k_expand_cluster, &cfg) == cudaSuccess && a > 0 &&
+                        cudaOccupancyMaxActiveClusters(&b, k_merge_cluster, &cfg) == cudaSuccess && b > 0;
+        cudaGetLastError();
+        if (ok) return nb;
+    }
+    return 0;
+}
+
 // The whole device-side build after the inputs are staged: top-down
 // expansion, leaves, bottom-up merge, layout, root masks, and the copy of
 // the results region to pinned host memory.  Stream-ordered; capturable.
@@ -1575,10 +1754,8 @@ cpvs_status plan_enqueue(const BuildPlan* P, cudaStream_t st, Timing* tm) {
         KernelTimer kt(tm, K_TABLE_CLEAR, st);
         CPVS_CUDA(cudaMemsetAsync(P->table, 0xFF, plan_table_slots(P) * 8, st));
     }
-    // the top level holds only roots
-    k_init_top<<<1, 256, 0, st>>>(P->lv[P->maxR], P->counts, P->maxR, P->inj_dev + P->inj_off[P->maxR],
-                                  (uint32_t)P->ninj[P->maxR]);
-    // top-down: the small top levels in one block, then one pass per level
+    // top-down: the small top levels as one cluster (which also places the
+    // roots), then one pass per level
     const int Ls = P->small_lo;
     const int exp_lo = std::max(Ls, P->bottom + 1);
     if (P->maxR >= exp_lo) {
@@ -1589,8 +1766,12 @@ cpvs_status plan_enqueue(const BuildPlan* P, cudaStream_t st, Timing* tm) {
             sl.ninj[L] = (uint32_t)P->ninj[L];
             sl.cap[L] = (uint32_t)P->cap[L];
         }
-        k_expand_small<<<1, kSmallThreads, 0, st>>>(P->lvt, P->counts, P->jobs_dev, njobs, P->maxR, exp_lo,
-                                                    P->inj_dev, sl, P->seg, err);
+        CPVS_CUDA(launch_cluster(k_expand_cluster, (uint32_t)P->cluster_blocks, st, P->lvt, P->counts, P->jobs_dev,
+                                 njobs, P->maxR, exp_lo, P->inj_dev, sl, P->seg, err));
+    } else {
+        // the top level holds only roots
+        k_init_top<<<1, 256, 0, st>>>(P->lv[P->maxR], P->counts, P->maxR, P->inj_dev + P->inj_off[P->maxR],
+                                      (uint32_t)P->ninj[P->maxR]);
     }
     for (int L = std::min(exp_lo - 1, P->maxR); L > P->bottom; --L) {
         KernelTimer kt(tm, K_EXPAND_WRITE, st);
@@ -1632,8 +1813,9 @@ cpvs_status plan_enqueue(const BuildPlan* P, cudaStream_t st, Timing* tm) {
     }
     if (merge_hi < P->maxR) {
         KernelTimer kt(tm, K_SCAN, st);
-        k_merge_small<<<1, kSmallThreads, 0, st>>>(P->lvt, P->counts, rv.level_u, std::max(merge_hi + 1, P->bottom),
-                                                   P->maxR, P->bottom, P->leafmasks ? 2 : -1, P->seg, err);
+        CPVS_CUDA(launch_cluster(k_merge_cluster, (uint32_t)P->cluster_blocks, st, P->lvt, P->counts, rv.level_u,
+                                 std::max(merge_hi + 1, P->bottom), P->maxR, P->bottom, P->leafmasks ? 2 : -1, P->seg,
+                                 err));
     }
     {
         KernelTimer kt(tm, K_LAYOUT, st);
@@ -1674,6 +1856,8 @@ cpvs_status plan_create(Ctx& ctx, const std::vector<JobSpec>& jobs, const std::v
     P->job_n = job_n;
     P->root_level.resize(P->njobs);
     P->max_grid = (uint32_t)std::max(ctx.num_sms, 1) * 8;
+    if (ctx.cluster_blocks < 0) ctx.cluster_blocks = probe_cluster_blocks();
+    P->cluster_blocks = ctx.cluster_blocks;
     for (uint32_t j = 0; j < P->njobs; ++j) {
         P->root_level[j] = (uint32_t)(log2_u32(job_n[j]) - 1);
         P->maxR = std::max(P->maxR, (int)P->root_level[j]);

@@ -205,6 +205,7 @@ struct Ctx {
     Timing timing;
     int device = 0;
     int num_sms = 0;
+    int cluster_blocks = -1;  // blocks per cluster of the small-level build kernels (-1: not probed yet)
     bool pageable_access = false;  // the GPU reads pageable host memory in place
     // lookup queries per thread: fixed by cpvs_ctx_set_option, else tuned
     // once per (DAG levels, NDC or voxel input)
