@@ -170,8 +170,9 @@ def run_ours(args, rank, world, local_rank):
     keep = {}
 
     def build_step():
-        mm = cp.MinMaxHierarchy(depth_dev, ctx=ctx, stream=stream, borrow=True)
-        sh = cp.CompressedShadow.create(mm, stream=stream)
+        # CompressedShadow::create(const ShadowMap*) shape: hierarchy (reading
+        # the resident map in place) + build in one call
+        sh = cp.CompressedShadow.from_depth(depth_dev, ctx=ctx, stream=stream)
         keep["sh"] = sh  # the previous step's DAG is freed as this one replaces it
         return sh
 
@@ -716,7 +717,7 @@ def run_served(args):
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--config", choices=tuple(WORKLOADS), default="c1")

@@ -522,40 +522,18 @@ __device__ __forceinline__ uint32_t child_uid(const LevelDev& child, uint32_t x)
     return CG ? __ldcg(child.uid + x) : child.uid[x];
 }
 
-template <bool CG = false>
-__device__ __forceinline__ uint64_t inner_hash(const LevelDev& cur, const LevelDev& child, uint32_t i) {
-    const uint32_t m = cur.mask[i];
-    uint64_t h = fmix64((((uint64_t)cur.job[i] + 1) << 32 | m) ^ kGolden);
-    const uint32_t k = partial_children(m);
-    if (!k) return h;
-    const uint32_t f = cur.first[i];
-    for (uint32_t r = 0; r < k; ++r)
-        h = fmix64(h ^ ((uint64_t)child_uid<CG>(child, f + r) + (uint64_t)(r + 1) * kGolden));
-    return h;
-}
-
-template <bool LEAF, bool CG = false>
-__device__ __forceinline__ bool same_node(const LevelDev& cur, const LevelDev& child, uint32_t a, uint32_t b) {
+// Two leaves are the same node when their jobs and all eight slice masks
+// are equal.
+__device__ __forceinline__ bool same_leaf(const LevelDev& cur, uint32_t a, uint32_t b) {
     if (cur.job[a] != cur.job[b]) return false;
-    if (LEAF) {
-        const ulonglong2* sa = reinterpret_cast<const ulonglong2*>(cur.slices + (size_t)a * 8);
-        const ulonglong2* sb = reinterpret_cast<const ulonglong2*>(cur.slices + (size_t)b * 8);
+    const ulonglong2* sa = reinterpret_cast<const ulonglong2*>(cur.slices + (size_t)a * 8);
+    const ulonglong2* sb = reinterpret_cast<const ulonglong2*>(cur.slices + (size_t)b * 8);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const ulonglong2 x = sa[q], y = sb[q];
-            if (x.x != y.x || x.y != y.y) return false;
-        }
-        return true;
-    } else {
-        const uint32_t m = cur.mask[a];
-        if (m != cur.mask[b]) return false;
-        const uint32_t k = partial_children(m);
-        if (!k) return true;
-        const uint32_t fa = cur.first[a], fb = cur.first[b];
-        for (uint32_t r = 0; r < k; ++r)
-            if (child_uid<CG>(child, fa + r) != child_uid<CG>(child, fb + r)) return false;
-        return true;
+    for (int q = 0; q < 4; ++q) {
+        const ulonglong2 x = sa[q], y = sb[q];
+        if (x.x != y.x || x.y != y.y) return false;
     }
+    return true;
 }
 
 // Inserts every node of level L into the table.  A slot holds
@@ -563,13 +541,22 @@ __device__ __forceinline__ bool same_node(const LevelDev& cur, const LevelDev& c
 // empty slot with CAS, later equal nodes lower it with atomicMin, so the slot
 // ends with the class's smallest (first-occurring) index.  The probe is
 // bounded by the table size (the table is at least twice the node count).
+template <bool CG>
+__device__ __forceinline__ void insert_inner(LevelDev& cur, const LevelDev& child, uint32_t i,
+                                             unsigned long long* table, uint64_t cap_mask, uint32_t* err);
+
 template <bool LEAF>
 __global__ void __launch_bounds__(kThreads)
     k_dedup_insert(LevelDev cur, LevelDev child, const uint32_t* __restrict__ counts, int L,
                    unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
     const uint32_t n = counts[L];
+    if (!LEAF) {
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            insert_inner<false>(cur, child, i, table, cap_mask, err);
+        return;
+    }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint64_t h = LEAF ? cur.hash[i] : inner_hash(cur, child, i);
+        const uint64_t h = cur.hash[i];
         const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | i;
         uint64_t s = h & cap_mask;
         bool placed = false;
@@ -583,7 +570,7 @@ __global__ void __launch_bounds__(kThreads)
                 }
                 cur_e = prev;
             }
-            if ((cur_e >> 32) == (key >> 32) && same_node<LEAF>(cur, child, i, (uint32_t)cur_e)) {
+            if ((cur_e >> 32) == (key >> 32) && same_leaf(cur, i, (uint32_t)cur_e)) {
                 // the slot only ever decreases: nothing to do when it already
                 // holds an earlier occurrence
                 if ((uint32_t)cur_e > i) atomicMin(&table[s], key);
@@ -962,11 +949,27 @@ __global__ void __launch_bounds__(kThreads)
 
 // Hash insert of inner node i into `table` (dedup_insert's rule: the slot
 // ends with the class's first occurrence); children are compared by their
-// class representatives (uid).
+// merged identities (uid).  The node's child identities, and on a tag match
+// the candidate's, are requested as independent loads before they are used,
+// so a node costs two dependent round trips for its children instead of one
+// per child.
+template <bool CG>
+__device__ __forceinline__ void load_child_ids(const LevelDev& child, uint32_t f, uint32_t k, uint32_t u[8]) {
+#pragma unroll
+    for (uint32_t r = 0; r < 8; ++r) u[r] = r < k ? child_uid<CG>(child, f + r) : 0u;
+}
+
 template <bool CG>
 __device__ __forceinline__ void insert_inner(LevelDev& cur, const LevelDev& child, uint32_t i,
                                              unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
-    const uint64_t h = inner_hash<CG>(cur, child, i);
+    const uint32_t m = cur.mask[i], j = cur.job[i];
+    const uint32_t k = partial_children(m);
+    uint32_t u[8];
+    load_child_ids<CG>(child, k ? cur.first[i] : 0u, k, u);
+    uint64_t h = fmix64((((uint64_t)j + 1) << 32 | m) ^ kGolden);
+#pragma unroll
+    for (uint32_t r = 0; r < 8; ++r)
+        if (r < k) h = fmix64(h ^ ((uint64_t)u[r] + (uint64_t)(r + 1) * kGolden));
     const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | i;
     uint64_t s = h & cap_mask;
     bool placed = false;
@@ -980,10 +983,20 @@ __device__ __forceinline__ void insert_inner(LevelDev& cur, const LevelDev& chil
             }
             e = prev;
         }
-        if ((e >> 32) == (key >> 32) && same_node<false, CG>(cur, child, i, (uint32_t)e)) {
-            if ((uint32_t)e > i) atomicMin(&table[s], key);
-            placed = true;
-            break;
+        if ((e >> 32) == (key >> 32)) {
+            const uint32_t b = (uint32_t)e;
+            bool same = cur.job[b] == j && cur.mask[b] == m;
+            if (same && k) {
+                uint32_t v[8];
+                load_child_ids<CG>(child, cur.first[b], k, v);
+#pragma unroll
+                for (uint32_t r = 0; r < 8; ++r) same = same && (r >= k || u[r] == v[r]);
+            }
+            if (same) {
+                if (b > i) atomicMin(&table[s], key);
+                placed = true;
+                break;
+            }
         }
         s = (s + 1) & cap_mask;
     }
