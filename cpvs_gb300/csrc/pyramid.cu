@@ -96,6 +96,64 @@ __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ i
     }
 }
 
+// Levels 1-6 of a 64x64 tile straight from the depth map, with the tile
+// size fixed at compile time: each thread reduces two horizontally adjacent
+// level-1 texels per step from two 16-byte loads (one per input row) and
+// stores them as one 16-byte (min,max,min,max) pair; a warp covers 512
+// contiguous bytes of each input row.  Levels 2-6 reduce in shared memory.
+// With `copy` the map is also written there as it is read.
+__global__ void __launch_bounds__(kThreads)
+    k_pyramid64(const float* __restrict__ in, uint32_t S, float2* __restrict__ out, uint32_t n,
+                float* __restrict__ copy) {
+    __shared__ float2 buf0[32 * 32];
+    __shared__ float2 buf1[16 * 16];
+    const uint32_t tiles_x = S >> 6;
+    const uint32_t tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+    {
+        const uint32_t So = S >> 1;
+        float2* dst = out;  // level 1 starts the pyramid array
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const uint32_t pidx = threadIdx.x + k * kThreads;  // 512 texel pairs: 32 rows x 16
+            const uint32_t oy = pidx >> 4, px = pidx & 15u;
+            const size_t r0 = (size_t)(ty * 64 + 2 * oy) * S + tx * 64 + 4 * px;
+            const float4 a = *reinterpret_cast<const float4*>(in + r0);
+            const float4 b = *reinterpret_cast<const float4*>(in + r0 + S);
+            if (copy) {
+                *reinterpret_cast<float4*>(copy + r0) = a;
+                *reinterpret_cast<float4*>(copy + r0 + S) = b;
+            }
+            const float2 v0 = make_float2(pmin(pmin(a.x, a.y), pmin(b.x, b.y)), pmax(pmax(a.x, a.y), pmax(b.x, b.y)));
+            const float2 v1 = make_float2(pmin(pmin(a.z, a.w), pmin(b.z, b.w)), pmax(pmax(a.z, a.w), pmax(b.z, b.w)));
+            *reinterpret_cast<float4*>(dst + (size_t)(ty * 32 + oy) * So + tx * 32 + 2 * px) =
+                make_float4(v0.x, v0.y, v1.x, v1.y);
+            buf0[oy * 32 + 2 * px] = v0;
+            buf0[oy * 32 + 2 * px + 1] = v1;
+        }
+    }
+    uint32_t So = S >> 1;
+    float2* src = buf0;
+    float2* nxt = buf1;
+#pragma unroll
+    for (int lvl = 2; lvl <= 6; ++lvl) {
+        __syncthreads();
+        const uint32_t h = 64u >> lvl, lh = 6 - lvl;  // output side of this level in the tile, log2
+        So >>= 1;
+        float2* dst = out + pyramid_level_offset_dev(n, lvl);
+        if (threadIdx.x < h * h) {
+            const uint32_t o = threadIdx.x, ox = o & (h - 1), oy = o >> lh, w = 2 * h;
+            const float2 a = src[(2 * oy) * w + 2 * ox], b = src[(2 * oy) * w + 2 * ox + 1];
+            const float2 c = src[(2 * oy + 1) * w + 2 * ox], d = src[(2 * oy + 1) * w + 2 * ox + 1];
+            const float2 v = make_float2(pmin(pmin(a.x, b.x), pmin(c.x, d.x)), pmax(pmax(a.y, b.y), pmax(c.y, d.y)));
+            dst[(size_t)(ty * h + oy) * So + tx * h + ox] = v;
+            nxt[o] = v;
+        }
+        float2* t = src;
+        src = nxt;
+        nxt = t;
+    }
+}
+
 // Partial-cell count of one texel for a z range [lo, hi): the cells z with
 // NOT(z+1 <= a) and NOT(z >= b), i.e. z in [floor(a), ceil(b)), where a and
 // b are the scaled min and max; a NaN bound excludes nothing (the
@@ -151,7 +209,9 @@ cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaS
     while (S > 1) {
         const uint32_t T = S < (uint32_t)kTile ? S : (uint32_t)kTile;
         const uint32_t tiles = (S / T) * (S / T);
-        if (first)
+        if (first && T == (uint32_t)kTile)
+            k_pyramid64<<<tiles, kThreads, 0, st>>>(depth, S, levels, n, depth_copy);
+        else if (first)
             k_pyramid<true><<<tiles, kThreads, 0, st>>>(depth, S, levels, n, L0, T, depth_copy);
         else
             k_pyramid<false><<<tiles, kThreads, 0, st>>>(levels + pyramid_level_offset(n, L0 - 1), S, levels, n, L0, T,
