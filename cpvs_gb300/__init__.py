@@ -56,6 +56,7 @@ _SIGS = {
     "cpvs_kernel_name": (C.c_char_p, [_u32]),
     "cpvs_raster_depth": (C.c_int, [_vp, _vp, _u32, _vp, _u32, C.c_float, _u32, _u32, _u32, _u32, _u32, _vp, _u32,
                                     _vp]),
+    "cpvs_raster_triangles": (C.c_int, [_vp, _vp, _u32, C.c_float, _u32, _u32, _u32, _u32, _u32, _vp, _u32, _vp]),
     "cpvs_hierarchy_create": (C.c_int, [_vp, _vp, _u32, _u32, _vp, C.POINTER(_vp)]),
     "cpvs_hierarchy_destroy": (None, [_vp]),
     "cpvs_hierarchy_num_levels": (_u32, [_vp]),
@@ -254,6 +255,28 @@ def raster_depth(sc, x0: int = 0, y0: int = 0, w: Optional[int] = None, h: Optio
                                   float(sc.plane), sc.n, x0, y0, w, h, _ptr(out), IO_DEVICE, _stream(stream)))
     if stream is None:
         torch.cuda.synchronize(dev)
+    return out
+
+
+def raster_triangles(tris, n: int, plane: float, x0: int = 0, y0: int = 0, w: Optional[int] = None,
+                     h: Optional[int] = None, ctx: Optional[Context] = None, stream=None):
+    """Depth map of (m, 9) float32 triangles (x0,y0,d0, x1,y1,d1, x2,y2,d2 in map
+    coordinates) over a plane, rasterised on the GPU (cpvs_raster_triangles).
+    numpy in -> numpy (h, w) out; CUDA tensor in -> CUDA tensor out."""
+    ctx = ctx or Context.default()
+    w = n if w is None else w
+    h = n if h is None else h
+    m = int(tris.shape[0])
+    if _is_device(tris):
+        import torch
+        out = torch.empty((h, w), dtype=torch.float32, device=tris.device)
+        _check(_lib.cpvs_raster_triangles(ctx.handle, _ptr(tris) if m else None, m, float(plane), n, x0, y0, w, h,
+                                          _ptr(out), IO_DEVICE, _stream(stream)))
+        return out
+    t = np.ascontiguousarray(tris, np.float32)
+    out = np.empty((h, w), np.float32)
+    _check(_lib.cpvs_raster_triangles(ctx.handle, t.ctypes.data if m else None, m, float(plane), n, x0, y0, w, h,
+                                      out.ctypes.data, 0, _stream(stream)))
     return out
 
 

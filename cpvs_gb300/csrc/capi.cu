@@ -478,6 +478,43 @@ cpvs_status cpvs_raster_depth(cpvs_ctx* ctx, const float* boxes, uint32_t num_bo
     return r;
 }
 
+cpvs_status cpvs_raster_triangles(cpvs_ctx* ctx, const float* tris, uint32_t num_tris, float plane, uint32_t n,
+                                  uint32_t x0, uint32_t y0, uint32_t w, uint32_t h, float* depth_out, uint32_t flags,
+                                  void* stream) {
+    if (!ctx || !depth_out || (num_tris && !tris)) return fail(CPVS_ERR_INVALID_ARG, "raster_triangles: null argument");
+    if (!is_pow2(n) || n > 65536 || (uint64_t)x0 + w > n || (uint64_t)y0 + h > n)
+        return fail(CPVS_ERR_INVALID_ARG, "raster_triangles: window must lie inside a power-of-two map of side <= 65536");
+    cpvs_status r = set_device(ctx);
+    if (r != CPVS_OK) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    cpvs::Ctx& c = ctx->c;
+    const uint64_t tb = (uint64_t)num_tris * 9 * 4, ob = (uint64_t)w * h * 4;
+    void* dt = nullptr;
+    bool dt_own = false;
+    r = stage_in(c, tris, tb, flags, st, &dt, &dt_own);
+    float* out = depth_out;
+    bool out_own = false;
+    if (r == CPVS_OK && !(flags & CPVS_IO_DEVICE)) {
+        out = static_cast<float*>(host_accessible(c, depth_out));
+        if (!out) {
+            r = c.alloc((void**)&out, std::max<uint64_t>(ob, 4), false, st);
+            out_own = r == CPVS_OK;
+        }
+    }
+    if (r == CPVS_OK)
+        r = cpvs::launch_raster_triangles(c, static_cast<const float*>(dt), num_tris, plane, n, x0, y0, w, h, out, st);
+    if (r == CPVS_OK && !(flags & CPVS_IO_DEVICE)) {
+        cudaError_t e = out_own ? cudaMemcpyAsync(depth_out, out, ob, cudaMemcpyDeviceToHost, st) : cudaSuccess;
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) r = cpvs::cuda_fail(e, "raster_triangles read-back");
+    } else if (r == CPVS_OK && dt_own) {
+        cudaStreamSynchronize(st);
+    }
+    if (dt_own) c.release(dt, std::max<uint64_t>(tb, 4), false, st);
+    if (out_own) c.release(out, std::max<uint64_t>(ob, 4), false, st);
+    return r;
+}
+
 // ---------------------------------------------------------------- shadow
 cpvs_status cpvs_shadow_create(cpvs_ctx* ctx, const cpvs_hierarchy* h, uint32_t z_tile_index, uint32_t z_tile_num,
                                uint32_t flags, void* stream, cpvs_shadow** out) {

@@ -71,6 +71,11 @@ cpvs_status launch_level_bounds(const float2* levels, uint32_t n, int lmin, cons
 // Depth map of a plane plus boxes (cx,cy,hx,hy,top) and spheres
 // (cx,cy,r,depth), window [x0,x0+w) x [y0,y0+h) of an n x n map (device
 // pointers).
+struct Ctx;
+// Depth map of triangles (9 floats each) over a plane; bins into tiles
+// first (one host synchronisation to size the bins).
+cpvs_status launch_raster_triangles(Ctx& c, const float* tris, uint32_t ntris, float plane, uint32_t n, uint32_t x0,
+                                    uint32_t y0, uint32_t w, uint32_t h, float* out, cudaStream_t st);
 cpvs_status launch_raster(const float* boxes, uint32_t nb, const float* spheres, uint32_t ns, float plane, uint32_t n,
                           uint32_t x0, uint32_t y0, uint32_t w, uint32_t h, float* out, cudaStream_t st,
                           Timing* timing = nullptr);

@@ -153,3 +153,64 @@ def ndc_queries_mixed(depth: np.ndarray, count: int, seed: int) -> np.ndarray:
     out[:half, 2] = vz * scale - 1.0
     out[half:] = (g.random((count - half, 3)) * 2.0 - 1.0).astype(np.float32)
     return out
+
+
+def rasterise_triangles(tris: np.ndarray, n: int, plane: float, x0: int = 0, y0: int = 0, w: int | None = None,
+                        h: int | None = None) -> np.ndarray:
+    """Host rasteriser for (m, 9) float32 triangles (x0,y0,d0, x1,y1,d1,
+    x2,y2,d2 in map coordinates [0,1]) over a plane: the rule of
+    cpvs_raster_triangles (include/cpvs.h) -- pixel centre inside the bounding
+    box, edge functions with the sign of the area, depth
+    ((e0 d0 + e1 d1) + e2 d2) / area -- in float32, round to nearest, in that
+    operation order; each pixel keeps the minimum (NaN propagates)."""
+    w = n if w is None else w
+    h = n if h is None else h
+    f = np.float32
+    cx_all = pixel_centres(n)
+    xs, ys = cx_all[x0:x0 + w], cx_all[y0:y0 + h]
+    depth = np.full((h, w), f(plane), f)
+    tris = np.asarray(tris, f).reshape(-1, 9)
+    with np.errstate(invalid="ignore", divide="ignore", over="ignore"):
+        for t in tris:
+            X0, Y0, D0, X1, Y1, D1, X2, Y2, D2 = (f(v) for v in t)
+            if np.isnan([X0, Y0, X1, Y1, X2, Y2]).any():
+                continue
+            minx, maxx = min(X0, X1, X2), max(X0, X1, X2)
+            miny, maxy = min(Y0, Y1, Y2), max(Y0, Y1, Y2)
+            ax = np.searchsorted(xs, minx, "left")
+            bx = np.searchsorted(xs, maxx, "right")
+            ay = np.searchsorted(ys, miny, "left")
+            by = np.searchsorted(ys, maxy, "right")
+            if ax >= bx or ay >= by:
+                continue
+            px = xs[ax:bx][None, :]
+            py = ys[ay:by][:, None]
+            e0 = (f(X2 - X1) * (py - Y1)) - (f(Y2 - Y1) * (px - X1))
+            e1 = (f(X0 - X2) * (py - Y2)) - (f(Y0 - Y2) * (px - X2))
+            e2 = (f(X1 - X0) * (py - Y0)) - (f(Y1 - Y0) * (px - X0))
+            area = (e0 + e1) + e2
+            inside = ((area > 0) & (e0 >= 0) & (e1 >= 0) & (e2 >= 0)) | \
+                     ((area < 0) & (e0 <= 0) & (e1 <= 0) & (e2 <= 0))
+            v = (((e0 * D0) + (e1 * D1)) + (e2 * D2)) / area
+            sub = depth[ay:by, ax:bx]
+            np.minimum(sub, np.where(inside, v, sub).astype(f), out=sub)
+    return depth
+
+
+def terrain_triangles(cells: int, seed: int, lo: float = 0.3, hi: float = 0.8) -> np.ndarray:
+    """A height-field mesh: a cells x cells grid of quads over [0,1]^2, each
+    split into two triangles sharing an edge, vertex depths uniform in
+    [lo, hi) (seeded); (2 cells^2, 9) float32."""
+    g = np.random.Generator(np.random.PCG64(seed))
+    hgt = (lo + (hi - lo) * g.random((cells + 1, cells + 1))).astype(np.float32)
+    c = np.linspace(0.0, 1.0, cells + 1, dtype=np.float32)
+    out = []
+    for j in range(cells):
+        for i in range(cells):
+            a = (c[i], c[j], hgt[j, i])
+            b = (c[i + 1], c[j], hgt[j, i + 1])
+            d = (c[i], c[j + 1], hgt[j + 1, i])
+            e = (c[i + 1], c[j + 1], hgt[j + 1, i + 1])
+            out.append((*a, *b, *e))
+            out.append((*a, *e, *d))
+    return np.asarray(out, np.float32)

@@ -144,6 +144,23 @@ CPVS_API cpvs_status cpvs_raster_depth(cpvs_ctx* ctx, const float* boxes, uint32
                                        uint32_t num_spheres, float plane, uint32_t n, uint32_t x0, uint32_t y0,
                                        uint32_t w, uint32_t h, float* depth_out, uint32_t flags, void* stream);
 
+/* Rasterises triangles over a ground plane at depth `plane` into the window
+ * [x0,x0+w) x [y0,y0+h) of an n x n depth map (the reference renders meshes
+ * into its shadow map under the light, src/DeferredRenderer.cpp:110-148,
+ * shader/create_sm.vert:10-17).  `tris` holds num_tris x 9 floats
+ * (x0,y0,d0, x1,y1,d1, x2,y2,d2): vertex positions in map coordinates [0,1]
+ * and their depths.  A triangle covers pixel centre p = ((x+0.5)/n, (y+0.5)/n)
+ * when p lies in its bounding box and the edge functions
+ * e0 = (x2-x1)(py-y1) - (y2-y1)(px-x1), e1 = (x0-x2)(py-y2) - (y0-y2)(px-x2),
+ * e2 = (x1-x0)(py-y0) - (y1-y0)(px-x0) all have the sign of
+ * area = (e0+e1)+e2 != 0 (zero included, either winding); its depth there is
+ * ((e0 d0 + e1 d1) + e2 d2) / area -- float32, round to nearest, no
+ * contraction, in that order -- and each pixel keeps the minimum (NaN
+ * propagates).  Buffers are host memory unless flags has CPVS_IO_DEVICE. */
+CPVS_API cpvs_status cpvs_raster_triangles(cpvs_ctx* ctx, const float* tris, uint32_t num_tris, float plane,
+                                           uint32_t n, uint32_t x0, uint32_t y0, uint32_t w, uint32_t h,
+                                           float* depth_out, uint32_t flags, void* stream);
+
 /* ---- compressed shadow (one DAG) ------------------------------------- */
 
 /* Builds the DAG of z-tile `z_tile_index` of `z_tile_num` from a hierarchy.
