@@ -203,7 +203,7 @@ cpvs_status build_into_shadows(cpvs_ctx* ctx, const std::vector<cpvs::SourceSpec
 void ensure_top(const cpvs_shadow* cs, cudaStream_t st) {
     cpvs_shadow* s = const_cast<cpvs_shadow*>(cs);
     if (s->top || s->top_bytes == ~0ull) return;
-    const int depth = cpvs::top_index_depth(s->num_levels, s->leafmasks);
+    const int depth = cpvs::top_index_depth(s->num_levels, s->leafmasks, s->words);
     if (depth <= 0 || s->ctx->c.alloc((void**)&s->top, uint64_t(4) << (3 * depth), true, st) != CPVS_OK ||
         cpvs::launch_top_index(s->dag, s->words, s->num_levels, s->leafmasks, s->top, st) != CPVS_OK) {
         if (s->top) s->ctx->c.release(s->top, uint64_t(4) << (3 * depth), true, st);

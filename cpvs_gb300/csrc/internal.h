@@ -17,7 +17,7 @@ namespace cpvs {
 // known to lie inside the DAG.
 constexpr uint64_t kDagPad = 16;
 // Levels below the root replaced by the dense top index in lookups.
-constexpr int kTopIndexDepth = 4;
+constexpr int kTopIndexDepth = 7;  // levels below the root resolved by the lookup's top grid, at most
 }  // namespace cpvs
 
 namespace cpvs {
@@ -107,7 +107,7 @@ void destroy_plans(Ctx& ctx);
 
 // -------------------------------------------------------------- lookup
 // Depth of the top index of a DAG (0: none) and its build: 8^depth words.
-int top_index_depth(uint32_t num_levels, bool leafmasks);
+int top_index_depth(uint32_t num_levels, bool leafmasks, uint64_t words);
 cpvs_status launch_top_index(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks,
                              uint32_t* out, cudaStream_t st);
 // `top` may be null (no top index).

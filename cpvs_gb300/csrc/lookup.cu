@@ -12,11 +12,14 @@
 // 9.4 MB), so every hop is kept short -- 32-bit offsets, one bounds check
 // per node (DAG buffers carry a zeroed tail of kDagPad words, so both reads
 // of a node stay inside the buffer once its offset is), and the child's
-// 2-bit class and rank from one shift and one popcount.  The first levels
-// below the root are replaced by a dense "top index" (8^depth words: the
-// node offset reached after `depth` hops, or a lit/shadow sentinel) staged
-// in shared memory by every CTA -- and each thread carries Q independent
-// queries (Q picked per DAG depth by timing Q = 1, 2, 4 on the first batch).
+// 2-bit class and rank from one shift and one popcount.  The first `depth`
+// levels below the root are replaced by a dense 3-D "top grid" of
+// (2^depth)^3 words, indexed by the top `depth` bits of the quantised x, y,
+// z: the node offset the descent reaches after those levels, or a lit /
+// shadow sentinel.  It lives in global memory (L2-resident; up to 7 levels,
+// never larger than the DAG), so one load replaces up to 7 dependent hops --
+// and each thread carries Q independent queries (Q picked per DAG depth by
+// timing Q = 1, 2, 4 on the first batch).
 #include "common.cuh"
 
 namespace cpvs {
@@ -64,16 +67,26 @@ __device__ __forceinline__ bool descend(const uint32_t* __restrict__ dag, uint32
     return (w >> (b & 31u)) & 1u;
 }
 
-// Top index: entry for the `depth` child indices taken below the root
-// (most significant first) = the node offset reached, or a sentinel when the
-// descent ended in a lit or shadowed child on the way.
+// Top grid: cell (cx, cy, cz) at index (cz << 2 depth) | (cy << depth) | cx
+// holds the node offset the descent reaches after the `depth` levels below
+// the root whose child bits are those of cx, cy, cz (most significant
+// first), or a sentinel when it ended in a lit or shadowed child on the way.
+__device__ __forceinline__ uint32_t top_cell(int32_t px, int32_t py, int32_t pz, int shift, int depth) {
+    const uint32_t m = (1u << depth) - 1u;
+    return ((((uint32_t)pz >> shift) & m) << (2 * depth)) | ((((uint32_t)py >> shift) & m) << depth) |
+           (((uint32_t)px >> shift) & m);
+}
+
 __global__ void k_top_index(const uint32_t* __restrict__ dag, uint32_t words, int depth, uint32_t* __restrict__ out) {
     const uint32_t cells = 1u << (3 * depth);
+    const uint32_t m = (1u << depth) - 1u;
     for (uint32_t cell = blockIdx.x * blockDim.x + threadIdx.x; cell < cells; cell += gridDim.x * blockDim.x) {
+        const uint32_t cx = cell & m, cy = (cell >> depth) & m, cz = cell >> (2 * depth);
         uint32_t off = 0, entry = 0;
         bool done = false;
         for (int d = 0; d < depth; ++d) {
-            const uint32_t c = (cell >> (3 * (depth - 1 - d))) & 7u;
+            const int b = depth - 1 - d;
+            const uint32_t c = ((cx >> b) & 1u) | (((cy >> b) & 1u) << 1) | (((cz >> b) & 1u) << 2);
             if (off >= words) {
                 entry = kCellShadow;
                 done = true;
@@ -102,12 +115,9 @@ __global__ void __launch_bounds__(kThreads)
     k_lookup(const uint32_t* __restrict__ dag, uint32_t words, int num_levels, bool leafmasks,
              const uint32_t* __restrict__ top, int depth, const void* __restrict__ q, uint64_t n,
              uint32_t* __restrict__ bits) {
-    extern __shared__ uint32_t s_top[];
-    const uint32_t cells = depth > 0 ? (1u << (3 * depth)) : 0u;
-    for (uint32_t i = threadIdx.x; i < cells; i += blockDim.x) s_top[i] = __ldg(top + i);
-    __syncthreads();
     const int lane = threadIdx.x & 31;
     const int root = num_levels - 2, min_level = leafmasks ? 3 : 0;
+    const int shift = root - depth + 1;  // the top grid takes bits root .. shift of each coordinate
     const uint64_t nwords = (n + 31) / 32;
     const uint64_t ngroups = (nwords + Q - 1) / Q;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -134,9 +144,7 @@ __global__ void __launch_bounds__(kThreads)
                 int level = root;
                 bool done = false;
                 if (depth > 0) {
-                    uint32_t cell = 0;
-                    for (int d = 0; d < depth; ++d) cell = (cell << 3) | (child2(px, py, pz, root - d) >> 1);
-                    const uint32_t e = s_top[cell];
+                    const uint32_t e = __ldg(top + top_cell(px, py, pz, shift, depth));
                     if (e >= kCellLit) {
                         lit = (e == kCellLit);
                         done = true;
@@ -183,9 +191,7 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
             for (int k = 0; k < Q; ++k) {
                 if (done[k]) continue;
-                uint32_t cell = 0;
-                for (int d = 0; d < depth; ++d) cell = (cell << 3) | (child2(px[k], py[k], pz[k], root - d) >> 1);
-                const uint32_t e = s_top[cell];
+                const uint32_t e = __ldg(top + top_cell(px[k], py[k], pz[k], shift, depth));
                 if (e >= kCellLit) {
                     lit[k] = (e == kCellLit);
                     done[k] = true;
@@ -452,15 +458,19 @@ int device_sms() {
 
 }  // namespace
 
-int top_index_depth(uint32_t num_levels, bool leafmasks) {
+int top_index_depth(uint32_t num_levels, bool leafmasks, uint64_t words) {
     const int root = (int)num_levels - 2, min_level = leafmasks ? 3 : 0;
-    const int d = root - min_level + 1;
-    return d < 0 ? 0 : (d > kTopIndexDepth ? kTopIndexDepth : d);
+    int d = root - min_level + 1;
+    if (d > kTopIndexDepth) d = kTopIndexDepth;
+    // no larger than the DAG itself (at least 64 KiB)
+    const uint64_t limit = words * 4 > 65536 ? words * 4 : 65536;
+    while (d > 0 && (uint64_t(4) << (3 * d)) > limit) --d;
+    return d < 0 ? 0 : d;
 }
 
 cpvs_status launch_top_index(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks,
                              uint32_t* out, cudaStream_t st) {
-    const int depth = top_index_depth(num_levels, leafmasks);
+    const int depth = top_index_depth(num_levels, leafmasks, words);
     if (depth == 0) return CPVS_OK;
     const uint32_t cells = 1u << (3 * depth);
     k_top_index<<<(cells + 255) / 256, 256, 0, st>>>(dag, (uint32_t)words, depth, out);
@@ -469,11 +479,10 @@ cpvs_status launch_top_index(const uint32_t* dag, uint64_t words, uint32_t num_l
 }
 
 template <bool NDC, int Q>
-void launch_lookup_q(uint32_t g, size_t smem, cudaStream_t st, const uint32_t* dag, uint64_t words,
-                     uint32_t num_levels, bool leafmasks, const uint32_t* top, int depth, const void* xyz, uint64_t n,
-                     uint32_t* bits) {
-    k_lookup<NDC, Q><<<g, kThreads, smem, st>>>(dag, (uint32_t)words, (int)num_levels, leafmasks, top, depth, xyz, n,
-                                                bits);
+void launch_lookup_q(uint32_t g, cudaStream_t st, const uint32_t* dag, uint64_t words, uint32_t num_levels,
+                     bool leafmasks, const uint32_t* top, int depth, const void* xyz, uint64_t n, uint32_t* bits) {
+    k_lookup<NDC, Q><<<g, kThreads, 0, st>>>(dag, (uint32_t)words, (int)num_levels, leafmasks, top, depth, xyz, n,
+                                             bits);
 }
 
 cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks,
@@ -483,16 +492,15 @@ cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_leve
     KernelTimer kt(timing, K_LOOKUP, st);
     const int Q = (queries_per_thread == 1 || queries_per_thread == 2) ? queries_per_thread : 4;
     const uint32_t g = lookup_grid(device_sms(), (n + Q - 1) / Q);
-    const int depth = top ? top_index_depth(num_levels, leafmasks) : 0;
-    const size_t smem = depth ? (size_t(4) << (3 * depth)) : 0;
+    const int depth = top ? top_index_depth(num_levels, leafmasks, words) : 0;
     if (ndc) {
-        if (Q == 1) launch_lookup_q<true, 1>(g, smem, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
-        else if (Q == 2) launch_lookup_q<true, 2>(g, smem, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
-        else launch_lookup_q<true, 4>(g, smem, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
+        if (Q == 1) launch_lookup_q<true, 1>(g, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
+        else if (Q == 2) launch_lookup_q<true, 2>(g, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
+        else launch_lookup_q<true, 4>(g, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
     } else {
-        if (Q == 1) launch_lookup_q<false, 1>(g, smem, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
-        else if (Q == 2) launch_lookup_q<false, 2>(g, smem, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
-        else launch_lookup_q<false, 4>(g, smem, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
+        if (Q == 1) launch_lookup_q<false, 1>(g, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
+        else if (Q == 2) launch_lookup_q<false, 2>(g, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
+        else launch_lookup_q<false, 4>(g, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
     }
     CPVS_CUDA(cudaGetLastError());
     return CPVS_OK;
