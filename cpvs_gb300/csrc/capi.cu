@@ -727,6 +727,10 @@ cpvs_status cpvs_grid_create(cpvs_ctx* ctx, uint32_t length, cpvs_grid** out) {
 
 static void grid_release_device(cpvs_grid* g) {
     cpvs::Ctx& c = g->ctx->c;
+    if (g->gtop) c.release(g->gtop, g->gtop_bytes, true, nullptr, g->last_use);
+    g->gtop = nullptr;
+    g->gtop_bytes = 0;
+    g->gtop_depth = 0;
     block_unref(g->block, g->last_use);
     if (g->cell_words) c.release(g->cell_words, g->cells.size() * 4, true, nullptr, g->last_use);
     g->block = nullptr;
@@ -910,14 +914,34 @@ cpvs_status cpvs_grid_words(const cpvs_grid* g, uint32_t* dag_out, uint64_t dag_
     return CPVS_OK;
 }
 
+// The grid's top index, built on its first lookup (stream-ordered).
+static void ensure_grid_top(const cpvs_grid* cg, cudaStream_t st) {
+    cpvs_grid* g = const_cast<cpvs_grid*>(cg);
+    if (g->gtop || g->gtop_bytes == ~0ull) return;
+    const int depth = cpvs::grid_top_depth(g->length, g->dag_levels, g->leafmasks, g->words);
+    const uint64_t bytes = uint64_t(4) << (3 * (cpvs::log2_u32(g->length) + depth));
+    if (depth <= 0 || g->ctx->c.alloc((void**)&g->gtop, bytes, true, st) != CPVS_OK ||
+        cpvs::launch_grid_top_index(g->dag, g->words, g->cell_words, g->length, g->dag_levels, depth, g->gtop, st) !=
+            CPVS_OK) {
+        if (g->gtop) g->ctx->c.release(g->gtop, bytes, true, st);
+        g->gtop = nullptr;
+        g->gtop_bytes = ~0ull;  // look up without it
+        cudaGetLastError();
+        return;
+    }
+    g->gtop_bytes = bytes;
+    g->gtop_depth = depth;
+}
+
 cpvs_status cpvs_grid_lookup_ndc(const cpvs_grid* g, const float* xyz, uint64_t n, uint32_t* bits_out, uint32_t flags,
                                  void* stream) {
     if (!g || !g->finalized) return fail(CPVS_ERR_INVALID_ARG, "grid_lookup_ndc: grid not finalized");
     cudaStream_t st = (cudaStream_t)stream;
     return lookup_common(g->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
+        ensure_grid_top(g, st);
         cpvs_status r = cpvs::launch_grid_lookup(g->dag, g->words, g->cell_words, g->length, g->dag_levels,
-                                                 g->leafmasks, static_cast<const float*>(q), n, bits, st,
-                                                 &g->ctx->c.timing);
+                                                 g->leafmasks, g->gtop, g->gtop_depth, static_cast<const float*>(q), n,
+                                                 bits, st, &g->ctx->c.timing);
         g->touch(st);
         return r;
     });
@@ -947,10 +971,11 @@ cpvs_status cpvs_grid_evaluate(const cpvs_grid* g, const float* positions, uint3
     const uint64_t obytes = u8 ? n : (n + 31) / 32 * 4;
     return io_common(g->ctx, positions, n * floats_per_pixel * 4, out, obytes, flags, st,
                      [&](const void* q, void* o) {
+                         ensure_grid_top(g, st);
                          cpvs_status r = cpvs::launch_grid_evaluate(
-                             g->dag, g->words, g->cell_words, g->length, g->dag_levels, g->leafmasks,
-                             static_cast<const float*>(q), floats_per_pixel, n, light_view_proj, g->filter_size, u8, o,
-                             st, &g->ctx->c.timing);
+                             g->dag, g->words, g->cell_words, g->length, g->dag_levels, g->leafmasks, g->gtop,
+                             g->gtop_depth, static_cast<const float*>(q), floats_per_pixel, n, light_view_proj,
+                             g->filter_size, u8, o, st, &g->ctx->c.timing);
                          g->touch(st);
                          return r;
                      });

@@ -144,13 +144,18 @@ cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_leve
 // World-space evaluation over a grid: n pixels of `fpp` floats (xyz first),
 // column-major 4x4 light view-projection, PCF footprint `filter`; output one
 // byte per pixel (u8) or one bit per pixel.
+// Grid top index: depth (levels of every cell DAG it resolves; 0: none) and
+// build into (length * 2^depth)^3 words.
+int grid_top_depth(uint32_t length, uint32_t dag_levels, bool leafmasks, uint64_t words);
+cpvs_status launch_grid_top_index(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
+                                  uint32_t dag_levels, int depth, uint32_t* out, cudaStream_t st);
 cpvs_status launch_grid_evaluate(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
-                                 uint32_t dag_levels, bool leafmasks, const float* positions, uint32_t fpp, uint64_t n,
-                                 const float* light_view_proj, uint32_t filter, bool u8, void* out, cudaStream_t st,
-                                 Timing* timing = nullptr);
+                                 uint32_t dag_levels, bool leafmasks, const uint32_t* gtop, int gdepth,
+                                 const float* positions, uint32_t fpp, uint64_t n, const float* light_view_proj,
+                                 uint32_t filter, bool u8, void* out, cudaStream_t st, Timing* timing = nullptr);
 cpvs_status launch_grid_lookup(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
-                               uint32_t dag_levels, bool leafmasks, const float* xyz, uint64_t n, uint32_t* bits,
-                               cudaStream_t st, Timing* timing = nullptr);
+                               uint32_t dag_levels, bool leafmasks, const uint32_t* gtop, int gdepth, const float* xyz,
+                               uint64_t n, uint32_t* bits, cudaStream_t st, Timing* timing = nullptr);
 
 // ------------------------------------------------------------ timing
 // Kernels timed (when a context's timing is on) with a CUDA event pair on

@@ -20,6 +20,8 @@
 // never larger than the DAG), so one load replaces up to 7 dependent hops --
 // and each thread carries Q independent queries (Q picked per DAG depth by
 // timing Q = 1, 2, 4 on the first batch).
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace cpvs {
@@ -267,15 +269,91 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// One grid sample at an integer path (shader/traverse.cs:75-88 routing):
+// outside the grid answers lit, a uniform cell its class, else the descent
+// of the cell's DAG with pointers relative to its first word.
+// With a grid top index (`gtop`, depth `gdepth` levels of every cell DAG;
+// see k_grid_top_index) the first levels are one load.
+struct GridTop {
+    const uint32_t* top;  // null: none
+    int depth;            // levels of each cell DAG it resolves
+    int bits;             // log2(length) + depth: index bits per axis
+};
+
+__device__ __forceinline__ bool grid_sample(const uint32_t* __restrict__ dag, uint32_t words,
+                                            const uint32_t* __restrict__ cells, uint32_t length, int dag_levels,
+                                            bool leafmasks, GridTop gt, int64_t px, int64_t py, int64_t pz) {
+    const int sh = dag_levels - 1;
+    const int64_t lim = (int64_t)length << sh;
+    if (px < 0 || py < 0 || pz < 0 || px >= lim || py >= lim || pz >= lim) return true;
+    const uint32_t cell = __ldg(cells + ((size_t)(pz >> sh) * length + (size_t)(py >> sh)) * length + (size_t)(px >> sh));
+    int level = dag_levels - 2;
+    uint32_t off = cell;
+    if (gt.top) {
+        const int s = sh - gt.depth;
+        const uint32_t e = __ldg(gt.top + ((((uint64_t)pz >> s) << (2 * gt.bits)) | (((uint64_t)py >> s) << gt.bits) |
+                                           ((uint64_t)px >> s)));
+        if (e >= kCellLit) return e == kCellLit;  // uniform cell, or the descent ended in the top levels
+        off = e;
+        level -= gt.depth;
+    } else {
+        if (cell == kCellShadow) return false;
+        if (cell == kCellLit) return true;
+    }
+    return descend(dag, words, cell, off, level, leafmasks ? 3 : 0, leafmasks, (int32_t)px, (int32_t)py, (int32_t)pz);
+}
+
+// Grid top index: entry (gx, gy, gz) at index (gz << 2 bits) | (gy << bits) | gx,
+// bits = log2(length) + depth, is the absolute DAG offset of the node that
+// the cell's descent reaches after `depth` levels, or a lit / shadow sentinel
+// (a uniform cell, or a lit / shadowed child on the way).
+__global__ void k_grid_top_index(const uint32_t* __restrict__ dag, uint32_t words,
+                                 const uint32_t* __restrict__ cells, uint32_t length, int dag_levels, int depth,
+                                 int bits, uint32_t* __restrict__ out) {
+    const uint64_t total = 1ull << (3 * bits);
+    const uint32_t m = (1u << bits) - 1u;
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t gx = (uint32_t)t & m, gy = (uint32_t)(t >> bits) & m, gz = (uint32_t)(t >> (2 * bits));
+        const uint32_t cell = cells[((size_t)(gz >> depth) * length + (gy >> depth)) * length + (gx >> depth)];
+        uint32_t entry;
+        if (cell >= kCellLit) {
+            entry = cell;
+        } else {
+            uint32_t off = cell;
+            entry = 0;
+            bool done = false;
+            for (int d = 0; d < depth; ++d) {
+                const int b = depth - 1 - d;
+                const uint32_t c = ((gx >> b) & 1u) | (((gy >> b) & 1u) << 1) | (((gz >> b) & 1u) << 2);
+                if (off >= words) {
+                    entry = kCellShadow;
+                    done = true;
+                    break;
+                }
+                const uint32_t mk = dag[off];
+                const uint32_t v = (mk >> (2u * c)) & 3u;
+                if (v != kPartial) {
+                    entry = (v == kVisible) ? kCellLit : kCellShadow;
+                    done = true;
+                    break;
+                }
+                off = cell + dag[off + 1u + __popc(mk & 0xAAAAu & ((1u << (2u * c)) - 1u))];
+            }
+            if (!done) entry = off;
+        }
+        out[t] = entry;
+    }
+}
+
 // Grid routing (shader/traverse.cs:75-88): the path at resolution
 // 2^(dag_levels+grid_levels-1), its top bits select the cell, the cell word
-// holds the DAG offset or a uniform-cell sentinel.
+// holds the DAG offset or a uniform-cell sentinel; then the cell's descent
+// (grid_sample, with the grid top index when there is one).
 __global__ void __launch_bounds__(kThreads)
     k_grid_lookup(const uint32_t* __restrict__ dag, uint32_t words, const uint32_t* __restrict__ cells,
-                  uint32_t length, int dag_levels, int grid_levels, bool leafmasks, const float* __restrict__ q,
-                  uint64_t n, uint32_t* __restrict__ bits) {
+                  uint32_t length, int dag_levels, int grid_levels, bool leafmasks, GridTop gt,
+                  const float* __restrict__ q, uint64_t n, uint32_t* __restrict__ bits) {
     const int lane = threadIdx.x & 31;
-    const int root = dag_levels - 2, min_level = leafmasks ? 3 : 0;
     const uint64_t nwords = (n + 31) / 32;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const float scale = (float)((1u << (dag_levels + grid_levels - 1)) - 1u);
@@ -285,38 +363,11 @@ __global__ void __launch_bounds__(kThreads)
         if (i < n) {
             const float* p = q + 3 * i;
             const int32_t px = quantise(p[0], scale), py = quantise(p[1], scale), pz = quantise(p[2], scale);
-            const int32_t gx = px >> (dag_levels - 1), gy = py >> (dag_levels - 1), gz = pz >> (dag_levels - 1);
-            if (gx < 0 || gy < 0 || gz < 0 || gx >= (int32_t)length || gy >= (int32_t)length || gz >= (int32_t)length) {
-                lit = true;
-            } else {
-                const uint32_t cell = __ldg(cells + ((size_t)gz * length + gy) * length + gx);
-                if (cell == kCellShadow)
-                    lit = false;
-                else if (cell == kCellLit)
-                    lit = true;
-                else
-                    lit = descend(dag, words, cell, cell, root, min_level, leafmasks, px, py, pz);
-            }
+            lit = grid_sample(dag, words, cells, length, dag_levels, leafmasks, gt, px, py, pz);
         }
         const uint32_t word = __ballot_sync(0xffffffffu, lit);
         if (lane == 0) bits[w] = word;
     }
-}
-
-// One grid sample at an integer path (shader/traverse.cs:75-88 routing):
-// outside the grid answers lit, a uniform cell its class, else the descent
-// of the cell's DAG with pointers relative to its first word.
-__device__ __forceinline__ bool grid_sample(const uint32_t* __restrict__ dag, uint32_t words,
-                                            const uint32_t* __restrict__ cells, uint32_t length, int dag_levels,
-                                            bool leafmasks, int64_t px, int64_t py, int64_t pz) {
-    const int sh = dag_levels - 1;
-    const int64_t lim = (int64_t)length << sh;
-    if (px < 0 || py < 0 || pz < 0 || px >= lim || py >= lim || pz >= lim) return true;
-    const uint32_t cell = __ldg(cells + ((size_t)(pz >> sh) * length + (size_t)(py >> sh)) * length + (size_t)(px >> sh));
-    if (cell == kCellShadow) return false;
-    if (cell == kCellLit) return true;
-    return descend(dag, words, cell, cell, dag_levels - 2, leafmasks ? 3 : 0, leafmasks, (int32_t)px, (int32_t)py,
-                   (int32_t)pz);
 }
 
 // World-space evaluation (src/CompressedShadowContainer.cpp:93-124,
@@ -337,8 +388,9 @@ struct EvalMatrix {
 template <bool U8>
 __global__ void __launch_bounds__(kThreads)
     k_grid_evaluate(const uint32_t* __restrict__ dag, uint32_t words, const uint32_t* __restrict__ cells,
-                    uint32_t length, int dag_levels, int grid_levels, bool leafmasks, const float* __restrict__ pos,
-                    uint32_t fpp, uint64_t n, EvalMatrix M, int filter, void* __restrict__ out) {
+                    uint32_t length, int dag_levels, int grid_levels, bool leafmasks, GridTop gt,
+                    const float* __restrict__ pos, uint32_t fpp, uint64_t n, EvalMatrix M, int filter,
+                    void* __restrict__ out) {
     const int lane = threadIdx.x & 31;
     const uint64_t nwords = (n + 31) / 32;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
@@ -362,13 +414,14 @@ __global__ void __launch_bounds__(kThreads)
             const int64_t py = quantise(__fdiv_rn(c[1], c[3]), scale);
             const int64_t pz = quantise(__fdiv_rn(c[2], c[3]), scale);
             if (filter <= 1) {
-                lit = grid_sample(dag, words, cells, length, dag_levels, leafmasks, px, py, pz);
+                lit = grid_sample(dag, words, cells, length, dag_levels, leafmasks, gt, px, py, pz);
                 cnt = lit ? 1u : 0u;
             } else {
                 for (int dy = lo; dy <= hi; ++dy)
                     for (int dx = lo; dx <= hi; ++dx)
-                        cnt += grid_sample(dag, words, cells, length, dag_levels, leafmasks, px + dx, py + dy, pz) ? 1u
-                                                                                                                 : 0u;
+                        cnt += grid_sample(dag, words, cells, length, dag_levels, leafmasks, gt, px + dx, py + dy, pz)
+                                   ? 1u
+                                   : 0u;
             }
         }
         if (U8) {
@@ -555,10 +608,33 @@ cpvs_status launch_segment_lookup(const MultiDag* dags, uint32_t ndags, const Lo
     return CPVS_OK;
 }
 
+int grid_top_depth(uint32_t length, uint32_t dag_levels, bool leafmasks, uint64_t words) {
+    const int root = (int)dag_levels - 2, min_level = leafmasks ? 3 : 0;
+    const int gl = log2_u32(length);
+    int d = root - min_level + 1;
+    if (d > kTopIndexDepth) d = kTopIndexDepth;
+    // no larger than the combined DAG (at least 64 KiB, at most 64 MiB)
+    uint64_t limit = words * 4 > 65536 ? words * 4 : 65536;
+    if (limit > (64ull << 20)) limit = 64ull << 20;
+    while (d > 0 && (uint64_t(4) << (3 * (gl + d))) > limit) --d;
+    return d < 0 ? 0 : d;
+}
+
+cpvs_status launch_grid_top_index(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
+                                  uint32_t dag_levels, int depth, uint32_t* out, cudaStream_t st) {
+    const int bits = log2_u32(length) + depth;
+    const uint64_t total = 1ull << (3 * bits);
+    const uint32_t g = (uint32_t)std::min<uint64_t>((total + 255) / 256, 152ull * 32);
+    k_grid_top_index<<<g, 256, 0, st>>>(dag, (uint32_t)words, cells, length, (int)dag_levels, depth, bits, out);
+    CPVS_CUDA(cudaGetLastError());
+    return CPVS_OK;
+}
+
 cpvs_status launch_grid_evaluate(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
-                                 uint32_t dag_levels, bool leafmasks, const float* positions, uint32_t fpp, uint64_t n,
-                                 const float* light_view_proj, uint32_t filter, bool u8, void* out, cudaStream_t st,
-                                 Timing* timing) {
+                                 uint32_t dag_levels, bool leafmasks, const uint32_t* gtop, int gdepth,
+                                 const float* positions, uint32_t fpp, uint64_t n, const float* light_view_proj,
+                                 uint32_t filter, bool u8, void* out, cudaStream_t st, Timing* timing) {
+    const GridTop gt{gtop, gtop ? gdepth : 0, (int)log2_u32(length) + (gtop ? gdepth : 0)};
     if (n == 0) return CPVS_OK;
     KernelTimer kt(timing, K_EVALUATE, st);
     EvalMatrix M;
@@ -566,24 +642,25 @@ cpvs_status launch_grid_evaluate(const uint32_t* dag, uint64_t words, const uint
     const uint32_t g = lookup_grid(device_sms(), n);
     if (u8)
         k_grid_evaluate<true><<<g, kThreads, 0, st>>>(dag, (uint32_t)words, cells, length, (int)dag_levels,
-                                                      log2_u32(length), leafmasks, positions, fpp, n, M, (int)filter,
-                                                      out);
+                                                      log2_u32(length), leafmasks, gt, positions, fpp, n, M,
+                                                      (int)filter, out);
     else
         k_grid_evaluate<false><<<g, kThreads, 0, st>>>(dag, (uint32_t)words, cells, length, (int)dag_levels,
-                                                       log2_u32(length), leafmasks, positions, fpp, n, M, (int)filter,
-                                                       out);
+                                                       log2_u32(length), leafmasks, gt, positions, fpp, n, M,
+                                                       (int)filter, out);
     CPVS_CUDA(cudaGetLastError());
     return CPVS_OK;
 }
 
 cpvs_status launch_grid_lookup(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
-                               uint32_t dag_levels, bool leafmasks, const float* xyz, uint64_t n, uint32_t* bits,
-                               cudaStream_t st, Timing* timing) {
+                               uint32_t dag_levels, bool leafmasks, const uint32_t* gtop, int gdepth, const float* xyz,
+                               uint64_t n, uint32_t* bits, cudaStream_t st, Timing* timing) {
     if (n == 0) return CPVS_OK;
     KernelTimer kt(timing, K_GRID_LOOKUP, st);
+    const GridTop gt{gtop, gtop ? gdepth : 0, (int)log2_u32(length) + (gtop ? gdepth : 0)};
     const uint32_t g = lookup_grid(device_sms(), n);
     k_grid_lookup<<<g, kThreads, 0, st>>>(dag, (uint32_t)words, cells, length, (int)dag_levels, log2_u32(length),
-                                          leafmasks, xyz, n, bits);
+                                          leafmasks, gt, xyz, n, bits);
     CPVS_CUDA(cudaGetLastError());
     return CPVS_OK;
 }

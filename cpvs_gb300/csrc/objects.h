@@ -76,6 +76,9 @@ struct cpvs_grid : DeviceObject {
     bool leafmasks = false;
     bool finalized = false;
     uint32_t filter_size = 1;  // PCF footprint of evaluate
+    uint32_t* gtop = nullptr;  // grid top index, built on the first lookup
+    uint64_t gtop_bytes = 0;   // ~0: none (too small, or its allocation failed)
+    int gtop_depth = 0;
 };
 
 
