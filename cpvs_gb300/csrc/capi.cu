@@ -215,6 +215,19 @@ void ensure_top(const cpvs_shadow* cs, cudaStream_t st) {
     s->top_bytes = uint64_t(4) << (3 * depth);
 }
 
+}  // namespace
+
+namespace cpvs {
+void shadow_ensure_top(const cpvs_shadow* s, cudaStream_t st) { ensure_top(s, st); }
+
+MultiDag shadow_table_entry(const cpvs_shadow* s) {
+    return MultiDag{s->dag, (uint32_t)s->words, s->num_levels, s->leafmasks ? 1u : 0u,
+                    s->top ? (uint32_t)top_index_depth(s->num_levels, s->leafmasks, s->words) : 0u, s->top};
+}
+}  // namespace cpvs
+
+namespace {
+
 // Queries per thread for a lookup on `s`: the context's fixed choice, or the
 // tuned one for this DAG depth (tuned on the first batch that needs it).
 int lookup_qpt(const cpvs_shadow* s, const void* q, bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st) {
@@ -683,15 +696,17 @@ cpvs_status cpvs_lookup_ndc_multi(const cpvs_shadow* const* shadows, uint32_t nu
     if (!shadows || num_shadows == 0) return fail(CPVS_ERR_INVALID_ARG, "lookup_multi: no shadows");
     if (n && !dag_index) return fail(CPVS_ERR_INVALID_ARG, "lookup_multi: null dag_index");
     cpvs_ctx* ctx = shadows[0] ? shadows[0]->ctx : nullptr;
-    std::vector<cpvs::MultiDag> table(num_shadows);
-    for (uint32_t i = 0; i < num_shadows; ++i) {
-        const cpvs_shadow* sh = shadows[i];
-        if (!sh || sh->ctx != ctx) return fail(CPVS_ERR_INVALID_ARG, "lookup_multi: shadows must share one context");
-        table[i] = cpvs::MultiDag{sh->dag, (uint32_t)sh->words, sh->num_levels, sh->leafmasks ? 1u : 0u, 0u};
-    }
+    for (uint32_t i = 0; i < num_shadows; ++i)
+        if (!shadows[i] || shadows[i]->ctx != ctx)
+            return fail(CPVS_ERR_INVALID_ARG, "lookup_multi: shadows must share one context");
     cudaStream_t st = (cudaStream_t)stream;
     cpvs_status r = set_device(ctx);
     if (r != CPVS_OK) return r;
+    std::vector<cpvs::MultiDag> table(num_shadows);
+    for (uint32_t i = 0; i < num_shadows; ++i) {
+        ensure_top(shadows[i], st);
+        table[i] = cpvs::shadow_table_entry(shadows[i]);
+    }
     cpvs::Ctx& c = ctx->c;
     cpvs::MultiDag* dtab = nullptr;
     const uint64_t tb = num_shadows * sizeof(cpvs::MultiDag);

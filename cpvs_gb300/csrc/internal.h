@@ -117,7 +117,8 @@ struct MultiDag {
     uint32_t words;
     uint32_t num_levels;
     uint32_t leafmasks;
-    uint32_t pad;
+    uint32_t top_depth;   // levels resolved by `top` (0: no top grid)
+    const uint32_t* top;  // the DAG's top grid, or null
 };
 cpvs_status launch_multi_lookup(const MultiDag* dags, uint32_t ndags, const uint32_t* ids, const float* xyz, uint64_t n,
                                 uint32_t* bits, cudaStream_t st, Timing* timing = nullptr);

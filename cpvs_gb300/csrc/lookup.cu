@@ -435,6 +435,21 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// One query against a table entry: its top grid first when it has one.
+__device__ __forceinline__ bool multi_descend(const MultiDag& D, int32_t px, int32_t py, int32_t pz) {
+    const int root = (int)D.num_levels - 2, min_level = D.leafmasks ? 3 : 0;
+    int level = root;
+    uint32_t off = 0;
+    if (D.top) {
+        const int depth = (int)D.top_depth;
+        const uint32_t e = __ldg(D.top + top_cell(px, py, pz, root - depth + 1, depth));
+        if (e >= kCellLit) return e == kCellLit;
+        off = e;
+        level = root - depth;
+    }
+    return descend(D.dag, D.words, 0u, off, level, min_level, D.leafmasks != 0, px, py, pz);
+}
+
 // Many resident DAGs at once: query i descends DAG dags[ids[i]] (its own
 // depth and leafmask mode); ids outside the table answer "shadow".
 __global__ void __launch_bounds__(kThreads)
@@ -453,8 +468,7 @@ __global__ void __launch_bounds__(kThreads)
                 const float scale = (float)((1u << (D.num_levels - 1)) - 1u);
                 const float* p = q + 3 * i;
                 const int32_t px = quantise(p[0], scale), py = quantise(p[1], scale), pz = quantise(p[2], scale);
-                lit = descend(D.dag, D.words, 0u, 0u, (int)D.num_levels - 2, D.leafmasks ? 3 : 0, D.leafmasks != 0,
-                              px, py, pz);
+                lit = multi_descend(D, px, py, pz);
             }
         }
         const uint32_t word = __ballot_sync(0xffffffffu, lit);
@@ -487,8 +501,7 @@ __global__ void __launch_bounds__(kThreads)
             const float scale = (float)((1u << (D.num_levels - 1)) - 1u);
             const float* p = sg.xyz + 3 * i;
             const int32_t px = quantise(p[0], scale), py = quantise(p[1], scale), pz = quantise(p[2], scale);
-            lit = descend(D.dag, D.words, 0u, 0u, (int)D.num_levels - 2, D.leafmasks ? 3 : 0, D.leafmasks != 0, px, py,
-                          pz);
+            lit = multi_descend(D, px, py, pz);
         }
         const uint32_t word = __ballot_sync(0xffffffffu, lit);
         if (lane == 0) sg.bits[lw] = word;

@@ -85,4 +85,9 @@ struct cpvs_grid : DeviceObject {
 namespace cpvs {
 // The address under which the GPU reads host memory `p` in place, or null.
 void* host_accessible(const Ctx& c, const void* p);
+// Builds the shadow's lookup top grid if it has none yet (stream-ordered,
+// on the context's thread).
+void shadow_ensure_top(const cpvs_shadow* s, cudaStream_t st);
+// The shadow as an entry of a multi-DAG lookup table (with its top grid).
+MultiDag shadow_table_entry(const cpvs_shadow* s);
 }  // namespace cpvs

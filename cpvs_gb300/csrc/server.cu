@@ -252,10 +252,7 @@ struct cpvs_server {
                 continue;
             }
             auto [it, fresh] = dag_of.try_emplace(e, ndags);
-            if (fresh) {
-                hdags[ndags++] = cpvs::MultiDag{e->sh->dag, (uint32_t)e->sh->words, e->sh->num_levels,
-                                                e->sh->leafmasks ? 1u : 0u, 0u};
-            }
+            if (fresh) hdags[ndags++] = cpvs::shadow_table_entry(e->sh);
             hsegs[nsegs++] = cpvs::LookupSegment{q, b, words, r->count, it->second, 0u};
             words += (r->count + 31) / 32;
             f.reqs.push_back(r);
@@ -394,7 +391,9 @@ struct cpvs_server {
             for (const Req& r : ok) complete(r, st, msg);
             return;
         }
-        // lookups launched after the DAGs are published run after the build
+        // their lookup top grids, then: lookups launched after the DAGs are
+        // published run after all of it
+        for (cpvs_shadow* sh : out) cpvs::shadow_ensure_top(sh, s_build);
         cudaEvent_t built = nullptr;
         if (cudaEventCreateWithFlags(&built, cudaEventDisableTiming) == cudaSuccess) {
             cudaEventRecord(built, s_build);
