@@ -61,8 +61,8 @@ struct LevelDev {
     uint32_t* job;
     uint32_t* mask;
     uint32_t* first;   // index of the first child in the level below
-    uint32_t* uid;     // merged identity (rank among the level's kept nodes)
-    uint32_t* slot;    // hash slot during the merge
+    uint32_t* uid;     // single-call builds: representative, then rank among the level's kept nodes
+    uint32_t* slot;    // hash slot of the node's class: its merged identity for the level above
     uint32_t* uniq;    // rank -> node index of the first occurrence
     uint32_t* woff;    // rank -> word offset (running over the level)
     uint64_t* slices;  // leaf level: 8 leafmasks per node
@@ -515,11 +515,17 @@ __global__ void __launch_bounds__(kThreads, 5)
 }
 
 // --------------------------------------------------------------- bottom-up
-// A child's merged identity; CG: written by other blocks of the same
-// launch, so read from L2.
+// A child's merged identity: the hash slot its class occupies.  Equal nodes
+// hash to the same start and probe the same sequence; a slot, once claimed,
+// keeps its class (later equal nodes only lower the representative index in
+// its lower half), so every member of a class ends on the class's slot and
+// no two classes share one.  The identity is thus final as soon as the
+// node's own insert returns, and the level above needs no pass that resolves
+// representatives first.  CG: written by other blocks of the same launch, so
+// read from L2.
 template <bool CG>
 __device__ __forceinline__ uint32_t child_uid(const LevelDev& child, uint32_t x) {
-    return CG ? __ldcg(child.uid + x) : child.uid[x];
+    return CG ? __ldcg(child.slot + x) : child.slot[x];
 }
 
 // Two leaves are the same node when their jobs and all eight slice masks
@@ -672,10 +678,10 @@ __global__ void __launch_bounds__(kThreads)
 // taken in order, so a block only waits on blocks that already run, and
 // every wait is bounded in time (a timeout sets error bit 32).  A kept
 // node's rank goes into the upper half of its hash slot (the lower half
-// keeps the class representative), so the level above and the emission read
-// a node's rank as table[slot] >> 32 and no remap pass runs.  The topmost
-// levels, which hold few nodes, run in one single-block launch for the
-// expansion and one for the merge.
+// keeps the class representative), so the emission reads a node's rank as
+// table[slot] >> 32 and no remap pass runs.  The topmost levels, which hold
+// few nodes, run in one cluster launch for the expansion and one for the
+// merge.
 
 constexpr unsigned long long kFlagAgg = 1ull << 62, kFlagInc = 2ull << 62, kFlagState = 3ull << 62;
 constexpr uint64_t kLookbackTimeoutNs = 200000000ull;  // 0.2 s
@@ -949,7 +955,7 @@ __global__ void __launch_bounds__(kThreads)
 
 // Hash insert of inner node i into `table` (dedup_insert's rule: the slot
 // ends with the class's first occurrence); children are compared by their
-// merged identities (uid).  The node's child identities, and on a tag match
+// merged identities (class slots).  The node's child identities, and on a tag match
 // the candidate's, are requested as independent loads before they are used,
 // so a node costs two dependent round trips for its children instead of one
 // per child.
@@ -1049,18 +1055,7 @@ __global__ void __launch_bounds__(kThreads)
         uint32_t rep[kScanItems];
 #pragma unroll
         for (int it = 0; it < kScanItems; ++it)
-            rep[it] = b0 + it < n ? (uint32_t)__ldcg(cur.table + sl[it]) : ~0u;
-        // the class representative (lower half of the slot) is the node's
-        // merged identity for the level above
-        if (full) {
-#pragma unroll
-            for (int h = 0; h < kScanItems; h += 4)
-                *reinterpret_cast<uint4*>(cur.uid + b0 + h) = make_uint4(rep[h], rep[h + 1], rep[h + 2], rep[h + 3]);
-        } else {
-#pragma unroll
-            for (int it = 0; it < kScanItems; ++it)
-                if (b0 + it < n) cur.uid[b0 + it] = rep[it];
-        }
+            rep[it] = b0 + it < n ? __ldcg(reinterpret_cast<const uint32_t*>(cur.table + sl[it])) : ~0u;
         uint32_t kept = 0, cnt = 0, words = 0;
 #pragma unroll
         for (int it = 0; it < kScanItems; ++it)
@@ -1277,7 +1272,6 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
             w[it] = 0;
             if (i < hi) {
                 const uint32_t rep = (uint32_t)__ldcg(cur.table + cur.slot[i]);
-                cur.uid[i] = rep;
                 if (rep == i) {
                     kept |= 1u << it;
                     w[it] = node_words(cur.mask[i], leaf);
@@ -1550,6 +1544,8 @@ struct BuildPlan {
     size_t hout_bytes = 0;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t done = nullptr;  // recorded after the emission that last read the scratch
+    // fork / join of the ranking passes' stream in the captured launch sequence
+    cudaEvent_t fork[CPVS_MAX_LEVELS] = {nullptr}, join = nullptr;
     bool tables_tuned = false;
     // single-pass levels: the levels >= small_lo run in the single-block
     // kernels; look-back tickets and flags (zeroed by every build)
@@ -1572,6 +1568,10 @@ void plan_release(Ctx& ctx, BuildPlan* P) {
     if (P->done) cudaEventSynchronize(P->done);
     if (P->exec) cudaGraphExecDestroy(P->exec);
     P->exec = nullptr;
+    for (cudaEvent_t& e : P->fork)
+        if (e) cudaEventDestroy(e), e = nullptr;
+    if (P->join) cudaEventDestroy(P->join);
+    P->join = nullptr;
     if (P->arena) ctx.release(P->arena, P->arena_bytes, true, nullptr);
     if (P->table) ctx.release(P->table, P->table_slots * 8, true, nullptr);
     P->arena = nullptr;
@@ -1611,7 +1611,7 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
     auto add = [&](size_t count, size_t elem) { bytes += align256(count * elem); };
     for (int L = P->bottom; L <= P->maxR; ++L) {
         const uint64_t c = std::max<uint64_t>(P->cap[L], 1);
-        for (int a = 0; a < 8; ++a) add(c, a == 0 ? 8 : 4);
+        for (int a = 0; a < 7; ++a) add(c, a == 0 ? 8 : 4);  // coord, job, mask, first, slot, uniq, woff
         if (P->leafmasks && L == 2) {
             add(c * 8, 8);
             add(c, 8);
@@ -1657,7 +1657,6 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
         l.job = A.take<uint32_t>(c);
         l.mask = A.take<uint32_t>(c);
         l.first = A.take<uint32_t>(c);
-        l.uid = A.take<uint32_t>(c);
         l.slot = A.take<uint32_t>(c);
         l.uniq = A.take<uint32_t>(c);
         l.woff = A.take<uint32_t>(c);
@@ -1749,11 +1748,16 @@ int probe_cluster_blocks() {
 // The whole device-side build after the inputs are staged: top-down
 // expansion, leaves, bottom-up merge, layout, root masks, and the copy of
 // the results region to pinned host memory.  Stream-ordered; capturable.
-cpvs_status plan_enqueue(const BuildPlan* P, cudaStream_t st, Timing* tm) {
+// With a second stream `rank_st` (capture only), each level's ranking pass
+// runs there, beside the inserts of the levels above it, which need only the
+// level's class slots; the layout waits for both streams.
+cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Timing* tm) {
     const uint32_t njobs = P->njobs;
     const size_t segn = (size_t)njobs * CPVS_MAX_LEVELS;
     const ResultView& rv = P->resv;
     uint32_t* err = rv.err;
+    const bool forked = rank_st && rank_st != st;
+    if (!forked) rank_st = st;
     CPVS_CUDA(cudaMemsetAsync(P->res, 0, result_bytes(njobs), st));
     CPVS_CUDA(cudaMemsetAsync(P->counts, 0, CPVS_MAX_LEVELS * 4, st));
     CPVS_CUDA(cudaMemsetAsync(P->segbuf + 6 * segn, 0, segn * 4, st));
@@ -1803,9 +1807,10 @@ cpvs_status plan_enqueue(const BuildPlan* P, cudaStream_t st, Timing* tm) {
                                                                                  njobs, 0, P->seg, err);
     }
     CPVS_CUDA(cudaGetLastError());
-    // bottom-up: one insert and one ranking pass per level, then the small
-    // top levels in one block
+    // bottom-up: per level an insert and the ranking pass (on rank_st), then
+    // the small top levels in one cluster
     const int merge_hi = std::min(Ls - 1, P->maxR);
+    bool branched = false;  // rank_st has joined the capture
     for (int L = P->bottom; L <= merge_hi; ++L) {
         const bool leaf = P->leafmasks && L == 2;
         const LevelDev child = (L > P->bottom) ? P->lv[L - 1] : P->lv[L];
@@ -1814,21 +1819,33 @@ cpvs_status plan_enqueue(const BuildPlan* P, cudaStream_t st, Timing* tm) {
             k_dedup_insert<false><<<plan_grid(P, P->cap[L], kThreads), kThreads, 0, st>>>(
                 P->lv[L], child, P->counts, L, P->lv[L].table, P->lv[L].table_mask, err);
         }
-        KernelTimer kt(tm, K_SCAN, st);
+        if (forked) {
+            if (!P->fork[L]) CPVS_CUDA(cudaEventCreateWithFlags(&P->fork[L], cudaEventDisableTiming));
+            CPVS_CUDA(cudaEventRecord(P->fork[L], st));
+            CPVS_CUDA(cudaStreamWaitEvent(rank_st, P->fork[L], 0));
+            branched = true;
+        }
+        KernelTimer kt(tm, K_SCAN, rank_st);
         const uint32_t g = plan_grid(P, P->cap[L], kScanTile);
         unsigned long long* fl = P->flags + P->scan_flag_off[L];
         unsigned int* ticket = P->tickets + CPVS_MAX_LEVELS + L;
         if (leaf)
-            k_merge_scan_lb<true><<<g, kThreads, 0, st>>>(P->lv[L], P->counts, rv.level_u, L, P->seg, ticket, fl, err);
+            k_merge_scan_lb<true><<<g, kThreads, 0, rank_st>>>(P->lv[L], P->counts, rv.level_u, L, P->seg, ticket,
+                                                               fl, err);
         else
-            k_merge_scan_lb<false><<<g, kThreads, 0, st>>>(P->lv[L], P->counts, rv.level_u, L, P->seg, ticket, fl,
-                                                           err);
+            k_merge_scan_lb<false><<<g, kThreads, 0, rank_st>>>(P->lv[L], P->counts, rv.level_u, L, P->seg, ticket,
+                                                                fl, err);
     }
     if (merge_hi < P->maxR) {
         KernelTimer kt(tm, K_SCAN, st);
         CPVS_CUDA(launch_cluster(k_merge_cluster, (uint32_t)P->cluster_blocks, st, P->lvt, P->counts, rv.level_u,
                                  std::max(merge_hi + 1, P->bottom), P->maxR, P->bottom, P->leafmasks ? 2 : -1, P->seg,
                                  err));
+    }
+    if (branched) {
+        if (!P->join) CPVS_CUDA(cudaEventCreateWithFlags(&P->join, cudaEventDisableTiming));
+        CPVS_CUDA(cudaEventRecord(P->join, rank_st));
+        CPVS_CUDA(cudaStreamWaitEvent(st, P->join, 0));
     }
     {
         KernelTimer kt(tm, K_LAYOUT, st);
@@ -2004,14 +2021,16 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         CPVS_CUDA(cudaMemcpyAsync(P->jobs_dev, hj, njobs * sizeof(JobDev), cudaMemcpyHostToDevice, st));
         CPVS_CUDA(cudaMemcpyAsync(P->inj_dev, hi, njobs * sizeof(Injected), cudaMemcpyHostToDevice, st));
         if (ctx.timing.on) {
-            cpvs_status r = plan_enqueue(P, st, &ctx.timing);
+            cpvs_status r = plan_enqueue(P, st, nullptr, &ctx.timing);
             if (r != CPVS_OK) return r;
         } else {
             if (!P->exec) {
                 if (!ctx.capture_stream) CPVS_CUDA(cudaStreamCreateWithFlags(&ctx.capture_stream, cudaStreamNonBlocking));
+                if (!ctx.capture_rank_stream)
+                    CPVS_CUDA(cudaStreamCreateWithFlags(&ctx.capture_rank_stream, cudaStreamNonBlocking));
                 cudaGraph_t graph = nullptr;
                 CPVS_CUDA(cudaStreamBeginCapture(ctx.capture_stream, cudaStreamCaptureModeThreadLocal));
-                cpvs_status r = plan_enqueue(P, ctx.capture_stream, nullptr);
+                cpvs_status r = plan_enqueue(P, ctx.capture_stream, ctx.capture_rank_stream, nullptr);
                 cudaError_t ec = cudaStreamEndCapture(ctx.capture_stream, &graph);
                 if (r != CPVS_OK) {
                     if (graph) cudaGraphDestroy(graph);

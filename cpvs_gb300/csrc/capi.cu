@@ -305,6 +305,7 @@ void cpvs_ctx_destroy(cpvs_ctx* ctx) {
     cpvs::destroy_plans(ctx->c);
     cudaDeviceSynchronize();
     if (ctx->c.capture_stream) cudaStreamDestroy(ctx->c.capture_stream);
+    if (ctx->c.capture_rank_stream) cudaStreamDestroy(ctx->c.capture_rank_stream);
     cudaStreamDestroy(ctx->c.free_stream);
     cudaMemPoolDestroy(ctx->c.pool);
     delete ctx;

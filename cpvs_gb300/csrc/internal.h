@@ -239,6 +239,7 @@ struct Ctx {
     // and the stream their launch sequences are captured on.
     struct PlanCache* plans = nullptr;
     cudaStream_t capture_stream = nullptr;
+    cudaStream_t capture_rank_stream = nullptr;  // the ranking passes' branch of a captured build
 };
 
 }  // namespace cpvs
