@@ -49,6 +49,37 @@ namespace cg = cooperative_groups;
 
 constexpr int kThreads = 256;
 
+// Programmatic dependent launch.  The build's kernels are launched so that
+// the next kernel of the stream may be scheduled while the current one
+// drains; each kernel first waits until its predecessor in the stream has
+// completed and its writes are visible (a no-op when launched without the
+// attribute), then lets its own successor be scheduled.  Every kernel so
+// launched waits at its start, so completion stays transitive along the
+// chain.
+__device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void chain_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void chain_enter() {
+    chain_wait();
+    chain_release();
+}
+
+// Zeroes up to four byte ranges (each starting 16-byte aligned) in one launch.
+struct ClearRanges {
+    char* p[4];
+    uint64_t n[4];
+};
+__global__ void __launch_bounds__(kThreads) k_clear(ClearRanges r) {
+    chain_enter();
+    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        uint4* q = reinterpret_cast<uint4*>(r.p[k]);
+        const uint64_t nv = r.n[k] / 16;
+        for (uint64_t i = t; i < nv; i += stride) q[i] = make_uint4(0u, 0u, 0u, 0u);
+        for (uint64_t i = nv * 16 + t; i < r.n[k]; i += stride) r.p[k][i] = 0;
+    }
+}
+
 struct JobDev {
     const float2* pyr;  // pyramid levels 1..log2(n)
     const float* depth;  // level 0
@@ -264,6 +295,7 @@ __global__ void __launch_bounds__(kThreads)
 __global__ void __launch_bounds__(kThreads)
     k_classify_bottom(LevelDev cur, const uint32_t* __restrict__ counts, const JobDev* __restrict__ jobs,
                       uint32_t njobs, int L, SegDev seg, uint32_t* err) {
+    chain_enter();
     const uint32_t n = counts[L];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t j = cur.job[i];
@@ -455,6 +487,7 @@ __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long lon
 __global__ void __launch_bounds__(kThreads, 5)
     k_leaf_insert(LevelDev lv, const uint32_t* __restrict__ counts, const JobDev* __restrict__ jobs, uint32_t njobs,
                   int L, SegDev seg, unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
+    chain_enter();
     const uint32_t n = counts[L];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint64_t M[8], h;
@@ -555,6 +588,7 @@ template <bool LEAF>
 __global__ void __launch_bounds__(kThreads)
     k_dedup_insert(LevelDev cur, LevelDev child, const uint32_t* __restrict__ counts, int L,
                    unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
+    chain_enter();
     const uint32_t n = counts[L];
     if (!LEAF) {
         for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
@@ -833,6 +867,7 @@ __global__ void __launch_bounds__(kThreads)
     k_expand_lb(LevelDev cur, LevelDev nxt, uint32_t* counts, const JobDev* __restrict__ jobs, uint32_t njobs,
                 int L, const Injected* __restrict__ inj, uint32_t ninj, SegDev seg, uint32_t cap_next,
                 unsigned int* ticket, unsigned long long* flags, uint32_t* err) {
+    chain_enter();
     __shared__ uint32_t sm[64];
     __shared__ uint32_t s_tile, s_excl;
     __shared__ uint64_t s_coord[kExpTile];
@@ -1018,6 +1053,7 @@ template <bool LEAF>
 __global__ void __launch_bounds__(kThreads)
     k_merge_scan_lb(LevelDev cur, const uint32_t* __restrict__ counts, uint32_t* level_u, int L, SegDev seg,
                     unsigned int* ticket, unsigned long long* flags, uint32_t* err) {
+    chain_enter();
     __shared__ uint32_t sm[64];
     __shared__ uint32_t s_tile;
     __shared__ uint2 s_excl;
@@ -1146,6 +1182,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
     k_expand_cluster(const LevelDev* __restrict__ lvt, uint32_t* counts, const JobDev* __restrict__ jobs,
                      uint32_t njobs, int Lhi, int Llo, const Injected* __restrict__ inj_all, SmallLevels sl,
                      SegDev seg, uint32_t* err) {
+    chain_enter();
     cg::cluster_group cl = cg::this_cluster();
     const uint32_t nb = cl.num_blocks(), rank = cl.block_rank();
     __shared__ uint32_t sm[64];
@@ -1250,6 +1287,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
 __global__ void __launch_bounds__(kClusterThreads, 1)
     k_merge_cluster(const LevelDev* __restrict__ lvt, const uint32_t* __restrict__ counts, uint32_t* level_u,
                     int Llo, int Lhi, int bottom, int leaf_level, SegDev seg, uint32_t* err) {
+    chain_enter();
     cg::cluster_group cl = cg::this_cluster();
     const uint32_t nb = cl.num_blocks(), rank = cl.block_rank();
     __shared__ uint32_t sm[64];
@@ -1326,6 +1364,7 @@ struct JobLayout {
 };
 
 __global__ void k_layout(SegDev seg, JobLayout lay, const uint32_t* __restrict__ root_level, uint32_t njobs, int bottom) {
+    chain_enter();
     // single block: each thread sums its jobs, then a block scan over jobs in
     // rounds of blockDim
     __shared__ uint32_t sm[64];
@@ -1393,6 +1432,7 @@ __global__ void __launch_bounds__(kThreads)
 
 // The top level of a batch: the roots of the jobs whose root lies there.
 __global__ void k_init_top(LevelDev top, uint32_t* counts, int L, const Injected* __restrict__ inj, uint32_t ninj) {
+    chain_enter();
     for (uint32_t r = threadIdx.x; r < ninj; r += blockDim.x) {
         top.coord[r] = inj[r].coord;
         top.job[r] = inj[r].job;
@@ -1403,6 +1443,7 @@ __global__ void k_init_top(LevelDev top, uint32_t* counts, int L, const Injected
 // Root mask of every job (the first word of its DAG).
 __global__ void k_root_masks(const LevelDev* __restrict__ lvt, SegDev seg, const uint32_t* __restrict__ root_level,
                              uint32_t njobs, uint32_t* out) {
+    chain_enter();
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < njobs; j += gridDim.x * blockDim.x) {
         const int L = (int)root_level[j];
         out[j] = lvt[L].mask[seg.nstart[seg_index(j, L)]];
@@ -1545,7 +1586,7 @@ struct BuildPlan {
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t done = nullptr;  // recorded after the emission that last read the scratch
     // fork / join of the ranking passes' stream in the captured launch sequence
-    cudaEvent_t fork[CPVS_MAX_LEVELS] = {nullptr}, join = nullptr;
+    cudaEvent_t fork[CPVS_MAX_LEVELS] = {nullptr}, join = nullptr, start = nullptr, tables = nullptr;
     bool tables_tuned = false;
     // single-pass levels: the levels >= small_lo run in the single-block
     // kernels; look-back tickets and flags (zeroed by every build)
@@ -1570,8 +1611,8 @@ void plan_release(Ctx& ctx, BuildPlan* P) {
     P->exec = nullptr;
     for (cudaEvent_t& e : P->fork)
         if (e) cudaEventDestroy(e), e = nullptr;
-    if (P->join) cudaEventDestroy(P->join);
-    P->join = nullptr;
+    for (cudaEvent_t* e : {&P->join, &P->start, &P->tables})
+        if (*e) cudaEventDestroy(*e), *e = nullptr;
     if (P->arena) ctx.release(P->arena, P->arena_bytes, true, nullptr);
     if (P->table) ctx.release(P->table, P->table_slots * 8, true, nullptr);
     P->arena = nullptr;
@@ -1701,21 +1742,32 @@ uint32_t plan_grid(const BuildPlan* P, uint64_t items, uint64_t per_block) {
     return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, P->max_grid));
 }
 
-// Cluster launch of a small-level kernel: `nb` blocks of 1024 threads, one
-// cluster.
+// Launch of a build kernel.  `chained`: the kernel may be scheduled while its
+// predecessor in the stream drains (it waits for it at its start).
+// `cluster` > 0: one cluster of that many blocks.
 template <typename... Exp, typename... Act>
-cudaError_t launch_cluster(void (*kernel)(Exp...), uint32_t nb, cudaStream_t st, Act&&... args) {
+cudaError_t launch_build(void (*kernel)(Exp...), uint32_t grid, uint32_t block, cudaStream_t st, bool chained,
+                         uint32_t cluster, Act&&... args) {
     cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(nb);
-    cfg.blockDim = dim3(kClusterThreads);
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
     cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = nb;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
+    cudaLaunchAttribute at[2];
+    uint32_t na = 0;
+    if (cluster) {
+        at[na].id = cudaLaunchAttributeClusterDimension;
+        at[na].val.clusterDim.x = cluster;
+        at[na].val.clusterDim.y = 1;
+        at[na].val.clusterDim.z = 1;
+        ++na;
+    }
+    if (chained) {
+        at[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[na].val.programmaticStreamSerializationAllowed = 1;
+        ++na;
+    }
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = na;
     return cudaLaunchKernelEx(&cfg, kernel, std::forward<Act>(args)...);
 }
 
@@ -1758,18 +1810,39 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
     uint32_t* err = rv.err;
     const bool forked = rank_st && rank_st != st;
     if (!forked) rank_st = st;
-    CPVS_CUDA(cudaMemsetAsync(P->res, 0, result_bytes(njobs), st));
-    CPVS_CUDA(cudaMemsetAsync(P->counts, 0, CPVS_MAX_LEVELS * 4, st));
-    CPVS_CUDA(cudaMemsetAsync(P->segbuf + 6 * segn, 0, segn * 4, st));
-    // look-back tickets and flags (adjacent in the arena), then every
-    // level's hash table
-    CPVS_CUDA(cudaMemsetAsync(P->tickets, 0,
-                              reinterpret_cast<const char*>(P->flags + P->flags_count) -
-                                  reinterpret_cast<const char*>(P->tickets),
-                              st));
+    const bool ch = forked;  // chained launches on the captured path
+    auto event = [](cudaEvent_t& e) -> cudaError_t {
+        return e ? cudaSuccess : cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    };
+    if (forked) {
+        CPVS_CUDA(event(P->start));
+        CPVS_CUDA(event(P->tables));
+        CPVS_CUDA(cudaEventRecord(P->start, st));
+        CPVS_CUDA(cudaStreamWaitEvent(rank_st, P->start, 0));
+    }
+    // every level's hash table, beside the expansion (needed from the
+    // leaves on)
     {
-        KernelTimer kt(tm, K_TABLE_CLEAR, st);
-        CPVS_CUDA(cudaMemsetAsync(P->table, 0xFF, plan_table_slots(P) * 8, st));
+        KernelTimer kt(tm, K_TABLE_CLEAR, rank_st);
+        CPVS_CUDA(cudaMemsetAsync(P->table, 0xFF, plan_table_slots(P) * 8, rank_st));
+    }
+    if (forked) CPVS_CUDA(cudaEventRecord(P->tables, rank_st));
+    // results, level counts, job bases, look-back tickets and flags (the
+    // last two adjacent in the arena)
+    {
+        ClearRanges cr{};
+        cr.p[0] = P->res;
+        cr.n[0] = result_bytes(njobs);
+        cr.p[1] = reinterpret_cast<char*>(P->counts);
+        cr.n[1] = CPVS_MAX_LEVELS * 4;
+        cr.p[2] = reinterpret_cast<char*>(P->segbuf + 6 * segn);
+        cr.n[2] = segn * 4;
+        cr.p[3] = reinterpret_cast<char*>(P->tickets);
+        cr.n[3] = reinterpret_cast<const char*>(P->flags + P->flags_count) - reinterpret_cast<const char*>(P->tickets);
+        uint64_t mx = 0;
+        for (int k = 0; k < 4; ++k) mx = std::max<uint64_t>(mx, cr.n[k]);
+        const uint32_t g = (uint32_t)std::min<uint64_t>((mx / 16 + kThreads - 1) / kThreads + 1, P->max_grid);
+        CPVS_CUDA(launch_build(k_clear, g, kThreads, st, false, 0, cr));
     }
     // top-down: the small top levels as one cluster (which also places the
     // roots), then one pass per level
@@ -1783,47 +1856,46 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
             sl.ninj[L] = (uint32_t)P->ninj[L];
             sl.cap[L] = (uint32_t)P->cap[L];
         }
-        CPVS_CUDA(launch_cluster(k_expand_cluster, (uint32_t)P->cluster_blocks, st, P->lvt, P->counts, P->jobs_dev,
-                                 njobs, P->maxR, exp_lo, P->inj_dev, sl, P->seg, err));
+        CPVS_CUDA(launch_build(k_expand_cluster, (uint32_t)P->cluster_blocks, kClusterThreads, st, ch,
+                               (uint32_t)P->cluster_blocks, P->lvt, P->counts, P->jobs_dev, njobs, P->maxR, exp_lo,
+                               P->inj_dev, sl, P->seg, err));
     } else {
         // the top level holds only roots
-        k_init_top<<<1, 256, 0, st>>>(P->lv[P->maxR], P->counts, P->maxR, P->inj_dev + P->inj_off[P->maxR],
-                                      (uint32_t)P->ninj[P->maxR]);
+        CPVS_CUDA(launch_build(k_init_top, 1, 256, st, ch, 0, P->lv[P->maxR], P->counts, P->maxR,
+                               P->inj_dev + P->inj_off[P->maxR], (uint32_t)P->ninj[P->maxR]));
     }
     for (int L = std::min(exp_lo - 1, P->maxR); L > P->bottom; --L) {
         KernelTimer kt(tm, K_EXPAND_WRITE, st);
-        k_expand_lb<<<plan_grid(P, P->cap[L], kExpTile), kThreads, 0, st>>>(
-            P->lv[L], P->lv[L - 1], P->counts, P->jobs_dev, njobs, L, P->inj_dev + P->inj_off[L - 1],
-            (uint32_t)P->ninj[L - 1], P->seg, (uint32_t)P->cap[L - 1], P->tickets + L, P->flags + P->exp_flag_off[L],
-            err);
+        CPVS_CUDA(launch_build(k_expand_lb, plan_grid(P, P->cap[L], kExpTile), kThreads, st, ch, 0, P->lv[L],
+                               P->lv[L - 1], P->counts, P->jobs_dev, njobs, L, P->inj_dev + P->inj_off[L - 1],
+                               (uint32_t)P->ninj[L - 1], P->seg, (uint32_t)P->cap[L - 1], P->tickets + L,
+                               P->flags + P->exp_flag_off[L], err));
     }
+    if (forked) CPVS_CUDA(cudaStreamWaitEvent(st, P->tables, 0));
     if (P->leafmasks) {
         KernelTimer kt(tm, K_LEAF_MASKS, st);
-        k_leaf_insert<<<plan_grid(P, P->cap[2], kThreads), kThreads, 0, st>>>(
-            P->lv[2], P->counts, P->jobs_dev, njobs, 2, P->seg, P->lv[2].table, P->lv[2].table_mask, err);
+        CPVS_CUDA(launch_build(k_leaf_insert, plan_grid(P, P->cap[2], kThreads), kThreads, st, ch, 0, P->lv[2],
+                               P->counts, P->jobs_dev, njobs, 2, P->seg, P->lv[2].table, P->lv[2].table_mask, err));
     } else {
         KernelTimer kt(tm, K_CLASSIFY_BOTTOM, st);
-        k_classify_bottom<<<plan_grid(P, P->cap[0], kThreads), kThreads, 0, st>>>(P->lv[0], P->counts, P->jobs_dev,
-                                                                                 njobs, 0, P->seg, err);
+        CPVS_CUDA(launch_build(k_classify_bottom, plan_grid(P, P->cap[0], kThreads), kThreads, st, ch, 0, P->lv[0],
+                               P->counts, P->jobs_dev, njobs, 0, P->seg, err));
     }
-    CPVS_CUDA(cudaGetLastError());
     // bottom-up: per level an insert and the ranking pass (on rank_st), then
     // the small top levels in one cluster
     const int merge_hi = std::min(Ls - 1, P->maxR);
-    bool branched = false;  // rank_st has joined the capture
     for (int L = P->bottom; L <= merge_hi; ++L) {
         const bool leaf = P->leafmasks && L == 2;
         const LevelDev child = (L > P->bottom) ? P->lv[L - 1] : P->lv[L];
         if (!leaf) {
             KernelTimer kt(tm, K_INSERT_INNER, st);
-            k_dedup_insert<false><<<plan_grid(P, P->cap[L], kThreads), kThreads, 0, st>>>(
-                P->lv[L], child, P->counts, L, P->lv[L].table, P->lv[L].table_mask, err);
+            CPVS_CUDA(launch_build(k_dedup_insert<false>, plan_grid(P, P->cap[L], kThreads), kThreads, st, ch, 0,
+                                   P->lv[L], child, P->counts, L, P->lv[L].table, P->lv[L].table_mask, err));
         }
         if (forked) {
-            if (!P->fork[L]) CPVS_CUDA(cudaEventCreateWithFlags(&P->fork[L], cudaEventDisableTiming));
+            CPVS_CUDA(event(P->fork[L]));
             CPVS_CUDA(cudaEventRecord(P->fork[L], st));
             CPVS_CUDA(cudaStreamWaitEvent(rank_st, P->fork[L], 0));
-            branched = true;
         }
         KernelTimer kt(tm, K_SCAN, rank_st);
         const uint32_t g = plan_grid(P, P->cap[L], kScanTile);
@@ -1835,24 +1907,26 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
         else
             k_merge_scan_lb<false><<<g, kThreads, 0, rank_st>>>(P->lv[L], P->counts, rv.level_u, L, P->seg, ticket,
                                                                 fl, err);
+        CPVS_CUDA(cudaGetLastError());
     }
     if (merge_hi < P->maxR) {
         KernelTimer kt(tm, K_SCAN, st);
-        CPVS_CUDA(launch_cluster(k_merge_cluster, (uint32_t)P->cluster_blocks, st, P->lvt, P->counts, rv.level_u,
-                                 std::max(merge_hi + 1, P->bottom), P->maxR, P->bottom, P->leafmasks ? 2 : -1, P->seg,
-                                 err));
+        CPVS_CUDA(launch_build(k_merge_cluster, (uint32_t)P->cluster_blocks, kClusterThreads, st, ch,
+                               (uint32_t)P->cluster_blocks, P->lvt, P->counts, rv.level_u,
+                               std::max(merge_hi + 1, P->bottom), P->maxR, P->bottom, P->leafmasks ? 2 : -1, P->seg,
+                               err));
     }
-    if (branched) {
-        if (!P->join) CPVS_CUDA(cudaEventCreateWithFlags(&P->join, cudaEventDisableTiming));
+    if (forked) {
+        CPVS_CUDA(event(P->join));
         CPVS_CUDA(cudaEventRecord(P->join, rank_st));
         CPVS_CUDA(cudaStreamWaitEvent(st, P->join, 0));
     }
     {
         KernelTimer kt(tm, K_LAYOUT, st);
-        k_layout<<<1, 1024, 0, st>>>(P->seg, P->lay, P->root_dev, njobs, P->bottom);
-        k_root_masks<<<(njobs + 255) / 256, 256, 0, st>>>(P->lvt, P->seg, P->root_dev, njobs, rv.root_mask);
+        CPVS_CUDA(launch_build(k_layout, 1, 1024, st, ch, 0, P->seg, P->lay, P->root_dev, njobs, P->bottom));
+        CPVS_CUDA(launch_build(k_root_masks, (njobs + 255) / 256, 256, st, ch, 0, P->lvt, P->seg, P->root_dev, njobs,
+                               rv.root_mask));
     }
-    CPVS_CUDA(cudaGetLastError());
     CPVS_CUDA(cudaMemcpyAsync(P->hout, P->res, result_bytes(njobs), cudaMemcpyDeviceToHost, st));
     return CPVS_OK;
 }
