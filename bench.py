@@ -196,11 +196,12 @@ def run_ours(args, rank, world, local_rank):
     clocks = ClockSampler(local_rank)
     clocks.start()
     # the SM clock takes a few hundred ms of load to ramp up from idle: build
-    # for about a second before the counted warm-up steps
+    # for about a second before the counted warm-up steps, back to back as in
+    # the timed region (each build waits for its own results inside the call)
     t_ramp = time.perf_counter()
     while time.perf_counter() - t_ramp < 1.0:
         build_step()
-        torch.cuda.synchronize(dev)
+    torch.cuda.synchronize(dev)
     for _ in range(args.warmup):
         build_step()
     barrier()

@@ -49,20 +49,6 @@ namespace cg = cooperative_groups;
 
 constexpr int kThreads = 256;
 
-// Programmatic dependent launch.  The build's kernels are launched so that
-// the next kernel of the stream may be scheduled while the current one
-// drains; each kernel first waits until its predecessor in the stream has
-// completed and its writes are visible (a no-op when launched without the
-// attribute), then lets its own successor be scheduled.  Every kernel so
-// launched waits at its start, so completion stays transitive along the
-// chain.
-__device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void chain_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-__device__ __forceinline__ void chain_enter() {
-    chain_wait();
-    chain_release();
-}
-
 // Zeroes up to four byte ranges (each starting 16-byte aligned) in one launch.
 struct ClearRanges {
     char* p[4];
@@ -1583,6 +1569,7 @@ struct BuildPlan {
     size_t hin_bytes = 0;
     char* hout = nullptr;
     size_t hout_bytes = 0;
+    std::vector<char> staged;  // the inputs last copied to jobs_dev / inj_dev (empty: none)
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t done = nullptr;  // recorded after the emission that last read the scratch
     // fork / join of the ranking passes' stream in the captured launch sequence
@@ -1620,6 +1607,7 @@ void plan_release(Ctx& ctx, BuildPlan* P) {
     if (P->hin) cudaFreeHost(P->hin);
     if (P->hout) cudaFreeHost(P->hout);
     P->hin = P->hout = nullptr;
+    P->staged.clear();
 }
 
 // Per-level table regions (consecutive, tcap[L] slots each) and the split
@@ -1742,35 +1730,6 @@ uint32_t plan_grid(const BuildPlan* P, uint64_t items, uint64_t per_block) {
     return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, P->max_grid));
 }
 
-// Launch of a build kernel.  `chained`: the kernel may be scheduled while its
-// predecessor in the stream drains (it waits for it at its start).
-// `cluster` > 0: one cluster of that many blocks.
-template <typename... Exp, typename... Act>
-cudaError_t launch_build(void (*kernel)(Exp...), uint32_t grid, uint32_t block, cudaStream_t st, bool chained,
-                         uint32_t cluster, Act&&... args) {
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(block);
-    cfg.stream = st;
-    cudaLaunchAttribute at[2];
-    uint32_t na = 0;
-    if (cluster) {
-        at[na].id = cudaLaunchAttributeClusterDimension;
-        at[na].val.clusterDim.x = cluster;
-        at[na].val.clusterDim.y = 1;
-        at[na].val.clusterDim.z = 1;
-        ++na;
-    }
-    if (chained) {
-        at[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        at[na].val.programmaticStreamSerializationAllowed = 1;
-        ++na;
-    }
-    cfg.attrs = at;
-    cfg.numAttrs = na;
-    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Act>(args)...);
-}
-
 // The largest cluster (16, else 8 blocks of 1024 threads) that both
 // small-level kernels can have resident on this device; 0 if none.
 int probe_cluster_blocks() {
@@ -1842,7 +1801,7 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
         uint64_t mx = 0;
         for (int k = 0; k < 4; ++k) mx = std::max<uint64_t>(mx, cr.n[k]);
         const uint32_t g = (uint32_t)std::min<uint64_t>((mx / 16 + kThreads - 1) / kThreads + 1, P->max_grid);
-        CPVS_CUDA(launch_build(k_clear, g, kThreads, st, false, 0, cr));
+        CPVS_CUDA(launch_kernel(k_clear, g, kThreads, st, false, 0, cr));
     }
     // top-down: the small top levels as one cluster (which also places the
     // roots), then one pass per level
@@ -1856,17 +1815,17 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
             sl.ninj[L] = (uint32_t)P->ninj[L];
             sl.cap[L] = (uint32_t)P->cap[L];
         }
-        CPVS_CUDA(launch_build(k_expand_cluster, (uint32_t)P->cluster_blocks, kClusterThreads, st, ch,
+        CPVS_CUDA(launch_kernel(k_expand_cluster, (uint32_t)P->cluster_blocks, kClusterThreads, st, ch,
                                (uint32_t)P->cluster_blocks, P->lvt, P->counts, P->jobs_dev, njobs, P->maxR, exp_lo,
                                P->inj_dev, sl, P->seg, err));
     } else {
         // the top level holds only roots
-        CPVS_CUDA(launch_build(k_init_top, 1, 256, st, ch, 0, P->lv[P->maxR], P->counts, P->maxR,
+        CPVS_CUDA(launch_kernel(k_init_top, 1, 256, st, ch, 0, P->lv[P->maxR], P->counts, P->maxR,
                                P->inj_dev + P->inj_off[P->maxR], (uint32_t)P->ninj[P->maxR]));
     }
     for (int L = std::min(exp_lo - 1, P->maxR); L > P->bottom; --L) {
         KernelTimer kt(tm, K_EXPAND_WRITE, st);
-        CPVS_CUDA(launch_build(k_expand_lb, plan_grid(P, P->cap[L], kExpTile), kThreads, st, ch, 0, P->lv[L],
+        CPVS_CUDA(launch_kernel(k_expand_lb, plan_grid(P, P->cap[L], kExpTile), kThreads, st, ch, 0, P->lv[L],
                                P->lv[L - 1], P->counts, P->jobs_dev, njobs, L, P->inj_dev + P->inj_off[L - 1],
                                (uint32_t)P->ninj[L - 1], P->seg, (uint32_t)P->cap[L - 1], P->tickets + L,
                                P->flags + P->exp_flag_off[L], err));
@@ -1874,11 +1833,11 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
     if (forked) CPVS_CUDA(cudaStreamWaitEvent(st, P->tables, 0));
     if (P->leafmasks) {
         KernelTimer kt(tm, K_LEAF_MASKS, st);
-        CPVS_CUDA(launch_build(k_leaf_insert, plan_grid(P, P->cap[2], kThreads), kThreads, st, ch, 0, P->lv[2],
+        CPVS_CUDA(launch_kernel(k_leaf_insert, plan_grid(P, P->cap[2], kThreads), kThreads, st, ch, 0, P->lv[2],
                                P->counts, P->jobs_dev, njobs, 2, P->seg, P->lv[2].table, P->lv[2].table_mask, err));
     } else {
         KernelTimer kt(tm, K_CLASSIFY_BOTTOM, st);
-        CPVS_CUDA(launch_build(k_classify_bottom, plan_grid(P, P->cap[0], kThreads), kThreads, st, ch, 0, P->lv[0],
+        CPVS_CUDA(launch_kernel(k_classify_bottom, plan_grid(P, P->cap[0], kThreads), kThreads, st, ch, 0, P->lv[0],
                                P->counts, P->jobs_dev, njobs, 0, P->seg, err));
     }
     // bottom-up: per level an insert and the ranking pass (on rank_st), then
@@ -1889,7 +1848,7 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
         const LevelDev child = (L > P->bottom) ? P->lv[L - 1] : P->lv[L];
         if (!leaf) {
             KernelTimer kt(tm, K_INSERT_INNER, st);
-            CPVS_CUDA(launch_build(k_dedup_insert<false>, plan_grid(P, P->cap[L], kThreads), kThreads, st, ch, 0,
+            CPVS_CUDA(launch_kernel(k_dedup_insert<false>, plan_grid(P, P->cap[L], kThreads), kThreads, st, ch, 0,
                                    P->lv[L], child, P->counts, L, P->lv[L].table, P->lv[L].table_mask, err));
         }
         if (forked) {
@@ -1911,7 +1870,7 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
     }
     if (merge_hi < P->maxR) {
         KernelTimer kt(tm, K_SCAN, st);
-        CPVS_CUDA(launch_build(k_merge_cluster, (uint32_t)P->cluster_blocks, kClusterThreads, st, ch,
+        CPVS_CUDA(launch_kernel(k_merge_cluster, (uint32_t)P->cluster_blocks, kClusterThreads, st, ch,
                                (uint32_t)P->cluster_blocks, P->lvt, P->counts, rv.level_u,
                                std::max(merge_hi + 1, P->bottom), P->maxR, P->bottom, P->leafmasks ? 2 : -1, P->seg,
                                err));
@@ -1923,8 +1882,8 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
     }
     {
         KernelTimer kt(tm, K_LAYOUT, st);
-        CPVS_CUDA(launch_build(k_layout, 1, 1024, st, ch, 0, P->seg, P->lay, P->root_dev, njobs, P->bottom));
-        CPVS_CUDA(launch_build(k_root_masks, (njobs + 255) / 256, 256, st, ch, 0, P->lvt, P->seg, P->root_dev, njobs,
+        CPVS_CUDA(launch_kernel(k_layout, 1, 1024, st, ch, 0, P->seg, P->lay, P->root_dev, njobs, P->bottom));
+        CPVS_CUDA(launch_kernel(k_root_masks, (njobs + 255) / 256, 256, st, ch, 0, P->lvt, P->seg, P->root_dev, njobs,
                                rv.root_mask));
     }
     CPVS_CUDA(cudaMemcpyAsync(P->hout, P->res, result_bytes(njobs), cudaMemcpyDeviceToHost, st));
@@ -2092,8 +2051,14 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
             const int R = (int)P->root_level[j];
             hi[P->inj_off[R] + fill[R]++] = Injected{pack_xyz(0, 0, 2 * jobs[j].z_idx), j, 0};
         }
-        CPVS_CUDA(cudaMemcpyAsync(P->jobs_dev, hj, njobs * sizeof(JobDev), cudaMemcpyHostToDevice, st));
-        CPVS_CUDA(cudaMemcpyAsync(P->inj_dev, hi, njobs * sizeof(Injected), cudaMemcpyHostToDevice, st));
+        // the device copies are read-only to the build: repeated builds of the
+        // same maps (same pyramid and map addresses) skip the two copies
+        const size_t staged_bytes = njobs * (sizeof(JobDev) + sizeof(Injected));
+        if (P->staged.size() != staged_bytes || std::memcmp(P->staged.data(), P->hin, staged_bytes) != 0) {
+            CPVS_CUDA(cudaMemcpyAsync(P->jobs_dev, hj, njobs * sizeof(JobDev), cudaMemcpyHostToDevice, st));
+            CPVS_CUDA(cudaMemcpyAsync(P->inj_dev, hi, njobs * sizeof(Injected), cudaMemcpyHostToDevice, st));
+            P->staged.assign(P->hin, P->hin + staged_bytes);
+        }
         if (ctx.timing.on) {
             cpvs_status r = plan_enqueue(P, st, nullptr, &ctx.timing);
             if (r != CPVS_OK) return r;

@@ -8,6 +8,47 @@
 
 namespace cpvs {
 
+// ------------------------------------------------------- chained launches
+// Programmatic dependent launch.  Kernels launched with `chained` set may be
+// scheduled while their predecessor in the stream drains; each such kernel
+// first waits until that predecessor has completed and its writes are
+// visible (a no-op when launched without the attribute), then lets its own
+// successor be scheduled.  Every chained kernel waits at its start, so
+// completion stays transitive along the chain.
+__device__ __forceinline__ void chain_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void chain_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void chain_enter() {
+    chain_wait();
+    chain_release();
+}
+
+// `cluster` > 0: one cluster of that many blocks.
+template <typename... Exp, typename... Act>
+inline cudaError_t launch_kernel(void (*kernel)(Exp...), uint32_t grid, uint32_t block, cudaStream_t st, bool chained,
+                                 uint32_t cluster, Act&&... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.stream = st;
+    cudaLaunchAttribute at[2];
+    uint32_t na = 0;
+    if (cluster) {
+        at[na].id = cudaLaunchAttributeClusterDimension;
+        at[na].val.clusterDim.x = cluster;
+        at[na].val.clusterDim.y = 1;
+        at[na].val.clusterDim.z = 1;
+        ++na;
+    }
+    if (chained) {
+        at[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[na].val.programmaticStreamSerializationAllowed = 1;
+        ++na;
+    }
+    cfg.attrs = at;
+    cfg.numAttrs = na;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<Act&&>(args)...);
+}
+
 // ---------------------------------------------------------------- classes
 // NodeVisibility (src/CompressedShadow.h:22-26).
 constexpr uint32_t kShadow = 0, kVisible = 1, kPartial = 2;

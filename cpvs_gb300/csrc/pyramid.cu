@@ -32,6 +32,7 @@ constexpr int kThreads = 256;
 template <bool FROM_DEPTH>
 __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ in, uint32_t S, float2* __restrict__ out,
                                                       uint32_t n, int L0, uint32_t T, float* __restrict__ copy) {
+    chain_enter();
     __shared__ float2 buf0[(kTile / 2) * (kTile / 2)];
     __shared__ float2 buf1[(kTile / 4) * (kTile / 4)];
     const uint32_t tiles_x = S / T;
@@ -105,6 +106,7 @@ __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ i
 __global__ void __launch_bounds__(kThreads)
     k_pyramid64(const float* __restrict__ in, uint32_t S, float2* __restrict__ out, uint32_t n,
                 float* __restrict__ copy) {
+    chain_enter();
     __shared__ float2 buf0[32 * 32];
     __shared__ float2 buf1[16 * 16];
     const uint32_t tiles_x = S >> 6;
@@ -209,14 +211,17 @@ cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaS
     while (S > 1) {
         const uint32_t T = S < (uint32_t)kTile ? S : (uint32_t)kTile;
         const uint32_t tiles = (S / T) * (S / T);
+        // chained: each pass may be scheduled while the work before it in
+        // the stream drains, and waits for it at its start
         if (first && T == (uint32_t)kTile)
-            k_pyramid64<<<tiles, kThreads, 0, st>>>(depth, S, levels, n, depth_copy);
+            CPVS_CUDA(launch_kernel(k_pyramid64, tiles, kThreads, st, true, 0, depth, S, levels, n, depth_copy));
         else if (first)
-            k_pyramid<true><<<tiles, kThreads, 0, st>>>(depth, S, levels, n, L0, T, depth_copy);
+            CPVS_CUDA(launch_kernel(k_pyramid<true>, tiles, kThreads, st, true, 0, static_cast<const void*>(depth), S,
+                                    levels, n, L0, T, depth_copy));
         else
-            k_pyramid<false><<<tiles, kThreads, 0, st>>>(levels + pyramid_level_offset(n, L0 - 1), S, levels, n, L0, T,
-                                                          nullptr);
-        CPVS_CUDA(cudaGetLastError());
+            CPVS_CUDA(launch_kernel(k_pyramid<false>, tiles, kThreads, st, true, 0,
+                                    static_cast<const void*>(levels + pyramid_level_offset(n, L0 - 1)), S, levels, n,
+                                    L0, T, static_cast<float*>(nullptr)));
         first = false;
         L0 += log2_u32(T);
         S /= T;
