@@ -986,6 +986,16 @@ __device__ __forceinline__ void load_child_ids(const LevelDev& child, uint32_t f
     for (uint32_t r = 0; r < 8; ++r) u[r] = r < k ? child_uid<CG>(child, f + r) : 0u;
 }
 
+// Signature hash of an inner node: job, child mask and the k child
+// identities in order.
+__device__ __forceinline__ uint64_t inner_hash(uint32_t j, uint32_t m, uint32_t k, const uint32_t u[8]) {
+    uint64_t h = fmix64((((uint64_t)j + 1) << 32 | m) ^ kGolden);
+#pragma unroll
+    for (uint32_t r = 0; r < 8; ++r)
+        if (r < k) h = fmix64(h ^ ((uint64_t)u[r] + (uint64_t)(r + 1) * kGolden));
+    return h;
+}
+
 template <bool CG>
 __device__ __forceinline__ void insert_inner(LevelDev& cur, const LevelDev& child, uint32_t i,
                                              unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
@@ -993,10 +1003,7 @@ __device__ __forceinline__ void insert_inner(LevelDev& cur, const LevelDev& chil
     const uint32_t k = partial_children(m);
     uint32_t u[8];
     load_child_ids<CG>(child, k ? cur.first[i] : 0u, k, u);
-    uint64_t h = fmix64((((uint64_t)j + 1) << 32 | m) ^ kGolden);
-#pragma unroll
-    for (uint32_t r = 0; r < 8; ++r)
-        if (r < k) h = fmix64(h ^ ((uint64_t)u[r] + (uint64_t)(r + 1) * kGolden));
+    const uint64_t h = inner_hash(j, m, k, u);
     const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | i;
     uint64_t s = h & cap_mask;
     bool placed = false;
@@ -1162,28 +1169,175 @@ __device__ __forceinline__ uint2 cluster_prefix(cg::cluster_group& cl, uint2 v, 
     return p;
 }
 
+// The topmost levels, while a level holds few enough nodes, run in the
+// cluster's first block alone with the level's node data in shared memory:
+// a level then costs one round of pyramid reads (expansion) or child reads
+// (merge) and a few block barriers, instead of several global round trips
+// and cluster barriers.  The merge keeps its hash table in shared memory;
+// every node's class slot there is also its slot in the level's global table
+// (the shared table is never larger), which receives the class's rank for
+// the emission.
+// Expansion: a level of at most kTopNodes nodes whose children fit in
+// kTopChildren runs in the first block (the children are gathered in shared
+// memory and written out coalesced); the first level that does not goes to
+// the cluster.  Merge: levels of at most kTopMergeNodes nodes.
+constexpr uint32_t kTopNodes = 2048;
+constexpr uint32_t kTopChildren = 8192;
+constexpr int kTopItems = kTopNodes / kClusterThreads;
+constexpr uint32_t kTopMergeNodes = 4096;
+constexpr int kTopMergeItems = kTopMergeNodes / kClusterThreads;
+constexpr uint32_t kTopTable = 2 * kTopMergeNodes;
+
+struct ExpandTopSmem {
+    uint64_t coord[2][kTopChildren];
+    uint32_t job[2][kTopChildren];
+    uint32_t mask[kTopNodes], first[kTopNodes];
+};
+struct MergeTopSmem {
+    unsigned long long table[kTopTable];
+    uint32_t mask[kTopMergeNodes], job[kTopMergeNodes], first[kTopMergeNodes];
+    uint32_t slot[2][kTopMergeNodes];
+};
+constexpr size_t kExpandClusterSmem = sizeof(ExpandTopSmem);
+constexpr size_t kMergeClusterSmem = sizeof(MergeTopSmem);
+
+// Expands levels Lhi, Lhi-1, ... (not below Llo) in one block, after placing
+// the roots of level Lhi, while a level fits (see above); writes the highest
+// level left to expand (Llo - 1 when none) to *next.
+__device__ __forceinline__ void expand_top(ExpandTopSmem& S, const LevelDev* __restrict__ lvt, uint32_t* counts,
+                                           const JobDev* __restrict__ jobs, uint32_t njobs, int Lhi, int Llo,
+                                           const Injected* __restrict__ inj_all, const SmallLevels& sl, SegDev seg,
+                                           uint32_t* err, uint32_t* sm, uint32_t* next) {
+    const uint32_t tid = threadIdx.x;
+    uint32_t n = sl.ninj[Lhi];
+    {
+        LevelDev top = lvt[Lhi];
+        const Injected* inj = inj_all + sl.inj_off[Lhi];
+        for (uint32_t r = tid; r < n; r += blockDim.x) {
+            const Injected q = inj[r];
+            top.coord[r] = q.coord;
+            top.job[r] = q.job;
+            if (r < kTopChildren) {
+                S.coord[0][r] = q.coord;
+                S.job[0][r] = q.job;
+            }
+        }
+        if (tid == 0) counts[Lhi] = n;
+    }
+    __syncthreads();
+    int b = 0, L = Lhi;
+    for (; L >= Llo && n <= kTopNodes; --L) {
+        LevelDev cur = lvt[L], nxt = lvt[L - 1];
+        // classification: node_mask (src/CompressedShadow.cpp:270-315)
+        bool bad_job = false, bad_node = false;
+#pragma unroll
+        for (int it = 0; it < kTopItems; ++it) {
+            const uint32_t i = tid + it * kClusterThreads;
+            if (i < n) {
+                const uint32_t j = S.job[b][i];
+                uint32_t m = 0;
+                if (j < njobs) {
+                    m = node_mask_nf(jobs[j], L, S.coord[b][i], bad_node);
+                } else {
+                    bad_job = true;
+                    S.job[b][i] = 0;
+                    cur.job[i] = 0;
+                }
+                S.mask[i] = m;
+            }
+        }
+        if (bad_job) atomicOr(err, 8u);
+        if (bad_node) atomicOr(err, 4u);
+        __syncthreads();
+        // children in node order: consecutive nodes per thread
+        const uint32_t i0 = tid * kTopItems;
+        uint32_t ksum = 0;
+#pragma unroll
+        for (int it = 0; it < kTopItems; ++it) ksum += i0 + it < n ? partial_children(S.mask[i0 + it]) : 0u;
+        uint2 tot;
+        const uint32_t pre = block_exclusive_scan2(make_uint2(ksum, 0u), tot, sm).x;
+        const uint32_t ninj = sl.ninj[L - 1], cap_next = sl.cap[L - 1];
+        const uint32_t total = ninj + tot.x;
+        if (total > kTopChildren) break;  // uniform: the cluster takes this level
+        uint32_t f = ninj + pre;
+#pragma unroll
+        for (int it = 0; it < kTopItems; ++it) {
+            const uint32_t i = i0 + it;
+            if (i < n) {
+                uint32_t m = S.mask[i];
+                const uint32_t k = partial_children(m);
+                if (f + k > cap_next) {
+                    atomicOr(err, 1u);  // more children than the level holds: not written, reported
+                    S.mask[i] = m & 0x5555u;
+                    S.first[i] = 0;
+                } else {
+                    S.first[i] = f;
+                    const uint64_t c = S.coord[b][i];
+                    const uint32_t j = S.job[b][i];
+                    const uint32_t x = unpack_x(c), y = unpack_y(c), z = unpack_z(c);
+                    uint32_t r = 0;
+                    for (uint32_t ch = 0; ch < 8; ++ch)
+                        if (m & (2u << (2u * ch))) {
+                            // cs::getChildCoordinates (src/CompressedShadowUtil.cpp:101-117)
+                            S.coord[b ^ 1][f + r] =
+                                pack_xyz((x + (ch & 1u)) * 2u, (y + ((ch >> 1) & 1u)) * 2u, (z + (ch >> 2)) * 2u);
+                            S.job[b ^ 1][f + r] = j;
+                            ++r;
+                        }
+                }
+                f += k;
+            }
+        }
+        const Injected* inj = inj_all + sl.inj_off[L - 1];
+        for (uint32_t r = tid; r < ninj; r += blockDim.x) {
+            const Injected q = inj[r];
+            S.coord[b ^ 1][r] = q.coord;
+            S.job[b ^ 1][r] = q.job;
+        }
+        __syncthreads();
+        // the level's node data and the children, coalesced
+        for (uint32_t i = tid; i < n; i += blockDim.x) {
+            const uint32_t j = S.job[b][i];
+            cur.mask[i] = S.mask[i];
+            cur.first[i] = S.first[i];
+            if (i == 0 || S.job[b][i - 1] != j) seg.nstart[seg_index(j, L)] = i;
+            if (i == n - 1 || S.job[b][i + 1] != j) seg.nend[seg_index(j, L)] = i + 1;
+        }
+        const uint32_t nn = total < cap_next ? total : cap_next;
+        for (uint32_t c = tid; c < nn; c += blockDim.x) {
+            nxt.coord[c] = S.coord[b ^ 1][c];
+            nxt.job[c] = S.job[b ^ 1][c];
+        }
+        if (tid == 0) {
+            if (total > cap_next) atomicOr(err, 1u);
+            counts[L - 1] = nn;
+        }
+        n = nn;
+        b ^= 1;
+        __syncthreads();
+    }
+    if (tid == 0) *next = (uint32_t)L;
+}
+
 // Expansion of levels Lhi (whose roots this kernel writes) down to Llo, each
-// into the level below it.
+// into the level below it: the topmost in the first block alone, the rest
+// across the cluster.
 __global__ void __launch_bounds__(kClusterThreads, 1)
     k_expand_cluster(const LevelDev* __restrict__ lvt, uint32_t* counts, const JobDev* __restrict__ jobs,
                      uint32_t njobs, int Lhi, int Llo, const Injected* __restrict__ inj_all, SmallLevels sl,
-                     SegDev seg, uint32_t* err) {
+                     SegDev seg, uint32_t* top_next, uint32_t* err) {
     chain_enter();
     cg::cluster_group cl = cg::this_cluster();
     const uint32_t nb = cl.num_blocks(), rank = cl.block_rank();
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
     __shared__ uint32_t sm[64];
     __shared__ uint2 s_tot[kClusterMaxBlocks];
-    if (rank == 0) {
-        LevelDev top = lvt[Lhi];
-        const Injected* inj = inj_all + sl.inj_off[Lhi];
-        for (uint32_t r = threadIdx.x; r < sl.ninj[Lhi]; r += blockDim.x) {
-            top.coord[r] = inj[r].coord;
-            top.job[r] = inj[r].job;
-        }
-        if (threadIdx.x == 0) counts[Lhi] = sl.ninj[Lhi];
-    }
+    if (rank == 0)
+        expand_top(*reinterpret_cast<ExpandTopSmem*>(dyn_smem), lvt, counts, jobs, njobs, Lhi, Llo, inj_all, sl, seg,
+                   err, sm, top_next);
     cl.sync();
-    for (int L = Lhi; L >= Llo; --L) {
+    const int Lstart = (int)__ldcg(top_next);
+    for (int L = Lstart; L >= Llo; --L) {
         LevelDev cur = lvt[L], nxt = lvt[L - 1];
         const uint32_t n = __ldcg(counts + L);
         const uint32_t per = (n + nb - 1) / nb;
@@ -1268,17 +1422,153 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
     }
 }
 
+// Merge of levels Llo..Lhi in one block (each level at most kTopMergeNodes
+// nodes): insert into the shared table (the leaf level was inserted into its
+// global table by the leaf kernel), then ranks and word offsets in node
+// order, as the multi-block passes compute them.
+__device__ __forceinline__ void merge_top(MergeTopSmem& S, const LevelDev* __restrict__ lvt, const uint32_t* __restrict__ counts,
+                          uint32_t* level_u, int Llo, int Lhi, int bottom, int leaf_level, SegDev seg, uint32_t* err,
+                          uint32_t* sm) {
+    const uint32_t tid = threadIdx.x;
+    int cb = 0;               // S.slot[cb]: class slots of the level below, when it ran here
+    bool child_here = false;
+    for (int L = Llo; L <= Lhi; ++L) {
+        LevelDev cur = lvt[L];
+        const LevelDev child = L > bottom ? lvt[L - 1] : lvt[L];
+        const bool leaf = L == leaf_level;
+        const uint32_t n = __ldcg(counts + L);
+        uint32_t* my_slot = S.slot[cb ^ 1];
+        const uint32_t* child_slot = S.slot[cb];
+        uint32_t T = 64;
+        while (T < 2 * n && T < kTopTable) T <<= 1;
+        if (T > cur.table_mask + 1) T = (uint32_t)(cur.table_mask + 1);
+        for (uint32_t i = tid; i < n; i += blockDim.x) {
+            S.mask[i] = __ldcg(cur.mask + i);
+            S.job[i] = __ldcg(cur.job + i);
+            if (!leaf) S.first[i] = __ldcg(cur.first + i);
+            else my_slot[i] = __ldcg(cur.slot + i);
+        }
+        if (!leaf)
+            for (uint32_t s = tid; s < T; s += blockDim.x) S.table[s] = kEmptySlot;
+        __syncthreads();
+        if (!leaf) {
+            for (uint32_t i = tid; i < n; i += blockDim.x) {
+                const uint32_t m = S.mask[i], j = S.job[i], k = partial_children(m);
+                const uint32_t f = k ? S.first[i] : 0u;
+                uint32_t u[8];
+#pragma unroll
+                for (uint32_t r = 0; r < 8; ++r)
+                    u[r] = r < k ? (child_here ? child_slot[f + r] : __ldcg(child.slot + f + r)) : 0u;
+                const uint64_t h = inner_hash(j, m, k, u);
+                const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | i;
+                uint32_t s = (uint32_t)h & (T - 1);
+                bool placed = false;
+                for (uint32_t probe = 0; probe < T; ++probe) {
+                    unsigned long long e = *reinterpret_cast<volatile unsigned long long*>(S.table + s);
+                    if (e == kEmptySlot) {
+                        const unsigned long long prev = atomicCAS(S.table + s, kEmptySlot, key);
+                        if (prev == kEmptySlot) {
+                            placed = true;
+                            break;
+                        }
+                        e = prev;
+                    }
+                    if ((e >> 32) == (key >> 32)) {
+                        const uint32_t bn = (uint32_t)e;
+                        bool same = S.job[bn] == j && S.mask[bn] == m;
+                        if (same && k) {
+                            const uint32_t fb = S.first[bn];
+#pragma unroll
+                            for (uint32_t r = 0; r < 8; ++r)
+                                if (r < k)
+                                    same = same && u[r] == (child_here ? child_slot[fb + r]
+                                                                       : __ldcg(child.slot + fb + r));
+                        }
+                        if (same) {
+                            if (bn > i) atomicMin(S.table + s, key);
+                            placed = true;
+                            break;
+                        }
+                    }
+                    s = (s + 1) & (T - 1);
+                }
+                if (!placed) atomicOr(err, 16u);  // table full: the result is void, reported
+                my_slot[i] = s;
+            }
+            __syncthreads();
+        }
+        // kept nodes (first occurrences) in node order: consecutive nodes per thread
+        const uint32_t i0 = tid * kTopMergeItems;
+        uint32_t kept = 0, cnt = 0, words = 0, rep[kTopMergeItems];
+#pragma unroll
+        for (int it = 0; it < kTopMergeItems; ++it) {
+            const uint32_t i = i0 + it;
+            rep[it] = ~0u;
+            if (i < n) {
+                const uint32_t s = my_slot[i];
+                rep[it] = leaf ? __ldcg(reinterpret_cast<const uint32_t*>(cur.table + s)) : (uint32_t)S.table[s];
+                if (rep[it] == i) {
+                    kept |= 1u << it;
+                    ++cnt;
+                    words += node_words(S.mask[i], leaf);
+                }
+            }
+        }
+        uint2 tot;
+        const uint2 pre = block_exclusive_scan2(make_uint2(cnt, words), tot, sm);
+        uint32_t qx = pre.x, qy = pre.y;
+#pragma unroll
+        for (int it = 0; it < kTopMergeItems; ++it) {
+            const uint32_t i = i0 + it;
+            if (i >= n) break;
+            const uint32_t j = S.job[i], s = my_slot[i];
+            if (i == 0 || S.job[i - 1] != j) {
+                seg.ustart[seg_index(j, L)] = qx;
+                seg.wstart[seg_index(j, L)] = qy;
+            }
+            if (!leaf) cur.slot[i] = s;
+            if (kept & (1u << it)) {
+                cur.uniq[qx] = i;
+                cur.woff[qx] = qy;
+                if (leaf)
+                    reinterpret_cast<uint32_t*>(cur.table + s)[1] = qx;  // upper half: the rank
+                else
+                    cur.table[s] = ((unsigned long long)qx << 32) | rep[it];
+                ++qx;
+                qy += node_words(S.mask[i], leaf);
+            }
+            if (i == n - 1 || S.job[i + 1] != j) {
+                seg.uend[seg_index(j, L)] = qx;
+                seg.wend[seg_index(j, L)] = qy;
+            }
+        }
+        if (tid == 0) {
+            level_u[2 * L] = tot.x;
+            level_u[2 * L + 1] = tot.y;
+        }
+        __syncthreads();
+        cb ^= 1;
+        child_here = true;
+    }
+}
+
 // Merge of levels Llo..Lhi (insert, then ranks and offsets); the leaf level
-// (leaf_level, or -1) was inserted by k_leaf_insert.
+// (leaf_level, or -1) was inserted by k_leaf_insert.  The lower levels run
+// across the cluster, the topmost (each at most kTopMergeNodes nodes) in the
+// first block alone.
 __global__ void __launch_bounds__(kClusterThreads, 1)
     k_merge_cluster(const LevelDev* __restrict__ lvt, const uint32_t* __restrict__ counts, uint32_t* level_u,
                     int Llo, int Lhi, int bottom, int leaf_level, SegDev seg, uint32_t* err) {
     chain_enter();
     cg::cluster_group cl = cg::this_cluster();
     const uint32_t nb = cl.num_blocks(), rank = cl.block_rank();
+    extern __shared__ __align__(16) unsigned char dyn_smem[];
     __shared__ uint32_t sm[64];
     __shared__ uint2 s_tot[kClusterMaxBlocks];
-    for (int L = Llo; L <= Lhi; ++L) {
+    // counts are final here (the expansion has completed)
+    int Ltop = Lhi + 1;
+    while (Ltop - 1 >= Llo && counts[Ltop - 1] <= kTopMergeNodes) --Ltop;
+    for (int L = Llo; L < Ltop; ++L) {
         LevelDev cur = lvt[L];
         const LevelDev child = L > bottom ? lvt[L - 1] : lvt[L];
         const bool leaf = L == leaf_level;
@@ -1338,8 +1628,11 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
             level_u[2 * L] = ctot.x;
             level_u[2 * L + 1] = ctot.y;
         }
-        cl.sync();  // identities visible to the level above
+        cl.sync();  // class slots visible to the level above
     }
+    if (rank == 0 && Ltop <= Lhi)
+        merge_top(*reinterpret_cast<MergeTopSmem*>(dyn_smem), lvt, counts, level_u, Ltop, Lhi, bottom, leaf_level, seg,
+                  err, sm);
 }
 
 // ------------------------------------------------------------------ layout
@@ -1579,7 +1872,7 @@ struct BuildPlan {
     // kernels; look-back tickets and flags (zeroed by every build)
     int small_lo = CPVS_MAX_LEVELS;
     int cluster_blocks = 0;  // blocks of the small-level cluster kernels (0: none)
-    unsigned int* tickets = nullptr;     // [2 * L_MAX]
+    unsigned int* tickets = nullptr;     // [2 * L_MAX + 1]
     unsigned long long* flags = nullptr;
     uint64_t flags_count = 0;
     uint64_t exp_flag_off[CPVS_MAX_LEVELS] = {0}, scan_flag_off[CPVS_MAX_LEVELS] = {0};
@@ -1664,7 +1957,7 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
         P->scan_flag_off[L] = P->flags_count;
         P->flags_count += P->scan_tiles_cap[L];
     }
-    add(2 * CPVS_MAX_LEVELS, 4);
+    add(2 * CPVS_MAX_LEVELS + 1, 4);
     add(P->flags_count, 8);
     P->arena_bytes = bytes;
     cpvs_status r = ctx.alloc((void**)&P->arena, bytes, true, st);
@@ -1704,7 +1997,7 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
     P->root_dev = A.take<uint32_t>(njobs);
     P->jobs_dev = A.take<JobDev>(njobs);
     P->inj_dev = A.take<Injected>(njobs);
-    P->tickets = A.take<unsigned int>(2 * CPVS_MAX_LEVELS);
+    P->tickets = A.take<unsigned int>(2 * CPVS_MAX_LEVELS + 1);  // + the expansion's first cluster level
     P->flags = A.take<unsigned long long>(P->flags_count);
     plan_bind_tables(P);
     // the device results region carries SegDev's arrays, so the six segment
@@ -1735,6 +2028,13 @@ uint32_t plan_grid(const BuildPlan* P, uint64_t items, uint64_t per_block) {
 int probe_cluster_blocks() {
     cudaFuncSetAttribute(k_expand_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     cudaFuncSetAttribute(k_merge_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (cudaFuncSetAttribute(k_expand_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kExpandClusterSmem) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(k_merge_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMergeClusterSmem) !=
+            cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
     cudaGetLastError();
     for (int nb : {16, 8}) {
         cudaLaunchConfig_t cfg{};
@@ -1748,8 +2048,10 @@ int probe_cluster_blocks() {
         cfg.attrs = at;
         cfg.numAttrs = 1;
         int a = 0, b = 0;
-        const bool ok = cudaOccupancyMaxActiveClusters(&a, k_expand_cluster, &cfg) == cudaSuccess && a > 0 &&
-                        cudaOccupancyMaxActiveClusters(&b, k_merge_cluster, &cfg) == cudaSuccess && b > 0;
+        cfg.dynamicSmemBytes = kExpandClusterSmem;
+        bool ok = cudaOccupancyMaxActiveClusters(&a, k_expand_cluster, &cfg) == cudaSuccess && a > 0;
+        cfg.dynamicSmemBytes = kMergeClusterSmem;
+        ok = ok && cudaOccupancyMaxActiveClusters(&b, k_merge_cluster, &cfg) == cudaSuccess && b > 0;
         cudaGetLastError();
         if (ok) return nb;
     }
@@ -1801,7 +2103,7 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
         uint64_t mx = 0;
         for (int k = 0; k < 4; ++k) mx = std::max<uint64_t>(mx, cr.n[k]);
         const uint32_t g = (uint32_t)std::min<uint64_t>((mx / 16 + kThreads - 1) / kThreads + 1, P->max_grid);
-        CPVS_CUDA(launch_kernel(k_clear, g, kThreads, st, false, 0, cr));
+        CPVS_CUDA(launch_kernel(k_clear, g, kThreads, 0, st, false, 0, cr));
     }
     // top-down: the small top levels as one cluster (which also places the
     // roots), then one pass per level
@@ -1815,17 +2117,17 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
             sl.ninj[L] = (uint32_t)P->ninj[L];
             sl.cap[L] = (uint32_t)P->cap[L];
         }
-        CPVS_CUDA(launch_kernel(k_expand_cluster, (uint32_t)P->cluster_blocks, kClusterThreads, st, ch,
+        CPVS_CUDA(launch_kernel(k_expand_cluster, (uint32_t)P->cluster_blocks, kClusterThreads, kExpandClusterSmem, st, ch,
                                (uint32_t)P->cluster_blocks, P->lvt, P->counts, P->jobs_dev, njobs, P->maxR, exp_lo,
-                               P->inj_dev, sl, P->seg, err));
+                               P->inj_dev, sl, P->seg, P->tickets + 2 * CPVS_MAX_LEVELS, err));
     } else {
         // the top level holds only roots
-        CPVS_CUDA(launch_kernel(k_init_top, 1, 256, st, ch, 0, P->lv[P->maxR], P->counts, P->maxR,
+        CPVS_CUDA(launch_kernel(k_init_top, 1, 256, 0, st, ch, 0, P->lv[P->maxR], P->counts, P->maxR,
                                P->inj_dev + P->inj_off[P->maxR], (uint32_t)P->ninj[P->maxR]));
     }
     for (int L = std::min(exp_lo - 1, P->maxR); L > P->bottom; --L) {
         KernelTimer kt(tm, K_EXPAND_WRITE, st);
-        CPVS_CUDA(launch_kernel(k_expand_lb, plan_grid(P, P->cap[L], kExpTile), kThreads, st, ch, 0, P->lv[L],
+        CPVS_CUDA(launch_kernel(k_expand_lb, plan_grid(P, P->cap[L], kExpTile), kThreads, 0, st, ch, 0, P->lv[L],
                                P->lv[L - 1], P->counts, P->jobs_dev, njobs, L, P->inj_dev + P->inj_off[L - 1],
                                (uint32_t)P->ninj[L - 1], P->seg, (uint32_t)P->cap[L - 1], P->tickets + L,
                                P->flags + P->exp_flag_off[L], err));
@@ -1833,11 +2135,11 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
     if (forked) CPVS_CUDA(cudaStreamWaitEvent(st, P->tables, 0));
     if (P->leafmasks) {
         KernelTimer kt(tm, K_LEAF_MASKS, st);
-        CPVS_CUDA(launch_kernel(k_leaf_insert, plan_grid(P, P->cap[2], kThreads), kThreads, st, ch, 0, P->lv[2],
+        CPVS_CUDA(launch_kernel(k_leaf_insert, plan_grid(P, P->cap[2], kThreads), kThreads, 0, st, ch, 0, P->lv[2],
                                P->counts, P->jobs_dev, njobs, 2, P->seg, P->lv[2].table, P->lv[2].table_mask, err));
     } else {
         KernelTimer kt(tm, K_CLASSIFY_BOTTOM, st);
-        CPVS_CUDA(launch_kernel(k_classify_bottom, plan_grid(P, P->cap[0], kThreads), kThreads, st, ch, 0, P->lv[0],
+        CPVS_CUDA(launch_kernel(k_classify_bottom, plan_grid(P, P->cap[0], kThreads), kThreads, 0, st, ch, 0, P->lv[0],
                                P->counts, P->jobs_dev, njobs, 0, P->seg, err));
     }
     // bottom-up: per level an insert and the ranking pass (on rank_st), then
@@ -1848,7 +2150,7 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
         const LevelDev child = (L > P->bottom) ? P->lv[L - 1] : P->lv[L];
         if (!leaf) {
             KernelTimer kt(tm, K_INSERT_INNER, st);
-            CPVS_CUDA(launch_kernel(k_dedup_insert<false>, plan_grid(P, P->cap[L], kThreads), kThreads, st, ch, 0,
+            CPVS_CUDA(launch_kernel(k_dedup_insert<false>, plan_grid(P, P->cap[L], kThreads), kThreads, 0, st, ch, 0,
                                    P->lv[L], child, P->counts, L, P->lv[L].table, P->lv[L].table_mask, err));
         }
         if (forked) {
@@ -1870,7 +2172,7 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
     }
     if (merge_hi < P->maxR) {
         KernelTimer kt(tm, K_SCAN, st);
-        CPVS_CUDA(launch_kernel(k_merge_cluster, (uint32_t)P->cluster_blocks, kClusterThreads, st, ch,
+        CPVS_CUDA(launch_kernel(k_merge_cluster, (uint32_t)P->cluster_blocks, kClusterThreads, kMergeClusterSmem, st, ch,
                                (uint32_t)P->cluster_blocks, P->lvt, P->counts, rv.level_u,
                                std::max(merge_hi + 1, P->bottom), P->maxR, P->bottom, P->leafmasks ? 2 : -1, P->seg,
                                err));
@@ -1882,8 +2184,8 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
     }
     {
         KernelTimer kt(tm, K_LAYOUT, st);
-        CPVS_CUDA(launch_kernel(k_layout, 1, 1024, st, ch, 0, P->seg, P->lay, P->root_dev, njobs, P->bottom));
-        CPVS_CUDA(launch_kernel(k_root_masks, (njobs + 255) / 256, 256, st, ch, 0, P->lvt, P->seg, P->root_dev, njobs,
+        CPVS_CUDA(launch_kernel(k_layout, 1, 1024, 0, st, ch, 0, P->seg, P->lay, P->root_dev, njobs, P->bottom));
+        CPVS_CUDA(launch_kernel(k_root_masks, (njobs + 255) / 256, 256, 0, st, ch, 0, P->lvt, P->seg, P->root_dev, njobs,
                                rv.root_mask));
     }
     CPVS_CUDA(cudaMemcpyAsync(P->hout, P->res, result_bytes(njobs), cudaMemcpyDeviceToHost, st));

@@ -22,13 +22,15 @@ __device__ __forceinline__ void chain_enter() {
     chain_release();
 }
 
-// `cluster` > 0: one cluster of that many blocks.
+// `smem`: dynamic shared memory bytes; `cluster` > 0: one cluster of that
+// many blocks.
 template <typename... Exp, typename... Act>
-inline cudaError_t launch_kernel(void (*kernel)(Exp...), uint32_t grid, uint32_t block, cudaStream_t st, bool chained,
-                                 uint32_t cluster, Act&&... args) {
+inline cudaError_t launch_kernel(void (*kernel)(Exp...), uint32_t grid, uint32_t block, size_t smem, cudaStream_t st,
+                                 bool chained, uint32_t cluster, Act&&... args) {
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute at[2];
     uint32_t na = 0;

@@ -214,12 +214,12 @@ cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaS
         // chained: each pass may be scheduled while the work before it in
         // the stream drains, and waits for it at its start
         if (first && T == (uint32_t)kTile)
-            CPVS_CUDA(launch_kernel(k_pyramid64, tiles, kThreads, st, true, 0, depth, S, levels, n, depth_copy));
+            CPVS_CUDA(launch_kernel(k_pyramid64, tiles, kThreads, 0, st, true, 0, depth, S, levels, n, depth_copy));
         else if (first)
-            CPVS_CUDA(launch_kernel(k_pyramid<true>, tiles, kThreads, st, true, 0, static_cast<const void*>(depth), S,
+            CPVS_CUDA(launch_kernel(k_pyramid<true>, tiles, kThreads, 0, st, true, 0, static_cast<const void*>(depth), S,
                                     levels, n, L0, T, depth_copy));
         else
-            CPVS_CUDA(launch_kernel(k_pyramid<false>, tiles, kThreads, st, true, 0,
+            CPVS_CUDA(launch_kernel(k_pyramid<false>, tiles, kThreads, 0, st, true, 0,
                                     static_cast<const void*>(levels + pyramid_level_offset(n, L0 - 1)), S, levels, n,
                                     L0, T, static_cast<float*>(nullptr)));
         first = false;
