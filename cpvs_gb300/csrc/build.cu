@@ -323,9 +323,13 @@ __global__ void __launch_bounds__(kThreads)
 //   fl_down(8 w + 1.5 * 2^23): the unit in the last place there is 1, so
 //       the sum is 1.5 * 2^23 + floor(8 w) and its bit pattern is
 //       0x4B400000 + count (count in the low four bits).
-__device__ __forceinline__ uint32_t lit_count_bits(float v, float c8) {
+// `s` is 0.125 for v = fl(d * H0).  When H0 is a power of two, d * H0 is
+// exact (a power-of-two scaling neither rounds nor, for H0 >= 1,
+// underflows; an overflow to infinity saturates alike), so the raw depth d
+// with s = H0 / 8 gives the same fused result without the product.
+__device__ __forceinline__ uint32_t lit_count_bits(float v, float s, float c8) {
     float w;
-    asm("fma.rm.sat.f32 %0, %1, %2, %3;" : "=f"(w) : "f"(v), "f"(0.125f), "f"(c8));
+    asm("fma.rm.sat.f32 %0, %1, %2, %3;" : "=f"(w) : "f"(v), "f"(s), "f"(c8));
     return __float_as_uint(__fmaf_rd(w, 8.0f, 12582912.0f));
 }
 constexpr uint32_t kCountBias = 0x4B400000u;
@@ -344,6 +348,26 @@ __device__ __forceinline__ uint32_t nibbles_to_planes(uint32_t w) {
     return delta_swap(w, 0x0000f0f0u, 12);
 }
 
+// Per texel row of a leaf: the eight lit counts, as nibbles, transposed into
+// count bit-planes (byte b = bit b of the row's eight counts).
+template <bool POW2>
+__device__ __forceinline__ void leaf_rows(const float* row0, uint32_t nmap, float H, float c8, uint32_t R[8]) {
+    const float s = POW2 ? __fmul_rn(H, 0.125f) : 0.125f;
+#pragma unroll
+    for (int y = 0; y < 8; ++y) {
+        const float4 a = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap));
+        const float4 b = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap + 4));
+        const float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        uint32_t w = 0;
+#pragma unroll
+        for (int x = 0; x < 8; ++x) w += lit_count_bits(POW2 ? v[x] : __fmul_rn(v[x], H), s, c8) << (4 * x);
+        // every term carried kCountBias above its nibble: remove them all
+        constexpr uint32_t bias = kCountBias + (kCountBias << 4) + (kCountBias << 8) + (kCountBias << 12) +
+                                  (kCountBias << 16) + (kCountBias << 20) + (kCountBias << 24) + (kCountBias << 28);
+        R[y] = nibbles_to_planes(w - bias);
+    }
+}
+
 // The eight 64-bit slice masks of leaf i (level-2 node: the 8x8x8 voxels at
 // 4 * its coordinate), its 16-bit class mask (01 lit / 00 shadow / 10
 // partial per slice, src/CompressedShadowUtil.cpp:59-99) and its signature
@@ -351,6 +375,7 @@ __device__ __forceinline__ uint32_t nibbles_to_planes(uint32_t w) {
 // into count bit-planes; slice s is then {texels with count > s}.  Returns
 // false for a stale slot (an internal check already failed): the caller
 // then treats it as an empty leaf of job 0.
+template <bool POW2>
 __device__ __forceinline__ bool leaf_compute(const LevelDev& lv, const JobDev* __restrict__ jobs, uint32_t njobs,
                                              uint32_t i, uint64_t M[8], uint32_t& mask, uint64_t& hash,
                                              uint32_t& j) {
@@ -366,23 +391,11 @@ __device__ __forceinline__ bool leaf_compute(const LevelDev& lv, const JobDev* _
         return false;
     }
     const uint32_t nmap = __ldg(&jobs[j].n);
-    const float H = __uint2float_rn(nmap * __ldg(&jobs[j].z_num));
+    const uint32_t Hu = nmap * __ldg(&jobs[j].z_num);
     const float c8 = __fmul_rn(__fsub_rn(0.5f, __uint2float_rn(bz)), 0.125f);  // exact: bz < 2^23
     const float* row0 = jobs[j].depth + (size_t)by * nmap + bx;
     uint32_t R[8];  // per row: byte b = count bit b of the row's 8 texels
-#pragma unroll
-    for (int y = 0; y < 8; ++y) {
-        const float4 a = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap));
-        const float4 b = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap + 4));
-        const float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-        uint32_t w = 0;
-#pragma unroll
-        for (int x = 0; x < 8; ++x) w += lit_count_bits(__fmul_rn(v[x], H), c8) << (4 * x);
-        // every term carried kCountBias above its nibble: remove them all
-        constexpr uint32_t bias = kCountBias + (kCountBias << 4) + (kCountBias << 8) + (kCountBias << 12) +
-                                  (kCountBias << 16) + (kCountBias << 20) + (kCountBias << 24) + (kCountBias << 28);
-        R[y] = nibbles_to_planes(w - bias);
-    }
+    leaf_rows<POW2>(row0, nmap, __uint2float_rn(Hu), c8, R);
     // gather byte b of rows 0..7 into plane b (row y at byte y): 4x4 byte
     // transposes of rows 0..3 and 4..7
     uint32_t plo[4], phi[4];
@@ -442,7 +455,7 @@ __global__ void __launch_bounds__(kThreads)
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint64_t M[8], h;
         uint32_t mask, j;
-        const bool ok = leaf_compute(lv, jobs, njobs, i, M, mask, h, j);
+        const bool ok = leaf_compute<false>(lv, jobs, njobs, i, M, mask, h, j);
         store_slices(lv, i, M);
         lv.mask[i] = mask;
         lv.hash[i] = h;
@@ -470,6 +483,7 @@ __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long lon
 // majority: c. 7.9 M leaves fold into 137 k classes at 8192^2) writes only
 // its class mask and slot.  The slot rule is dedup_insert's: it ends with
 // the class's smallest index, the first occurrence.
+template <bool POW2>
 __global__ void __launch_bounds__(kThreads, 5)
     k_leaf_insert(LevelDev lv, const uint32_t* __restrict__ counts, const JobDev* __restrict__ jobs, uint32_t njobs,
                   int L, SegDev seg, unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
@@ -478,7 +492,7 @@ __global__ void __launch_bounds__(kThreads, 5)
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint64_t M[8], h;
         uint32_t mask, j;
-        if (!leaf_compute(lv, jobs, njobs, i, M, mask, h, j)) {
+        if (!leaf_compute<POW2>(lv, jobs, njobs, i, M, mask, h, j)) {
             atomicOr(err, 4u);
             lv.job[i] = 0;
         } else {
@@ -1757,13 +1771,21 @@ __global__ void __launch_bounds__(kThreads)
         uint32_t* dst = out + at;
         dst[0] = m;
         if (leaf) {
+            // the eight slices as four 16-byte loads, all issued first
+            const ulonglong2* sp = reinterpret_cast<const ulonglong2*>(cur.slices + (size_t)i * 8);
+            uint64_t v[8];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const ulonglong2 t = sp[q];
+                v[2 * q] = t.x;
+                v[2 * q + 1] = t.y;
+            }
             uint32_t r = 0;
 #pragma unroll
             for (uint32_t q = 0; q < 8; ++q)
                 if (((m >> (2u * q)) & 3u) == kPartial) {
-                    const uint64_t v = cur.slices[(size_t)i * 8 + q];
-                    dst[1 + 2 * r] = (uint32_t)v;
-                    dst[2 + 2 * r] = (uint32_t)(v >> 32);
+                    dst[1 + 2 * r] = (uint32_t)v[q];
+                    dst[2 + 2 * r] = (uint32_t)(v[q] >> 32);
                     ++r;
                 }
         } else {
@@ -1773,7 +1795,15 @@ __global__ void __launch_bounds__(kThreads)
                 const uint32_t f = cur.first[i];
                 const uint32_t sc = seg_index(j, L - 1);
                 const uint32_t cb = lay.base[sc] - seg.wstart[sc];
-                for (uint32_t r = 0; r < k; ++r) dst[1 + r] = cb + child.woff[rank_of(child, f + r)];
+                // the children's slots, ranks and offsets, each as independent loads
+                uint32_t x[8];
+#pragma unroll
+                for (uint32_t r = 0; r < 8; ++r) x[r] = r < k ? child.slot[f + r] : 0u;
+#pragma unroll
+                for (uint32_t r = 0; r < 8; ++r) x[r] = r < k ? (uint32_t)(__ldcg(child.table + x[r]) >> 32) : 0u;
+#pragma unroll
+                for (uint32_t r = 0; r < 8; ++r)
+                    if (r < k) dst[1 + r] = cb + child.woff[x[r]];
             }
         }
     }
@@ -1834,6 +1864,7 @@ inline ResultView result_view(char* base, uint32_t njobs) {
 // long as the data fit its capacities; otherwise rebuilt larger.
 struct BuildPlan {
     bool leafmasks = false;
+    bool pow2 = false;  // every job's level-0 height (map side x z tiles) is a power of two
     int bottom = 0, maxR = 0;
     uint32_t njobs = 0;
     std::vector<uint32_t> job_n, root_level;
@@ -2135,8 +2166,9 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
     if (forked) CPVS_CUDA(cudaStreamWaitEvent(st, P->tables, 0));
     if (P->leafmasks) {
         KernelTimer kt(tm, K_LEAF_MASKS, st);
-        CPVS_CUDA(launch_kernel(k_leaf_insert, plan_grid(P, P->cap[2], kThreads), kThreads, 0, st, ch, 0, P->lv[2],
-                               P->counts, P->jobs_dev, njobs, 2, P->seg, P->lv[2].table, P->lv[2].table_mask, err));
+        CPVS_CUDA(launch_kernel(P->pow2 ? k_leaf_insert<true> : k_leaf_insert<false>,
+                                plan_grid(P, P->cap[2], kThreads), kThreads, 0, st, ch, 0, P->lv[2], P->counts,
+                                P->jobs_dev, njobs, 2, P->seg, P->lv[2].table, P->lv[2].table_mask, err));
     } else {
         KernelTimer kt(tm, K_CLASSIFY_BOTTOM, st);
         CPVS_CUDA(launch_kernel(k_classify_bottom, plan_grid(P, P->cap[0], kThreads), kThreads, 0, st, ch, 0, P->lv[0],
@@ -2192,8 +2224,8 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
     return CPVS_OK;
 }
 
-bool same_shape(const BuildPlan* P, bool leafmasks, const std::vector<uint32_t>& job_n) {
-    return P->leafmasks == leafmasks && P->job_n == job_n;
+bool same_shape(const BuildPlan* P, bool leafmasks, bool pow2, const std::vector<uint32_t>& job_n) {
+    return P->leafmasks == leafmasks && P->pow2 == pow2 && P->job_n == job_n;
 }
 
 // Capacities from per-job level bounds (+25% slack) and table sizes.  A
@@ -2309,8 +2341,11 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
     const uint32_t njobs = (uint32_t)jobs.size();
     if (njobs == 0) return fail(CPVS_ERR_INVALID_ARG, "build_dags: no jobs");
     std::vector<uint32_t> job_n(njobs);
+    bool pow2 = true;  // the leaf pass may then skip the depth product (exact for these heights)
     for (uint32_t j = 0; j < njobs; ++j) {
         const SourceSpec& S = sources[jobs[j].source];
+        const uint64_t h0 = (uint64_t)S.n * jobs[j].z_num;
+        pow2 = pow2 && (h0 & (h0 - 1)) == 0;
         const int nl = log2_u32(S.n) + 1;
         // leafmasks need numLevels-3 >= 2 (src/CompressedShadow.cpp:20-27)
         if (leafmasks && nl - 3 < 2) return fail(CPVS_ERR_INVALID_ARG, "build_dags: map too small for leafmasks");
@@ -2319,12 +2354,13 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
     if (!ctx.plans) ctx.plans = new PlanCache;
     BuildPlan* P = nullptr;
     for (BuildPlan* q : ctx.plans->plans)
-        if (same_shape(q, leafmasks, job_n)) P = q;
+        if (same_shape(q, leafmasks, pow2, job_n)) P = q;
     if (!P) {
         std::vector<unsigned long long> bounds;
         cpvs_status r = prepass_bounds(ctx, sources, jobs, (leafmasks ? 2 : 0) + 1, st, bounds);
         if (r != CPVS_OK) return r;
         r = plan_create(ctx, jobs, sources, leafmasks, job_n, bounds, st, &P);
+        if (r == CPVS_OK) P->pow2 = pow2;
         if (r != CPVS_OK) return r;
         // keep a few shapes; drop the oldest
         if (ctx.plans->plans.size() >= 8) {
