@@ -517,15 +517,19 @@ __global__ void __launch_bounds__(kThreads, 5)
                 e = prev;
             }
             if ((e >> 32) == (key >> 32)) {
+                // the candidate's job and masks in one round of loads (it
+                // published its masks before its index reached the slot)
                 const uint32_t r = (uint32_t)e;
-                bool same = (r < n) && (__ldcg(lv.job + r) == lv.job[i]);
+                bool same = r < n;
                 if (same) {
                     const ulonglong2* o = reinterpret_cast<const ulonglong2*>(lv.slices + (size_t)r * 8);
+                    const uint32_t jr = __ldcg(lv.job + r);
+                    ulonglong2 x[4];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const ulonglong2 x = __ldcg(o + q);
-                        same = same && x.x == M[2 * q] && x.y == M[2 * q + 1];
-                    }
+                    for (int q = 0; q < 4; ++q) x[q] = __ldcg(o + q);
+                    same = jr == j;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) same = same && x[q].x == M[2 * q] && x[q].y == M[2 * q + 1];
                 }
                 if (same) {
                     if (r > i) {

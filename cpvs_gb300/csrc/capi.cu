@@ -363,8 +363,11 @@ cpvs_status cpvs_ctx_kernel_times(cpvs_ctx* ctx, double* total_ms, uint64_t* lau
 const char* cpvs_kernel_name(uint32_t id) { return cpvs::kernel_name((int)id); }
 
 // ------------------------------------------------------------- hierarchy
-cpvs_status cpvs_hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n, uint32_t flags, void* stream,
-                                  cpvs_hierarchy** out) {
+namespace {
+// `first_level`: the lowest pyramid level stored (1 for a hierarchy handed to
+// the caller).
+cpvs_status hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n, uint32_t flags, void* stream,
+                             int first_level, cpvs_hierarchy** out) {
     if (!ctx || !depth || !out) return fail(CPVS_ERR_INVALID_ARG, "hierarchy_create: null argument");
     *out = nullptr;
     cpvs_status r = check_map_size(n, 2);
@@ -378,6 +381,7 @@ cpvs_status cpvs_hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n,
     auto* h = new cpvs_hierarchy;
     h->ctx = ctx;
     h->n = n;
+    h->first_level = first_level;
     const bool borrow = (flags & CPVS_IO_DEVICE) && (flags & CPVS_FLAG_BORROW_INPUT);
     if (borrow) {
         h->depth = const_cast<float*>(depth);
@@ -403,14 +407,14 @@ cpvs_status cpvs_hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n,
     }
     if (r == CPVS_OK) {
         if (in_place) {
-            r = cpvs::launch_pyramid(in_place, n, h->levels, st, &c.timing, h->depth);
+            r = cpvs::launch_pyramid(in_place, n, h->levels, st, &c.timing, h->depth, first_level);
             // the caller may reuse its buffer on return: wait for the read
             if (r == CPVS_OK) {
                 const cudaError_t e = cudaStreamSynchronize(st);
                 if (e != cudaSuccess) r = cpvs::cuda_fail(e, "hierarchy read of the host map");
             }
         } else {
-            r = cpvs::launch_pyramid(h->depth, n, h->levels, st, &c.timing);
+            r = cpvs::launch_pyramid(h->depth, n, h->levels, st, &c.timing, nullptr, first_level);
         }
     }
     h->touch(st);
@@ -421,6 +425,13 @@ cpvs_status cpvs_hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n,
     *out = h;
     return CPVS_OK;
 }
+}  // namespace
+
+cpvs_status cpvs_hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n, uint32_t flags, void* stream,
+                                  cpvs_hierarchy** out) {
+    return hierarchy_create(ctx, depth, n, flags, stream, 1, out);
+}
+
 
 void cpvs_hierarchy_destroy(cpvs_hierarchy* h) {
     if (!h) return;
@@ -438,7 +449,8 @@ cpvs_status cpvs_hierarchy_level(const cpvs_hierarchy* h, uint32_t level, float*
                                  void* stream) {
     if (!h || !host_out) return fail(CPVS_ERR_INVALID_ARG, "hierarchy_level: null argument");
     const uint32_t nl = cpvs_hierarchy_num_levels(h);
-    if (level < 1 || level >= nl) return fail(CPVS_ERR_INVALID_ARG, "hierarchy_level: level out of range");
+    if ((int)level < h->first_level || level >= nl)
+        return fail(CPVS_ERR_INVALID_ARG, "hierarchy_level: level out of range");
     const uint64_t s = h->n >> level;
     if (capacity < 2 * s * s) return fail(CPVS_ERR_CAPACITY, "hierarchy_level: buffer too small");
     cpvs_status r = set_device(h->ctx);
@@ -613,7 +625,7 @@ cpvs_status cpvs_shadow_create_from_depth(cpvs_ctx* ctx, const float* depth, uin
     // The temporary hierarchy is gone before this call returns, so a device
     // map can be read in place.
     cpvs_hierarchy* h = nullptr;
-    r = cpvs_hierarchy_create(ctx, depth, n, flags | CPVS_FLAG_BORROW_INPUT, stream, &h);
+    r = cpvs::hierarchy_create_for_build(ctx, depth, n, flags | CPVS_FLAG_BORROW_INPUT, flags, stream, &h);
     if (r != CPVS_OK) return r;
     r = cpvs_shadow_create(ctx, h, z_tile_index, z_tile_num, flags, stream, out);
     cpvs_hierarchy_destroy(h);
@@ -998,3 +1010,14 @@ cpvs_status cpvs_grid_evaluate(const cpvs_grid* g, const float* positions, uint3
 }
 
 }  // extern "C"
+namespace cpvs {
+// With leafmasks a build reads pyramid levels 3 and up only (the leaves read
+// the map itself): levels 1 and 2, the bulk of the pyramid, are reduced on
+// chip but never stored.
+cpvs_status hierarchy_create_for_build(cpvs_ctx* ctx, const float* depth, uint32_t n, uint32_t flags,
+                                       uint32_t build_flags, void* stream, cpvs_hierarchy** out) {
+    const uint32_t nl = (uint32_t)log2_u32(n) + 1;
+    const bool leaf = (build_flags & CPVS_FLAG_LEAFMASKS) && n >= 2 && (nl - 3 >= 2);
+    return hierarchy_create(ctx, depth, n, flags, stream, leaf ? 3 : 1, out);
+}
+}  // namespace cpvs

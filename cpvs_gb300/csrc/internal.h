@@ -54,8 +54,10 @@ inline int log2_u32(uint32_t n) {
 // Builds levels 1..log2(n) of the min-max pyramid of `depth` into `levels`.
 struct Timing;
 // `depth_copy` (optional): the map is also copied there while it is read.
+// Levels below `store_from` are reduced but not stored (the first pass must
+// still store its last level, which the next pass reads: store_from <= 3).
 cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaStream_t st, Timing* timing = nullptr,
-                           float* depth_copy = nullptr);
+                           float* depth_copy = nullptr, int store_from = 1);
 
 // One z-tile of a source map whose per-level node bounds are wanted.
 struct BoundJob {

@@ -27,6 +27,7 @@ struct cpvs_hierarchy : DeviceObject {
     float* depth = nullptr;    // device n*n
     bool owns_depth = true;    // false when borrowed from the caller
     float2* levels = nullptr;  // device pyramid
+    int first_level = 1;       // lowest pyramid level stored (a build's temporary hierarchy may skip some)
     uint64_t bytes = 0;
 };
 
@@ -90,4 +91,8 @@ void* host_accessible(const Ctx& c, const void* p);
 void shadow_ensure_top(const cpvs_shadow* s, cudaStream_t st);
 // The shadow as an entry of a multi-DAG lookup table (with its top grid).
 MultiDag shadow_table_entry(const cpvs_shadow* s);
+// A hierarchy that only feeds builds with the given flags (destroyed after
+// them): with leafmasks, pyramid levels 1 and 2 are not stored.
+cpvs_status hierarchy_create_for_build(cpvs_ctx* ctx, const float* depth, uint32_t n, uint32_t flags,
+                                       uint32_t build_flags, void* stream, cpvs_hierarchy** out);
 }  // namespace cpvs

@@ -25,13 +25,15 @@ constexpr int kTile = 64;
 constexpr int kThreads = 256;
 
 // in: level `L0-1` of side S (the depth map when FROM_DEPTH), out: pyramid
-// level array; writes levels L0 .. L0+log2(T)-1 of this CTA's tile.  With
+// level array; writes levels L0 .. L0+log2(T)-1 of this CTA's tile, those
+// below `store_from` only into shared memory.  With
 // `copy` (FROM_DEPTH only) the depth map is also written there as it is
 // read: a map in host memory that the GPU reads in place crosses the host
 // link once, while it is reduced, instead of in a separate copy first.
 template <bool FROM_DEPTH>
 __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ in, uint32_t S, float2* __restrict__ out,
-                                                      uint32_t n, int L0, uint32_t T, float* __restrict__ copy) {
+                                                      uint32_t n, int L0, uint32_t T, float* __restrict__ copy,
+                                                      int store_from) {
     chain_enter();
     __shared__ float2 buf0[(kTile / 2) * (kTile / 2)];
     __shared__ float2 buf1[(kTile / 4) * (kTile / 4)];
@@ -65,7 +67,7 @@ __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ i
                 hi = pmax(pmax(r0.y, r0.w), pmax(r1.y, r1.w));
             }
             const float2 v = make_float2(lo, hi);
-            dst[(size_t)(ty * half + oy) * So + tx * half + ox] = v;
+            if (L0 >= store_from) dst[(size_t)(ty * half + oy) * So + tx * half + ox] = v;
             buf0[o] = v;
         }
     }
@@ -84,7 +86,7 @@ __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ i
             const float2 a = src[(2 * oy) * half + 2 * ox], b = src[(2 * oy) * half + 2 * ox + 1];
             const float2 c = src[(2 * oy + 1) * half + 2 * ox], d = src[(2 * oy + 1) * half + 2 * ox + 1];
             const float2 v = make_float2(pmin(pmin(a.x, b.x), pmin(c.x, d.x)), pmax(pmax(a.y, b.y), pmax(c.y, d.y)));
-            dst[(size_t)(ty * h2 + oy) * So + tx * h2 + ox] = v;
+            if (L >= store_from) dst[(size_t)(ty * h2 + oy) * So + tx * h2 + ox] = v;
             nxt[o] = v;
         }
         // the next level reads what this one wrote: swap, and reuse the
@@ -102,10 +104,11 @@ __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ i
 // level-1 texels per step from two 16-byte loads (one per input row) and
 // stores them as one 16-byte (min,max,min,max) pair; a warp covers 512
 // contiguous bytes of each input row.  Levels 2-6 reduce in shared memory.
-// With `copy` the map is also written there as it is read.
+// With `copy` the map is also written there as it is read; levels below
+// `store_from` stay in shared memory.
 __global__ void __launch_bounds__(kThreads)
     k_pyramid64(const float* __restrict__ in, uint32_t S, float2* __restrict__ out, uint32_t n,
-                float* __restrict__ copy) {
+                float* __restrict__ copy, int store_from) {
     chain_enter();
     __shared__ float2 buf0[32 * 32];
     __shared__ float2 buf1[16 * 16];
@@ -127,8 +130,9 @@ __global__ void __launch_bounds__(kThreads)
             }
             const float2 v0 = make_float2(pmin(pmin(a.x, a.y), pmin(b.x, b.y)), pmax(pmax(a.x, a.y), pmax(b.x, b.y)));
             const float2 v1 = make_float2(pmin(pmin(a.z, a.w), pmin(b.z, b.w)), pmax(pmax(a.z, a.w), pmax(b.z, b.w)));
-            *reinterpret_cast<float4*>(dst + (size_t)(ty * 32 + oy) * So + tx * 32 + 2 * px) =
-                make_float4(v0.x, v0.y, v1.x, v1.y);
+            if (store_from <= 1)
+                *reinterpret_cast<float4*>(dst + (size_t)(ty * 32 + oy) * So + tx * 32 + 2 * px) =
+                    make_float4(v0.x, v0.y, v1.x, v1.y);
             buf0[oy * 32 + 2 * px] = v0;
             buf0[oy * 32 + 2 * px + 1] = v1;
         }
@@ -147,7 +151,7 @@ __global__ void __launch_bounds__(kThreads)
             const float2 a = src[(2 * oy) * w + 2 * ox], b = src[(2 * oy) * w + 2 * ox + 1];
             const float2 c = src[(2 * oy + 1) * w + 2 * ox], d = src[(2 * oy + 1) * w + 2 * ox + 1];
             const float2 v = make_float2(pmin(pmin(a.x, b.x), pmin(c.x, d.x)), pmax(pmax(a.y, b.y), pmax(c.y, d.y)));
-            dst[(size_t)(ty * h + oy) * So + tx * h + ox] = v;
+            if (lvl >= store_from) dst[(size_t)(ty * h + oy) * So + tx * h + ox] = v;
             nxt[o] = v;
         }
         float2* t = src;
@@ -203,7 +207,7 @@ __global__ void __launch_bounds__(kBoundThreads)
 }  // namespace
 
 cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaStream_t st, Timing* timing,
-                           float* depth_copy) {
+                           float* depth_copy, int store_from) {
     KernelTimer kt(timing, K_PYRAMID, st);
     uint32_t S = n;
     int L0 = 1;
@@ -214,14 +218,15 @@ cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaS
         // chained: each pass may be scheduled while the work before it in
         // the stream drains, and waits for it at its start
         if (first && T == (uint32_t)kTile)
-            CPVS_CUDA(launch_kernel(k_pyramid64, tiles, kThreads, 0, st, true, 0, depth, S, levels, n, depth_copy));
+            CPVS_CUDA(launch_kernel(k_pyramid64, tiles, kThreads, 0, st, true, 0, depth, S, levels, n, depth_copy,
+                                    store_from));
         else if (first)
             CPVS_CUDA(launch_kernel(k_pyramid<true>, tiles, kThreads, 0, st, true, 0, static_cast<const void*>(depth), S,
-                                    levels, n, L0, T, depth_copy));
+                                    levels, n, L0, T, depth_copy, store_from));
         else
             CPVS_CUDA(launch_kernel(k_pyramid<false>, tiles, kThreads, 0, st, true, 0,
                                     static_cast<const void*>(levels + pyramid_level_offset(n, L0 - 1)), S, levels, n,
-                                    L0, T, static_cast<float*>(nullptr)));
+                                    L0, T, static_cast<float*>(nullptr), store_from));
         first = false;
         L0 += log2_u32(T);
         S /= T;

@@ -371,7 +371,7 @@ struct cpvs_server {
         std::vector<Req> ok;
         for (const Req& r : batch) {
             cpvs_hierarchy* h = nullptr;
-            const cpvs_status st = cpvs_hierarchy_create(ctx, r->depth, r->n, 0, s_build, &h);
+            const cpvs_status st = cpvs::hierarchy_create_for_build(ctx, r->depth, r->n, 0, cfg.flags, s_build, &h);
             if (st != CPVS_OK) {
                 complete(r, st, cpvs_last_error());
                 continue;
