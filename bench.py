@@ -122,11 +122,13 @@ class ClockSampler:
 # cache (a depth texel shared by the leaves above it, a hot hash slot) count
 # once.  These divide the kernel's CUDA-event time for `roofline.achieved`.
 def kernel_alg_bytes(name: str, n: int, tree: list, uniq: list, dag_words: int) -> float:
-    texels = sum((n >> L) ** 2 for L in range(1, int(np.log2(n)) + 1))
     leaves = tree[2] if len(tree) > 2 else 0
+    # a build with leafmasks stores pyramid levels 3 and up (levels 1-2 stay on chip)
+    first = 3 if leaves else 1
+    texels = sum((n >> L) ** 2 for L in range(first, int(np.log2(n)) + 1))
     inner = sum(tree[3:])
     uleaves = uniq[2] if len(uniq) > 2 else 0
-    if name == "pyramid":          # depth read once, every pyramid texel written once
+    if name == "pyramid":          # depth read once, every stored pyramid texel written once
         return 4.0 * n * n + 8.0 * texels
     if name == "leaf_masks":       # depth map once; per leaf coord + job in, class mask + slot out, one slot
         # probe; the 64 B of masks only for the class representatives
@@ -136,7 +138,7 @@ def kernel_alg_bytes(name: str, n: int, tree: list, uniq: list, dag_words: int) 
         return inner * (8 + 4 + 32 + 8) + (leaves + inner) * 12
     if name == "insert_inner":     # per inner node mask + job + first + slot probe + slot out; 4 B per child id
         return inner * (4 + 4 + 4 + 8 + 4) + (leaves + inner) * 4
-    if name == "scan":             # per node slot + mask + job + table entry in, merged id out
+    if name == "scan":             # per node slot + mask + job + table entry in; rank, offset out
         return (leaves + inner) * (4 + 4 + 4 + 8 + 4)
     if name == "emit":
         return 4.0 * dag_words
@@ -320,7 +322,7 @@ def run_ours(args, rank, world, local_rank):
         "data": "synthetic: seeded scene rasterised to a float32 depth map (no dataset involved)",
         "config": {"workload": f"{args.config}: {wl['desc']}", "map_side": n, "voxels_per_dag": int(voxels),
                    "dag_words": dag_words, "lookups_per_batch": nq,
-                   "l2": "inputs larger than L2 (256 MiB map + 171 MiB pyramid per step)" if n >= 8192 else
+                   "l2": "inputs larger than L2 (256 MiB map read per step)" if n >= 8192 else
                          "map smaller than L2: later steps may hit L2",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "e2e": {"value": round(world * voxels / (e2e_build_ms * 1e-3) / 1e9, 1), "unit": "Gvoxel/s",
