@@ -194,6 +194,43 @@ __device__ __forceinline__ uint32_t node_mask_nf(const JobDev& J, int L, uint64_
     return m;
 }
 
+// node_mask_nf for L > 0 with the level's texels at P (W x W, global or
+// shared memory).
+__device__ __forceinline__ uint32_t node_mask_at(const float2* P, uint32_t W, float H, uint64_t c, bool& bad) {
+    const uint32_t x = unpack_x(c), y = unpack_y(c), z = unpack_z(c);
+    if (x + 1u >= W || y + 1u >= W) {
+        bad = true;
+        return 0u;
+    }
+    const float4 r0 = *reinterpret_cast<const float4*>(P + (size_t)y * W + x);
+    const float4 r1 = *reinterpret_cast<const float4*>(P + (size_t)(y + 1) * W + x);
+    const float mn[4] = {r0.x, r0.z, r1.x, r1.z}, mx[4] = {r0.y, r0.w, r1.y, r1.w};
+    uint32_t m = 0;
+#pragma unroll
+    for (uint32_t ch = 0; ch < 8; ++ch) {
+        const uint32_t t = ch & 3u, zc = z + (ch >> 2);
+        m |= classify_cell(zc, __fmul_rn(mn[t], H), __fmul_rn(mx[t], H)) << (2u * ch);
+    }
+    return m;
+}
+
+// Asynchronous block-wide copy of `bytes` (rounded up to 16) from global to
+// shared memory, both 16-byte aligned; the source array must extend to the
+// rounded size (arena arrays are padded to 256 bytes).  The copies bypass L1
+// (data written by other blocks of the launch is read from L2); fetch_wait
+// completes every copy the block issued.
+__device__ __forceinline__ void fetch_async(void* dst, const void* src, uint32_t bytes) {
+    const uint32_t n16 = (bytes + 15u) / 16u;
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    const char* g = static_cast<const char*>(src);
+    for (uint32_t k = threadIdx.x; k < n16; k += blockDim.x)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d + 16u * k), "l"(g + 16u * k) : "memory");
+}
+__device__ __forceinline__ void fetch_wait() {
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
+}
+
 // ---------------------------------------------------------------- top-down
 // Pass 1: per-CTA sum of partial children over its chunk of level L.
 __global__ void __launch_bounds__(kThreads)
@@ -376,11 +413,9 @@ __device__ __forceinline__ void leaf_rows(const float* row0, uint32_t nmap, floa
 // false for a stale slot (an internal check already failed): the caller
 // then treats it as an empty leaf of job 0.
 template <bool POW2>
-__device__ __forceinline__ bool leaf_compute(const LevelDev& lv, const JobDev* __restrict__ jobs, uint32_t njobs,
-                                             uint32_t i, uint64_t M[8], uint32_t& mask, uint64_t& hash,
-                                             uint32_t& j) {
-    const uint64_t c = lv.coord[i];
-    j = lv.job[i];
+// `c` and `j`: the leaf's coordinate and job (j becomes 0 for a stale slot).
+__device__ __forceinline__ bool leaf_compute(const JobDev* __restrict__ jobs, uint32_t njobs, uint64_t c,
+                                             uint64_t M[8], uint32_t& mask, uint64_t& hash, uint32_t& j) {
     const uint32_t bx = unpack_x(c) * 4u, by = unpack_y(c) * 4u, bz = unpack_z(c) * 4u;
     if (j >= njobs || bx + 8u > __ldg(&jobs[j].n) || by + 8u > __ldg(&jobs[j].n)) {
 #pragma unroll
@@ -455,7 +490,8 @@ __global__ void __launch_bounds__(kThreads)
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint64_t M[8], h;
         uint32_t mask, j;
-        const bool ok = leaf_compute<false>(lv, jobs, njobs, i, M, mask, h, j);
+        j = lv.job[i];
+        const bool ok = leaf_compute<false>(jobs, njobs, lv.coord[i], M, mask, h, j);
         store_slices(lv, i, M);
         lv.mask[i] = mask;
         lv.hash[i] = h;
@@ -489,10 +525,21 @@ __global__ void __launch_bounds__(kThreads, 5)
                   int L, SegDev seg, unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
     chain_enter();
     const uint32_t n = counts[L];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    // the next leaf's coordinate and job are requested one iteration ahead
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint64_t c_next = i < n ? lv.coord[i] : 0ull;
+    uint32_t j_next = i < n ? lv.job[i] : 0u;
+    for (; i < n; i += stride) {
+        const uint64_t c = c_next;
+        uint32_t j = j_next;
+        if (i + stride < n) {
+            c_next = lv.coord[i + stride];
+            j_next = lv.job[i + stride];
+        }
         uint64_t M[8], h;
-        uint32_t mask, j;
-        if (!leaf_compute<POW2>(lv, jobs, njobs, i, M, mask, h, j)) {
+        uint32_t mask;
+        if (!leaf_compute<POW2>(jobs, njobs, c, M, mask, h, j)) {
             atomicOr(err, 4u);
             lv.job[i] = 0;
         } else {
@@ -584,9 +631,10 @@ __device__ __forceinline__ bool same_leaf(const LevelDev& cur, uint32_t a, uint3
 // empty slot with CAS, later equal nodes lower it with atomicMin, so the slot
 // ends with the class's smallest (first-occurring) index.  The probe is
 // bounded by the table size (the table is at least twice the node count).
+// Returns (slot, mask, job) of the node.
 template <bool CG>
-__device__ __forceinline__ void insert_inner(LevelDev& cur, const LevelDev& child, uint32_t i,
-                                             unsigned long long* table, uint64_t cap_mask, uint32_t* err);
+__device__ __forceinline__ uint3 insert_inner(LevelDev& cur, const LevelDev& child, uint32_t i,
+                                              unsigned long long* table, uint64_t cap_mask, uint32_t* err);
 
 template <bool LEAF>
 __global__ void __launch_bounds__(kThreads)
@@ -1015,8 +1063,8 @@ __device__ __forceinline__ uint64_t inner_hash(uint32_t j, uint32_t m, uint32_t 
 }
 
 template <bool CG>
-__device__ __forceinline__ void insert_inner(LevelDev& cur, const LevelDev& child, uint32_t i,
-                                             unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
+__device__ __forceinline__ uint3 insert_inner(LevelDev& cur, const LevelDev& child, uint32_t i,
+                                              unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
     const uint32_t m = cur.mask[i], j = cur.job[i];
     const uint32_t k = partial_children(m);
     uint32_t u[8];
@@ -1054,6 +1102,7 @@ __device__ __forceinline__ void insert_inner(LevelDev& cur, const LevelDev& chil
     }
     if (!placed) atomicOr(err, 16u);  // table full: the result is void, reported
     cur.slot[i] = (uint32_t)s;
+    return make_uint3((uint32_t)s, m, j);
 }
 
 // Kept nodes of level L in node order: rank, word offset, the rank in the
@@ -1206,15 +1255,21 @@ constexpr uint32_t kTopMergeNodes = 4096;
 constexpr int kTopMergeItems = kTopMergeNodes / kClusterThreads;
 constexpr uint32_t kTopTable = 2 * kTopMergeNodes;
 
+constexpr uint32_t kTopPyrSide = 32;     // expansion: pyramid levels of side <= 32 held on chip (one job)
+constexpr uint32_t kTopPyr = 1366;       // their texels: 32^2 + 16^2 + ... + 1, rounded up to even
+constexpr uint32_t kTopJobs = 32;        // job tables of at most this many jobs held on chip
 struct ExpandTopSmem {
     uint64_t coord[2][kTopChildren];
     uint32_t job[2][kTopChildren];
     uint32_t mask[kTopNodes], first[kTopNodes];
+    float2 pyr[kTopPyr];
 };
+constexpr uint32_t kTopPreload = 8192;  // merge: node data of all top levels held at once
+constexpr uint32_t kTopSlots = 8192;    // merge: class slots of a level (the one below the top levels included)
 struct MergeTopSmem {
     unsigned long long table[kTopTable];
-    uint32_t mask[kTopMergeNodes], job[kTopMergeNodes], first[kTopMergeNodes];
-    uint32_t slot[2][kTopMergeNodes];
+    uint32_t mask[kTopPreload], job[kTopPreload], first[kTopPreload];
+    uint32_t slot[2][kTopSlots];
 };
 constexpr size_t kExpandClusterSmem = sizeof(ExpandTopSmem);
 constexpr size_t kMergeClusterSmem = sizeof(MergeTopSmem);
@@ -1222,11 +1277,14 @@ constexpr size_t kMergeClusterSmem = sizeof(MergeTopSmem);
 // Expands levels Lhi, Lhi-1, ... (not below Llo) in one block, after placing
 // the roots of level Lhi, while a level fits (see above); writes the highest
 // level left to expand (Llo - 1 when none) to *next.
-__device__ __forceinline__ void expand_top(ExpandTopSmem& S, const LevelDev* __restrict__ lvt, uint32_t* counts,
-                                           const JobDev* __restrict__ jobs, uint32_t njobs, int Lhi, int Llo,
+// `lvt` and `jobs` may be shared-memory copies; with Lp <= Lhi, S.pyr holds
+// pyramid levels Lp.. of the single job's map.
+__device__ __forceinline__ void expand_top(ExpandTopSmem& S, const LevelDev* lvt, uint32_t* counts,
+                                           const JobDev* jobs, uint32_t njobs, int Lhi, int Llo,
                                            const Injected* __restrict__ inj_all, const SmallLevels& sl, SegDev seg,
-                                           uint32_t* err, uint32_t* sm, uint32_t* next) {
+                                           uint32_t* err, uint32_t* sm, uint32_t* next, int Lp) {
     const uint32_t tid = threadIdx.x;
+    const uint64_t pyr_base = Lp <= Lhi ? pyramid_level_offset_dev(jobs[0].n, Lp) : 0ull;
     uint32_t n = sl.ninj[Lhi];
     {
         LevelDev top = lvt[Lhi];
@@ -1255,7 +1313,14 @@ __device__ __forceinline__ void expand_top(ExpandTopSmem& S, const LevelDev* __r
                 const uint32_t j = S.job[b][i];
                 uint32_t m = 0;
                 if (j < njobs) {
-                    m = node_mask_nf(jobs[j], L, S.coord[b][i], bad_node);
+                    const JobDev& J = jobs[j];
+                    if (L >= Lp) {
+                        const uint32_t W = J.n >> L;
+                        m = node_mask_at(S.pyr + (pyramid_level_offset_dev(J.n, L) - pyr_base), W,
+                                         __uint2float_rn(W * J.z_num), S.coord[b][i], bad_node);
+                    } else {
+                        m = node_mask_nf(J, L, S.coord[b][i], bad_node);
+                    }
                 } else {
                     bad_job = true;
                     S.job[b][i] = 0;
@@ -1350,80 +1415,109 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     __shared__ uint32_t sm[64];
     __shared__ uint2 s_tot[kClusterMaxBlocks];
+    // the level table and (small) job table on chip, and for one job the
+    // top pyramid levels that the first block classifies against
+    __shared__ __align__(16) LevelDev s_lv[CPVS_MAX_LEVELS];
+    __shared__ __align__(16) JobDev s_jobs[kTopJobs];
+    fetch_async(s_lv, lvt, (uint32_t)(CPVS_MAX_LEVELS * sizeof(LevelDev)));
+    if (njobs <= kTopJobs) fetch_async(s_jobs, jobs, (uint32_t)(njobs * sizeof(JobDev)));
+    int Lp = CPVS_MAX_LEVELS;
+    if (rank == 0 && njobs == 1) {
+        ExpandTopSmem& S = *reinterpret_cast<ExpandTopSmem*>(dyn_smem);
+        const float2* pyr = jobs[0].pyr;
+        const uint32_t nm = jobs[0].n, lg = 31u - (uint32_t)__clz((int)nm);
+        Lp = lg > 5u ? (int)(lg - 5u) : 1;  // side (nm >> Lp) <= kTopPyrSide
+        const uint64_t o = pyramid_level_offset_dev(nm, Lp);
+        fetch_async(S.pyr, pyr + o, (uint32_t)((pyramid_level_offset_dev(nm, (int)lg + 1) - o) * sizeof(float2)));
+    }
+    fetch_wait();
+    const JobDev* jt = njobs <= kTopJobs ? s_jobs : jobs;
     if (rank == 0)
-        expand_top(*reinterpret_cast<ExpandTopSmem*>(dyn_smem), lvt, counts, jobs, njobs, Lhi, Llo, inj_all, sl, seg,
-                   err, sm, top_next);
+        expand_top(*reinterpret_cast<ExpandTopSmem*>(dyn_smem), s_lv, counts, jt, njobs, Lhi, Llo, inj_all, sl, seg,
+                   err, sm, top_next, Lp);
     cl.sync();
     const int Lstart = (int)__ldcg(top_next);
+    // the cluster levels: each block takes a contiguous range of the level,
+    // kClusterItems consecutive nodes per thread; its node data stays in
+    // registers and shared memory, and the next level's size follows from
+    // the cluster total, so a level costs two rounds of loads (node data,
+    // then pyramid texels) and two cluster barriers
+    uint32_t* s_job = reinterpret_cast<uint32_t*>(dyn_smem);  // [kClusterItems * kClusterThreads + 2]
+    uint32_t n = Lstart >= Llo ? __ldcg(counts + Lstart) : 0u;
     for (int L = Lstart; L >= Llo; --L) {
-        LevelDev cur = lvt[L], nxt = lvt[L - 1];
-        const uint32_t n = __ldcg(counts + L);
-        const uint32_t per = (n + nb - 1) / nb;
+        LevelDev cur = s_lv[L], nxt = s_lv[L - 1];
+        const uint32_t per = ((n + nb - 1) / nb + 3u) & ~3u;
         const uint32_t lo = min(n, rank * per), hi = min(n, lo + per);
         if (hi - lo > (uint32_t)(kClusterItems * kClusterThreads)) atomicOr(err, 1u);  // the plan sized this level
-        uint32_t m[kClusterItems], jv[kClusterItems], ksum = 0;
+        const uint32_t i0 = lo + threadIdx.x * kClusterItems;
+        uint32_t m[kClusterItems], jv[kClusterItems], ksum = 0, badj = 0;
         uint64_t cv[kClusterItems];
-        bool bad_job = false, bad_node = false;
+        bool bad_node = false;
 #pragma unroll
         for (int it = 0; it < kClusterItems; ++it) {
-            const uint32_t i = lo + it * kClusterThreads + threadIdx.x;
+            const uint32_t i = i0 + it;
+            jv[it] = i < hi ? __ldcg(cur.job + i) : 0u;
+            cv[it] = i < hi ? __ldcg(cur.coord + i) : 0ull;
+        }
+        // the jobs of the range's neighbours (for the segment boundaries)
+        if (threadIdx.x == 0) {
+            s_job[0] = lo > 0 && lo < n ? __ldcg(cur.job + lo - 1) : ~0u;
+            s_job[1 + (hi - lo)] = hi < n ? __ldcg(cur.job + hi) : ~0u;
+        }
+#pragma unroll
+        for (int it = 0; it < kClusterItems; ++it) {
+            const uint32_t i = i0 + it;
             m[it] = 0;
-            jv[it] = 0;
-            cv[it] = 0;
             if (i < hi) {
-                jv[it] = __ldcg(cur.job + i);
-                cv[it] = __ldcg(cur.coord + i);
                 if (jv[it] < njobs) {
-                    m[it] = node_mask_nf(jobs[jv[it]], L, cv[it], bad_node);
+                    m[it] = node_mask_nf(jt[jv[it]], L, cv[it], bad_node);
                 } else {
-                    bad_job = true;
+                    badj |= 1u << it;
                     jv[it] = 0;
                 }
             }
+            if (i < hi) s_job[1 + threadIdx.x * kClusterItems + it] = jv[it];
             ksum += partial_children(m[it]);
         }
-        if (bad_job) atomicOr(err, 8u);
+        if (badj) atomicOr(err, 8u);
         if (bad_node) atomicOr(err, 4u);
         uint2 btot, ctot;
-        block_exclusive_scan2(make_uint2(ksum, 0u), btot, sm);
+        const uint32_t pre = block_exclusive_scan2(make_uint2(ksum, 0u), btot, sm).x;
         const uint2 bpre = cluster_prefix(cl, btot, s_tot, ctot);
         const uint32_t ninj = sl.ninj[L - 1], cap_next = sl.cap[L - 1];
-        uint32_t run = ninj + bpre.x;
+        uint32_t f = ninj + bpre.x + pre;
 #pragma unroll
         for (int it = 0; it < kClusterItems; ++it) {
-            const uint32_t i = lo + it * kClusterThreads + threadIdx.x;
-            const bool in = i < hi;
-            uint32_t mi = in ? m[it] : 0u;
+            const uint32_t i = i0 + it;
+            if (i >= hi) break;
+            uint32_t mi = m[it];
             const uint32_t k = partial_children(mi);
-            uint2 tot;
-            const uint32_t f = run + block_exclusive_scan2(make_uint2(k, 0u), tot, sm).x;
-            if (in) {
-                if (f + k > cap_next) {
-                    atomicOr(err, 1u);  // more children than the level holds: not written, reported
-                    mi &= 0x5555u;
-                    cur.first[i] = 0;
-                } else {
-                    cur.first[i] = f;
-                    const uint32_t x = unpack_x(cv[it]), y = unpack_y(cv[it]), z = unpack_z(cv[it]);
-                    uint32_t r = 0;
+            if (f + k > cap_next) {
+                atomicOr(err, 1u);  // more children than the level holds: not written, reported
+                mi &= 0x5555u;
+                cur.first[i] = 0;
+            } else {
+                cur.first[i] = f;
+                const uint32_t x = unpack_x(cv[it]), y = unpack_y(cv[it]), z = unpack_z(cv[it]);
+                uint32_t r = 0;
 #pragma unroll
-                    for (uint32_t ch = 0; ch < 8; ++ch)
-                        if (mi & (2u << (2u * ch))) {
-                            // cs::getChildCoordinates (src/CompressedShadowUtil.cpp:101-117)
-                            nxt.coord[f + r] =
-                                pack_xyz((x + (ch & 1u)) * 2u, (y + ((ch >> 1) & 1u)) * 2u, (z + (ch >> 2)) * 2u);
-                            nxt.job[f + r] = jv[it];
-                            ++r;
-                        }
-                }
-                cur.mask[i] = mi;
-                if (jv[it] == 0 && __ldcg(cur.job + i) != 0) cur.job[i] = 0;
-                const uint32_t j = jv[it];
-                if (i == 0 || __ldcg(cur.job + i - 1) != j) seg.nstart[seg_index(j, L)] = i;
-                if (i == n - 1 || __ldcg(cur.job + i + 1) != j) seg.nend[seg_index(j, L)] = i + 1;
+                for (uint32_t ch = 0; ch < 8; ++ch)
+                    if (mi & (2u << (2u * ch))) {
+                        // cs::getChildCoordinates (src/CompressedShadowUtil.cpp:101-117)
+                        nxt.coord[f + r] =
+                            pack_xyz((x + (ch & 1u)) * 2u, (y + ((ch >> 1) & 1u)) * 2u, (z + (ch >> 2)) * 2u);
+                        nxt.job[f + r] = jv[it];
+                        ++r;
+                    }
             }
-            run += tot.x;
+            cur.mask[i] = mi;
+            if (badj & (1u << it)) cur.job[i] = 0;
+            const uint32_t j = jv[it], li = 1 + threadIdx.x * kClusterItems + it;
+            if (i == 0 || s_job[li - 1] != j) seg.nstart[seg_index(j, L)] = i;
+            if (i == n - 1 || s_job[li + 1] != j) seg.nend[seg_index(j, L)] = i + 1;
+            f += k;
         }
+        const uint32_t total = ninj + ctot.x;
         if (rank == 0) {
             const Injected* inj = inj_all + sl.inj_off[L - 1];
             for (uint32_t r = threadIdx.x; r < ninj; r += blockDim.x) {
@@ -1431,11 +1525,11 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
                 nxt.job[r] = inj[r].job;
             }
             if (threadIdx.x == 0) {
-                const uint32_t total = ninj + ctot.x;
                 if (total > cap_next) atomicOr(err, 1u);
                 counts[L - 1] = total < cap_next ? total : cap_next;
             }
         }
+        n = total < cap_next ? total : cap_next;
         cl.sync();
     }
 }
@@ -1443,36 +1537,66 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
 // Merge of levels Llo..Lhi in one block (each level at most kTopMergeNodes
 // nodes): insert into the shared table (the leaf level was inserted into its
 // global table by the leaf kernel), then ranks and word offsets in node
-// order, as the multi-block passes compute them.
-__device__ __forceinline__ void merge_top(MergeTopSmem& S, const LevelDev* __restrict__ lvt, const uint32_t* __restrict__ counts,
-                          uint32_t* level_u, int Llo, int Lhi, int bottom, int leaf_level, SegDev seg, uint32_t* err,
-                          uint32_t* sm) {
+// order, as the multi-block passes compute them.  The node data of all these
+// levels, and the class slots of the level below them, are loaded into
+// shared memory up front when they fit, so a level then runs on chip.
+__device__ __forceinline__ void merge_top(MergeTopSmem& S, const LevelDev* lvt,
+                                          const uint32_t* __restrict__ counts, const uint32_t* s_cnt,
+                                          uint32_t* level_u, int Llo, int Lhi, int bottom, int leaf_level,
+                                          SegDev seg, uint32_t* err, uint32_t* sm) {
     const uint32_t tid = threadIdx.x;
-    int cb = 0;               // S.slot[cb]: class slots of the level below, when it ran here
+    uint32_t base[CPVS_MAX_LEVELS], total = 0;  // level offsets, multiples of four nodes
+    for (int L = Llo; L <= Lhi; ++L) {
+        base[L] = total;
+        total += (s_cnt[L] + 3u) & ~3u;
+    }
+    const bool pre = total <= kTopPreload;
+    if (pre)
+        for (int L = Llo; L <= Lhi; ++L) {
+            const LevelDev& cur = lvt[L];
+            fetch_async(S.mask + base[L], cur.mask, s_cnt[L] * 4u);
+            fetch_async(S.job + base[L], cur.job, s_cnt[L] * 4u);
+            if (L != leaf_level) fetch_async(S.first + base[L], cur.first, s_cnt[L] * 4u);
+        }
+    int cb = 0;  // S.slot[cb]: class slots of the level below
     bool child_here = false;
+    if (Llo > bottom) {
+        const uint32_t nc = __ldcg(counts + Llo - 1);
+        if (((nc + 3u) & ~3u) <= kTopSlots) {
+            fetch_async(S.slot[0], lvt[Llo - 1].slot, nc * 4u);
+            child_here = true;
+        }
+    }
+    fetch_wait();
     for (int L = Llo; L <= Lhi; ++L) {
         LevelDev cur = lvt[L];
         const LevelDev child = L > bottom ? lvt[L - 1] : lvt[L];
         const bool leaf = L == leaf_level;
-        const uint32_t n = __ldcg(counts + L);
+        const uint32_t n = s_cnt[L];
+        const uint32_t off = pre ? base[L] : 0u;
         uint32_t* my_slot = S.slot[cb ^ 1];
         const uint32_t* child_slot = S.slot[cb];
+        const uint32_t* mask = S.mask + off;
+        const uint32_t* job = S.job + off;
+        const uint32_t* first = S.first + off;
         uint32_t T = 64;
         while (T < 2 * n && T < kTopTable) T <<= 1;
         if (T > cur.table_mask + 1) T = (uint32_t)(cur.table_mask + 1);
         for (uint32_t i = tid; i < n; i += blockDim.x) {
-            S.mask[i] = __ldcg(cur.mask + i);
-            S.job[i] = __ldcg(cur.job + i);
-            if (!leaf) S.first[i] = __ldcg(cur.first + i);
-            else my_slot[i] = __ldcg(cur.slot + i);
+            if (!pre) {
+                S.mask[i] = __ldcg(cur.mask + i);
+                S.job[i] = __ldcg(cur.job + i);
+                if (!leaf) S.first[i] = __ldcg(cur.first + i);
+            }
+            if (leaf) my_slot[i] = __ldcg(cur.slot + i);
         }
         if (!leaf)
             for (uint32_t s = tid; s < T; s += blockDim.x) S.table[s] = kEmptySlot;
         __syncthreads();
         if (!leaf) {
             for (uint32_t i = tid; i < n; i += blockDim.x) {
-                const uint32_t m = S.mask[i], j = S.job[i], k = partial_children(m);
-                const uint32_t f = k ? S.first[i] : 0u;
+                const uint32_t m = mask[i], j = job[i], k = partial_children(m);
+                const uint32_t f = k ? first[i] : 0u;
                 uint32_t u[8];
 #pragma unroll
                 for (uint32_t r = 0; r < 8; ++r)
@@ -1493,9 +1617,9 @@ __device__ __forceinline__ void merge_top(MergeTopSmem& S, const LevelDev* __res
                     }
                     if ((e >> 32) == (key >> 32)) {
                         const uint32_t bn = (uint32_t)e;
-                        bool same = S.job[bn] == j && S.mask[bn] == m;
+                        bool same = job[bn] == j && mask[bn] == m;
                         if (same && k) {
-                            const uint32_t fb = S.first[bn];
+                            const uint32_t fb = first[bn];
 #pragma unroll
                             for (uint32_t r = 0; r < 8; ++r)
                                 if (r < k)
@@ -1528,19 +1652,19 @@ __device__ __forceinline__ void merge_top(MergeTopSmem& S, const LevelDev* __res
                 if (rep[it] == i) {
                     kept |= 1u << it;
                     ++cnt;
-                    words += node_words(S.mask[i], leaf);
+                    words += node_words(mask[i], leaf);
                 }
             }
         }
         uint2 tot;
-        const uint2 pre = block_exclusive_scan2(make_uint2(cnt, words), tot, sm);
-        uint32_t qx = pre.x, qy = pre.y;
+        const uint2 pr = block_exclusive_scan2(make_uint2(cnt, words), tot, sm);
+        uint32_t qx = pr.x, qy = pr.y;
 #pragma unroll
         for (int it = 0; it < kTopMergeItems; ++it) {
             const uint32_t i = i0 + it;
             if (i >= n) break;
-            const uint32_t j = S.job[i], s = my_slot[i];
-            if (i == 0 || S.job[i - 1] != j) {
+            const uint32_t j = job[i], s = my_slot[i];
+            if (i == 0 || job[i - 1] != j) {
                 seg.ustart[seg_index(j, L)] = qx;
                 seg.wstart[seg_index(j, L)] = qy;
             }
@@ -1553,9 +1677,9 @@ __device__ __forceinline__ void merge_top(MergeTopSmem& S, const LevelDev* __res
                 else
                     cur.table[s] = ((unsigned long long)qx << 32) | rep[it];
                 ++qx;
-                qy += node_words(S.mask[i], leaf);
+                qy += node_words(mask[i], leaf);
             }
-            if (i == n - 1 || S.job[i + 1] != j) {
+            if (i == n - 1 || job[i + 1] != j) {
                 seg.uend[seg_index(j, L)] = qx;
                 seg.wend[seg_index(j, L)] = qy;
             }
@@ -1583,64 +1707,82 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
     extern __shared__ __align__(16) unsigned char dyn_smem[];
     __shared__ uint32_t sm[64];
     __shared__ uint2 s_tot[kClusterMaxBlocks];
-    // counts are final here (the expansion has completed)
+    // counts are final here (the expansion has completed); the level table
+    // on chip
+    __shared__ uint32_t s_cnt[CPVS_MAX_LEVELS];
+    __shared__ __align__(16) LevelDev s_lv[CPVS_MAX_LEVELS];
+    if (threadIdx.x < CPVS_MAX_LEVELS)
+        s_cnt[threadIdx.x] = (int)threadIdx.x >= Llo && (int)threadIdx.x <= Lhi ? counts[threadIdx.x] : 0u;
+    fetch_async(s_lv, lvt, (uint32_t)(CPVS_MAX_LEVELS * sizeof(LevelDev)));
+    fetch_wait();
     int Ltop = Lhi + 1;
-    while (Ltop - 1 >= Llo && counts[Ltop - 1] <= kTopMergeNodes) --Ltop;
+    while (Ltop - 1 >= Llo && s_cnt[Ltop - 1] <= kTopMergeNodes) --Ltop;
+    // the cluster levels: each block takes a contiguous range; the insert
+    // runs over it strided (one node per thread and round), and the node's
+    // slot, mask and job go to shared memory for the ranking pass, which
+    // takes kClusterItems consecutive nodes per thread
+    constexpr uint32_t kRange = kClusterItems * kClusterThreads;
+    uint32_t* s_slot = reinterpret_cast<uint32_t*>(dyn_smem);
+    uint32_t* s_mask = s_slot + kRange;
+    uint32_t* s_job = s_mask + kRange;  // [kRange + 2]: the range's jobs between its neighbours'
     for (int L = Llo; L < Ltop; ++L) {
-        LevelDev cur = lvt[L];
-        const LevelDev child = L > bottom ? lvt[L - 1] : lvt[L];
+        LevelDev cur = s_lv[L];
+        const LevelDev child = L > bottom ? s_lv[L - 1] : s_lv[L];
         const bool leaf = L == leaf_level;
-        const uint32_t n = counts[L];
-        const uint32_t per = (n + nb - 1) / nb;
+        const uint32_t n = s_cnt[L];
+        const uint32_t per = ((n + nb - 1) / nb + 3u) & ~3u;
         const uint32_t lo = min(n, rank * per), hi = min(n, lo + per);
-        if (!leaf)
-            for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x)
-                insert_inner<true>(cur, child, i, cur.table, cur.table_mask, err);
-        cl.sync();  // every slot final
-        uint32_t kept = 0, cnt = 0, words = 0, w[kClusterItems];
-#pragma unroll
-        for (int it = 0; it < kClusterItems; ++it) {
-            const uint32_t i = lo + it * kClusterThreads + threadIdx.x;
-            w[it] = 0;
-            if (i < hi) {
-                const uint32_t rep = (uint32_t)__ldcg(cur.table + cur.slot[i]);
-                if (rep == i) {
-                    kept |= 1u << it;
-                    w[it] = node_words(cur.mask[i], leaf);
-                    ++cnt;
-                    words += w[it];
-                }
-            }
+        for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+            uint3 r;
+            if (!leaf)
+                r = insert_inner<true>(cur, child, i, cur.table, cur.table_mask, err);
+            else
+                r = make_uint3(cur.slot[i], cur.mask[i], cur.job[i]);
+            s_slot[i - lo] = r.x;
+            s_mask[i - lo] = r.y;
+            s_job[1 + i - lo] = r.z;
         }
+        if (threadIdx.x == 0) {
+            s_job[0] = lo > 0 && lo < n ? cur.job[lo - 1] : ~0u;
+            s_job[1 + (hi - lo)] = hi < n ? cur.job[hi] : ~0u;
+        }
+        cl.sync();  // every slot final
+        const uint32_t i0 = lo + threadIdx.x * kClusterItems;
+        uint32_t rep[kClusterItems], kept = 0, cnt = 0, words = 0;
+#pragma unroll
+        for (int it = 0; it < kClusterItems; ++it)
+            rep[it] = i0 + it < hi ? __ldcg(reinterpret_cast<const uint32_t*>(cur.table + s_slot[i0 + it - lo])) : ~0u;
+#pragma unroll
+        for (int it = 0; it < kClusterItems; ++it)
+            if (rep[it] == i0 + it) {
+                kept |= 1u << it;
+                ++cnt;
+                words += node_words(s_mask[i0 + it - lo], leaf);
+            }
         uint2 btot, ctot;
-        block_exclusive_scan2(make_uint2(cnt, words), btot, sm);
+        const uint2 pre = block_exclusive_scan2(make_uint2(cnt, words), btot, sm);
         const uint2 bpre = cluster_prefix(cl, btot, s_tot, ctot);
-        uint32_t rx = bpre.x, ry = bpre.y;
+        uint32_t qx = bpre.x + pre.x, qy = bpre.y + pre.y;
 #pragma unroll
         for (int it = 0; it < kClusterItems; ++it) {
-            const uint32_t i = lo + it * kClusterThreads + threadIdx.x;
-            const bool kp = (kept >> it) & 1u;
-            uint2 tot;
-            const uint2 p = block_exclusive_scan2(make_uint2(kp ? 1u : 0u, w[it]), tot, sm);
-            if (i < hi) {
-                const uint32_t qx = rx + p.x, qy = ry + p.y;
-                const uint32_t j = cur.job[i];
-                if (i == 0 || cur.job[i - 1] != j) {
-                    seg.ustart[seg_index(j, L)] = qx;
-                    seg.wstart[seg_index(j, L)] = qy;
-                }
-                if (kp) {
-                    cur.uniq[qx] = i;
-                    cur.woff[qx] = qy;
-                    reinterpret_cast<uint32_t*>(cur.table + cur.slot[i])[1] = qx;
-                }
-                if (i == n - 1 || cur.job[i + 1] != j) {
-                    seg.uend[seg_index(j, L)] = qx + (kp ? 1u : 0u);
-                    seg.wend[seg_index(j, L)] = qy + w[it];
-                }
+            const uint32_t i = i0 + it;
+            if (i >= hi) break;
+            const uint32_t li = i - lo, j = s_job[1 + li];
+            if (i == 0 || s_job[li] != j) {
+                seg.ustart[seg_index(j, L)] = qx;
+                seg.wstart[seg_index(j, L)] = qy;
             }
-            rx += tot.x;
-            ry += tot.y;
+            if (kept & (1u << it)) {
+                cur.uniq[qx] = i;
+                cur.woff[qx] = qy;
+                reinterpret_cast<uint32_t*>(cur.table + s_slot[li])[1] = qx;  // upper half: the rank
+                ++qx;
+                qy += node_words(s_mask[li], leaf);
+            }
+            if (i == n - 1 || s_job[2 + li] != j) {
+                seg.uend[seg_index(j, L)] = qx;
+                seg.wend[seg_index(j, L)] = qy;
+            }
         }
         if (rank == 0 && threadIdx.x == 0) {
             level_u[2 * L] = ctot.x;
@@ -1649,8 +1791,8 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
         cl.sync();  // class slots visible to the level above
     }
     if (rank == 0 && Ltop <= Lhi)
-        merge_top(*reinterpret_cast<MergeTopSmem*>(dyn_smem), lvt, counts, level_u, Ltop, Lhi, bottom, leaf_level, seg,
-                  err, sm);
+        merge_top(*reinterpret_cast<MergeTopSmem*>(dyn_smem), s_lv, counts, s_cnt, level_u, Ltop, Lhi, bottom,
+                  leaf_level, seg, err, sm);
 }
 
 // ------------------------------------------------------------------ layout
@@ -1875,6 +2017,7 @@ struct BuildPlan {
     uint64_t cap[CPVS_MAX_LEVELS] = {0}, tcap[CPVS_MAX_LEVELS] = {0}, ninj[CPVS_MAX_LEVELS] = {0};
     uint64_t inj_off[CPVS_MAX_LEVELS + 1] = {0};
     uint32_t max_grid = 0;
+    uint32_t leaf_grid = 0, insert_grid = 0;  // one wave of the leaf and inner insert kernels
     // device memory
     char* arena = nullptr;
     size_t arena_bytes = 0;
@@ -2058,6 +2201,18 @@ uint32_t plan_grid(const BuildPlan* P, uint64_t items, uint64_t per_block) {
     return (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(g, P->max_grid));
 }
 
+// Blocks of `kernel` (kThreads each) resident on the whole GPU at once: the
+// grid of a grid-stride kernel, so that all of it runs in one wave.
+template <typename K>
+uint32_t resident_blocks(K kernel, int num_sms) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, 0) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    return (uint32_t)(per_sm * std::max(num_sms, 1));
+}
+
 // The largest cluster (16, else 8 blocks of 1024 threads) that both
 // small-level kernels can have resident on this device; 0 if none.
 int probe_cluster_blocks() {
@@ -2171,7 +2326,8 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
     if (P->leafmasks) {
         KernelTimer kt(tm, K_LEAF_MASKS, st);
         CPVS_CUDA(launch_kernel(P->pow2 ? k_leaf_insert<true> : k_leaf_insert<false>,
-                                plan_grid(P, P->cap[2], kThreads), kThreads, 0, st, ch, 0, P->lv[2], P->counts,
+                                std::min(plan_grid(P, P->cap[2], kThreads), P->leaf_grid), kThreads, 0, st, ch, 0,
+                                P->lv[2], P->counts,
                                 P->jobs_dev, njobs, 2, P->seg, P->lv[2].table, P->lv[2].table_mask, err));
     } else {
         KernelTimer kt(tm, K_CLASSIFY_BOTTOM, st);
@@ -2186,7 +2342,8 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
         const LevelDev child = (L > P->bottom) ? P->lv[L - 1] : P->lv[L];
         if (!leaf) {
             KernelTimer kt(tm, K_INSERT_INNER, st);
-            CPVS_CUDA(launch_kernel(k_dedup_insert<false>, plan_grid(P, P->cap[L], kThreads), kThreads, 0, st, ch, 0,
+            CPVS_CUDA(launch_kernel(k_dedup_insert<false>, std::min(plan_grid(P, P->cap[L], kThreads), P->insert_grid),
+                                    kThreads, 0, st, ch, 0,
                                    P->lv[L], child, P->counts, L, P->lv[L].table, P->lv[L].table_mask, err));
         }
         if (forked) {
@@ -2257,6 +2414,8 @@ cpvs_status plan_create(Ctx& ctx, const std::vector<JobSpec>& jobs, const std::v
     P->job_n = job_n;
     P->root_level.resize(P->njobs);
     P->max_grid = (uint32_t)std::max(ctx.num_sms, 1) * 8;
+    P->leaf_grid = std::min(P->max_grid, resident_blocks(k_leaf_insert<true>, ctx.num_sms));
+    P->insert_grid = std::min(P->max_grid, resident_blocks(k_dedup_insert<false>, ctx.num_sms));
     if (ctx.cluster_blocks < 0) ctx.cluster_blocks = probe_cluster_blocks();
     P->cluster_blocks = ctx.cluster_blocks;
     for (uint32_t j = 0; j < P->njobs; ++j) {

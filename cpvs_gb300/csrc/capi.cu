@@ -377,7 +377,7 @@ cpvs_status hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n, uint
     cudaStream_t st = (cudaStream_t)stream;
     cpvs::Ctx& c = ctx->c;
     const uint64_t dbytes = (uint64_t)n * n * 4;
-    const uint64_t lbytes = cpvs::pyramid_texels(n) * 8;
+    const uint64_t lbytes = cpvs::pyramid_bytes(n);
     auto* h = new cpvs_hierarchy;
     h->ctx = ctx;
     h->n = n;
@@ -438,7 +438,7 @@ void cpvs_hierarchy_destroy(cpvs_hierarchy* h) {
     cpvs::Ctx& c = h->ctx->c;
     cudaSetDevice(c.device);
     if (h->depth && h->owns_depth) c.release(h->depth, (uint64_t)h->n * h->n * 4, true, nullptr, h->last_use);
-    if (h->levels) c.release(h->levels, cpvs::pyramid_texels(h->n) * 8, true, nullptr, h->last_use);
+    if (h->levels) c.release(h->levels, cpvs::pyramid_bytes(h->n), true, nullptr, h->last_use);
     delete h;
 }
 

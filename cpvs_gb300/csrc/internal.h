@@ -45,6 +45,9 @@ inline uint64_t pyramid_texels(uint32_t n) {
     for (uint32_t s = n >> 1; s >= 1; s >>= 1) o += (uint64_t)s * s;
     return o;
 }
+// Device bytes of a pyramid: its texels plus 16 bytes, so that reads
+// rounded up to 16-byte chunks stay inside the allocation.
+inline uint64_t pyramid_bytes(uint32_t n) { return pyramid_texels(n) * 8 + 16; }
 inline int log2_u32(uint32_t n) {
     int l = 0;
     while ((1u << l) < n) ++l;
