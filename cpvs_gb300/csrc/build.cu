@@ -631,10 +631,11 @@ __device__ __forceinline__ bool same_leaf(const LevelDev& cur, uint32_t a, uint3
 // empty slot with CAS, later equal nodes lower it with atomicMin, so the slot
 // ends with the class's smallest (first-occurring) index.  The probe is
 // bounded by the table size (the table is at least twice the node count).
-// Returns (slot, mask, job) of the node.
+// Node i with mask m, job j, first child f; returns its slot.
 template <bool CG>
-__device__ __forceinline__ uint3 insert_inner(LevelDev& cur, const LevelDev& child, uint32_t i,
-                                              unsigned long long* table, uint64_t cap_mask, uint32_t* err);
+__device__ __forceinline__ uint32_t insert_inner(LevelDev& cur, const LevelDev& child, uint32_t i, uint32_t m,
+                                                 uint32_t j, uint32_t f, unsigned long long* table,
+                                                 uint64_t cap_mask, uint32_t* err);
 
 template <bool LEAF>
 __global__ void __launch_bounds__(kThreads)
@@ -643,8 +644,20 @@ __global__ void __launch_bounds__(kThreads)
     chain_enter();
     const uint32_t n = counts[L];
     if (!LEAF) {
-        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-            insert_inner<false>(cur, child, i, table, cap_mask, err);
+        // the next node's mask, job and first child are requested one
+        // iteration ahead
+        const uint32_t stride = gridDim.x * blockDim.x;
+        uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+        uint32_t m_n = i < n ? cur.mask[i] : 0u, j_n = i < n ? cur.job[i] : 0u, f_n = i < n ? cur.first[i] : 0u;
+        for (; i < n; i += stride) {
+            const uint32_t m = m_n, j = j_n, f = f_n;
+            if (i + stride < n) {
+                m_n = cur.mask[i + stride];
+                j_n = cur.job[i + stride];
+                f_n = cur.first[i + stride];
+            }
+            insert_inner<false>(cur, child, i, m, j, f, table, cap_mask, err);
+        }
         return;
     }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -1063,12 +1076,12 @@ __device__ __forceinline__ uint64_t inner_hash(uint32_t j, uint32_t m, uint32_t 
 }
 
 template <bool CG>
-__device__ __forceinline__ uint3 insert_inner(LevelDev& cur, const LevelDev& child, uint32_t i,
-                                              unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
-    const uint32_t m = cur.mask[i], j = cur.job[i];
+__device__ __forceinline__ uint32_t insert_inner(LevelDev& cur, const LevelDev& child, uint32_t i, uint32_t m,
+                                                 uint32_t j, uint32_t f, unsigned long long* table,
+                                                 uint64_t cap_mask, uint32_t* err) {
     const uint32_t k = partial_children(m);
     uint32_t u[8];
-    load_child_ids<CG>(child, k ? cur.first[i] : 0u, k, u);
+    load_child_ids<CG>(child, k ? f : 0u, k, u);
     const uint64_t h = inner_hash(j, m, k, u);
     const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | i;
     uint64_t s = h & cap_mask;
@@ -1084,11 +1097,13 @@ __device__ __forceinline__ uint3 insert_inner(LevelDev& cur, const LevelDev& chi
             e = prev;
         }
         if ((e >> 32) == (key >> 32)) {
+            // the candidate's job, mask and first child in one round of loads
             const uint32_t b = (uint32_t)e;
-            bool same = cur.job[b] == j && cur.mask[b] == m;
+            const uint32_t jb = cur.job[b], mb = cur.mask[b], fb = cur.first[b];
+            bool same = jb == j && mb == m;
             if (same && k) {
                 uint32_t v[8];
-                load_child_ids<CG>(child, cur.first[b], k, v);
+                load_child_ids<CG>(child, fb, k, v);
 #pragma unroll
                 for (uint32_t r = 0; r < 8; ++r) same = same && (r >= k || u[r] == v[r]);
             }
@@ -1102,7 +1117,7 @@ __device__ __forceinline__ uint3 insert_inner(LevelDev& cur, const LevelDev& chi
     }
     if (!placed) atomicOr(err, 16u);  // table full: the result is void, reported
     cur.slot[i] = (uint32_t)s;
-    return make_uint3((uint32_t)s, m, j);
+    return (uint32_t)s;
 }
 
 // Kept nodes of level L in node order: rank, word offset, the rank in the
@@ -1734,10 +1749,12 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
         const uint32_t lo = min(n, rank * per), hi = min(n, lo + per);
         for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
             uint3 r;
+            r.y = cur.mask[i];
+            r.z = cur.job[i];
             if (!leaf)
-                r = insert_inner<true>(cur, child, i, cur.table, cur.table_mask, err);
+                r.x = insert_inner<true>(cur, child, i, r.y, r.z, cur.first[i], cur.table, cur.table_mask, err);
             else
-                r = make_uint3(cur.slot[i], cur.mask[i], cur.job[i]);
+                r.x = cur.slot[i];
             s_slot[i - lo] = r.x;
             s_mask[i - lo] = r.y;
             s_job[1 + i - lo] = r.z;
