@@ -1224,6 +1224,7 @@ __global__ void __launch_bounds__(kThreads)
 constexpr int kClusterThreads = 1024;
 constexpr int kClusterItems = 4;
 constexpr int kClusterMaxBlocks = 16;
+constexpr uint64_t kClusterLevelCap = 16384;  // planned nodes of a level that the cluster kernels take, at most
 
 struct SmallLevels {
     uint32_t inj_off[CPVS_MAX_LEVELS];
@@ -2103,7 +2104,9 @@ void plan_release(Ctx& ctx, BuildPlan* P) {
 // cluster kernels (a level is small when it and every level above it hold
 // at most kClusterItems * 1024 nodes per cluster block).
 void plan_bind_tables(BuildPlan* P) {
-    const uint64_t small_cap = (uint64_t)P->cluster_blocks * kClusterThreads * kClusterItems;
+    // a level of more nodes runs faster as its own launches over every SM
+    const uint64_t small_cap =
+        std::min<uint64_t>((uint64_t)P->cluster_blocks * kClusterThreads * kClusterItems, kClusterLevelCap);
     uint64_t off = 0;
     for (int L = P->bottom; L <= P->maxR; ++L) {
         P->lv[L].table = P->table + off;
