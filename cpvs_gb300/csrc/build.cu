@@ -1224,7 +1224,7 @@ __global__ void __launch_bounds__(kThreads)
 constexpr int kClusterThreads = 1024;
 constexpr int kClusterItems = 4;
 constexpr int kClusterMaxBlocks = 16;
-constexpr uint64_t kClusterLevelCap = 16384;  // planned nodes of a level that the cluster kernels take, at most
+constexpr uint64_t kClusterLevelCap = 8192;  // planned nodes of a level that the cluster kernels take, at most
 
 struct SmallLevels {
     uint32_t inj_off[CPVS_MAX_LEVELS];
