@@ -385,10 +385,10 @@ __device__ __forceinline__ uint32_t nibbles_to_planes(uint32_t w) {
     return delta_swap(w, 0x0000f0f0u, 12);
 }
 
-// Per texel row of a leaf: the eight lit counts, as nibbles, transposed into
-// count bit-planes (byte b = bit b of the row's eight counts).
+// Per texel row of a leaf: the eight lit counts as nibbles (texel x at bits
+// 4x..4x+3).
 template <bool POW2>
-__device__ __forceinline__ void leaf_rows(const float* row0, uint32_t nmap, float H, float c8, uint32_t R[8]) {
+__device__ __forceinline__ void leaf_rows(const float* row0, uint32_t nmap, float H, float c8, uint32_t W[8]) {
     const float s = POW2 ? __fmul_rn(H, 0.125f) : 0.125f;
 #pragma unroll
     for (int y = 0; y < 8; ++y) {
@@ -401,7 +401,7 @@ __device__ __forceinline__ void leaf_rows(const float* row0, uint32_t nmap, floa
         // every term carried kCountBias above its nibble: remove them all
         constexpr uint32_t bias = kCountBias + (kCountBias << 4) + (kCountBias << 8) + (kCountBias << 12) +
                                   (kCountBias << 16) + (kCountBias << 20) + (kCountBias << 24) + (kCountBias << 28);
-        R[y] = nibbles_to_planes(w - bias);
+        W[y] = w - bias;
     }
 }
 
@@ -409,11 +409,14 @@ __device__ __forceinline__ void leaf_rows(const float* row0, uint32_t nmap, floa
 // 4 * its coordinate), its 16-bit class mask (01 lit / 00 shadow / 10
 // partial per slice, src/CompressedShadowUtil.cpp:59-99) and its signature
 // hash.  Per texel row: the eight lit counts, packed as nibbles, transposed
-// into count bit-planes; slice s is then {texels with count > s}.  Returns
-// false for a stale slot (an internal check already failed): the caller
-// then treats it as an empty leaf of job 0.
+// into count bit-planes; slice s is then {texels with count > s}.  Two common
+// kinds of leaf skip the transposes: all 64 counts equal to k (a flat patch
+// of surface: slices 0..k-1 full, the rest empty) and all counts 0 or 8 (a
+// wall crossing the leaf: every slice the set of count-8 texels).  Every path
+// gives the same masks for the same leaf, so the same hash.  `c` and `j` are the leaf's coordinate and
+// job.  Returns false for a stale slot (an internal check already failed):
+// the caller then treats it as an empty leaf of job 0 (j becomes 0).
 template <bool POW2>
-// `c` and `j`: the leaf's coordinate and job (j becomes 0 for a stale slot).
 __device__ __forceinline__ bool leaf_compute(const JobDev* __restrict__ jobs, uint32_t njobs, uint64_t c,
                                              uint64_t M[8], uint32_t& mask, uint64_t& hash, uint32_t& j) {
     const uint32_t bx = unpack_x(c) * 4u, by = unpack_y(c) * 4u, bz = unpack_z(c) * 4u;
@@ -429,39 +432,75 @@ __device__ __forceinline__ bool leaf_compute(const JobDev* __restrict__ jobs, ui
     const uint32_t Hu = nmap * __ldg(&jobs[j].z_num);
     const float c8 = __fmul_rn(__fsub_rn(0.5f, __uint2float_rn(bz)), 0.125f);  // exact: bz < 2^23
     const float* row0 = jobs[j].depth + (size_t)by * nmap + bx;
-    uint32_t R[8];  // per row: byte b = count bit b of the row's 8 texels
-    leaf_rows<POW2>(row0, nmap, __uint2float_rn(Hu), c8, R);
-    // gather byte b of rows 0..7 into plane b (row y at byte y): 4x4 byte
-    // transposes of rows 0..3 and 4..7
-    uint32_t plo[4], phi[4];
+    uint32_t W[8];
+    leaf_rows<POW2>(row0, nmap, __uint2float_rn(Hu), c8, W);
+    const uint32_t k0 = W[0] & 0xFu, rep = k0 * 0x11111111u;
+    bool uniform = true, binary = true;
 #pragma unroll
-    for (int half = 0; half < 2; ++half) {
-        const uint32_t r0 = R[4 * half], r1 = R[4 * half + 1], r2 = R[4 * half + 2], r3 = R[4 * half + 3];
-        const uint32_t A = __byte_perm(r0, r1, 0x5140), B = __byte_perm(r0, r1, 0x7362);
-        const uint32_t C = __byte_perm(r2, r3, 0x5140), D = __byte_perm(r2, r3, 0x7362);
-        uint32_t* dst = half ? phi : plo;
-        dst[0] = __byte_perm(A, C, 0x5410);
-        dst[1] = __byte_perm(A, C, 0x7632);
-        dst[2] = __byte_perm(B, D, 0x5410);
-        dst[3] = __byte_perm(B, D, 0x7632);
+    for (int y = 0; y < 8; ++y) {
+        uniform = uniform && W[y] == rep;
+        binary = binary && (W[y] & 0x77777777u) == 0u;
     }
-    const uint64_t P0 = plo[0] | ((uint64_t)phi[0] << 32), P1 = plo[1] | ((uint64_t)phi[1] << 32);
-    const uint64_t P2 = plo[2] | ((uint64_t)phi[2] << 32), P3 = plo[3] | ((uint64_t)phi[3] << 32);
-    // slice s = {t : k_t >= s+1}, k_t in [0, 8]
-    M[0] = P0 | P1 | P2 | P3;
-    M[1] = P1 | P2 | P3;
-    M[2] = P3 | P2 | (P1 & P0);
-    M[3] = P3 | P2;
-    M[4] = P3 | (P2 & (P1 | P0));
-    M[5] = P3 | (P2 & P1);
-    M[6] = P3 | (P2 & P1 & P0);
-    M[7] = P3;
-    mask = 0;
+    if (uniform) {
+#pragma unroll
+        for (uint32_t q = 0; q < 8; ++q) M[q] = q < k0 ? ~0ull : 0ull;
+        mask = 0x5555u & ((1u << (2u * k0)) - 1u);
+    } else if (binary) {
+        // every count is 0 or 8 (a wall of the shadow volume crossing the
+        // leaf): all eight slices are the set of count-8 texels, and every
+        // slice is partial.  Bit 3 of each row's nibbles, gathered to a byte.
+        uint64_t p3 = 0;
+#pragma unroll
+        for (int y = 0; y < 8; ++y) {
+            uint32_t x = (W[y] >> 3) & 0x11111111u;
+            x = (x | (x >> 3)) & 0x03030303u;
+            x = (x | (x >> 6)) & 0x000F000Fu;
+            x = (x | (x >> 12)) & 0xFFu;
+            p3 |= (uint64_t)x << (8 * y);
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) M[q] = p3;
+        mask = 0xAAAAu;
+    } else {
+        // per row: byte b = count bit b of the row's 8 texels; then byte b of
+        // rows 0..7 into plane b (row y at byte y): 4x4 byte transposes of
+        // rows 0..3 and 4..7
+        uint32_t R[8];
+#pragma unroll
+        for (int y = 0; y < 8; ++y) R[y] = nibbles_to_planes(W[y]);
+        uint32_t plo[4], phi[4];
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const uint32_t r0 = R[4 * half], r1 = R[4 * half + 1], r2 = R[4 * half + 2], r3 = R[4 * half + 3];
+            const uint32_t A = __byte_perm(r0, r1, 0x5140), B = __byte_perm(r0, r1, 0x7362);
+            const uint32_t C = __byte_perm(r2, r3, 0x5140), D = __byte_perm(r2, r3, 0x7362);
+            uint32_t* dst = half ? phi : plo;
+            dst[0] = __byte_perm(A, C, 0x5410);
+            dst[1] = __byte_perm(A, C, 0x7632);
+            dst[2] = __byte_perm(B, D, 0x5410);
+            dst[3] = __byte_perm(B, D, 0x7632);
+        }
+        const uint64_t P0 = plo[0] | ((uint64_t)phi[0] << 32), P1 = plo[1] | ((uint64_t)phi[1] << 32);
+        const uint64_t P2 = plo[2] | ((uint64_t)phi[2] << 32), P3 = plo[3] | ((uint64_t)phi[3] << 32);
+        // slice s = {t : k_t >= s+1}, k_t in [0, 8]
+        M[0] = P0 | P1 | P2 | P3;
+        M[1] = P1 | P2 | P3;
+        M[2] = P3 | P2 | (P1 & P0);
+        M[3] = P3 | P2;
+        M[4] = P3 | (P2 & (P1 | P0));
+        M[5] = P3 | (P2 & P1);
+        M[6] = P3 | (P2 & P1 & P0);
+        M[7] = P3;
+        mask = 0;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const uint32_t cls = (M[q] == ~0ull) ? kVisible : (M[q] == 0ull ? kShadow : kPartial);
+            mask |= cls << (2 * q);
+        }
+    }
     uint64_t h = (uint64_t)(j + 1) * kGolden;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-        const uint32_t cls = (M[q] == ~0ull) ? kVisible : (M[q] == 0ull ? kShadow : kPartial);
-        mask |= cls << (2 * q);
         h = (h ^ M[q]) * 0xD6E8FEB86659FD93ull;
         h ^= h >> 32;
     }
