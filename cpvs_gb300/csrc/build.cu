@@ -1292,10 +1292,9 @@ __device__ __forceinline__ uint2 cluster_prefix(cg::cluster_group& cl, uint2 v, 
 }
 
 // The topmost levels, while a level holds few enough nodes, run in the
-// cluster's first block alone with the level's node data in shared memory:
-// a level then costs one round of pyramid reads (expansion) or child reads
-// (merge) and a few block barriers, instead of several global round trips
-// and cluster barriers.  The merge keeps its hash table in shared memory;
+// cluster's first block alone with the level's node data in shared memory
+// (and, for one job, the top pyramid levels): a level then costs a few block
+// barriers instead of several global round trips and cluster barriers.  The merge keeps its hash table in shared memory;
 // every node's class slot there is also its slot in the level's global table
 // (the shared table is never larger), which receives the class's rank for
 // the emission.
@@ -1310,7 +1309,7 @@ constexpr uint32_t kTopMergeNodes = 4096;
 constexpr int kTopMergeItems = kTopMergeNodes / kClusterThreads;
 constexpr uint32_t kTopTable = 2 * kTopMergeNodes;
 
-constexpr uint32_t kTopPyrSide = 32;     // expansion: pyramid levels of side <= 32 held on chip (one job)
+constexpr uint32_t kTopPyrLog = 5;       // expansion: pyramid levels of side <= 2^5 held on chip (one job)
 constexpr uint32_t kTopPyr = 1366;       // their texels: 32^2 + 16^2 + ... + 1, rounded up to even
 constexpr uint32_t kTopJobs = 32;        // job tables of at most this many jobs held on chip
 struct ExpandTopSmem {
@@ -1481,7 +1480,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
         ExpandTopSmem& S = *reinterpret_cast<ExpandTopSmem*>(dyn_smem);
         const float2* pyr = jobs[0].pyr;
         const uint32_t nm = jobs[0].n, lg = 31u - (uint32_t)__clz((int)nm);
-        Lp = lg > 5u ? (int)(lg - 5u) : 1;  // side (nm >> Lp) <= kTopPyrSide
+        Lp = lg > kTopPyrLog ? (int)(lg - kTopPyrLog) : 1;  // side (nm >> Lp) <= 2^kTopPyrLog
         const uint64_t o = pyramid_level_offset_dev(nm, Lp);
         fetch_async(S.pyr, pyr + o, (uint32_t)((pyramid_level_offset_dev(nm, (int)lg + 1) - o) * sizeof(float2)));
     }
