@@ -509,7 +509,11 @@ __device__ __forceinline__ bool leaf_compute(const JobDev* __restrict__ jobs, ui
 }
 
 __device__ __forceinline__ void leaf_segments(const LevelDev& lv, SegDev& seg, uint32_t i, uint32_t n, uint32_t j,
-                                              int L) {
+                                              int L, uint32_t njobs, uint32_t* err) {
+    if (j >= njobs) {
+        atomicOr(err, 128u);  // a node's job out of range: reported, not followed
+        return;
+    }
     if (i == 0 || lv.job[i - 1] != j) seg.nstart[seg_index(j, L)] = i;
     if (i == n - 1 || lv.job[i + 1] != j) seg.nend[seg_index(j, L)] = i + 1;
 }
@@ -539,7 +543,7 @@ __global__ void __launch_bounds__(kThreads)
             lv.job[i] = 0;
             continue;
         }
-        leaf_segments(lv, seg, i, n, j, L);
+        leaf_segments(lv, seg, i, n, j, L, njobs, err);
     }
 }
 
@@ -582,7 +586,7 @@ __global__ void __launch_bounds__(kThreads, 5)
             atomicOr(err, 4u);
             lv.job[i] = 0;
         } else {
-            leaf_segments(lv, seg, i, n, j, L);
+            leaf_segments(lv, seg, i, n, j, L, njobs, err);
         }
         lv.mask[i] = mask;
         const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | i;
@@ -1166,7 +1170,7 @@ __device__ __forceinline__ uint32_t insert_inner(LevelDev& cur, const LevelDev& 
 template <bool LEAF>
 __global__ void __launch_bounds__(kThreads)
     k_merge_scan_lb(LevelDev cur, const uint32_t* __restrict__ counts, uint32_t* level_u, int L, SegDev seg,
-                    unsigned int* ticket, unsigned long long* flags, uint32_t* err) {
+                    uint32_t njobs, unsigned int* ticket, unsigned long long* flags, uint32_t* err) {
     chain_enter();
     __shared__ uint32_t sm[64];
     __shared__ uint32_t s_tile;
@@ -1226,7 +1230,8 @@ __global__ void __launch_bounds__(kThreads)
         for (int it = 0; it < kScanItems; ++it) {
             const uint32_t i = b0 + it;
             if (i >= n) break;
-            const uint32_t j = jb[it];
+            const uint32_t j = jb[it] < njobs ? jb[it] : 0u;
+            if (jb[it] >= njobs) atomicOr(err, 128u);  // a node's job out of range: reported, not followed
             const uint32_t jl = it == 0 ? jprev : jb[it - 1];
             const uint32_t jr = it == kScanItems - 1 ? jnext : jb[it + 1];
             if (i == 0 || jl != j) {
@@ -1953,7 +1958,7 @@ struct EmitLevels {
 
 __global__ void __launch_bounds__(kThreads)
     k_emit_all(const LevelDev* __restrict__ lvt, EmitLevels el, int bottom, int top, bool leafmasks, SegDev seg,
-               JobLayout lay, uint32_t* __restrict__ out, uint64_t total_words, uint32_t* err) {
+               JobLayout lay, uint32_t njobs, uint32_t* __restrict__ out, uint64_t total_words, uint32_t* err) {
     const uint32_t U = el.ustart[top + 1];
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < U; g += gridDim.x * blockDim.x) {
         int L = bottom;
@@ -1963,6 +1968,10 @@ __global__ void __launch_bounds__(kThreads)
         const bool leaf = leafmasks && L == 2;
         const uint32_t i = cur.uniq[u];
         const uint32_t j = cur.job[i];
+        if (j >= njobs) {
+            atomicOr(err, 128u);  // a node's job out of range: reported, not followed
+            continue;
+        }
         const uint32_t sj = seg_index(j, L);
         const uint32_t m = cur.mask[i];
         const uint64_t at = lay.job_off[j] + lay.base[sj] + (cur.woff[u] - seg.wstart[sj]);
@@ -2003,9 +2012,16 @@ __global__ void __launch_bounds__(kThreads)
                 for (uint32_t r = 0; r < 8; ++r) x[r] = r < k ? child.slot[f + r] : 0u;
 #pragma unroll
                 for (uint32_t r = 0; r < 8; ++r) x[r] = r < k ? (uint32_t)(__ldcg(child.table + x[r]) >> 32) : 0u;
+                const uint32_t kept_below = el.ustart[L] - el.ustart[L - 1];  // ranks of the level below
 #pragma unroll
-                for (uint32_t r = 0; r < 8; ++r)
-                    if (r < k) dst[1 + r] = cb + child.woff[x[r]];
+                for (uint32_t r = 0; r < 8; ++r) {
+                    if (r >= k) break;
+                    if (x[r] >= kept_below) {
+                        atomicOr(err, 256u);  // a child without a rank: reported, not followed
+                        break;
+                    }
+                    dst[1 + r] = cb + child.woff[x[r]];
+                }
             }
         }
     }
@@ -2414,10 +2430,10 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
         unsigned long long* fl = P->flags + P->scan_flag_off[L];
         unsigned int* ticket = P->tickets + CPVS_MAX_LEVELS + L;
         if (leaf)
-            k_merge_scan_lb<true><<<g, kThreads, 0, rank_st>>>(P->lv[L], P->counts, rv.level_u, L, P->seg, ticket,
+            k_merge_scan_lb<true><<<g, kThreads, 0, rank_st>>>(P->lv[L], P->counts, rv.level_u, L, P->seg, njobs, ticket,
                                                                fl, err);
         else
-            k_merge_scan_lb<false><<<g, kThreads, 0, rank_st>>>(P->lv[L], P->counts, rv.level_u, L, P->seg, ticket,
+            k_merge_scan_lb<false><<<g, kThreads, 0, rank_st>>>(P->lv[L], P->counts, rv.level_u, L, P->seg, njobs, ticket,
                                                                 fl, err);
         CPVS_CUDA(cudaGetLastError());
     }
@@ -2701,7 +2717,8 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         const uint32_t U = el.ustart[P->maxR + 1];
         if (U)
             k_emit_all<<<plan_grid(P, U, kThreads), kThreads, 0, st>>>(P->lvt, el, P->bottom, P->maxR, P->leafmasks,
-                                                                       P->seg, P->lay, out.dag, total, P->resv.err);
+                                                                       P->seg, P->lay, njobs, out.dag, total,
+                                                                       P->resv.err);
         CPVS_CUDA(cudaGetLastError());
         CPVS_CUDA(cudaEventRecord(P->done, st));
     }
