@@ -199,13 +199,17 @@ cpvs_status build_into_shadows(cpvs_ctx* ctx, const std::vector<cpvs::SourceSpec
     return CPVS_OK;
 }
 
-// The shadow's top index, built on its first lookup (stream-ordered).
-void ensure_top(const cpvs_shadow* cs, cudaStream_t st) {
+// The shadow's top index, built on its first lookup (stream-ordered), at
+// most max_factor times the DAG's size: a lookup of its own affords 8x (one
+// more level resolved by one load), a server that keeps many DAGs resident
+// under a budget 1x.
+constexpr uint32_t kTopFactor = 8;
+void ensure_top(const cpvs_shadow* cs, cudaStream_t st, uint32_t max_factor = kTopFactor) {
     cpvs_shadow* s = const_cast<cpvs_shadow*>(cs);
     if (s->top || s->top_bytes == ~0ull) return;
-    const int depth = cpvs::top_index_depth(s->num_levels, s->leafmasks, s->words);
+    const int depth = cpvs::top_index_depth(s->num_levels, s->leafmasks, s->words, max_factor);
     if (depth <= 0 || s->ctx->c.alloc((void**)&s->top, uint64_t(4) << (3 * depth), true, st) != CPVS_OK ||
-        cpvs::launch_top_index(s->dag, s->words, s->num_levels, s->leafmasks, s->top, st) != CPVS_OK) {
+        cpvs::launch_top_index(s->dag, s->words, depth, s->top, st) != CPVS_OK) {
         if (s->top) s->ctx->c.release(s->top, uint64_t(4) << (3 * depth), true, st);
         s->top = nullptr;
         s->top_bytes = ~0ull;  // look up without it
@@ -213,16 +217,17 @@ void ensure_top(const cpvs_shadow* cs, cudaStream_t st) {
         return;
     }
     s->top_bytes = uint64_t(4) << (3 * depth);
+    s->top_depth = depth;
 }
 
 }  // namespace
 
 namespace cpvs {
-void shadow_ensure_top(const cpvs_shadow* s, cudaStream_t st) { ensure_top(s, st); }
+void shadow_ensure_top(const cpvs_shadow* s, cudaStream_t st, uint32_t max_factor) { ensure_top(s, st, max_factor); }
 
 MultiDag shadow_table_entry(const cpvs_shadow* s) {
     return MultiDag{s->dag, (uint32_t)s->words, s->num_levels, s->leafmasks ? 1u : 0u,
-                    s->top ? (uint32_t)top_index_depth(s->num_levels, s->leafmasks, s->words) : 0u, s->top};
+                    s->top ? (uint32_t)s->top_depth : 0u, s->top};
 }
 }  // namespace cpvs
 
@@ -234,7 +239,8 @@ int lookup_qpt(const cpvs_shadow* s, const void* q, bool ndc, uint64_t n, uint32
     cpvs::Ctx& c = s->ctx->c;
     if (c.lookup_qpt) return c.lookup_qpt;
     int& t = c.lookup_qpt_tuned[s->num_levels % CPVS_MAX_LEVELS][ndc ? 1 : 0];
-    if (!t) t = cpvs::tune_lookup(s->dag, s->words, s->num_levels, s->leafmasks, s->top, q, ndc, n, bits, st);
+    if (!t)
+        t = cpvs::tune_lookup(s->dag, s->words, s->num_levels, s->leafmasks, s->top, s->top_depth, q, ndc, n, bits, st);
     return t;
 }
 
@@ -684,8 +690,9 @@ cpvs_status cpvs_shadow_lookup_ndc(const cpvs_shadow* s, const float* xyz, uint6
     cudaStream_t st = (cudaStream_t)stream;
     return lookup_common(s->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
         ensure_top(s, st);
-        cpvs_status r = cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, s->top, q, true, n, bits,
-                                            st, &s->ctx->c.timing, lookup_qpt(s, q, true, n, bits, st));
+        cpvs_status r =
+            cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, s->top, s->top_depth, q, true, n, bits,
+                                st, &s->ctx->c.timing, lookup_qpt(s, q, true, n, bits, st));
         s->touch(st);
         return r;
     });
@@ -697,8 +704,9 @@ cpvs_status cpvs_shadow_lookup_voxel(const cpvs_shadow* s, const int32_t* xyz, u
     cudaStream_t st = (cudaStream_t)stream;
     return lookup_common(s->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
         ensure_top(s, st);
-        cpvs_status r = cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, s->top, q, false, n,
-                                            bits, st, &s->ctx->c.timing, lookup_qpt(s, q, false, n, bits, st));
+        cpvs_status r =
+            cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, s->top, s->top_depth, q, false, n,
+                                bits, st, &s->ctx->c.timing, lookup_qpt(s, q, false, n, bits, st));
         s->touch(st);
         return r;
     });

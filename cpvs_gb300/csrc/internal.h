@@ -17,7 +17,7 @@ namespace cpvs {
 // known to lie inside the DAG.
 constexpr uint64_t kDagPad = 16;
 // Levels below the root replaced by the dense top index in lookups.
-constexpr int kTopIndexDepth = 7;  // levels below the root resolved by the lookup's top grid, at most
+constexpr int kTopIndexDepth = 8;  // levels below the root resolved by the lookup's top grid, at most
 }  // namespace cpvs
 
 namespace cpvs {
@@ -111,10 +111,10 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
 void destroy_plans(Ctx& ctx);
 
 // -------------------------------------------------------------- lookup
-// Depth of the top index of a DAG (0: none) and its build: 8^depth words.
-int top_index_depth(uint32_t num_levels, bool leafmasks, uint64_t words);
-cpvs_status launch_top_index(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks,
-                             uint32_t* out, cudaStream_t st);
+// Depth of the top index of a DAG (0: none), its 8^depth words at most
+// max_factor times the DAG's size (at least 64 KiB), and its build.
+int top_index_depth(uint32_t num_levels, bool leafmasks, uint64_t words, uint32_t max_factor);
+cpvs_status launch_top_index(const uint32_t* dag, uint64_t words, int depth, uint32_t* out, cudaStream_t st);
 // `top` may be null (no top index).
 // One resident DAG in a multi-DAG lookup table.
 struct MultiDag {
@@ -142,10 +142,10 @@ cpvs_status launch_segment_lookup(const MultiDag* dags, uint32_t ndags, const Lo
 // Times queries_per_thread = 1, 2, 4 on the first 2^22 queries (writing
 // their bits) and returns the fastest.
 int tune_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks, const uint32_t* top,
-                const void* xyz, bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st);
+                int top_depth, const void* xyz, bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st);
 // `queries_per_thread` (1, 2 or 4): independent descents each thread carries.
 cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks,
-                          const uint32_t* top, const void* xyz, bool ndc, uint64_t n, uint32_t* bits,
+                          const uint32_t* top, int top_depth, const void* xyz, bool ndc, uint64_t n, uint32_t* bits,
                           cudaStream_t st, Timing* timing = nullptr, int queries_per_thread = 4);
 // World-space evaluation over a grid: n pixels of `fpp` floats (xyz first),
 // column-major 4x4 light view-projection, PCF footprint `filter`; output one

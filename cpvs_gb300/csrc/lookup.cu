@@ -16,8 +16,8 @@
 // levels below the root are replaced by a dense 3-D "top grid" of
 // (2^depth)^3 words, indexed by the top `depth` bits of the quantised x, y,
 // z: the node offset the descent reaches after those levels, or a lit /
-// shadow sentinel.  It lives in global memory (L2-resident; up to 7 levels,
-// never larger than the DAG), so one load replaces up to 7 dependent hops --
+// shadow sentinel.  It lives in global memory (L2-resident; up to 8 levels,
+// at most 8x the DAG's size), so one load replaces up to 8 dependent hops --
 // and each thread carries Q independent queries (Q picked per DAG depth by
 // timing Q = 1, 2, 4 on the first batch).
 #include <algorithm>
@@ -524,20 +524,18 @@ int device_sms() {
 
 }  // namespace
 
-int top_index_depth(uint32_t num_levels, bool leafmasks, uint64_t words) {
+int top_index_depth(uint32_t num_levels, bool leafmasks, uint64_t words, uint32_t max_factor) {
     const int root = (int)num_levels - 2, min_level = leafmasks ? 3 : 0;
     int d = root - min_level + 1;
     if (d > kTopIndexDepth) d = kTopIndexDepth;
-    // no larger than the DAG itself (at least 64 KiB)
-    const uint64_t limit = words * 4 > 65536 ? words * 4 : 65536;
+    // no larger than max_factor times the DAG (at least 64 KiB)
+    const uint64_t limit = words * 4 * max_factor > 65536 ? words * 4 * max_factor : 65536;
     while (d > 0 && (uint64_t(4) << (3 * d)) > limit) --d;
     return d < 0 ? 0 : d;
 }
 
-cpvs_status launch_top_index(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks,
-                             uint32_t* out, cudaStream_t st) {
-    const int depth = top_index_depth(num_levels, leafmasks, words);
-    if (depth == 0) return CPVS_OK;
+cpvs_status launch_top_index(const uint32_t* dag, uint64_t words, int depth, uint32_t* out, cudaStream_t st) {
+    if (depth <= 0) return CPVS_OK;
     const uint32_t cells = 1u << (3 * depth);
     k_top_index<<<(cells + 255) / 256, 256, 0, st>>>(dag, (uint32_t)words, depth, out);
     CPVS_CUDA(cudaGetLastError());
@@ -552,13 +550,13 @@ void launch_lookup_q(uint32_t g, cudaStream_t st, const uint32_t* dag, uint64_t 
 }
 
 cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks,
-                          const uint32_t* top, const void* xyz, bool ndc, uint64_t n, uint32_t* bits,
+                          const uint32_t* top, int top_depth, const void* xyz, bool ndc, uint64_t n, uint32_t* bits,
                           cudaStream_t st, Timing* timing, int queries_per_thread) {
     if (n == 0) return CPVS_OK;
     KernelTimer kt(timing, K_LOOKUP, st);
     const int Q = (queries_per_thread == 1 || queries_per_thread == 2) ? queries_per_thread : 4;
     const uint32_t g = lookup_grid(device_sms(), (n + Q - 1) / Q);
-    const int depth = top ? top_index_depth(num_levels, leafmasks, words) : 0;
+    const int depth = top ? top_depth : 0;
     if (ndc) {
         if (Q == 1) launch_lookup_q<true, 1>(g, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
         else if (Q == 2) launch_lookup_q<true, 2>(g, st, dag, words, num_levels, leafmasks, top, depth, xyz, n, bits);
@@ -573,7 +571,7 @@ cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_leve
 }
 
 int tune_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks, const uint32_t* top,
-                const void* xyz, bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st) {
+                int top_depth, const void* xyz, bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st) {
     // a few million queries (tens of microseconds per launch), best of three
     // timed runs after a warm-up, so that launch-to-launch noise does not pick
     // the variant
@@ -590,7 +588,7 @@ int tune_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool l
         for (int rep = 0; rep < 4; ++rep) {  // the first run warms the caches
             float t = 0.f;
             cudaEventRecord(a, st);
-            launch_lookup(dag, words, num_levels, leafmasks, top, xyz, ndc, sample, bits, st, nullptr, q);
+            launch_lookup(dag, words, num_levels, leafmasks, top, top_depth, xyz, ndc, sample, bits, st, nullptr, q);
             cudaEventRecord(b, st);
             cudaEventSynchronize(b);
             cudaEventElapsedTime(&t, a, b);

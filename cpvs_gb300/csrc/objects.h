@@ -59,6 +59,7 @@ struct cpvs_shadow : DeviceObject {
     uint64_t words = 0;
     uint32_t* top = nullptr;   // dense top index for lookups, built on the first lookup
     uint64_t top_bytes = 0;
+    int top_depth = 0;         // levels below the root that `top` resolves
     uint32_t num_levels = 0;
     bool leafmasks = false;
     uint32_t root_mask = 0;
@@ -88,7 +89,7 @@ namespace cpvs {
 void* host_accessible(const Ctx& c, const void* p);
 // Builds the shadow's lookup top grid if it has none yet (stream-ordered,
 // on the context's thread).
-void shadow_ensure_top(const cpvs_shadow* s, cudaStream_t st);
+void shadow_ensure_top(const cpvs_shadow* s, cudaStream_t st, uint32_t max_factor);
 // The shadow as an entry of a multi-DAG lookup table (with its top grid).
 MultiDag shadow_table_entry(const cpvs_shadow* s);
 // A hierarchy that only feeds builds with the given flags (destroyed after

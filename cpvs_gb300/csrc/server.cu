@@ -393,7 +393,7 @@ struct cpvs_server {
         }
         // their lookup top grids, then: lookups launched after the DAGs are
         // published run after all of it
-        for (cpvs_shadow* sh : out) cpvs::shadow_ensure_top(sh, s_build);
+        for (cpvs_shadow* sh : out) cpvs::shadow_ensure_top(sh, s_build, 1);
         cudaEvent_t built = nullptr;
         if (cudaEventCreateWithFlags(&built, cudaEventDisableTiming) == cudaSuccess) {
             cudaEventRecord(built, s_build);
