@@ -1863,7 +1863,10 @@ struct JobLayout {
     uint32_t* base;     // [job * L_MAX + level]: word offset of the level in the job's DAG
 };
 
-__global__ void k_layout(SegDev seg, JobLayout lay, const uint32_t* __restrict__ root_level, uint32_t njobs, int bottom) {
+// With `root_mask` (and `lvt`), also the root mask of every job (the first
+// word of its DAG).
+__global__ void k_layout(SegDev seg, JobLayout lay, const uint32_t* __restrict__ root_level, uint32_t njobs, int bottom,
+                         const LevelDev* __restrict__ lvt, uint32_t* root_mask) {
     chain_enter();
     // single block: each thread sums its jobs, then a block scan over jobs in
     // rounds of blockDim
@@ -1873,6 +1876,10 @@ __global__ void k_layout(SegDev seg, JobLayout lay, const uint32_t* __restrict__
         const uint32_t j = j0 + threadIdx.x;
         uint64_t total = 0;
         if (j < njobs) {
+            if (root_mask) {
+                const int R = (int)root_level[j];
+                root_mask[j] = lvt[R].mask[seg.nstart[seg_index(j, R)]];
+            }
             for (int L = (int)root_level[j]; L >= bottom; --L) {
                 const uint32_t s = seg_index(j, L);
                 lay.base[s] = (uint32_t)total;
@@ -1938,16 +1945,6 @@ __global__ void k_init_top(LevelDev top, uint32_t* counts, int L, const Injected
         top.job[r] = inj[r].job;
     }
     if (threadIdx.x == 0) counts[L] = ninj;
-}
-
-// Root mask of every job (the first word of its DAG).
-__global__ void k_root_masks(const LevelDev* __restrict__ lvt, SegDev seg, const uint32_t* __restrict__ root_level,
-                             uint32_t njobs, uint32_t* out) {
-    chain_enter();
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < njobs; j += gridDim.x * blockDim.x) {
-        const int L = (int)root_level[j];
-        out[j] = lvt[L].mask[seg.nstart[seg_index(j, L)]];
-    }
 }
 
 // Emission of every level in one launch: global kept-node index g maps to
@@ -2451,9 +2448,8 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
     }
     {
         KernelTimer kt(tm, K_LAYOUT, st);
-        CPVS_CUDA(launch_kernel(k_layout, 1, 1024, 0, st, ch, 0, P->seg, P->lay, P->root_dev, njobs, P->bottom));
-        CPVS_CUDA(launch_kernel(k_root_masks, (njobs + 255) / 256, 256, 0, st, ch, 0, P->lvt, P->seg, P->root_dev, njobs,
-                               rv.root_mask));
+        CPVS_CUDA(launch_kernel(k_layout, 1, 1024, 0, st, ch, 0, P->seg, P->lay, P->root_dev, njobs, P->bottom,
+                                static_cast<const LevelDev*>(P->lvt), rv.root_mask));
     }
     CPVS_CUDA(cudaMemcpyAsync(P->hout, P->res, result_bytes(njobs), cudaMemcpyDeviceToHost, st));
     return CPVS_OK;
@@ -2917,7 +2913,7 @@ extern "C" CPVS_API cpvs_status cpvs_shadow_build_noalloc(const float* depth, ui
         }
         k_dedup_remap<<<gi, kThreads, 0, st>>>(lv[L], counts, L, table);
     }
-    k_layout<<<1, 1024, 0, st>>>(seg, lay, root_dev, 1, bottom);
+    k_layout<<<1, 1024, 0, st>>>(seg, lay, root_dev, 1, bottom, nullptr, nullptr);
     CPVS_CUDA(cudaGetLastError());
     uint64_t hoff[2] = {0, 0};
     uint32_t hlu[2 * CPVS_MAX_LEVELS] = {0};
