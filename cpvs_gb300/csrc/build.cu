@@ -903,59 +903,6 @@ __device__ uint2 lookback(unsigned long long* flags, uint32_t tile, uint2 agg, u
     return excl;
 }
 
-// Rank (merged identity) of node x of a merged level: upper half of its slot.
-__device__ __forceinline__ uint32_t rank_of(const LevelDev& lv, uint32_t x) {
-    return (uint32_t)(__ldcg(lv.table + lv.slot[x]) >> 32);
-}
-
-// Classifies node i of level L, writing its mask; false and mask 0 for a
-// node whose job is out of range (only after an internal check failed).
-__device__ __forceinline__ uint32_t classify_node(LevelDev& cur, const JobDev* __restrict__ jobs, uint32_t njobs,
-                                                  int L, uint32_t i, uint32_t* err) {
-    const uint32_t j = cur.job[i];
-    uint32_t m = 0;
-    if (j < njobs) {
-        m = node_mask(jobs[j], L, cur.coord[i], err);
-    } else {
-        atomicOr(err, 8u);
-        cur.job[i] = 0;  // keep later passes' job lookups in range
-    }
-    cur.mask[i] = m;
-    return m;
-}
-
-// Writes the children of node i (mask m, first child at f) into level L-1,
-// or drops them when they would exceed the level's capacity; records job
-// boundaries at level L.
-__device__ __forceinline__ void write_children(LevelDev& cur, LevelDev& nxt, SegDev& seg, int L, uint32_t n,
-                                               uint32_t i, uint32_t m, uint32_t f, uint32_t cap_next,
-                                               uint32_t* err) {
-    const uint32_t k = partial_children(m);
-    if (f + k > cap_next) {
-        // more children than the level bound: drop them (the count already
-        // includes them; their slots keep stale coordinates, which
-        // node_mask rejects) and report
-        atomicOr(err, 1u);
-        cur.mask[i] = m & 0x5555u;
-        cur.first[i] = 0;
-        return;
-    }
-    cur.first[i] = f;
-    const uint64_t c = cur.coord[i];
-    const uint32_t x = unpack_x(c), y = unpack_y(c), z = unpack_z(c), j = cur.job[i];
-    uint32_t r = 0;
-#pragma unroll
-    for (uint32_t ch = 0; ch < 8; ++ch)
-        if (m & (2u << (2u * ch))) {
-            // cs::getChildCoordinates (src/CompressedShadowUtil.cpp:101-117)
-            nxt.coord[f + r] = pack_xyz((x + (ch & 1u)) * 2u, (y + ((ch >> 1) & 1u)) * 2u, (z + (ch >> 2)) * 2u);
-            nxt.job[f + r] = j;
-            ++r;
-        }
-    if (i == 0 || cur.job[i - 1] != j) seg.nstart[seg_index(j, L)] = i;
-    if (i == n - 1 || cur.job[i + 1] != j) seg.nend[seg_index(j, L)] = i + 1;
-}
-
 // 8-bit set of the partial children (bit ch) of a 16-bit class mask.
 __device__ __forceinline__ uint32_t partial_set(uint32_t m) {
     uint32_t pb = 0;

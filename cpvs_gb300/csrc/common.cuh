@@ -74,31 +74,12 @@ __device__ __forceinline__ bool voxel_lit(uint32_t zc, float d_scaled) {
     return mid <= d_scaled;
 }
 
-// getChildOffset (src/CompressedShadow.cpp:394-402): rank of child `c`
-// among the partially visible children of `mask`.
-__host__ __device__ __forceinline__ uint32_t child_rank(uint32_t mask, uint32_t c) {
-#ifdef __CUDA_ARCH__
-    return __popc(mask & (0xAAAAu >> (16u - 2u * c)));
-#else
-    return (uint32_t)__builtin_popcount(mask & (0xAAAAu >> (16u - 2u * c)));
-#endif
-}
-
 __host__ __device__ __forceinline__ uint32_t partial_children(uint32_t mask) {
 #ifdef __CUDA_ARCH__
     return __popc(mask & 0xAAAAu);
 #else
     return (uint32_t)__builtin_popcount(mask & 0xAAAAu);
 #endif
-}
-
-// Spreads the low 8 bits of x to the even bit positions 0,2,...,14.
-__host__ __device__ __forceinline__ uint32_t spread8(uint32_t x) {
-    x &= 0xFFu;
-    x = (x | (x << 4)) & 0x0F0Fu;
-    x = (x | (x << 2)) & 0x3333u;
-    x = (x | (x << 1)) & 0x5555u;
-    return x;
 }
 
 // Float2 offset of pyramid level L (L >= 1) in the packed level array of an
