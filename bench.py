@@ -23,6 +23,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -183,6 +184,11 @@ def run_ours(args, rank, world, local_rank):
             torch.distributed.barrier()
         torch.cuda.synchronize(dev)
 
+    if args.part == "frame":
+        # profiling aid: the 4K frame (evaluate + shade) alone
+        fr = measure_frame(cp, torch, ctx, build_step(), q_dev, stream, args.steps, args.warmup, barrier)
+        print(json.dumps({"part": "frame", "ms_per_frame": fr["ms_per_frame"]}), flush=True)
+        return
     if args.part != "all":
         # profiling aid: the build steps or the lookup batches alone
         sh = build_step()
@@ -278,6 +284,9 @@ def run_ours(args, rank, world, local_rank):
         sh.lookup_ndc_packed(q_pinned, bits_host, stream=stream)
     barrier()
     e2e_lookup_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    # one rendered frame against this DAG (4K G-buffer; needs that many lookup points)
+    frame = (measure_frame(cp, torch, ctx, sh, q_dev, stream, args.steps, args.warmup, barrier)
+             if world == 1 and nq >= 3840 * 2160 else None)
     clk = clocks.stop()
 
     # slowest rank
@@ -351,11 +360,100 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": int(launches),
         "clocks": clk,
     }
+    if frame is not None:
+        fr = frame["shade_roofline"]
+        fr.update({"peak": peak, "unit": "GB/s", "frac": round(fr["achieved"] / peak, 4), "peak_kind": peak_kind})
+        line["frame"] = frame
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(depth, q_host, args.config, sample_queries=1 << 22)
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def measure_frame(cp, torch, ctx, sh, q_dev, stream, steps, warmup, barrier, width=3840, height=2160):
+    """One frame of the reference's renderer after the precompute
+    (DeferredRenderer::doAllShading): evaluate the DAG at every pixel of a
+    3840x2160 rgba32f G-buffer, then the shading pass.  Light space is the
+    world here (identity view-projection); the positions are the workload's
+    own lookup points (half on the shadow casters' surfaces), the normals
+    random unit vectors and the albedo random.  The G-buffer (398 MB) is
+    larger than L2."""
+    dev = q_dev.device
+    npix = width * height
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(3)
+    pos = torch.ones((height, width, 4), dtype=torch.float32, device=dev)
+    pos[..., :3] = q_dev[:npix].reshape(height, width, 3)
+    nrm = torch.randn((height, width, 4), generator=gen, device=dev)
+    nrm[..., :3] /= nrm[..., :3].norm(dim=-1, keepdim=True)
+    alb = torch.rand((height, width, 4), generator=gen, device=dev)
+    out = torch.empty((height, width, 4), dtype=torch.float32, device=dev)
+    vis = torch.empty((height, width), dtype=torch.uint8, device=dev)
+    grid = cp.CompressedShadowContainer.of(sh)
+    grid.copy_to_gpu(stream=stream)
+    M = np.eye(4, dtype=np.float32)
+    light = (0.3, 0.4, -1.0)
+
+    def one():
+        grid.evaluate(pos, M, out=vis, stream=stream)
+        cp.shade(nrm, alb, light, visibilities=vis, out=out, ctx=ctx, stream=stream)
+    for _ in range(warmup):
+        one()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.enable_timing(True)
+    e0.record(stream)
+    for _ in range(steps):
+        one()
+    e1.record(stream)
+    barrier()
+    kt = ctx.kernel_times()
+    ctx.enable_timing(False)
+    frame_ms = e0.elapsed_time(e1) / steps
+    ev, sd = kt["evaluate"], kt["shade"]
+    shade_ms = sd[0] / max(sd[1], 1)
+    shade_bytes = npix * (16 + 16 + 1 + 16)  # normal, albedo, visibility byte in; colour out
+    return {"pixels": npix, "resolution": f"{width}x{height}", "ms_per_frame": round(frame_ms, 4),
+            "fps": round(1e3 / frame_ms, 1), "evaluate_ms": round(ev[0] / max(ev[1], 1), 4),
+            "shade_ms": round(shade_ms, 4),
+            "path": "cpvs_grid_evaluate (u8, filter 1) + cpvs_shade, G-buffer resident in HBM",
+            "shade_roofline": {"bound": "hbm", "kernel": "shade", "alg_bytes_per_launch": shade_bytes,
+                               "achieved": round(shade_bytes / (shade_ms * 1e-3) / 1e9, 1)},
+            "gpu_launches": int(ev[1] + sd[1])}
+
+
+def host_cpu() -> dict:
+    """The host's core count and CPU model (lscpu's name where it has one)."""
+    model = platform.processor() or platform.machine()
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().startswith("Model name:"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"nproc": os.cpu_count() or 1, "cpu": model, "arch": platform.machine()}
+
+
+def cpu_parallel_builds(jobs, label):
+    """Independent DAG builds of the CPU restatement, one per host core at a
+    time (the oracle holds no shared state; its calls release the GIL), as
+    the reference runs one create per thread over z-tiles.  `jobs`: (map,
+    z_index, z_num).  Returns the bounded-sample CPU baseline."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle.oracle import Oracle
+    O = Oracle()
+    workers = min(os.cpu_count() or 1, len(jobs))
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        list(ex.map(lambda j: O.build(j[0], j[1], j[2], threads=1), jobs))
+    wall = time.perf_counter() - t0
+    voxels = sum(float(j[0].shape[0]) ** 3 for j in jobs)  # a z-tile DAG covers N^3 voxels too
+    return {"value": round(voxels / wall / 1e9, 3), "unit": "Gvoxel/s", "cores": workers, "kind": "port",
+            "sample": f"{len(jobs)} DAG builds ({label}) on {workers} threads, {wall:.2f} s wall",
+            "host": host_cpu()}
 
 
 def cpu_baseline(depth, q, config, sample_queries, threads=None):
@@ -373,12 +471,19 @@ def cpu_baseline(depth, q, config, sample_queries, threads=None):
     t0 = time.perf_counter()
     O.lookup_ndc(b.dag, b.num_levels, b.leafmasks, qs, threads=threads)
     look_s = time.perf_counter() - t0
+    q1 = np.ascontiguousarray(q[:1 << 20])
+    t0 = time.perf_counter()
+    O.lookup_ndc(b.dag, b.num_levels, b.leafmasks, q1, threads=1)
+    look1_s = time.perf_counter() - t0
     return {"value": round(float(n) ** 3 / build_s / 1e9, 3), "unit": "Gvoxel/s", "cores": 4, "kind": "port",
             "sample": f"one full {config} build ({n}^2 map, pyramid on 4 threads, SVO/merge/compress on 1 thread, "
                       f"{build_s:.2f} s); hash-indexed first-occurrence merge (the reference's linear scan gives "
                       f"the same DAG more slowly)",
             "lookup": {"value": round(qs.shape[0] / look_s / 1e9, 4), "unit": "Glookups/s", "cores": threads,
-                       "sample": f"{qs.shape[0]} of the {config} queries"}}
+                       "sample": f"{qs.shape[0]} of the {config} queries",
+                       "one_core": {"value": round(q1.shape[0] / look1_s / 1e9, 4), "unit": "Glookups/s",
+                                    "sample": f"{q1.shape[0]} queries on 1 thread"}},
+            "host": host_cpu()}
 
 
 def run_reference(args, rank, world):
@@ -419,7 +524,8 @@ def run_reference(args, rank, world):
                    "note": f"steps capped at {steps} (bounded CPU sample)"},
         "cpu_baseline": {"value": round(v, 3), "unit": "Gvoxel/s", "cores": 4, "kind": "port",
                          "sample": f"full {n}^2 build per step: pyramid on 4 threads, SVO/merge/compress on 1 thread "
-                                   f"(the reference's threading); hash-indexed first-occurrence merge"},
+                                   f"(the reference's threading); hash-indexed first-occurrence merge",
+                         "host": host_cpu()},
         "e2e": {"value": round(v, 3), "unit": "Gvoxel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "lookup": {"value": round(sample / statistics.mean(tl) / 1e9, 4), "unit": "Glookups/s", "cores": threads,
                    "sample": f"{sample} queries per step"},
@@ -598,6 +704,14 @@ def run_batched(args):
                    "path": "cpvs_grid_lookup_ndc" if args.config == "c2" else "cpvs_lookup_ndc_multi"},
         "clocks": clk,
     }
+    if not args.no_cpu_baseline:
+        if args.config == "c2":
+            # the 8 z-tile DAGs of the first two xy tiles
+            jobs = [(maps[t].cpu().numpy(), z, L) for t in (0, 1) for z in range(L)]
+            line["cpu_baseline"] = cpu_parallel_builds(jobs, "8 z-tiles of 2 of the 64 xy tiles of 4096^2")
+        else:
+            jobs = [(m.cpu().numpy(), 0, 1) for m in maps[:16]]
+            line["cpu_baseline"] = cpu_parallel_builds(jobs, "the first 16 of the 64 lights")
     print(json.dumps(line), flush=True)
 
 
@@ -726,7 +840,7 @@ def main():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--config", choices=tuple(WORKLOADS), default="c1")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--part", choices=("all", "build", "lookup"), default="all",
+    ap.add_argument("--part", choices=("all", "build", "lookup", "frame"), default="all",
                     help="profiling aid: run only the build steps or only the lookup batches (no JSON line)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":

@@ -100,6 +100,7 @@ _SIGS = {
     "cpvs_grid_deserialize": (C.c_int, [_vp, _vp, _u64, _vp, _vp]),
     "cpvs_grid_evaluate": (C.c_int, [_vp, _vp, _u32, _u32, _u32, _vp, _u32, _vp, _vp]),
     "cpvs_shadow_build_noalloc": (C.c_int, [_vp, _u32, _u32, _u32, _u32, _vp, _u64, C.POINTER(_u64), _vp]),
+    "cpvs_shade": (C.c_int, [_vp, _u32, _u32, _vp, _u32, _vp, _vp, _vp, _u32, _vp, _u32, _vp, _vp, _vp, _vp]),
 }
 
 _lib: Optional[C.CDLL] = None
@@ -256,6 +257,59 @@ def raster_depth(sc, x0: int = 0, y0: int = 0, w: Optional[int] = None, h: Optio
     if stream is None:
         torch.cuda.synchronize(dev)
     return out
+
+
+def shade(normals, albedo, light_direction, visibilities=None, positions=None, shadow_map=None,
+          light_view_proj=None, out=None, ctx: Optional[Context] = None, stream=None):
+    """The deferred shading pass (shader/shade.frag:34-56) on G-buffer
+    images: (H, W, C>=3) normals, (H, W, 4) albedo and a light direction,
+    with either the (H, W) uint8 visibilities of
+    CompressedShadowContainer.evaluate (renderShadow on) or the plain
+    shadow-map test of (H, W, C>=3) world positions against a square depth
+    map under `light_view_proj` (4x4 acting on column vectors, or 16 floats
+    column-major).  Returns (H, W, 4) float32 colours: a CUDA tensor for CUDA
+    tensors in, else a numpy array (the images then go through the device)."""
+    import torch
+    ctx = ctx or Context.default()
+    host = not _is_device(normals)
+    dev = torch.device("cuda", ctx.device)
+
+    def on_dev(a, dtype):
+        if a is None:
+            return None
+        t = a if _is_device(a) else torch.from_numpy(np.ascontiguousarray(a))
+        return t.to(device=dev, dtype=dtype).contiguous()
+
+    nrm, alb = on_dev(normals, torch.float32), on_dev(albedo, torch.float32)
+    h, w, fpn = (int(v) for v in nrm.shape)
+    if tuple(alb.shape) != (h, w, 4):
+        raise ValueError("albedo must be (H, W, 4)")
+    light = np.ascontiguousarray(np.asarray(light_direction, np.float32).reshape(3))
+    vis = on_dev(visibilities, torch.uint8)
+    pos = sm = None
+    colmajor = None
+    fpp = side = 0
+    if vis is None:
+        pos, sm = on_dev(positions, torch.float32), on_dev(shadow_map, torch.float32)
+        if pos is None or sm is None or light_view_proj is None:
+            raise ValueError("without visibilities, positions, shadow_map and light_view_proj are needed")
+        fpp, side = int(pos.shape[-1]), int(sm.shape[0])
+        if sm.dim() != 2 or int(sm.shape[1]) != side:
+            raise ValueError("shadow_map must be square")
+        M = np.asarray(light_view_proj, np.float32)
+        colmajor = np.ascontiguousarray(M.T.ravel() if M.shape == (4, 4) else M.ravel(), np.float32)
+    elif tuple(vis.shape) != (h, w):
+        raise ValueError("visibilities must be (H, W)")
+    res = out if (out is not None and not host) else torch.empty((h, w, 4), dtype=torch.float32, device=dev)
+    _check(_lib.cpvs_shade(ctx.handle, w, h, _ptr(nrm), fpn, _ptr(alb), _ptr(vis) if vis is not None else None,
+                           _ptr(pos) if pos is not None else None, fpp, _ptr(sm) if sm is not None else None, side,
+                           colmajor.ctypes.data if colmajor is not None else None, light.ctypes.data, _ptr(res),
+                           _stream(stream)))
+    if host:
+        return res.cpu().numpy()
+    if stream is None:
+        torch.cuda.synchronize(dev)
+    return res
 
 
 def raster_triangles(tris, n: int, plane: float, x0: int = 0, y0: int = 0, w: Optional[int] = None,

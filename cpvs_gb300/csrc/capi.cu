@@ -1,7 +1,9 @@
 // C ABI of the library (include/cpvs.h): handles, validation, memory budget,
-// host <-> device staging.  All compute is in pyramid.cu, build.cu and
-// lookup.cu; nothing here computes a result on the host.
+// host <-> device staging.  All compute is in pyramid.cu, build.cu,
+// lookup.cu, raster.cu and shade.cu; nothing here computes a result on the
+// host.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <functional>
 #include <string>
@@ -1015,6 +1017,58 @@ cpvs_status cpvs_grid_evaluate(const cpvs_grid* g, const float* positions, uint3
                          g->touch(st);
                          return r;
                      });
+}
+
+cpvs_status cpvs_shade(cpvs_ctx* ctx, uint32_t width, uint32_t height, const float* normals, uint32_t normal_floats,
+                       const float* albedo, const uint8_t* visibilities, const float* positions,
+                       uint32_t position_floats, const float* shadow_map, uint32_t shadow_map_side,
+                       const float* light_view_proj, const float* light_direction, float* rgba_out, void* stream) {
+    if (!ctx) return fail(CPVS_ERR_INVALID_ARG, "shade: null context");
+    if (!light_direction) return fail(CPVS_ERR_INVALID_ARG, "shade: null light direction");
+    for (int k = 0; k < 3; ++k)
+        if (!std::isfinite(light_direction[k])) return fail(CPVS_ERR_INVALID_ARG, "shade: light direction not finite");
+    if (light_direction[0] == 0.f && light_direction[1] == 0.f && light_direction[2] == 0.f)
+        return fail(CPVS_ERR_INVALID_ARG, "shade: zero light direction");
+    const uint64_t n = (uint64_t)width * height;
+    if (n == 0) return CPVS_OK;
+    if (normal_floats < 3) return fail(CPVS_ERR_INVALID_ARG, "shade: fewer than 3 floats per normal");
+    const bool map_test = visibilities == nullptr;
+    if (map_test) {
+        if (position_floats < 3) return fail(CPVS_ERR_INVALID_ARG, "shade: fewer than 3 floats per position");
+        if (!light_view_proj) return fail(CPVS_ERR_INVALID_ARG, "shade: null matrix for the shadow-map test");
+        if (shadow_map_side == 0 || shadow_map_side > (1u << 16))
+            return fail(CPVS_ERR_INVALID_ARG, "shade: shadow map side outside [1, 65536]");
+    }
+    cpvs_status r = set_device(ctx);
+    if (r != CPVS_OK) return r;
+    const cpvs::Ctx& c = ctx->c;
+    // every pixel buffer must be one the GPU reads (or writes) in place
+    auto view = [&](const void* p) -> void* {
+        if (!p) return nullptr;
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return const_cast<void*>(p);
+        return host_accessible(c, p);
+    };
+    const float* nrm = static_cast<const float*>(view(normals));
+    const float* alb = static_cast<const float*>(view(albedo));
+    float* out = static_cast<float*>(view(rgba_out));
+    if (!nrm || !alb || !out) return fail(CPVS_ERR_INVALID_ARG, "shade: a buffer the GPU cannot reach (or null)");
+    const uint8_t* vis = nullptr;
+    const float *pos = nullptr, *sm = nullptr;
+    if (map_test) {
+        pos = static_cast<const float*>(view(positions));
+        sm = static_cast<const float*>(view(shadow_map));
+        if (!pos || !sm) return fail(CPVS_ERR_INVALID_ARG, "shade: a buffer the GPU cannot reach (or null)");
+    } else {
+        vis = static_cast<const uint8_t*>(view(visibilities));
+        if (!vis) return fail(CPVS_ERR_INVALID_ARG, "shade: a buffer the GPU cannot reach");
+    }
+    return cpvs::launch_shade(n, nrm, normal_floats, alb, vis, pos, position_floats, sm, shadow_map_side,
+                              light_view_proj, light_direction, out, (cudaStream_t)stream, &ctx->c.timing);
 }
 
 }  // extern "C"

@@ -162,6 +162,12 @@ cpvs_status launch_grid_evaluate(const uint32_t* dag, uint64_t words, const uint
 cpvs_status launch_grid_lookup(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
                                uint32_t dag_levels, bool leafmasks, const uint32_t* gtop, int gdepth, const float* xyz,
                                uint64_t n, uint32_t* bits, cudaStream_t st, Timing* timing = nullptr);
+// Deferred shading of n pixels (device buffers; visibilities null selects
+// the shadow-map test on positions, shadow_map and light_view_proj).
+cpvs_status launch_shade(uint64_t n, const float* normals, uint32_t normal_floats, const float* albedo,
+                         const uint8_t* visibilities, const float* positions, uint32_t position_floats,
+                         const float* shadow_map, uint32_t shadow_map_side, const float* light_view_proj,
+                         const float* light_direction, float* out, cudaStream_t st, Timing* timing = nullptr);
 
 // ------------------------------------------------------------ timing
 // Kernels timed (when a context's timing is on) with a CUDA event pair on
@@ -186,6 +192,7 @@ enum KernelId : int {
     K_RASTER,
     K_MULTI_LOOKUP,
     K_EVALUATE,
+    K_SHADE,
     K_COUNT
 };
 const char* kernel_name(int id);

@@ -8,7 +8,8 @@ const char* kernel_name(int id) {
     static const char* names[K_COUNT] = {
         "pyramid",      "level_bounds", "expand_count", "expand_write", "leaf_masks", "classify_bottom",
         "table_clear",  "insert_leaf",  "insert_inner", "resolve",      "scan",       "remap",
-        "layout",       "emit",         "lookup",       "grid_lookup", "raster",      "multi_lookup", "evaluate"};
+        "layout",       "emit",         "lookup",       "grid_lookup", "raster",      "multi_lookup", "evaluate",
+        "shade"};
     return (id >= 0 && id < K_COUNT) ? names[id] : "";
 }
 

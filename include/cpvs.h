@@ -344,6 +344,31 @@ CPVS_API cpvs_status cpvs_grid_evaluate(const cpvs_grid* g, const float* positio
                                         uint32_t floats_per_pixel, const float* light_view_proj, uint32_t flags,
                                         void* out, void* stream);
 
+/* Deferred shading of one frame (shader/shade.frag:34-56, drawn by
+ * DeferredRenderer::doAllShading, src/DeferredRenderer.cpp:319-348) on
+ * buffers instead of G-buffer textures.  All pixel buffers are row-major
+ * width x height images the GPU can read (device memory, or host memory the
+ * GPU reaches in place); `rgba_out` receives 4 floats per pixel.
+ *   normals:  `normal_floats` (>= 3) floats per pixel, xyz first.
+ *   albedo:   4 floats per pixel (the diffuse buffer's rgba).
+ *   visibilities: cpvs_grid_evaluate's CPVS_EVAL_U8 output (renderShadow != 0:
+ *     vis = byte / 255); or NULL for the shader's shadow-map branch
+ *     (renderShadow == 0): `positions` (`position_floats` >= 3 per pixel) go
+ *     through `light_view_proj` as in cpvs_grid_evaluate, s = c.xyz / c.w *
+ *     0.5 + 0.5, and vis = 0 when the `shadow_map_side`^2 float depth map
+ *     `shadow_map` at texel (floor(s.x * side), floor(s.y * side)) is below
+ *     s.z, else 1 (nearest filtering; outside the map the border depth 1.0,
+ *     src/ShadowMap.cpp:3-9).
+ *   light_direction: 3 host floats (normalised here; not all zero).
+ * colour = ((0.15 + max(0, dot(N, L)) * vis) * albedo.rgb, albedo.a), every
+ * float operation one IEEE round-to-nearest step in the order written, no
+ * contraction.  Stream-ordered; returns after the launch. */
+CPVS_API cpvs_status cpvs_shade(cpvs_ctx* ctx, uint32_t width, uint32_t height, const float* normals,
+                                uint32_t normal_floats, const float* albedo, const uint8_t* visibilities,
+                                const float* positions, uint32_t position_floats, const float* shadow_map,
+                                uint32_t shadow_map_side, const float* light_view_proj, const float* light_direction,
+                                float* rgba_out, void* stream);
+
 /* A request loop that takes builds and lookup batches of any size from any
  * host thread, keeps the built DAGs resident in HBM under a byte budget
  * (least recently used first out), and batches continuously: a dispatcher

@@ -17,6 +17,7 @@
  * the reference's algorithm intends and reports the condition.
  */
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <functional>
@@ -575,6 +576,61 @@ void oracle_grid_evaluate(const uint32_t* dag, const uint32_t* cell_offset, uint
             out[i] = (f == 1) ? (uint8_t)(cnt ? 255u : 0u) : (uint8_t)((255u * cnt + f2 / 2u) / f2);
         }
     });
+}
+
+/* The deferred shading fragment shader (shader/shade.frag:34-56) per pixel,
+ * with the texture reads as buffer reads.  Float32, no contraction, each
+ * operation in the order written:
+ *   L = l / sqrt((lx*lx + ly*ly) + lz*lz)                    normalize(light.direction)
+ *   diffuse = max(0, (Nx*Lx + Ny*Ly) + Nz*Lz)                max(0.0, dot(N, L))
+ *   vis = max(byte / 255, 0)                                 renderShadow != 0: the r8 image
+ *   or evaluateShadowMap (:23-32): c = M * (pos, 1) as in oracle_grid_evaluate,
+ *      s = c.xyz / c.w * 0.5 + 0.5, depth texel (floor(s.x*side), floor(s.y*side))
+ *      of the nearest-filtered map, 1.0 (the border colour set by
+ *      clampShadowMap, src/ShadowMap.cpp:3-9) outside it; vis = d < s.z ? 0 : 1
+ *   colour = ((0.15 + diffuse*vis) * albedo.rgb, albedo.a)   ambient 0.15 (:21)
+ * `vis` null selects the shadow-map branch. */
+void oracle_shade(uint64_t n, const float* nrm, uint32_t fpn, const float* alb, const uint8_t* vis, const float* pos,
+                  uint32_t fpp, const float* sm, uint32_t side, const float* m, const float* light, float* out) {
+    const float len = std::sqrt(light[0] * light[0] + light[1] * light[1] + light[2] * light[2]);
+    const float lx = light[0] / len, ly = light[1] / len, lz = light[2] / len;
+    const float fside = (float)side;
+    for (uint64_t i = 0; i < n; ++i) {
+        float v;
+        if (vis) {
+            v = (float)vis[i] / 255.0f;
+            v = v > 0.0f ? v : 0.0f;
+        } else {
+            const float x = pos[fpp * i], y = pos[fpp * i + 1], z = pos[fpp * i + 2];
+            float c[4];
+            for (int r = 0; r < 4; ++r) {
+                float t = m[r] * x;
+                t = t + m[4 + r] * y;
+                t = t + m[8 + r] * z;
+                c[r] = t + m[12 + r];
+            }
+            float s[3];
+            for (int k = 0; k < 3; ++k) {
+                s[k] = c[k] / c[3];
+                s[k] = s[k] * 0.5f;
+                s[k] = s[k] + 0.5f;
+            }
+            const float fx = std::floor(s[0] * fside), fy = std::floor(s[1] * fside);
+            float d = 1.0f;
+            if (fx >= 0.0f && fx < fside && fy >= 0.0f && fy < fside) d = sm[(uint64_t)fy * side + (uint64_t)fx];
+            v = (d < s[2]) ? 0.0f : 1.0f;
+        }
+        const float nx = nrm[fpn * i], ny = nrm[fpn * i + 1], nz = nrm[fpn * i + 2];
+        float dot = nx * lx;
+        dot = dot + ny * ly;
+        dot = dot + nz * lz;
+        const float diffuse = dot > 0.0f ? dot : 0.0f;
+        const float scattered = 0.15f + diffuse * v;
+        out[4 * i] = scattered * alb[4 * i];
+        out[4 * i + 1] = scattered * alb[4 * i + 1];
+        out[4 * i + 2] = scattered * alb[4 * i + 2];
+        out[4 * i + 3] = alb[4 * i + 3];
+    }
 }
 
 }  // extern "C"

@@ -96,6 +96,8 @@ class Oracle:
                                              C.c_uint64, _u8p, C.c_int]
         L.oracle_grid_evaluate.argtypes = [_u32p, _u32p, C.c_uint32, C.c_uint32, C.c_int, _f32p, C.c_uint64,
                                            C.c_uint32, _f32p, C.c_uint32, _u8p, C.c_int]
+        L.oracle_shade.argtypes = [C.c_uint64, _f32p, C.c_uint32, _f32p, C.c_void_p, C.c_void_p, C.c_uint32,
+                                   C.c_void_p, C.c_uint32, C.c_void_p, _f32p, _f32p]
         L.oracle_merge_level.argtypes = [_u32p, C.c_uint32, C.c_uint32, _u32p, _u32p]
         L.oracle_merge_level.restype = C.c_uint32
         self.lib = L
@@ -162,6 +164,27 @@ class Oracle:
                                       np.ascontiguousarray(cell_offsets, np.uint32), length, dag_levels,
                                       int(leafmasks), pos, h * w, fpp, m, filter_size, out, threads)
         return out.reshape(h, w)
+
+    def shade(self, normals, albedo, light_direction, visibilities=None, positions=None, shadow_map=None,
+              light_view_proj_colmajor=None):
+        """(H, W, 4) float32 colours of the shading pass: (H, W, C>=3) normals,
+        (H, W, 4) albedo, and either (H, W) uint8 visibilities or the
+        shadow-map test on (H, W, C>=3) positions against a square depth map."""
+        h, w, fpn = normals.shape
+        nrm = np.ascontiguousarray(normals, np.float32).reshape(-1)
+        alb = np.ascontiguousarray(albedo, np.float32).reshape(-1)
+        light = np.ascontiguousarray(light_direction, np.float32).reshape(3)
+        out = np.zeros((h, w, 4), np.float32)
+        if visibilities is not None:
+            vis = np.ascontiguousarray(visibilities, np.uint8).reshape(-1)
+            self.lib.oracle_shade(h * w, nrm, fpn, alb, vis.ctypes.data, None, 0, None, 0, None, light, out.reshape(-1))
+        else:
+            pos = np.ascontiguousarray(positions, np.float32)
+            sm = np.ascontiguousarray(shadow_map, np.float32)
+            m = np.ascontiguousarray(light_view_proj_colmajor, np.float32).reshape(16)
+            self.lib.oracle_shade(h * w, nrm, fpn, alb, None, pos.ctypes.data, pos.shape[-1], sm.ctypes.data,
+                                  sm.shape[0], m.ctypes.data, light, out.reshape(-1))
+        return out
 
     def grid_lookup_ndc(self, dag, cell_offsets, length, dag_levels, leafmasks, xyz, threads: int = 1):
         q = np.ascontiguousarray(xyz, np.float32).reshape(-1)
