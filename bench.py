@@ -706,9 +706,10 @@ def run_batched(args):
     }
     if not args.no_cpu_baseline:
         if args.config == "c2":
-            # the 8 z-tile DAGs of the first two xy tiles
-            jobs = [(maps[t].cpu().numpy(), z, L) for t in (0, 1) for z in range(L)]
-            line["cpu_baseline"] = cpu_parallel_builds(jobs, "8 z-tiles of 2 of the 64 xy tiles of 4096^2")
+            # the 8 z-tile DAGs of the 8 xy tiles on the grid's diagonal (1/8 of the DAGs)
+            diag = [t * (L + 1) for t in range(L)]
+            jobs = [(maps[t].cpu().numpy(), z, L) for t in diag for z in range(L)]
+            line["cpu_baseline"] = cpu_parallel_builds(jobs, "8 z-tiles of the 8 diagonal xy tiles of 4096^2")
         else:
             jobs = [(m.cpu().numpy(), 0, 1) for m in maps[:16]]
             line["cpu_baseline"] = cpu_parallel_builds(jobs, "the first 16 of the 64 lights")
