@@ -375,10 +375,12 @@ def measure_frame(cp, torch, ctx, sh, q_dev, stream, steps, warmup, barrier, wid
     """One frame of the reference's renderer after the precompute
     (DeferredRenderer::doAllShading): evaluate the DAG at every pixel of a
     3840x2160 rgba32f G-buffer, then the shading pass.  Light space is the
-    world here (identity view-projection); the positions are the workload's
-    own lookup points (half on the shadow casters' surfaces), the normals
-    random unit vectors and the albedo random.  The G-buffer (398 MB) is
-    larger than L2."""
+    world here (identity view-projection); the positions are the first
+    8.3 M of the workload's lookup points, all on the depth surface (where a
+    G-buffer's positions lie; each descends to a leaf) and in random order
+    (a rendered frame's neighbouring pixels would be neighbouring voxels);
+    the normals are random unit vectors and the albedo random.  The G-buffer
+    (398 MB) is larger than L2."""
     dev = q_dev.device
     npix = width * height
     gen = torch.Generator(device=dev)

@@ -164,6 +164,29 @@ def _is_device(a) -> bool:
     return not isinstance(a, np.ndarray) and getattr(a, "is_cuda", False)
 
 
+def _checked(a, dtype, min_elems: int, name: str, device: Optional[int] = None):
+    """`a` (numpy array or torch tensor), checked as a buffer the library
+    reads or writes `min_elems` elements of `dtype` through its data pointer:
+    C-contiguous, of that element size and kind (float or integer), large
+    enough, and -- with `device` -- a CUDA tensor on that device.  A buffer
+    failing any of these would be read or written out of bounds, so it is
+    refused with ValueError before the call."""
+    dt = np.dtype(dtype)
+    if isinstance(a, np.ndarray):
+        contiguous, size, numel, is_float = a.flags.c_contiguous, a.itemsize, a.size, a.dtype.kind == "f"
+    else:
+        contiguous, size, numel, is_float = a.is_contiguous(), a.element_size(), a.numel(), a.dtype.is_floating_point
+    if device is not None and not (_is_device(a) and a.device.index == device):
+        raise ValueError(f"{name}: expected a CUDA tensor on device {device}")
+    if not contiguous:
+        raise ValueError(f"{name}: must be contiguous")
+    if size != dt.itemsize or is_float != (dt.kind == "f"):
+        raise ValueError(f"{name}: elements must be {dt.itemsize}-byte {'floats' if dt.kind == 'f' else 'integers'}")
+    if numel < min_elems:
+        raise ValueError(f"{name}: {numel} elements, at least {min_elems} needed")
+    return a
+
+
 def _host_array(a, dtype):
     """A C-contiguous host buffer for `a` without copying when it already is
     one (numpy array or CPU tensor, pinned or not)."""
@@ -251,6 +274,7 @@ def raster_depth(sc, x0: int = 0, y0: int = 0, w: Optional[int] = None, h: Optio
     spheres = torch.from_numpy(np.ascontiguousarray(sc.spheres, np.float32)).to(dev)
     if out is None:
         out = torch.empty((h, w), dtype=torch.float32, device=dev)
+    _checked(out, np.float32, h * w, "out", ctx.device)
     nb, ns = int(sc.boxes.shape[0]), int(sc.spheres.shape[0])
     _check(_lib.cpvs_raster_depth(ctx.handle, _ptr(boxes) if nb else None, nb, _ptr(spheres) if ns else None, ns,
                                   float(sc.plane), sc.n, x0, y0, w, h, _ptr(out), IO_DEVICE, _stream(stream)))
@@ -301,6 +325,7 @@ def shade(normals, albedo, light_direction, visibilities=None, positions=None, s
     elif tuple(vis.shape) != (h, w):
         raise ValueError("visibilities must be (H, W)")
     res = out if (out is not None and not host) else torch.empty((h, w, 4), dtype=torch.float32, device=dev)
+    _checked(res, np.float32, h * w * 4, "out", ctx.device)
     _check(_lib.cpvs_shade(ctx.handle, w, h, _ptr(nrm), fpn, _ptr(alb), _ptr(vis) if vis is not None else None,
                            _ptr(pos) if pos is not None else None, fpp, _ptr(sm) if sm is not None else None, side,
                            colmajor.ctypes.data if colmajor is not None else None, light.ctypes.data, _ptr(res),
@@ -484,8 +509,9 @@ class CompressedShadow:
         there and a view of it is returned, uncached."""
         if out is not None:
             n = self.dag_size()
-            if int(out.numel() if hasattr(out, "numel") else out.size) < n:
-                raise ValueError("get_dag: output buffer too small")
+            if _is_device(out):
+                raise ValueError("get_dag: out must be host memory")
+            _checked(out, np.uint32, n, "get_dag: out")
             _check(_lib.cpvs_shadow_dag_words(self.handle, _ptr(out), n, None, _stream(stream)))
             return out[:n]
         if self._dag is None:
@@ -523,6 +549,8 @@ class CompressedShadow:
             import torch
             if out is None:
                 out = torch.empty((n + 31) // 32, dtype=torch.int32, device=points.device)
+            _checked(points, np.float32 if ndc else np.int32, 3 * n, "points", self.ctx.device)
+            _checked(out, np.int32, (n + 31) // 32, "out", self.ctx.device)
             _check(fn(self.handle, _ptr(points), n, _ptr(out), IO_DEVICE, _stream(stream)))
             return out
         pts = np.ascontiguousarray(points, np.float32 if ndc else np.int32)
@@ -537,6 +565,10 @@ class CompressedShadow:
         and out happen inside the call."""
         n = int(points.shape[0])
         pts = _host_array(points, np.float32)
+        if _is_device(words_out):
+            raise ValueError("words_out must be host memory")
+        _checked(pts, np.float32, 3 * n, "points")
+        _checked(words_out, np.uint32, (n + 31) // 32, "words_out")
         _check(_lib.cpvs_shadow_lookup_ndc(self.handle, _ptr(pts), n, _ptr(words_out), 0, _stream(stream)))
         return words_out
 
@@ -566,11 +598,17 @@ def lookup_ndc_multi(shadows, dag_index, points, out=None, stream=None):
         import torch
         if out is None:
             out = torch.empty((n + 31) // 32, dtype=torch.int32, device=points.device)
+        dev = points.device.index
+        _checked(points, np.float32, 3 * n, "points", dev)
+        _checked(dag_index, np.uint32, n, "dag_index", dev)
+        _checked(out, np.int32, (n + 31) // 32, "out", dev)
         _check(_lib.cpvs_lookup_ndc_multi(tab, len(shadows), _ptr(dag_index), _ptr(points), n, _ptr(out), IO_DEVICE,
                                           _stream(stream)))
         return out
     pts = _host_array(points, np.float32)
     ids = _host_array(dag_index, np.uint32)
+    _checked(pts, np.float32, 3 * n, "points")
+    _checked(ids, np.uint32, n, "dag_index")
     words = np.zeros(max((n + 31) // 32, 1), np.uint32)
     _check(_lib.cpvs_lookup_ndc_multi(tab, len(shadows), _ptr(ids), _ptr(pts), n, words.ctypes.data, 0,
                                       _stream(stream)))
@@ -635,6 +673,8 @@ class CompressedShadowContainer:
             import torch
             if out is None:
                 out = torch.empty((n + 31) // 32, dtype=torch.int32, device=points.device)
+            _checked(points, np.float32, 3 * n, "points", self.ctx.device)
+            _checked(out, np.int32, (n + 31) // 32, "out", self.ctx.device)
             _check(_lib.cpvs_grid_lookup_ndc(self.handle, _ptr(points), n, _ptr(out), IO_DEVICE, _stream(stream)))
             return out
         pts = np.ascontiguousarray(points, np.float32)
@@ -697,6 +737,11 @@ class CompressedShadowContainer:
             if out is None:
                 out = (torch.empty((n + 31) // 32, dtype=torch.int32, device=positions.device) if packed
                        else torch.empty((h, w), dtype=torch.uint8, device=positions.device))
+            _checked(positions, np.float32, n * fpp, "positions", self.ctx.device)
+            if packed:
+                _checked(out, np.int32, (n + 31) // 32, "out", self.ctx.device)
+            else:
+                _checked(out, np.uint8, n, "out", self.ctx.device)
             _check(_lib.cpvs_grid_evaluate(self.handle, _ptr(positions), w, h, fpp, colmajor.ctypes.data,
                                            flags | IO_DEVICE, _ptr(out), _stream(stream)))
             return out

@@ -73,3 +73,30 @@ def test_no_device_is_an_error_not_a_fallback(lib):
     h = C.c_void_p()
     assert lib.cpvs_ctx_create(0, C.byref(h)) == 4   # CPVS_ERR_DEVICE
     assert not h.value
+
+
+def test_python_buffers_are_checked_before_the_call():
+    """Buffers the library would read or write by pointer are refused when
+    they are too small, strided, of the wrong element type, or not where the
+    call needs them -- before any device work."""
+    import numpy as np
+    import torch
+    from cpvs_gb300 import _checked
+    a = np.zeros((4, 3), np.float32)
+    assert _checked(a, np.float32, 12, "a") is a
+    with pytest.raises(ValueError, match="at least"):
+        _checked(a, np.float32, 13, "a")
+    with pytest.raises(ValueError, match="contiguous"):
+        _checked(np.zeros((3, 4), np.float32).T, np.float32, 12, "a")
+    with pytest.raises(ValueError, match="floats"):
+        _checked(np.zeros(12, np.int32), np.float32, 12, "a")
+    with pytest.raises(ValueError, match="integers"):
+        _checked(np.zeros(12, np.float32), np.uint32, 12, "a")
+    with pytest.raises(ValueError, match="1-byte"):
+        _checked(np.zeros(12, np.int32), np.uint8, 12, "a")
+    t = torch.zeros(8, dtype=torch.int32)
+    assert _checked(t, np.uint32, 8, "t") is t
+    with pytest.raises(ValueError, match="CUDA tensor"):
+        _checked(t, np.uint32, 8, "t", device=0)
+    with pytest.raises(ValueError, match="contiguous"):
+        _checked(torch.zeros(4, 4)[:, 1], np.float32, 4, "t")
