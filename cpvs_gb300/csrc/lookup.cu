@@ -19,7 +19,10 @@
 // shadow sentinel.  It lives in global memory (L2-resident; up to 8 levels,
 // at most 8x the DAG's size), so one load replaces up to 8 dependent hops --
 // and each thread carries Q independent queries (Q picked per DAG depth by
-// timing Q = 1, 2, 4 on the first batch).
+// timing Q = 1, 2, 4 on the first batch).  Query points and answer words are
+// touched once, so they go through the caches evict-first (ld/st .cs): a
+// batch streams hundreds of MB past L2 and would otherwise push the DAG and
+// its top grid out of it.
 #include <algorithm>
 
 #include "common.cuh"
@@ -133,14 +136,14 @@ __global__ void __launch_bounds__(kThreads)
                 int32_t px, py, pz;
                 if (NDC) {
                     const float* p = static_cast<const float*>(q) + 3 * i;
-                    px = quantise(p[0], scale);
-                    py = quantise(p[1], scale);
-                    pz = quantise(p[2], scale);
+                    px = quantise(__ldcs(p), scale);
+                    py = quantise(__ldcs(p + 1), scale);
+                    pz = quantise(__ldcs(p + 2), scale);
                 } else {
                     const int32_t* p = static_cast<const int32_t*>(q) + 3 * i;
-                    px = p[0];
-                    py = p[1];
-                    pz = p[2];
+                    px = __ldcs(p);
+                    py = __ldcs(p + 1);
+                    pz = __ldcs(p + 2);
                 }
                 uint32_t off = 0;
                 int level = root;
@@ -158,7 +161,7 @@ __global__ void __launch_bounds__(kThreads)
                 if (!done) lit = descend(dag, words, 0u, off, level, min_level, leafmasks, px, py, pz);
             }
             const uint32_t word = __ballot_sync(0xffffffffu, lit);
-            if (lane == 0) bits[w] = word;
+            if (lane == 0) __stcs(bits + w, word);
         }
         return;
     }
@@ -176,14 +179,14 @@ __global__ void __launch_bounds__(kThreads)
             if (i < n) {
                 if (NDC) {
                     const float* p = static_cast<const float*>(q) + 3 * i;
-                    px[k] = quantise(p[0], scale);
-                    py[k] = quantise(p[1], scale);
-                    pz[k] = quantise(p[2], scale);
+                    px[k] = quantise(__ldcs(p), scale);
+                    py[k] = quantise(__ldcs(p + 1), scale);
+                    pz[k] = quantise(__ldcs(p + 2), scale);
                 } else {
                     const int32_t* p = static_cast<const int32_t*>(q) + 3 * i;
-                    px[k] = p[0];
-                    py[k] = p[1];
-                    pz[k] = p[2];
+                    px[k] = __ldcs(p);
+                    py[k] = __ldcs(p + 1);
+                    pz[k] = __ldcs(p + 2);
                 }
                 done[k] = false;
             }
@@ -264,7 +267,7 @@ __global__ void __launch_bounds__(kThreads)
         for (int k = 0; k < Q; ++k) {
             const uint32_t word = __ballot_sync(0xffffffffu, lit[k]);
             const uint64_t wi = gidx * Q + k;
-            if (lane == 0 && wi < nwords) bits[wi] = word;
+            if (lane == 0 && wi < nwords) __stcs(bits + wi, word);
         }
     }
 }
@@ -362,11 +365,11 @@ __global__ void __launch_bounds__(kThreads)
         bool lit = false;
         if (i < n) {
             const float* p = q + 3 * i;
-            const int32_t px = quantise(p[0], scale), py = quantise(p[1], scale), pz = quantise(p[2], scale);
+            const int32_t px = quantise(__ldcs(p), scale), py = quantise(__ldcs(p + 1), scale), pz = quantise(__ldcs(p + 2), scale);
             lit = grid_sample(dag, words, cells, length, dag_levels, leafmasks, gt, px, py, pz);
         }
         const uint32_t word = __ballot_sync(0xffffffffu, lit);
-        if (lane == 0) bits[w] = word;
+        if (lane == 0) __stcs(bits + w, word);
     }
 }
 
@@ -403,7 +406,7 @@ __global__ void __launch_bounds__(kThreads)
         uint32_t cnt = 0;
         if (i < n) {
             const float* p = pos + (size_t)fpp * i;
-            const float x = p[0], y = p[1], z = p[2];
+            const float x = __ldcs(p), y = __ldcs(p + 1), z = __ldcs(p + 2);
             float c[4];
 #pragma unroll
             for (int r = 0; r < 4; ++r)
@@ -426,11 +429,11 @@ __global__ void __launch_bounds__(kThreads)
         }
         if (U8) {
             if (i < n)
-                static_cast<uint8_t*>(out)[i] =
-                    filter <= 1 ? (uint8_t)(cnt ? 255u : 0u) : (uint8_t)((255u * cnt + f2 / 2u) / f2);
+                __stcs(static_cast<uint8_t*>(out) + i,
+                       filter <= 1 ? (uint8_t)(cnt ? 255u : 0u) : (uint8_t)((255u * cnt + f2 / 2u) / f2));
         } else {
             const uint32_t word = __ballot_sync(0xffffffffu, lit);
-            if (lane == 0) static_cast<uint32_t*>(out)[w] = word;
+            if (lane == 0) __stcs(static_cast<uint32_t*>(out) + w, word);
         }
     }
 }
@@ -462,17 +465,17 @@ __global__ void __launch_bounds__(kThreads)
         const uint64_t i = w * 32 + (uint64_t)lane;
         bool lit = false;
         if (i < n) {
-            const uint32_t id = ids[i];
+            const uint32_t id = __ldcs(ids + i);
             if (id < ndags) {
                 const MultiDag D = dags[id];
                 const float scale = (float)((1u << (D.num_levels - 1)) - 1u);
                 const float* p = q + 3 * i;
-                const int32_t px = quantise(p[0], scale), py = quantise(p[1], scale), pz = quantise(p[2], scale);
+                const int32_t px = quantise(__ldcs(p), scale), py = quantise(__ldcs(p + 1), scale), pz = quantise(__ldcs(p + 2), scale);
                 lit = multi_descend(D, px, py, pz);
             }
         }
         const uint32_t word = __ballot_sync(0xffffffffu, lit);
-        if (lane == 0) bits[w] = word;
+        if (lane == 0) __stcs(bits + w, word);
     }
 }
 
@@ -500,11 +503,11 @@ __global__ void __launch_bounds__(kThreads)
             const MultiDag D = dags[sg.dag];
             const float scale = (float)((1u << (D.num_levels - 1)) - 1u);
             const float* p = sg.xyz + 3 * i;
-            const int32_t px = quantise(p[0], scale), py = quantise(p[1], scale), pz = quantise(p[2], scale);
+            const int32_t px = quantise(__ldcs(p), scale), py = quantise(__ldcs(p + 1), scale), pz = quantise(__ldcs(p + 2), scale);
             lit = multi_descend(D, px, py, pz);
         }
         const uint32_t word = __ballot_sync(0xffffffffu, lit);
-        if (lane == 0) sg.bits[lw] = word;
+        if (lane == 0) __stcs(sg.bits + lw, word);
     }
 }
 
