@@ -577,8 +577,14 @@ int tune_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool l
                 int top_depth, const void* xyz, bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st) {
     // a few million queries (tens of microseconds per launch), best of three
     // timed runs after a warm-up, so that launch-to-launch noise does not pick
-    // the variant
+    // the variant.  A batch may be ordered (surface points first, say), so a
+    // large one is sampled in four chunks spread over it: chunk c starts at
+    // c*n/4 rounded down to a whole answer word; chunks of sample/4 (a
+    // multiple of 32, at most n/4) end inside the batch and its answer words.
     const uint64_t sample = n < (1ull << 22) ? n : (1ull << 22);
+    const int chunks = n > sample ? 4 : 1;
+    const uint64_t per = chunks == 1 ? sample : (sample / chunks) & ~31ull;
+    const size_t qbytes = 12;  // three floats or three int32 per query
     cudaEvent_t a = nullptr, b = nullptr;
     if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
         cudaGetLastError();
@@ -591,7 +597,11 @@ int tune_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool l
         for (int rep = 0; rep < 4; ++rep) {  // the first run warms the caches
             float t = 0.f;
             cudaEventRecord(a, st);
-            launch_lookup(dag, words, num_levels, leafmasks, top, top_depth, xyz, ndc, sample, bits, st, nullptr, q);
+            for (int c = 0; c < chunks; ++c) {
+                const uint64_t off = (n / chunks * c) & ~31ull;
+                launch_lookup(dag, words, num_levels, leafmasks, top, top_depth,
+                              static_cast<const char*>(xyz) + off * qbytes, ndc, per, bits + off / 32, st, nullptr, q);
+            }
             cudaEventRecord(b, st);
             cudaEventSynchronize(b);
             cudaEventElapsedTime(&t, a, b);
