@@ -139,8 +139,8 @@ struct LookupSegment {
 };
 cpvs_status launch_segment_lookup(const MultiDag* dags, uint32_t ndags, const LookupSegment* segs, uint32_t nsegs,
                                   uint64_t total_words, cudaStream_t st, Timing* timing = nullptr);
-// Times queries_per_thread = 1, 2, 4 on the first 2^22 queries (writing
-// their bits) and returns the fastest.
+// Times queries_per_thread = 1, 2, 4 on up to 2^24 of the queries, in four
+// chunks spread over the batch (writing their bits), and returns the fastest.
 int tune_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks, const uint32_t* top,
                 int top_depth, const void* xyz, bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st);
 // `queries_per_thread` (1, 2 or 4): independent descents each thread carries.

@@ -575,13 +575,16 @@ cpvs_status launch_lookup(const uint32_t* dag, uint64_t words, uint32_t num_leve
 
 int tune_lookup(const uint32_t* dag, uint64_t words, uint32_t num_levels, bool leafmasks, const uint32_t* top,
                 int top_depth, const void* xyz, bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st) {
-    // a few million queries (tens of microseconds per launch), best of three
-    // timed runs after a warm-up, so that launch-to-launch noise does not pick
-    // the variant.  A batch may be ordered (surface points first, say), so a
-    // large one is sampled in four chunks spread over it: chunk c starts at
-    // c*n/4 rounded down to a whole answer word; chunks of sample/4 (a
-    // multiple of 32, at most n/4) end inside the batch and its answer words.
-    const uint64_t sample = n < (1ull << 22) ? n : (1ull << 22);
+    // up to 2^24 queries (~0.1 ms per launch), best of three timed runs
+    // after a warm-up, so that launch-to-launch noise does not pick the
+    // variant.  The sample's 201 MB of points exceed L2 as a large batch's do:
+    // a sample that stays in L2 after the warm-up favours the variants that
+    // hide latency over the one that streams best.  A batch may be ordered
+    // (surface points first, say), so a large one is sampled in four chunks
+    // spread over it: chunk c starts at c*n/4 rounded down to a whole answer
+    // word; chunks of sample/4 (a multiple of 32, at most n/4) end inside the
+    // batch and its answer words.
+    const uint64_t sample = n < (1ull << 24) ? n : (1ull << 24);
     const int chunks = n > sample ? 4 : 1;
     const uint64_t per = chunks == 1 ? sample : (sample / chunks) & ~31ull;
     const size_t qbytes = 12;  // three floats or three int32 per query
