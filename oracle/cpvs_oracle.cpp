@@ -15,6 +15,13 @@
  * Each function names the reference lines it restates.  Where the reference
  * is undefined (see `ref_defined` below) this restatement produces the DAG
  * the reference's algorithm intends and reports the condition.
+ *
+ * Parity unpinned: the shader restatements (oracle_grid_evaluate's float
+ * transform and oracle_shade) follow the GLSL of shader/traverse.cs and
+ * shader/shade.frag, which cannot run here (no graphics stack on this machine);
+ * their float32 operation order is this build's definition, and the GPU path
+ * is checked against it bit for bit.  The lookup part of evaluate is pinned
+ * like the other lookups.
  */
 #include <algorithm>
 #include <cmath>
