@@ -2665,8 +2665,8 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         CPVS_CUDA(cudaGetLastError());
         CPVS_CUDA(cudaEventRecord(P->done, st));
     }
-    // size the hash tables to the unique counts seen (1.5x, load <= 2/3);
-    // a later build that needs more grows them back
+    // size the hash tables to the unique counts seen (3x rounded up to a
+    // power of two, load <= 1/3); a later build that needs more grows them back
     if (!P->tables_tuned) {
         bool changed = false;
         for (int L = P->bottom; L <= P->maxR; ++L) {
