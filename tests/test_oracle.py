@@ -209,3 +209,39 @@ def test_oracle_matches_reference_build_fresh_maps(oracle):
         assert nl == b.num_levels
         assert np.array_equal(dag, b.dag), (trial, n, zi, zn)
         assert np.array_equal(vis, oracle.lookup_ndc(b.dag, b.num_levels, b.leafmasks, q))
+
+
+def _all_voxels(n):
+    zz, yy, xx = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    return np.stack([xx.ravel(), yy.ravel(), zz.ravel()], 1).astype(np.int32)
+
+
+@pytest.mark.parametrize("kind", ["uniform", "scene", "quantised"])
+def test_every_voxel_answer_is_the_direct_depth_test(oracle, kind):
+    """A size-independent property of the whole build: every voxel's answer
+    from the DAG equals the per-voxel test of cs::absoluteVisible
+    (src/CompressedShadowUtil.h:51-57) applied to the map directly -- lit iff
+    the float32 voxel centre (Z + (Z+1)) * 0.5 <= fl(d * n * zTileNum) for the
+    global voxel height Z = z + t*n of z-tile t.  It holds exactly because a
+    level's height is the map's divided by a power of two, so the min/max
+    classification of an inner node never contradicts its voxels."""
+    from cpvs_gb300 import scene
+    n = 64
+    g = np.random.default_rng(11)
+    if kind == "uniform":
+        d = g.uniform(0, 1, (n, n)).astype(np.float32)
+    elif kind == "scene":
+        d = scene.rasterise(scene.make_scene(n, 0.9, 10, 2, 3))
+    else:
+        d = (np.floor(g.uniform(0, 1, (n, n)) * n) / n).astype(np.float32)
+    q = _all_voxels(n)
+    f32 = np.float32
+    for K, leaf in ((1, True), (4, True), (1, False), (2, False)):
+        for t in range(K):
+            b = oracle.build(d, t, K, leafmasks=leaf)
+            got = oracle.lookup_voxel(b.dag, b.num_levels, b.leafmasks, q)
+            Z = q[:, 2].astype(np.int64) + t * n
+            mid = (Z.astype(f32) + (Z + 1).astype(f32)) * f32(0.5)
+            dh = d[q[:, 1], q[:, 0]].astype(f32) * f32(n * K)
+            want = np.where(mid <= dh, 1, 0)
+            assert np.array_equal(got, want), (kind, K, t, leaf)
