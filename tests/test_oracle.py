@@ -245,3 +245,54 @@ def test_every_voxel_answer_is_the_direct_depth_test(oracle, kind):
             dh = d[q[:, 1], q[:, 0]].astype(f32) * f32(n * K)
             want = np.where(mid <= dh, 1, 0)
             assert np.array_equal(got, want), (kind, K, t, leaf)
+
+
+def _walk_dag(dag, num_levels, leafmasks):
+    """Parses a DAG from its root, level by level: returns per level the node
+    offsets and words, after checking the reference's layout
+    (src/CompressedShadow.cpp:306-392): each level's nodes lie back to back,
+    levels follow each other top-down from word 0, and a level's nodes are in
+    the order of their first reference from the level above (parents in
+    order, children in index order)."""
+    levels = {}
+    frontier, L, expect = [0], num_levels - 2, 0
+    while frontier:
+        nodes, refs = [], []
+        for off in frontier:
+            assert off == expect, ("level not contiguous", L, off, expect)
+            m = int(dag[off])
+            k = bin(m & 0xAAAA).count("1")
+            leaf = leafmasks and L == 2
+            size = 1 + (2 * k if leaf else k)
+            words = tuple(int(w) for w in dag[off:off + size])
+            nodes.append(words)
+            if not leaf:
+                refs.extend(words[1:])
+            expect = off + size
+        levels[L] = nodes
+        first = list(dict.fromkeys(refs))  # first-occurrence order
+        assert first == sorted(first), ("children not in first-occurrence order", L)
+        frontier, L = first, L - 1
+    assert expect == len(dag), ("words outside the reachable nodes", expect, len(dag))
+    return levels
+
+
+@pytest.mark.parametrize("leaf", [True, False])
+def test_dag_is_minimal_and_laid_out_as_the_reference(oracle, leaf):
+    """No two nodes of a level are equal (the merge is complete), every word
+    belongs to a reachable node, and the per-level node counts are the
+    unique counts the build reports."""
+    from cpvs_gb300 import scene
+    g = np.random.default_rng(2)
+    maps = [g.uniform(0, 1, (64, 64)).astype(np.float32),
+            scene.rasterise(scene.make_scene(256, 0.9, 40, 4, 12)),
+            (np.floor(g.uniform(0, 1, (128, 128)) * 8) / 8).astype(np.float32)]
+    for d in maps:
+        for t, K in ((0, 1), (1, 2)):
+            b = oracle.build(d, t, K, leafmasks=leaf)
+            if not b.ref_defined:
+                continue
+            levels = _walk_dag(b.dag, b.num_levels, b.leafmasks)
+            for L, nodes in levels.items():
+                assert len(set(nodes)) == len(nodes), ("duplicate nodes", L)
+                assert len(nodes) == b.unique_nodes[L], (L, len(nodes), b.unique_nodes[L])
