@@ -296,3 +296,14 @@ def test_dag_is_minimal_and_laid_out_as_the_reference(oracle, leaf):
             for L, nodes in levels.items():
                 assert len(set(nodes)) == len(nodes), ("duplicate nodes", L)
                 assert len(nodes) == b.unique_nodes[L], (L, len(nodes), b.unique_nodes[L])
+
+
+def test_reference_dags_have_the_layout_the_walker_checks(golden, golden_cases):
+    """The same layout and minimality checks hold for every DAG the
+    reference itself wrote into the golden fixtures, so they restate the
+    reference's format rather than the oracle's."""
+    for key in golden_cases:
+        nl, _tv, lm = golden[f"{key}/meta"].tolist()
+        levels = _walk_dag(golden[f"{key}/dag"], nl, bool(lm))
+        for L, nodes in levels.items():
+            assert len(set(nodes)) == len(nodes), (key, L)
