@@ -12,7 +12,8 @@
  *   - `stream` is a cudaStream_t passed as void* (NULL = the legacy default
  *     stream).  Calls are stream-ordered; calls that return host data
  *     synchronise that stream before returning.
- *   - Pointers are host memory unless the call's flags say CPVS_IO_DEVICE.
+ *   - Pointers are host memory unless the call's flags say CPVS_IO_DEVICE
+ *     (cpvs_shade, which has no flags, takes any buffer the GPU can reach).
  *   - Handles are immutable after creation and may be read from several host
  *     threads; a cpvs_ctx must not be used by two host threads at once.
  *   - Visibility classes follow the reference's NodeVisibility
@@ -199,7 +200,8 @@ CPVS_API void cpvs_shadow_destroy(cpvs_shadow* s);
 CPVS_API uint32_t cpvs_shadow_num_levels(const cpvs_shadow* s);
 /* 1 if the DAG uses 64-bit leafmasks. */
 CPVS_API int cpvs_shadow_uses_leafmasks(const cpvs_shadow* s);
-/* CompressedShadow::getTotalVisibility (src/CompressedShadow.cpp:66-72). */
+/* CompressedShadow::getTotalVisibility (src/CompressedShadow.cpp:66-72);
+ * CPVS_PARTIAL ("descend to know") for a null shadow. */
 CPVS_API cpvs_visibility cpvs_shadow_total_visibility(const cpvs_shadow* s);
 /* Number of 32-bit words in the DAG. */
 CPVS_API uint64_t cpvs_shadow_dag_size(const cpvs_shadow* s);

@@ -100,3 +100,30 @@ def test_python_buffers_are_checked_before_the_call():
         _checked(t, np.uint32, 8, "t", device=0)
     with pytest.raises(ValueError, match="contiguous"):
         _checked(torch.zeros(4, 4)[:, 1], np.float32, 4, "t")
+
+
+def test_every_entry_point_refuses_null_handles(lib):
+    """Every entry point called with null handles and pointers (sizes 1)
+    returns CPVS_ERR_INVALID_ARG, or a neutral value for the queries, without
+    touching the device."""
+    import ctypes as C
+    import cpvs_gb300
+    not_status = {"cpvs_abi_version", "cpvs_shadow_uses_leafmasks", "cpvs_shadow_total_visibility",
+                  "cpvs_ctx_get_option"}
+    called = 0
+    for name, (res, args) in sorted(cpvs_gb300._SIGS.items()):
+        if res is C.c_char_p:
+            continue
+        vals = [None if (a is C.c_void_p or (isinstance(a, type) and issubclass(a, C._Pointer)))
+                else (0.0 if a is C.c_float else 1) for a in args]
+        r = getattr(lib, name)(*vals)
+        called += 1
+        if res is C.c_int and name not in not_status:
+            assert r == 1, (name, r, lib.cpvs_last_error())
+        elif name == "cpvs_shadow_total_visibility":
+            assert r == 2
+        elif name == "cpvs_ctx_get_option":
+            assert r == -1
+        elif res is not None and name != "cpvs_abi_version":
+            assert not r, (name, r)  # sizes and counts of nothing are 0, handles null
+    assert called >= 50
