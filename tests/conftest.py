@@ -11,6 +11,9 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 GOLDEN = os.path.join(ROOT, "tests", "golden", "reference_fixtures.npz")
+# the reference's own answers on the two benchmarked plain-method workloads
+# (tests/golden/make_golden_configs.py)
+GOLDEN_CONFIGS = os.path.join(ROOT, "tests", "golden", "reference_configs.npz")
 
 
 def pytest_configure(config):
@@ -26,6 +29,11 @@ def oracle():
 @pytest.fixture(scope="session")
 def golden():
     return np.load(GOLDEN)
+
+
+@pytest.fixture(scope="session")
+def golden_configs():
+    return np.load(GOLDEN_CONFIGS)
 
 
 @pytest.fixture(scope="session")

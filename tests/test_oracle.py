@@ -307,3 +307,36 @@ def test_reference_dags_have_the_layout_the_walker_checks(golden, golden_cases):
         levels = _walk_dag(golden[f"{key}/dag"], nl, bool(lm))
         for L, nodes in levels.items():
             assert len(set(nodes)) == len(nodes), (key, L)
+
+
+def _sha(a):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("name", ["c0", "c1"])
+def test_oracle_matches_reference_at_config_scale(oracle, golden_configs, name):
+    """The benchmarked workloads themselves (1024^2, 40 boxes; 8192^2, 500
+    boxes and 64 spheres), against what the reference's own create and
+    traverse wrote (tests/golden/make_golden_configs.py): the DAG (words at
+    1024^2, length and SHA-256 at 8192^2), per-level tree and unique node
+    counts, numLevels, and the answers on 2^16 mixed NDC points."""
+    from cpvs_gb300 import scene
+    g = golden_configs
+    d = scene.rasterise(scene.config_scene(name))
+    assert _sha(d) == str(g[f"{name}/map_sha256"]), "the scene generator no longer reproduces the map"
+    b = oracle.build(d, threads=4)
+    nl, tv, words = g[f"{name}/meta"].tolist()
+    assert b.num_levels == nl and b.dag.size == words
+    assert _sha(b.dag) == str(g[f"{name}/dag_sha256"])
+    if name == "c0":
+        assert np.array_equal(b.dag, g["c0/dag"])
+    assert list(b.unique_nodes) == g[f"{name}/unique_nodes"].tolist()
+    assert list(b.tree_nodes) == g[f"{name}/tree_nodes"].tolist()
+    q = scene.ndc_queries_mixed(d, 1 << 16, int(g[f"{name}/ndc_seed"]))
+    assert _sha(q) == str(g[f"{name}/ndc_sha256"])
+    assert np.array_equal(oracle.lookup_ndc(b.dag, nl, True, q, threads=4), g[f"{name}/ndc_vis"])
+    if name == "c0":
+        v = scene.voxel_queries(1 << 20, 1024, 0)[:1 << 16]
+        assert _sha(v) == str(g["c0/voxel_sha256"])
+        assert np.array_equal(oracle.lookup_voxel(b.dag, nl, True, v, threads=4), g["c0/voxel_vis"])
