@@ -8,9 +8,10 @@
  * memory and a byte per pixel out.  Differences a caller can see:
  *   - DAGs live on the GPU; getDAG() reads them back once and caches them;
  *   - traverse(position, tryLeafmasks) answers one point by a GPU lookup
- *     (batch with lookup() instead).  It follows the DAG's own leafmask mode:
- *     tryLeafmasks = false on a leafmask DAG (which the reference reads past
- *     its leaf level) is not reproduced;
+ *     (batch with lookup() instead).  tryLeafmasks must match the DAG's
+ *     leafmask mode: a mismatch (which the reference answers by reading leaf
+ *     nodes as inner nodes, src/CompressedShadow.cpp:408-430) throws
+ *     cpvs::Error with CPVS_ERR_INVALID_ARG;
  *   - errors throw cpvs::Error (the reference asserts).
  * By default the classes are also declared in the global namespace, like
  * the reference's; define CPVS_NO_GLOBAL_NAMES to keep them in cpvs::.
@@ -176,7 +177,8 @@ public:
     CompressedShadow& operator=(const CompressedShadow&) = delete;
 
     NodeVisibility traverse(const vec3 position, bool tryLeafmasks = true) {
-        (void)tryLeafmasks;
+        if (tryLeafmasks != (cpvs_shadow_uses_leafmasks(m_s) == 1))
+            throw Error(CPVS_ERR_INVALID_ARG, "CompressedShadow::traverse: tryLeafmasks must match the DAG's leafmask mode");
         const float p[3] = {position.x, position.y, position.z};
         uint32_t bits = 0;
         check(cpvs_shadow_lookup_ndc(m_s, p, 1, &bits, 0, nullptr));

@@ -62,6 +62,16 @@ int main(int argc, char** argv) {
         for (size_t i = 0; i < npts; ++i)
             trav[i] = (uint8_t)cs->traverse(vec3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]));
         write_file(out + ".trav", trav.data(), trav.size());
+        // tryLeafmasks that does not match the DAG's mode is refused, not misread
+        if (n >= 16) {
+            bool refused = false;
+            try {
+                cs->traverse(vec3(0.f, 0.f, 0.f), false);
+            } catch (const cpvs::Error& e) {
+                refused = e.status == CPVS_ERR_INVALID_ARG;
+            }
+            if (!refused) return 5;
+        }
 
         // the container path: copyToGPU, setFilterSize, evaluate
         CompressedShadowContainer container(std::move(cs));
