@@ -4,7 +4,7 @@ Run in a checkout where the reference is present (it is read, never
 modified):
 
     make -C oracle ref            # the reference's own CPU build, in place
-    python tests/golden/make_golden.py [/path/to/reference]
+    python tests/golden/make_golden.py [/path/to/reference]   # default: $CPVS_REFERENCE_DIR
 
 Inputs:
   * the depth images of the reference's unit tests, parsed from
@@ -122,4 +122,4 @@ def main(ref_dir: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CPVS_REFERENCE_DIR", "/root/reference"))
