@@ -129,19 +129,23 @@ def kernel_alg_bytes(name: str, n: int, tree: list, uniq: list, dag_words: int) 
     texels = sum((n >> L) ** 2 for L in range(first, int(np.log2(n)) + 1))
     inner = sum(tree[3:])
     uleaves = uniq[2] if len(uniq) > 2 else 0
-    if name == "pyramid":          # depth read once, every stored pyramid texel written once
+    cols = (n // 8) ** 2
+    if name == "k_pyramid64":      # depth read once, every stored pyramid texel written once
         return 4.0 * n * n + 8.0 * texels
-    if name == "leaf_masks":       # depth map once; per leaf coord + job in, class mask + slot out, one slot
-        # probe; the 64 B of masks only for the class representatives
-        return 4.0 * n * n + leaves * (8 + 4 + 4 + 4 + 8) + uleaves * 64
-    if name == "expand_write":     # per inner node coord + job + 2x2 pyramid texels in, mask + first out;
+    if name == "k_leaf_columns":   # depth map once, the level-3 bounds once, a record per column; per leaf
+        # class its masks, job and record (the 16 B run entries, one or more per column, are not counted)
+        return 4.0 * n * n + cols * (8 + 8) + uleaves * (64 + 4 + 8)
+    if name == "k_leaf_resolve":   # per leaf coord + job in, class id + class mask out; each column's
+        # record once
+        return leaves * (8 + 4 + 4 + 4) + cols * 8
+    if name == "k_expand":         # per inner node coord + job + 2x2 pyramid texels in, mask + first out;
         # 12 B per child written
         return inner * (8 + 4 + 32 + 8) + (leaves + inner) * 12
-    if name == "insert_inner":     # per inner node mask + job + first + slot probe + slot out; 4 B per child id
+    if name == "k_dedup_insert":   # per inner node mask + job + first + slot probe + slot out; 4 B per child id
         return inner * (4 + 4 + 4 + 8 + 4) + (leaves + inner) * 4
-    if name == "scan":             # per node slot + mask + job + table entry in; rank, offset out
+    if name == "k_merge_scan":     # per node slot + mask + job + table entry in; rank, offset out
         return (leaves + inner) * (4 + 4 + 4 + 8 + 4)
-    if name == "emit":
+    if name == "k_emit_all":
         return 4.0 * dag_words
     return 0.0
 
@@ -243,7 +247,7 @@ def run_ours(args, rank, world, local_rank):
     e1.record(stream)
     barrier()
     lookup_ms = e0.elapsed_time(e1) / args.steps
-    lk = ctx.kernel_times()["lookup"]
+    lk = ctx.kernel_times()["k_lookup"]
     ctx.enable_timing(False)
     # the tuner's alternatives (queries carried per thread), for the record
     variants = {}
@@ -303,7 +307,7 @@ def run_ours(args, rank, world, local_rank):
         return
 
     peak, peak_kind = peaks()
-    build_kernels = {k: v for k, v in ktimes.items() if v[1] and k not in ("lookup", "grid_lookup")}
+    build_kernels = {k: v for k, v in ktimes.items() if v[1] and k not in ("k_lookup", "k_grid_lookup")}
     dom = max(build_kernels, key=lambda k: build_kernels[k][0])
     dom_ms_launch = build_kernels[dom][0] / build_kernels[dom][1]
     dom_launches_per_step = build_kernels[dom][1] / args.steps
@@ -413,14 +417,14 @@ def measure_frame(cp, torch, ctx, sh, q_dev, stream, steps, warmup, barrier, wid
     kt = ctx.kernel_times()
     ctx.enable_timing(False)
     frame_ms = e0.elapsed_time(e1) / steps
-    ev, sd = kt["evaluate"], kt["shade"]
+    ev, sd = kt["k_grid_evaluate"], kt["k_shade"]
     shade_ms = sd[0] / max(sd[1], 1)
     shade_bytes = npix * (16 + 16 + 1 + 16)  # normal, albedo, visibility byte in; colour out
     return {"pixels": npix, "resolution": f"{width}x{height}", "ms_per_frame": round(frame_ms, 4),
             "fps": round(1e3 / frame_ms, 1), "evaluate_ms": round(ev[0] / max(ev[1], 1), 4),
             "shade_ms": round(shade_ms, 4),
             "path": "cpvs_grid_evaluate (u8, filter 1) + cpvs_shade, G-buffer resident in HBM",
-            "shade_roofline": {"bound": "hbm", "kernel": "shade", "alg_bytes_per_launch": shade_bytes,
+            "shade_roofline": {"bound": "hbm", "kernel": "k_shade", "alg_bytes_per_launch": shade_bytes,
                                "achieved": round(shade_bytes / (shade_ms * 1e-3) / 1e9, 1)},
             "gpu_launches": int(ev[1] + sd[1])}
 

@@ -35,7 +35,6 @@
 // another, so nothing can hang.
 #include <algorithm>
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include <cooperative_groups.h>
@@ -70,6 +69,8 @@ struct JobDev {
     const float2* pyr;  // pyramid levels 1..log2(n)
     const float* depth;  // level 0
     uint32_t n, num_levels, z_idx, z_num;
+    uint32_t group;      // leaf column group of its source (build plans with leafmasks)
+    uint32_t pad;
 };
 
 // Per-level node arrays (capacity `cap`).
@@ -232,6 +233,13 @@ __device__ __forceinline__ void fetch_wait() {
 }
 
 // ---------------------------------------------------------------- top-down
+// The multi-pass kernels (k_expand_count, k_expand_write, k_classify_bottom,
+// k_leaf_masks, k_dedup_insert<true>, k_dedup_resolve, k_dedup_scan,
+// k_dedup_remap, k_emit) serve only the allocation-free build
+// (cpvs_shadow_build_noalloc, at the end of this file): it has no plan, so
+// no look-back flags or tickets.  Changes to the node layout or the error
+// bits of the main path must be mirrored in them.
+//
 // Pass 1: per-CTA sum of partial children over its chunk of level L.
 __global__ void __launch_bounds__(kThreads)
     k_expand_count(LevelDev cur, const uint32_t* __restrict__ counts, const JobDev* __restrict__ jobs, uint32_t njobs,
@@ -405,46 +413,37 @@ __device__ __forceinline__ void leaf_rows(const float* row0, uint32_t nmap, floa
     }
 }
 
-// The eight 64-bit slice masks of leaf i (level-2 node: the 8x8x8 voxels at
-// 4 * its coordinate), its 16-bit class mask (01 lit / 00 shadow / 10
-// partial per slice, src/CompressedShadowUtil.cpp:59-99) and its signature
-// hash.  Per texel row: the eight lit counts, packed as nibbles, transposed
-// into count bit-planes; slice s is then {texels with count > s}.  Two common
-// kinds of leaf skip the transposes: all 64 counts equal to k (a flat patch
-// of surface: slices 0..k-1 full, the rest empty) and all counts 0 or 8 (a
-// wall crossing the leaf: every slice the set of count-8 texels).  Every path
-// gives the same masks for the same leaf, so the same hash.  `c` and `j` are the leaf's coordinate and
-// job.  Returns false for a stale slot (an internal check already failed):
-// the caller then treats it as an empty leaf of job 0 (j becomes 0).
-template <bool POW2>
-__device__ __forceinline__ bool leaf_compute(const JobDev* __restrict__ jobs, uint32_t njobs, uint64_t c,
-                                             uint64_t M[8], uint32_t& mask, uint64_t& hash, uint32_t& j) {
-    const uint32_t bx = unpack_x(c) * 4u, by = unpack_y(c) * 4u, bz = unpack_z(c) * 4u;
-    if (j >= njobs || bx + 8u > __ldg(&jobs[j].n) || by + 8u > __ldg(&jobs[j].n)) {
+// The eight 64-bit slice masks of a leaf and its 16-bit class mask (01 lit /
+// 00 shadow / 10 partial per slice, src/CompressedShadowUtil.cpp:59-99) from
+// the lit counts of its 8x8 texels (W[y]: row y, texel x at nibble x).  Per
+// texel row the eight counts, packed as nibbles, are transposed into count
+// bit-planes; slice s is then {texels with count > s}.  Two common kinds of
+// leaf skip the transposes: all 64 counts equal to k (a flat patch of
+// surface: slices 0..k-1 full, the rest empty) and all counts 0 or 8 (a wall
+// crossing the leaf: every slice the set of count-8 texels).  Every path
+// gives the same masks for the same counts.
+// A leaf whose 64 counts all equal k (k0 receives it): its slices 0..k-1
+// are full, the rest empty.  These are the only leaves with such masks.
+__device__ __forceinline__ bool leaf_uniform(const uint32_t W[8], uint32_t& k0) {
+    k0 = W[0] & 0xFu;
+    const uint32_t rep = k0 * 0x11111111u;
+    bool uniform = true;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) M[q] = 0ull;
-        mask = 0;
-        j = 0;
-        hash = 0;
-        return false;
-    }
-    const uint32_t nmap = __ldg(&jobs[j].n);
-    const uint32_t Hu = nmap * __ldg(&jobs[j].z_num);
-    const float c8 = __fmul_rn(__fsub_rn(0.5f, __uint2float_rn(bz)), 0.125f);  // exact: bz < 2^23
-    const float* row0 = jobs[j].depth + (size_t)by * nmap + bx;
-    uint32_t W[8];
-    leaf_rows<POW2>(row0, nmap, __uint2float_rn(Hu), c8, W);
-    const uint32_t k0 = W[0] & 0xFu, rep = k0 * 0x11111111u;
-    bool uniform = true, binary = true;
+    for (int y = 0; y < 8; ++y) uniform = uniform && W[y] == rep;
+    return uniform;
+}
+__device__ __forceinline__ uint32_t uniform_class_mask(uint32_t k) { return 0x5555u & ((1u << (2u * k)) - 1u); }
+
+__device__ __forceinline__ void leaf_masks_from_counts(const uint32_t W[8], uint64_t M[8], uint32_t& mask) {
+    uint32_t k0;
+    const bool uniform = leaf_uniform(W, k0);
+    bool binary = true;
 #pragma unroll
-    for (int y = 0; y < 8; ++y) {
-        uniform = uniform && W[y] == rep;
-        binary = binary && (W[y] & 0x77777777u) == 0u;
-    }
+    for (int y = 0; y < 8; ++y) binary = binary && (W[y] & 0x77777777u) == 0u;
     if (uniform) {
 #pragma unroll
         for (uint32_t q = 0; q < 8; ++q) M[q] = q < k0 ? ~0ull : 0ull;
-        mask = 0x5555u & ((1u << (2u * k0)) - 1u);
+        mask = uniform_class_mask(k0);
     } else if (binary) {
         // every count is 0 or 8 (a wall of the shadow volume crossing the
         // leaf): all eight slices are the set of count-8 texels, and every
@@ -498,13 +497,43 @@ __device__ __forceinline__ bool leaf_compute(const JobDev* __restrict__ jobs, ui
             mask |= cls << (2 * q);
         }
     }
+}
+
+// Signature hash of a leaf: its job and its eight slice masks.
+__device__ __forceinline__ uint64_t leaf_hash(uint32_t j, const uint64_t M[8]) {
     uint64_t h = (uint64_t)(j + 1) * kGolden;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         h = (h ^ M[q]) * 0xD6E8FEB86659FD93ull;
         h ^= h >> 32;
     }
-    hash = fmix64(h);
+    return fmix64(h);
+}
+
+// The slice masks, class mask and signature hash of the leaf at level-2
+// coordinate `c` of job `j` (the 8x8x8 voxels at 4c), read from the depth
+// map.  Returns false for a stale slot (an internal check already failed):
+// the caller then treats it as an empty leaf of job 0 (j becomes 0).
+template <bool POW2>
+__device__ __forceinline__ bool leaf_compute(const JobDev* __restrict__ jobs, uint32_t njobs, uint64_t c,
+                                             uint64_t M[8], uint32_t& mask, uint64_t& hash, uint32_t& j) {
+    const uint32_t bx = unpack_x(c) * 4u, by = unpack_y(c) * 4u, bz = unpack_z(c) * 4u;
+    if (j >= njobs || bx + 8u > __ldg(&jobs[j].n) || by + 8u > __ldg(&jobs[j].n)) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) M[q] = 0ull;
+        mask = 0;
+        j = 0;
+        hash = 0;
+        return false;
+    }
+    const uint32_t nmap = __ldg(&jobs[j].n);
+    const uint32_t Hu = nmap * __ldg(&jobs[j].z_num);
+    const float c8 = __fmul_rn(__fsub_rn(0.5f, __uint2float_rn(bz)), 0.125f);  // exact: bz < 2^23
+    const float* row0 = jobs[j].depth + (size_t)by * nmap + bx;
+    uint32_t W[8];
+    leaf_rows<POW2>(row0, nmap, __uint2float_rn(Hu), c8, W);
+    leaf_masks_from_counts(W, M, mask);
+    hash = leaf_hash(j, M);
     return true;
 }
 
@@ -553,91 +582,396 @@ __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long lon
     return v;
 }
 
-// Leaf masks fused with the leaf level's dedup insert: each leaf keeps its
-// masks in registers and looks its class up in the (cleared) table right
-// away.  Only a leaf that becomes, even for a while, its class's
-// representative stores its masks -- before it publishes itself in the slot
-// (fence, then CAS or atomicMin), so a reader that sees its index in a slot
-// (acquire load) reads complete masks.  Every other leaf (the vast
-// majority: c. 7.9 M leaves fold into 137 k classes at 8192^2) writes only
-// its class mask and slot.  The slot rule is dedup_insert's: it ends with
-// the class's smallest index, the first occurrence.
+// ------------------------------------------------------------ leaf columns
+// The leaf level (level 2 with leafmasks) of a build plan is computed per
+// texel column instead of per leaf.  A leaf at level-2 coordinate c covers
+// the 8x8 texels of level-3 texel (c.x/2, c.y/2) -- its column -- and the
+// voxels of level-3 z-cell zc = c.z/2.  Its parent classified exactly that
+// (column, z-cell) as partial against the column's level-3 min/max, so
+// every leaf lies in its column's partial z-cells [zlo, zhi]; along them
+// the eight slice masks change only where some texel's highest lit voxel
+// Z_t (lit iff z + 0.5 <= fl(d * H0)) enters or leaves the z-cell: a texel
+// counts 8 lit voxels while 8 zc + 7 <= Z_t, then between 1 and 7 for at
+// most one z-cell, then 0.  The partial z-cells of a column therefore fall
+// into runs of equal leaves (the c1 workload: 7.3 M leaves, 1.24 M runs).
+//
+// k_leaf_columns (one thread per column, beside the expansion) walks the
+// runs of every column of the batch's maps over the z-tiles of the jobs that
+// use it, computes each run's masks once from the map, and inserts the
+// class (job, masks) into a hash table; a class's identity is the index of
+// the run entry that first claimed it.  k_leaf_resolve (after the expansion
+// has listed the leaves in breadth-first order) looks each leaf's run up
+// and lowers its class's first-occurrence index -- the class record keeps
+// (rank << 32 | smallest leaf index), as the inner levels' table slots do.
+// Leaves of a column whose ancestors are not all partial get runs too
+// (never referenced, never kept); a run covers at least one leaf cell, so
+// the runs fit in the level's planned capacity.
+
+struct LeafGroupDev {      // one source map and z_num; its jobs' z-tiles are distinct
+    const float2* lvl3;    // pyramid level 3 of the map: (n/8)^2 (min, max) pairs
+    const float* depth;    // the map, n x n
+    uint32_t n, z_num;
+    uint32_t job_lo, job_cnt;  // its jobs in the z-tile table, ordered by z_idx
+    uint64_t col_base;         // its first column record
+};
+
+struct LeafColumns {
+    const LeafGroupDev* groups;
+    const uint2* ztiles;        // (z_idx, job) per job, by group, ordered by z_idx
+    const uint32_t* meta;       // [0] groups, [1] column records in use
+    uint2* colrec;              // per column: first run entry, run count
+    uint4* runs;                // per run: last z-cell, class id, class mask, job
+    uint32_t run_cap;
+    unsigned int* run_ctr;      // run entries reserved (zeroed per build)
+    uint64_t* cls_slices;       // per class id: the 8 slice masks
+    uint32_t* cls_job;          // per class id: its job
+    unsigned long long* crec;   // per class id: rank << 32 | first occurrence
+    unsigned long long* table;  // class hash table: tag << 32 | class id
+    uint64_t table_mask;
+    uint32_t njobs;             // uniform classes: id run_cap + 9 * job + k (all counts k)
+    uint32_t* pending;          // run entries of non-uniform leaves, for k_leaf_classes
+    unsigned int* pending_ctr;  // their count (zeroed per build)
+};
+
+// Lit counts of the column at (row0, row stride nmap) for the leaf of
+// z-cell zc (W as leaf_rows gives them), and the last z-cell through which
+// the leaf stays the same: zc itself when a texel is partly lit there, else
+// the first z-cell after which a fully lit texel stops being full (or zmax).
+// A texel with count 8 has Z_t >= 8 zc + 7 and stays full through
+// floor((Z_t - 7) / 8) = floor(v / 8 - 0.9375) with v = fl(d * H0): one
+// fused multiply-add rounded down gives that floor exactly (the exact value
+// is rounded toward the integer below it, which is representable).  NaN
+// depths count 0 everywhere; +inf counts 8 everywhere (its run never ends).
 template <bool POW2>
-__global__ void __launch_bounds__(kThreads, 5)
-    k_leaf_insert(LevelDev lv, const uint32_t* __restrict__ counts, const JobDev* __restrict__ jobs, uint32_t njobs,
-                  int L, SegDev seg, unsigned long long* table, uint64_t cap_mask, uint32_t* err) {
-    chain_enter();
-    const uint32_t n = counts[L];
-    const uint32_t stride = gridDim.x * blockDim.x;
-    // the next leaf's coordinate and job are requested one iteration ahead
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint64_t c_next = i < n ? lv.coord[i] : 0ull;
-    uint32_t j_next = i < n ? lv.job[i] : 0u;
-    for (; i < n; i += stride) {
-        const uint64_t c = c_next;
-        uint32_t j = j_next;
-        if (i + stride < n) {
-            c_next = lv.coord[i + stride];
-            j_next = lv.job[i + stride];
+__device__ __forceinline__ uint32_t column_counts(const float* row0, uint32_t nmap, float H, uint32_t zc,
+                                                  uint32_t zmax, uint32_t W[8]) {
+    const float s = POW2 ? __fmul_rn(H, 0.125f) : 0.125f;
+    const float c8 = __fmul_rn(__fsub_rn(0.5f, __uint2float_rn(8u * zc)), 0.125f);  // exact: 8 zc < 2^23
+    constexpr uint32_t bias = kCountBias + (kCountBias << 4) + (kCountBias << 8) + (kCountBias << 12) +
+                              (kCountBias << 16) + (kCountBias << 20) + (kCountBias << 24) + (kCountBias << 28);
+    float vfull = __int_as_float(0x7f800000);  // smallest v among the fully lit texels
+    uint32_t part = 0;
+    // all sixteen 16-byte loads of the 8x8 footprint in flight at once
+    float4 r[16];
+#pragma unroll
+    for (int y = 0; y < 8; ++y) {
+        r[2 * y] = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap));
+        r[2 * y + 1] = __ldg(reinterpret_cast<const float4*>(row0 + (size_t)y * nmap + 4));
+    }
+#pragma unroll
+    for (int y = 0; y < 8; ++y) {
+        const float4 a = r[2 * y], b = r[2 * y + 1];
+        const float d[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+        uint32_t w = 0;
+#pragma unroll
+        for (int x = 0; x < 8; ++x) {
+            const float v = POW2 ? d[x] : __fmul_rn(d[x], H);
+            const uint32_t cb = lit_count_bits(v, s, c8);
+            w += cb << (4 * x);
+            vfull = cb == kCountBias + 8u ? fminf(vfull, v) : vfull;
         }
-        uint64_t M[8], h;
-        uint32_t mask;
-        if (!leaf_compute<POW2>(jobs, njobs, c, M, mask, h, j)) {
-            atomicOr(err, 4u);
-            lv.job[i] = 0;
-        } else {
-            leaf_segments(lv, seg, i, n, j, L, njobs, err);
+        W[y] = w - bias;
+        part |= W[y] & 0x77777777u;  // some count in 1..7
+    }
+    if (part) return zc;
+    float t;
+    asm("fma.rm.f32 %0, %1, %2, %3;" : "=f"(t) : "f"(vfull), "f"(s), "f"(-0.9375f));
+    t = floorf(t);
+    return t >= __uint2float_rn(zmax) ? zmax : (uint32_t)t;  // t >= zc here (the texel is full at zc)
+}
+
+// Inserts the class of run entry `cid` (job j, masks M, hash h) into the
+// class hash table and returns the class id: the entry index of the run that
+// claimed the class's slot.  Every run's masks and job were stored at its own
+// entry index by the column pass, an earlier kernel, so a slot's claimant is
+// compared straight from memory (no publication order to keep).
+__device__ __forceinline__ uint32_t leaf_class_insert(const LeafColumns& lc, uint64_t h, uint32_t j,
+                                                      const uint64_t M[8], uint32_t cid, uint32_t* err) {
+    const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | cid;
+    uint64_t s = h & lc.table_mask;
+    for (uint64_t probe = 0; probe <= lc.table_mask; ++probe) {
+        unsigned long long e = __ldcg(&lc.table[s]);
+        if (e == kEmptySlot) {
+            e = atomicCAS(&lc.table[s], kEmptySlot, key);
+            if (e == kEmptySlot) return cid;
         }
-        lv.mask[i] = mask;
-        const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | i;
-        uint64_t s = h & cap_mask;
-        bool placed = false, published = false;
-        for (uint64_t probe = 0; probe <= cap_mask; ++probe) {
-            unsigned long long e = ld_acquire(&table[s]);
-            if (e == kEmptySlot) {
-                store_slices(lv, i, M);
-                __threadfence();
-                published = true;
-                const unsigned long long prev = atomicCAS(&table[s], kEmptySlot, key);
-                if (prev == kEmptySlot) {
-                    placed = true;
-                    break;
-                }
-                __threadfence();  // acquire: the winner's masks are read below
-                e = prev;
+        if ((e >> 32) == (key >> 32)) {
+            const uint32_t r = (uint32_t)e;
+            if (r < lc.run_cap) {
+                const ulonglong2* o = reinterpret_cast<const ulonglong2*>(lc.cls_slices + (size_t)r * 8);
+                const uint32_t jr = __ldg(lc.cls_job + r);
+                ulonglong2 x[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) x[q] = __ldg(o + q);
+                bool same = jr == j;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) same = same && x[q].x == M[2 * q] && x[q].y == M[2 * q + 1];
+                if (same) return r;
             }
-            if ((e >> 32) == (key >> 32)) {
-                // the candidate's job and masks in one round of loads (it
-                // published its masks before its index reached the slot)
-                const uint32_t r = (uint32_t)e;
-                bool same = r < n;
-                if (same) {
-                    const ulonglong2* o = reinterpret_cast<const ulonglong2*>(lv.slices + (size_t)r * 8);
-                    const uint32_t jr = __ldcg(lv.job + r);
-                    ulonglong2 x[4];
+        }
+        s = (s + 1) & lc.table_mask;
+    }
+    atomicOr(err, 16u);  // table full: the result is void, reported (the plan grows)
+    return cid;
+}
+
+// One thread per non-uniform run: its class id into the run entry.
+__global__ void __launch_bounds__(kThreads) k_leaf_classes(LeafColumns lc, uint32_t* err) {
+    const uint32_t np = *lc.pending_ctr;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+        const uint32_t cid = lc.pending[p];
+        if (cid >= lc.run_cap) {
+            atomicOr(err, 512u);
+            continue;
+        }
+        const ulonglong2* o = reinterpret_cast<const ulonglong2*>(lc.cls_slices + (size_t)cid * 8);
+        uint64_t M[8];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) x[q] = __ldcg(o + q);
-                    same = jr == j;
+        for (int q = 0; q < 4; ++q) {
+            const ulonglong2 t = o[q];
+            M[2 * q] = t.x;
+            M[2 * q + 1] = t.y;
+        }
+        const uint32_t j = lc.cls_job[cid];
+        lc.runs[cid].y = leaf_class_insert(lc, leaf_hash(j, M), j, M, cid, err);
+    }
+}
+
+// Partial z-cells [zlo, zhi] of a column against its level-3 bounds b
+// (min, max) and level-3 height H3: !((zc+1) <= lo) && !(zc >= hi)
+// (cs::visible, src/CompressedShadowUtil.h:35-43) with lo/hi the bounds
+// times H3, a contiguous range; NaN bounds are partial.  Empty: zlo > zhi.
+__device__ __forceinline__ void column_partial_range(float2 b, uint32_t H3, uint32_t& zlo, uint32_t& zhi) {
+    const float Hf = __uint2float_rn(H3);
+    const float lo_s = __fmul_rn(b.x, Hf), hi_s = __fmul_rn(b.y, Hf);
+    zlo = lo_s != lo_s ? 0u : (uint32_t)fminf(fmaxf(floorf(lo_s), 0.f), Hf);
+    const float top = hi_s != hi_s ? Hf : fminf(fmaxf(ceilf(hi_s), 0.f), Hf);  // zhi + 1
+    if (top == 0.f) {
+        zlo = 1u;
+        zhi = 0u;
+    } else {
+        zhi = (uint32_t)top - 1u;
+    }
+}
+
+// Column q of the batch: its group, its coordinates and its partial range.
+struct ColumnAt {
+    uint32_t g, C, cx, cy, zlo, zhi;
+};
+__device__ __forceinline__ ColumnAt column_at(const LeafColumns& lc, uint32_t ngroups, uint64_t q) {
+    uint32_t lo = 0, hi = ngroups;  // the last group whose first column is <= q
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&lc.groups[mid].col_base) <= q) lo = mid; else hi = mid;
+    }
+    ColumnAt c;
+    c.g = lo;
+    const LeafGroupDev& G = lc.groups[lo];
+    c.C = __ldg(&G.n) >> 3;
+    const uint32_t local = (uint32_t)(q - __ldg(&G.col_base)), lg = 31u - (uint32_t)__clz((int)c.C);
+    c.cx = local & (c.C - 1u);
+    c.cy = local >> lg;
+    column_partial_range(__ldg(G.lvl3 + local), c.C * __ldg(&G.z_num), c.zlo, c.zhi);
+    return c;
+}
+
+// Partial leaf cells of a column over its group's z-tiles.
+__device__ __forceinline__ uint32_t column_cells(const LeafColumns& lc, const ColumnAt& c) {
+    const LeafGroupDev& G = lc.groups[c.g];
+    const uint32_t jl = __ldg(&G.job_lo), jc = __ldg(&G.job_cnt);
+    uint32_t cells = 0;
+    for (uint32_t k = 0; k < jc && c.zlo <= c.zhi; ++k) {
+        const uint32_t z0 = __ldg(&lc.ztiles[jl + k].x) * c.C;
+        const uint32_t a = max(c.zlo, z0), e = min(c.zhi, z0 + c.C - 1u);
+        if (a <= e) cells += e - a + 1u;
+    }
+    return cells;
+}
+
+// The runs of every column of the batch's maps.  A block takes a chunk of
+// kColChunk columns, kColItems per thread: it counts their partial leaf
+// cells, reserves that many run entries with one atomic add, then each
+// thread walks the runs of its columns in one flat loop -- a lane that
+// finishes a column moves on to its next one while its neighbours are still
+// inside theirs, so the warp steps through runs, not through the longest
+// column of each round.  Uniform leaves (all 64 counts equal to k: flat
+// surface, the most frequent classes) take the fixed class id
+// run_cap + 9 * job + k; the first block writes those classes' masks and
+// empty records.  Every other run stores its masks at its own entry and
+// joins the pending list that k_leaf_classes deduplicates.
+constexpr int kColItems = 2;
+constexpr uint32_t kColChunk = kThreads * kColItems;
+
+template <bool POW2>
+__global__ void __launch_bounds__(kThreads, 2) k_leaf_columns(LeafColumns lc, uint32_t* err) {
+    __shared__ uint32_t sm[64];
+    __shared__ uint32_t s_base;
+    const uint32_t ngroups = lc.meta[0];
+    const uint64_t ncols = lc.meta[1];
+    if (blockIdx.x == 0)
+        for (uint32_t u = threadIdx.x; u < 9u * lc.njobs; u += blockDim.x) {
+            const uint32_t id = lc.run_cap + u, k = u % 9u;
+            ulonglong2* o = reinterpret_cast<ulonglong2*>(lc.cls_slices + (size_t)id * 8);
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) same = same && x[q].x == M[2 * q] && x[q].y == M[2 * q + 1];
-                }
-                if (same) {
-                    if (r > i) {
-                        // an earlier occurrence: publish, then lower the slot
-                        if (!published) {
-                            store_slices(lv, i, M);
-                            __threadfence();
-                        }
-                        atomicMin(&table[s], key);
+            for (uint32_t q = 0; q < 4; ++q)
+                o[q] = make_ulonglong2(2 * q < k ? ~0ull : 0ull, 2 * q + 1 < k ? ~0ull : 0ull);
+            lc.cls_job[id] = u / 9u;
+            lc.crec[id] = kEmptySlot;
+        }
+    for (uint64_t chunk = blockIdx.x; chunk * kColChunk < ncols; chunk += gridDim.x) {
+        const uint64_t q0 = chunk * kColChunk + threadIdx.x;
+        uint32_t sum = 0;
+#pragma unroll
+        for (int it = 0; it < kColItems; ++it) {
+            const uint64_t q = q0 + (uint64_t)it * kThreads;
+            if (q < ncols) sum += column_cells(lc, column_at(lc, ngroups, q));
+        }
+        uint2 tot;
+        const uint32_t pre = block_exclusive_scan2(make_uint2(sum, 0u), tot, sm).x;
+        if (threadIdx.x == 0) s_base = tot.x ? atomicAdd(lc.run_ctr, tot.x) : 0u;
+        __syncthreads();
+        const uint32_t base = s_base;
+        __syncthreads();
+        const bool fits = (uint64_t)base + tot.x <= lc.run_cap;
+        if (!fits && threadIdx.x == 0) atomicOr(err, 1u);  // more runs than the plan holds: reported, the plan grows
+        // flat walk: column `it` of this thread, job `k` of its group, the
+        // current range [zc, e] of that job's z-tile
+        uint32_t off = base + pre;  // entry base of the current column
+        int it = 0;
+        bool open = false;  // column `it` is open: its record is not written yet
+        uint64_t q = 0;
+        ColumnAt c{};
+        uint32_t cells = 0, nrun = 0, jl = 0, jc = 0, k = 0, zc = 1, e = 0, job = 0, nmap = 0;
+        const float* row0 = nullptr;
+        float H0 = 0.f;
+        for (;;) {
+            // the next non-empty range: the next job of the open column, or
+            // the next column
+            while (zc > e) {
+                if (open) {
+                    if (++k < jc) {
+                        const uint2 zt = __ldg(&lc.ztiles[jl + k]);
+                        const uint32_t z0 = zt.x * c.C;
+                        zc = max(c.zlo, z0);
+                        e = min(c.zhi, z0 + c.C - 1u);
+                        job = zt.y;
+                        continue;
                     }
-                    placed = true;
+                    lc.colrec[q] = make_uint2(off, nrun);
+                    off += cells;
+                    open = false;
+                    ++it;
+                }
+                if (it >= kColItems) break;
+                q = q0 + (uint64_t)it * kThreads;
+                if (q >= ncols) {
+                    it = kColItems;
                     break;
                 }
+                c = column_at(lc, ngroups, q);
+                cells = column_cells(lc, c);
+                nrun = 0;
+                const LeafGroupDev& G = lc.groups[c.g];
+                jl = __ldg(&G.job_lo);
+                jc = (cells && fits) ? __ldg(&G.job_cnt) : 0u;  // no cells: the record only
+                nmap = __ldg(&G.n);
+                row0 = G.depth + (size_t)(c.cy * 8u) * nmap + c.cx * 8u;
+                H0 = __uint2float_rn(nmap * __ldg(&G.z_num));
+                open = true;
+                k = ~0u;  // the next ++k is job 0
+                zc = 1;
+                e = 0;
             }
-            s = (s + 1) & cap_mask;
+            if (it >= kColItems) break;
+            // one run: the leaf at z-cell zc and every following one equal to it
+            uint32_t W[8];
+            const uint32_t last = column_counts<POW2>(row0, nmap, H0, zc, e, W);
+            const uint32_t cid = off + nrun;
+            uint32_t id, mask, k0;
+            const bool uni = leaf_uniform(W, k0);
+            if (uni) {
+                id = lc.run_cap + 9u * job + k0;
+                mask = uniform_class_mask(k0);
+            } else {
+                // masks, job and an empty record at the run's own entry; the
+                // class id follows in k_leaf_classes
+                uint64_t M[8];
+                leaf_masks_from_counts(W, M, mask);
+                ulonglong2* o = reinterpret_cast<ulonglong2*>(lc.cls_slices + (size_t)cid * 8);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) o[q] = make_ulonglong2(M[2 * q], M[2 * q + 1]);
+                lc.cls_job[cid] = job;
+                lc.crec[cid] = kEmptySlot;
+                id = cid;
+            }
+            // the non-uniform runs of the warp's active lanes join the
+            // pending list with one atomic add
+            const unsigned act = __activemask();
+            const unsigned want = __ballot_sync(act, !uni);
+            if (want) {
+                const int lead = __ffs((int)want) - 1;
+                const uint32_t lane = threadIdx.x & 31u;
+                uint32_t at = 0;
+                if ((int)lane == lead) at = atomicAdd(lc.pending_ctr, (unsigned)__popc(want));
+                at = __shfl_sync(act, at, lead);
+                if (!uni) lc.pending[at + __popc(want & ((1u << lane) - 1u))] = cid;
+            }
+            lc.runs[cid] = make_uint4(last, id, mask, job);
+            ++nrun;
+            zc = last + 1u;
         }
-        if (!placed) atomicOr(err, 16u);  // table full: the result is void, reported
-        lv.slot[i] = (uint32_t)s;
+    }
+}
+
+// Every leaf (breadth-first order) takes its class from its column's runs:
+// class id (its merged identity for level 3) and class mask; then the
+// class's first-occurrence index is lowered to the leaf's if smaller.
+// Leaves of one class in one warp: only the first (lowest index) updates.
+__device__ __forceinline__ uint32_t leaf_class_of(const LeafColumns& lc, const JobDev* __restrict__ jobs,
+                                                  uint32_t njobs, uint64_t c, uint32_t j, uint32_t& mask, bool& ok) {
+    ok = false;
+    mask = 0;
+    if (j >= njobs) return 0;
+    const LeafGroupDev& G = lc.groups[__ldg(&jobs[j].group)];
+    const uint32_t C = __ldg(&G.n) >> 3;
+    const uint32_t cx = unpack_x(c) >> 1, cy = unpack_y(c) >> 1, zc = unpack_z(c) >> 1;
+    if (cx >= C || cy >= C) return 0;
+    const uint2 rec = lc.colrec[__ldg(&G.col_base) + (uint64_t)cy * C + cx];
+    for (uint32_t k = 0; k < rec.y; ++k) {
+        const uint4 e = lc.runs[rec.x + k];
+        if (zc <= e.x) {
+            ok = e.w == j && e.y < lc.run_cap + 9u * lc.njobs;
+            mask = e.z;
+            return e.y;
+        }
+    }
+    return 0;
+}
+
+__global__ void __launch_bounds__(kThreads)
+    k_leaf_resolve(LevelDev lv, const uint32_t* __restrict__ counts, const JobDev* __restrict__ jobs, uint32_t njobs,
+                   SegDev seg, LeafColumns lc, uint32_t* err) {
+    chain_enter();
+    const uint32_t n = counts[2];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t j = lv.job[i], mask = 0;
+        bool ok;
+        uint32_t id = leaf_class_of(lc, jobs, njobs, lv.coord[i], j, mask, ok);
+        if (!ok) {
+            atomicOr(err, 512u);  // a leaf outside its column's runs: reported, not followed
+            j = j < njobs ? j : 0u;
+            lv.job[i] = j;
+            id = 0;
+            mask = 0;
+        }
+        lv.slot[i] = id;
+        lv.mask[i] = mask;
+        leaf_segments(lv, seg, i, n, j, 2, njobs, err);
+        const unsigned same = __match_any_sync(__activemask(), id);
+        if ((threadIdx.x & 31u) == (uint32_t)(__ffs((int)same) - 1)) {
+            const uint32_t r = __ldcg(reinterpret_cast<const uint32_t*>(lc.crec + id));
+            if (r > i) atomicMin(lc.crec + id, 0xFFFFFFFF00000000ull | i);
+        }
     }
 }
 
@@ -1926,8 +2260,9 @@ __global__ void __launch_bounds__(kThreads)
         uint32_t* dst = out + at;
         dst[0] = m;
         if (leaf) {
-            // the eight slices as four 16-byte loads, all issued first
-            const ulonglong2* sp = reinterpret_cast<const ulonglong2*>(cur.slices + (size_t)i * 8);
+            // the class's eight slices (leaf masks are stored per class id,
+            // which is the leaf's slot) as four 16-byte loads, all issued first
+            const ulonglong2* sp = reinterpret_cast<const ulonglong2*>(cur.slices + (size_t)cur.slot[i] * 8);
             uint64_t v[8];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
@@ -2019,6 +2354,25 @@ inline ResultView result_view(char* base, uint32_t njobs) {
     return v;
 }
 
+// Inputs staged per build, one contiguous block in pinned host memory and
+// one on the device (one copy): job table, roots, and for leafmask plans the
+// leaf column groups, the z-tile table and the column pass's counts.
+struct StageLayout {
+    size_t jobs, inj, groups, ztiles, meta, bytes;
+};
+inline StageLayout stage_layout(uint32_t njobs) {
+    auto a16 = [](size_t b) { return (b + 15) & ~(size_t)15; };
+    StageLayout L{};
+    size_t o = 0;
+    L.jobs = o; o += a16(njobs * sizeof(JobDev));
+    L.inj = o; o += a16(njobs * sizeof(Injected));
+    L.groups = o; o += a16(njobs * sizeof(LeafGroupDev));
+    L.ztiles = o; o += a16(njobs * sizeof(uint2));
+    L.meta = o; o += 16;
+    L.bytes = o;
+    return L;
+}
+
 }  // namespace
 
 // A build plan: capacities, scratch and the captured launch sequence for
@@ -2033,7 +2387,7 @@ struct BuildPlan {
     uint64_t cap[CPVS_MAX_LEVELS] = {0}, tcap[CPVS_MAX_LEVELS] = {0}, ninj[CPVS_MAX_LEVELS] = {0};
     uint64_t inj_off[CPVS_MAX_LEVELS + 1] = {0};
     uint32_t max_grid = 0;
-    uint32_t leaf_grid = 0, insert_grid = 0;  // one wave of the leaf and inner insert kernels
+    uint32_t insert_grid = 0;  // one wave of the inner insert kernel
     // device memory
     char* arena = nullptr;
     size_t arena_bytes = 0;
@@ -2049,14 +2403,28 @@ struct BuildPlan {
     char* res = nullptr;  // device results region (ResultView layout)
     ResultView resv{};
     uint32_t* root_dev = nullptr;
+    char* stage_dev = nullptr;  // StageLayout: the per-build inputs on the device
     JobDev* jobs_dev = nullptr;
     Injected* inj_dev = nullptr;
+    // leaf column pass (leafmask plans): groups and z-tiles (staged), the
+    // run entries (cap[2]) and per-column records (grown to the batch's
+    // columns), its counts, the class hash table (the leaf level's table
+    // region; the level's own `table` is the class records)
+    LeafGroupDev* groups_dev = nullptr;
+    uint2* ztiles_dev = nullptr;
+    uint32_t* lmeta = nullptr;  // [0] groups, [1] columns, [2] run entries reserved, [3] pending runs
+    uint32_t* pending = nullptr;  // non-uniform run entries (cap[2])
+    uint4* runs = nullptr;
+    uint2* colrec = nullptr;
+    uint64_t colrec_cap = 0;
+    unsigned long long* ltable = nullptr;
+    uint64_t ltable_mask = 0;
     // pinned host staging
     char* hin = nullptr;
     size_t hin_bytes = 0;
     char* hout = nullptr;
     size_t hout_bytes = 0;
-    std::vector<char> staged;  // the inputs last copied to jobs_dev / inj_dev (empty: none)
+    std::vector<char> staged;  // the inputs last copied to stage_dev (empty: none)
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t done = nullptr;  // recorded after the emission that last read the scratch
     // fork / join of the ranking passes' stream in the captured launch sequence
@@ -2088,6 +2456,9 @@ void plan_release(Ctx& ctx, BuildPlan* P) {
     for (cudaEvent_t* e : {&P->join, &P->start, &P->tables})
         if (*e) cudaEventDestroy(*e), *e = nullptr;
     if (P->arena) ctx.release(P->arena, P->arena_bytes, true, nullptr);
+    if (P->colrec) ctx.release(P->colrec, P->colrec_cap * sizeof(uint2), true, nullptr);
+    P->colrec = nullptr;
+    P->colrec_cap = 0;
     if (P->table) ctx.release(P->table, P->table_slots * 8, true, nullptr);
     P->arena = nullptr;
     P->table = nullptr;
@@ -2111,6 +2482,15 @@ void plan_bind_tables(BuildPlan* P) {
         P->lv[L].table_mask = P->tcap[L] - 1;
         off += P->tcap[L];
     }
+    if (P->leafmasks) {
+        // the leaf classes' hash table is the level's table region; the
+        // level's `table` (read by the ranking and the emission) is the
+        // per-class record array
+        P->ltable = P->lv[2].table;
+        P->ltable_mask = P->lv[2].table_mask;
+        P->lv[2].table = reinterpret_cast<unsigned long long*>(P->lv[2].hash);
+        P->lv[2].table_mask = 0;
+    }
     P->small_lo = P->maxR + 1;
     while (P->small_lo > P->bottom && P->cap[P->small_lo - 1] <= small_cap) --P->small_lo;
 }
@@ -2131,8 +2511,12 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
         const uint64_t c = std::max<uint64_t>(P->cap[L], 1);
         for (int a = 0; a < 7; ++a) add(c, a == 0 ? 8 : 4);  // coord, job, mask, first, slot, uniq, woff
         if (P->leafmasks && L == 2) {
-            add(c * 8, 8);
-            add(c, 8);
+            const uint64_t cls = c + 9ull * njobs;  // run entries + the uniform classes
+            add(cls * 8, 8);  // class slice masks
+            add(cls, 8);      // class records
+            add(cls, 4);      // class jobs
+            add(c, 16);       // run entries
+            add(c, 4);        // pending run list
         }
     }
     add(CPVS_MAX_LEVELS, sizeof(LevelDev));
@@ -2141,8 +2525,7 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
     add(segn * 7, 4);
     bytes += result_bytes(njobs);
     add(njobs, 4);
-    add(njobs, sizeof(JobDev));
-    add(njobs, sizeof(Injected));
+    add(stage_layout(njobs).bytes, 1);
     // look-back flags: per level, expansion tiles and 2 x merge tiles
     P->flags_count = 0;
     for (int L = P->bottom; L <= P->maxR; ++L) {
@@ -2179,8 +2562,14 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
         l.uniq = A.take<uint32_t>(c);
         l.woff = A.take<uint32_t>(c);
         if (P->leafmasks && L == 2) {
-            l.slices = A.take<uint64_t>(c * 8);
-            l.hash = A.take<uint64_t>(c);
+            // leaf level: per class id (a run entry index) its masks, job
+            // (in `uid`) and record (in `hash`); the run entries
+            const uint64_t cls = c + 9ull * njobs;
+            l.slices = A.take<uint64_t>(cls * 8);
+            l.hash = A.take<uint64_t>(cls);
+            l.uid = A.take<uint32_t>(cls);
+            P->runs = A.take<uint4>(c);
+            P->pending = A.take<uint32_t>(c);
         }
     }
     P->lvt = A.take<LevelDev>(CPVS_MAX_LEVELS);
@@ -2191,8 +2580,13 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
     A.used += result_bytes(njobs);
     P->resv = result_view(P->res, njobs);
     P->root_dev = A.take<uint32_t>(njobs);
-    P->jobs_dev = A.take<JobDev>(njobs);
-    P->inj_dev = A.take<Injected>(njobs);
+    const StageLayout SL = stage_layout(njobs);
+    P->stage_dev = A.take<char>(SL.bytes);
+    P->jobs_dev = reinterpret_cast<JobDev*>(P->stage_dev + SL.jobs);
+    P->inj_dev = reinterpret_cast<Injected*>(P->stage_dev + SL.inj);
+    P->groups_dev = reinterpret_cast<LeafGroupDev*>(P->stage_dev + SL.groups);
+    P->ztiles_dev = reinterpret_cast<uint2*>(P->stage_dev + SL.ztiles);
+    P->lmeta = reinterpret_cast<uint32_t*>(P->stage_dev + SL.meta);
     P->tickets = A.take<unsigned int>(2 * CPVS_MAX_LEVELS + 1);  // + the expansion's first cluster level
     P->flags = A.take<unsigned long long>(P->flags_count);
     plan_bind_tables(P);
@@ -2203,7 +2597,7 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
     P->seg = SegDev{sg, sg + segn, sg + 2 * segn, sg + 3 * segn, sg + 4 * segn, sg + 5 * segn};
     P->lay = JobLayout{P->resv.job_off, P->segbuf + 6 * segn};
     // pinned staging
-    P->hin_bytes = njobs * (sizeof(JobDev) + sizeof(Injected)) + 256;
+    P->hin_bytes = SL.bytes;
     P->hout_bytes = result_bytes(njobs);
     CPVS_CUDA(cudaMallocHost((void**)&P->hin, P->hin_bytes));
     CPVS_CUDA(cudaMallocHost((void**)&P->hout, P->hout_bytes));
@@ -2266,6 +2660,29 @@ int probe_cluster_blocks() {
     return 0;
 }
 
+// The column pass's view of a leafmask plan (all null otherwise).
+LeafColumns plan_leaf_columns(const BuildPlan* P) {
+    LeafColumns lc{};
+    if (!P->leafmasks) return lc;
+    const LevelDev& l = P->lv[2];
+    lc.groups = P->groups_dev;
+    lc.ztiles = P->ztiles_dev;
+    lc.meta = P->lmeta;
+    lc.colrec = P->colrec;
+    lc.runs = P->runs;
+    lc.run_cap = (uint32_t)std::max<uint64_t>(P->cap[2], 1);
+    lc.run_ctr = P->lmeta + 2;
+    lc.cls_slices = l.slices;
+    lc.cls_job = l.uid;
+    lc.crec = l.table;
+    lc.table = P->ltable;
+    lc.table_mask = P->ltable_mask;
+    lc.njobs = P->njobs;
+    lc.pending = P->pending;
+    lc.pending_ctr = P->lmeta + 3;
+    return lc;
+}
+
 // The whole device-side build after the inputs are staged: top-down
 // expansion, leaves, bottom-up merge, layout, root masks, and the copy of
 // the results region to pinned host memory.  Stream-ordered; capturable.
@@ -2294,6 +2711,28 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
     {
         KernelTimer kt(tm, K_TABLE_CLEAR, rank_st);
         CPVS_CUDA(cudaMemsetAsync(P->table, 0xFF, plan_table_slots(P) * 8, rank_st));
+    }
+    // the leaf classes of every column, beside the expansion (they need
+    // only the maps, their level-3 bounds and the cleared tables)
+    const LeafColumns lc = plan_leaf_columns(P);
+    if (P->leafmasks) {
+        KernelTimer kt(tm, K_LEAF_COLUMNS, rank_st);
+        CPVS_CUDA(cudaMemsetAsync(P->lmeta + 2, 0, 8, rank_st));
+        // one block per chunk of columns (the column records are sized to
+        // the batch's columns; a larger batch re-captures the sequence)
+        const uint32_t cg = (uint32_t)std::max<uint64_t>(
+            1, std::min<uint64_t>((P->colrec_cap + kColChunk - 1) / kColChunk, P->max_grid));
+        if (P->pow2)
+            k_leaf_columns<true><<<cg, kThreads, 0, rank_st>>>(lc, err);
+        else
+            k_leaf_columns<false><<<cg, kThreads, 0, rank_st>>>(lc, err);
+        CPVS_CUDA(cudaGetLastError());
+    }
+    if (P->leafmasks) {
+        // the classes of the non-uniform runs (one thread each)
+        KernelTimer kt(tm, K_LEAF_CLASSES, rank_st);
+        k_leaf_classes<<<plan_grid(P, P->cap[2], kThreads), kThreads, 0, rank_st>>>(lc, err);
+        CPVS_CUDA(cudaGetLastError());
     }
     if (forked) CPVS_CUDA(cudaEventRecord(P->tables, rank_st));
     // results, level counts, job bases, look-back tickets and flags (the
@@ -2342,11 +2781,9 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
     }
     if (forked) CPVS_CUDA(cudaStreamWaitEvent(st, P->tables, 0));
     if (P->leafmasks) {
-        KernelTimer kt(tm, K_LEAF_MASKS, st);
-        CPVS_CUDA(launch_kernel(P->pow2 ? k_leaf_insert<true> : k_leaf_insert<false>,
-                                std::min(plan_grid(P, P->cap[2], kThreads), P->leaf_grid), kThreads, 0, st, ch, 0,
-                                P->lv[2], P->counts,
-                                P->jobs_dev, njobs, 2, P->seg, P->lv[2].table, P->lv[2].table_mask, err));
+        KernelTimer kt(tm, K_LEAF_RESOLVE, st);
+        CPVS_CUDA(launch_kernel(k_leaf_resolve, plan_grid(P, P->cap[2], kThreads), kThreads, 0, st, ch, 0, P->lv[2],
+                                P->counts, P->jobs_dev, njobs, P->seg, lc, err));
     } else {
         KernelTimer kt(tm, K_CLASSIFY_BOTTOM, st);
         CPVS_CUDA(launch_kernel(k_classify_bottom, plan_grid(P, P->cap[0], kThreads), kThreads, 0, st, ch, 0, P->lv[0],
@@ -2431,7 +2868,6 @@ cpvs_status plan_create(Ctx& ctx, const std::vector<JobSpec>& jobs, const std::v
     P->job_n = job_n;
     P->root_level.resize(P->njobs);
     P->max_grid = (uint32_t)std::max(ctx.num_sms, 1) * 8;
-    P->leaf_grid = std::min(P->max_grid, resident_blocks(k_leaf_insert<true>, ctx.num_sms));
     P->insert_grid = std::min(P->max_grid, resident_blocks(k_dedup_insert<false>, ctx.num_sms));
     if (ctx.cluster_blocks < 0) ctx.cluster_blocks = probe_cluster_blocks();
     P->cluster_blocks = ctx.cluster_blocks;
@@ -2556,26 +2992,88 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
     // the previous build with this plan may still be emitting from its
     // scratch on another stream
     CPVS_CUDA(cudaStreamWaitEvent(st, P->done, 0));
+    // leaf column groups: the jobs that share a map and a z_num, with
+    // distinct z-tiles (a repeated z-tile starts another group)
+    std::vector<uint32_t> job_group(njobs, 0);
+    std::vector<uint32_t> grp_source, grp_znum;
+    std::vector<std::vector<uint2>> grp_tiles;  // (z_idx, job)
+    uint64_t ncols = 0;
+    if (leafmasks) {
+        for (uint32_t j = 0; j < njobs; ++j) {
+            uint32_t g = 0;
+            for (; g < grp_source.size(); ++g) {
+                if (grp_source[g] != jobs[j].source || grp_znum[g] != jobs[j].z_num) continue;
+                bool taken = false;
+                for (const uint2& t : grp_tiles[g]) taken = taken || t.x == jobs[j].z_idx;
+                if (!taken) break;
+            }
+            if (g == grp_source.size()) {
+                grp_source.push_back(jobs[j].source);
+                grp_znum.push_back(jobs[j].z_num);
+                grp_tiles.emplace_back();
+                const uint64_t c = sources[jobs[j].source].n / 8;
+                ncols += c * c;
+            }
+            grp_tiles[g].push_back(make_uint2(jobs[j].z_idx, j));
+            job_group[j] = g;
+        }
+        for (auto& t : grp_tiles) std::sort(t.begin(), t.end(), [](uint2 a, uint2 b) { return a.x < b.x; });
+        if (ncols >= (1ull << 32)) return fail(CPVS_ERR_BUDGET, "build_dags: more than 2^32 leaf columns");
+    }
     ResultView hv{};
     for (int attempt = 0;; ++attempt) {
-        // stage this batch's inputs: job table (pyramid and map pointers,
-        // z-tile), and roots in root-level order
-        JobDev* hj = reinterpret_cast<JobDev*>(P->hin);
-        Injected* hi = reinterpret_cast<Injected*>(P->hin + njobs * sizeof(JobDev));
+        // column records for this batch's maps (kept; grown when a batch
+        // has more columns: the launch sequence is captured anew)
+        if (leafmasks && ncols > P->colrec_cap) {
+            if (P->colrec) {
+                CPVS_CUDA(cudaStreamSynchronize(st));
+                ctx.release(P->colrec, P->colrec_cap * sizeof(uint2), true, nullptr);
+                P->colrec = nullptr;
+                P->colrec_cap = 0;
+            }
+            cpvs_status r = ctx.alloc((void**)&P->colrec, ncols * sizeof(uint2), true, st);
+            if (r != CPVS_OK) return r;
+            P->colrec_cap = ncols;
+            if (P->exec) {
+                cudaGraphExecDestroy(P->exec);
+                P->exec = nullptr;
+            }
+        }
+        // stage this batch's inputs (StageLayout): job table (pyramid and
+        // map pointers, z-tile, column group), roots in root-level order,
+        // the column groups and their z-tiles
+        const StageLayout SL = stage_layout(njobs);
+        std::memset(P->hin, 0, SL.bytes);
+        JobDev* hj = reinterpret_cast<JobDev*>(P->hin + SL.jobs);
+        Injected* hi = reinterpret_cast<Injected*>(P->hin + SL.inj);
         std::vector<uint64_t> fill(CPVS_MAX_LEVELS, 0);
         for (uint32_t j = 0; j < njobs; ++j) {
             const SourceSpec& S = sources[jobs[j].source];
-            hj[j] = JobDev{S.levels, S.depth, S.n, P->root_level[j] + 2, jobs[j].z_idx, jobs[j].z_num};
+            hj[j] = JobDev{S.levels, S.depth, S.n, P->root_level[j] + 2, jobs[j].z_idx, jobs[j].z_num, job_group[j], 0};
             const int R = (int)P->root_level[j];
             hi[P->inj_off[R] + fill[R]++] = Injected{pack_xyz(0, 0, 2 * jobs[j].z_idx), j, 0};
         }
+        if (leafmasks) {
+            LeafGroupDev* hg = reinterpret_cast<LeafGroupDev*>(P->hin + SL.groups);
+            uint2* hz = reinterpret_cast<uint2*>(P->hin + SL.ztiles);
+            uint32_t* hm = reinterpret_cast<uint32_t*>(P->hin + SL.meta);
+            uint32_t zo = 0;
+            uint64_t cb = 0;
+            for (size_t g = 0; g < grp_source.size(); ++g) {
+                const SourceSpec& S = sources[grp_source[g]];
+                hg[g] = LeafGroupDev{S.levels + pyramid_level_offset(S.n, 3), S.depth, S.n, grp_znum[g], zo,
+                                     (uint32_t)grp_tiles[g].size(), cb};
+                for (const uint2& t : grp_tiles[g]) hz[zo++] = t;
+                cb += (uint64_t)(S.n / 8) * (S.n / 8);
+            }
+            hm[0] = (uint32_t)grp_source.size();
+            hm[1] = (uint32_t)ncols;
+        }
         // the device copies are read-only to the build: repeated builds of the
-        // same maps (same pyramid and map addresses) skip the two copies
-        const size_t staged_bytes = njobs * (sizeof(JobDev) + sizeof(Injected));
-        if (P->staged.size() != staged_bytes || std::memcmp(P->staged.data(), P->hin, staged_bytes) != 0) {
-            CPVS_CUDA(cudaMemcpyAsync(P->jobs_dev, hj, njobs * sizeof(JobDev), cudaMemcpyHostToDevice, st));
-            CPVS_CUDA(cudaMemcpyAsync(P->inj_dev, hi, njobs * sizeof(Injected), cudaMemcpyHostToDevice, st));
-            P->staged.assign(P->hin, P->hin + staged_bytes);
+        // same maps (same pyramid and map addresses) skip the copy
+        if (P->staged.size() != SL.bytes || std::memcmp(P->staged.data(), P->hin, SL.bytes) != 0) {
+            CPVS_CUDA(cudaMemcpyAsync(P->stage_dev, P->hin, SL.bytes, cudaMemcpyHostToDevice, st));
+            P->staged.assign(P->hin, P->hin + SL.bytes);
         }
         if (ctx.timing.on) {
             cpvs_status r = plan_enqueue(P, st, nullptr, &ctx.timing);
@@ -2701,34 +3199,38 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
 // owns and pre-reserves all GPU memory.  For them, cpvs_shadow_build_noalloc
 // builds a DAG with every scratch buffer (pyramid, per-level node arrays,
 // hash table) carved out of the fixed array below, which each GPU that loads
-// this library keeps until the process exits.  It runs the same kernels as
-// build_dags; the caller passes the depth map and the output buffer.
+// this library keeps until the process exits.  The caller passes the depth
+// map and the output buffer.
+//
+// It does not run build_dags' launch sequence.  It uses the multi-pass
+// kernels, which need no look-back flags, tickets or per-plan tables:
+// k_pyramid, k_expand_count + k_expand_write per level, k_leaf_masks (or
+// k_classify_bottom without leafmasks), per level k_dedup_insert,
+// k_dedup_resolve, k_dedup_scan and k_dedup_remap, then k_layout and k_emit
+// per level.  It is those kernels' only user, so a change to the node
+// layout, the error bits or the segment bookkeeping of the main path must be
+// mirrored there; tests/test_zz_no_alloc.py compares this build word for
+// word with the allocating build and with the oracle.
 // ---------------------------------------------------------------------------
 namespace cpvs {
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;  // 8 MiB per device
-constexpr uint32_t kNoAllocMaxSide = 256;
+constexpr uint32_t kNoAllocMaxSide = 256;         // with leafmasks
+constexpr uint32_t kNoAllocMaxSideNoLeaf = 64;    // without: the full octree down to level 0
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-// Device address of g_noalloc_scratch on each device (host code cannot use
-// the symbol itself as a device pointer).  Looked up on a device's first call.
-std::mutex g_noalloc_mu;
-void* g_noalloc_addr[256] = {nullptr};
-
+// Device address of g_noalloc_scratch on the current device (host code
+// cannot use the symbol itself as a device pointer).  Looked up on every
+// call, with the device current: the lookup allocates nothing once the
+// module is loaded, and an address kept across calls would go stale if the
+// application reset the device or tore down its primary context.
 cpvs_status noalloc_scratch_address(void** out) {
-    int dev = 0;
-    CPVS_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 256) return fail(CPVS_ERR_DEVICE, "noalloc: device index out of range");
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-        g_noalloc_addr[dev] = p;
-    }
-    *out = g_noalloc_addr[dev];
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    *out = p;
     return CPVS_OK;
 }
 
@@ -2746,6 +3248,11 @@ extern "C" CPVS_API cpvs_status cpvs_shadow_build_noalloc(const float* depth, ui
         return fail(CPVS_ERR_INVALID_ARG, "noalloc: map side must be a power of two in [8, " +
                                               std::to_string(kNoAllocMaxSide) + "], got " + std::to_string(n) +
                                               " (larger maps: cpvs_shadow_create_from_depth)");
+    if (flags & ~CPVS_FLAG_LEAFMASKS)
+        return fail(CPVS_ERR_INVALID_ARG, "noalloc: unknown flag bits " + std::to_string(flags & ~CPVS_FLAG_LEAFMASKS));
+    if (!(flags & CPVS_FLAG_LEAFMASKS) && n > kNoAllocMaxSideNoLeaf)
+        return fail(CPVS_ERR_INVALID_ARG, "noalloc: without leafmasks the map side must not exceed " +
+                                              std::to_string(kNoAllocMaxSideNoLeaf) + ", got " + std::to_string(n));
     if (z_tile_num == 0 || z_tile_index >= z_tile_num)
         return fail(CPVS_ERR_INVALID_ARG, "noalloc: need z_tile_index < z_tile_num");
     if ((uint64_t)n * z_tile_num > (1ull << 23))

@@ -171,16 +171,17 @@ cpvs_status launch_shade(uint64_t n, const float* normals, uint32_t normal_float
 
 // ------------------------------------------------------------ timing
 // Kernels timed (when a context's timing is on) with a CUDA event pair on
-// the launching stream around every launch.
+// the launching stream around every launch; kernel_name() gives the kernel
+// (or, for K_EXPAND_WRITE and K_SCAN, the kernels) each id times.
 enum KernelId : int {
     K_PYRAMID = 0,
     K_LEVEL_BOUNDS,
     K_EXPAND_COUNT,
     K_EXPAND_WRITE,
-    K_LEAF_MASKS,
+    K_LEAF_COLUMNS,
     K_CLASSIFY_BOTTOM,
     K_TABLE_CLEAR,
-    K_INSERT_LEAF,
+    K_LEAF_RESOLVE,
     K_INSERT_INNER,
     K_RESOLVE,
     K_SCAN,
@@ -193,6 +194,7 @@ enum KernelId : int {
     K_MULTI_LOOKUP,
     K_EVALUATE,
     K_SHADE,
+    K_LEAF_CLASSES,
     K_COUNT
 };
 const char* kernel_name(int id);

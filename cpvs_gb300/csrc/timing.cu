@@ -6,10 +6,11 @@ namespace cpvs {
 
 const char* kernel_name(int id) {
     static const char* names[K_COUNT] = {
-        "pyramid",      "level_bounds", "expand_count", "expand_write", "leaf_masks", "classify_bottom",
-        "table_clear",  "insert_leaf",  "insert_inner", "resolve",      "scan",       "remap",
-        "layout",       "emit",         "lookup",       "grid_lookup", "raster",      "multi_lookup", "evaluate",
-        "shade"};
+        "k_pyramid64",      "k_level_bounds", "k_expand_count", "k_expand",      "k_leaf_columns",
+        "k_classify_bottom", "table_clear",    "k_leaf_resolve", "k_dedup_insert", "k_dedup_resolve",
+        "k_merge_scan",      "k_dedup_remap",  "k_layout",       "k_emit_all",     "k_lookup",
+        "k_grid_lookup",     "k_raster",       "k_multi_lookup", "k_grid_evaluate", "k_shade",
+        "k_leaf_classes"};
     return (id >= 0 && id < K_COUNT) ? names[id] : "";
 }
 

@@ -237,17 +237,20 @@ CPVS_API cpvs_status cpvs_shadow_lookup_voxel(const cpvs_shadow* s, const int32_
  * synchronise the device) or a plugin inside a host application that owns
  * all GPU memory.  All scratch lives in a fixed 8 MiB array compiled into
  * this library, which every GPU that loads the library holds until the
- * process exits; maps are limited to n <= 256 (power of two, >= 8;
- * without leafmasks only sizes whose full octree fits the array).
- * `depth` is a device n*n float32 map; the DAG (the same words
- * cpvs_shadow_create_from_depth builds) is written to the device buffer
- * `dag_out` of `dag_capacity` words, and `*dag_words` receives its size
- * (also when the buffer is too small: CPVS_ERR_CAPACITY).  The calling
- * thread's current device is used; the first call on each device looks up
- * the array's device address (no allocation), so make that first call
- * before any stream capture.  All calls share the one array: calls whose
- * work overlaps on the GPU (other streams or host threads) race and must be
- * serialised by the caller.  Returns after the build has finished. */
+ * process exits; maps are limited to n <= 256 with CPVS_FLAG_LEAFMASKS and
+ * n <= 64 without (power of two, >= 8); other flag bits are rejected
+ * (CPVS_ERR_INVALID_ARG).  `depth` is a device n*n float32 map; the DAG
+ * (the same words cpvs_shadow_create_from_depth builds) is written to the
+ * device buffer `dag_out` of `dag_capacity` words, and `*dag_words`
+ * receives its size (also when the buffer is too small: CPVS_ERR_CAPACITY).
+ * The calling thread's current device is used; every call looks up the
+ * array's device address there.  The first call on a device may load this
+ * library's GPU code (CUDA loads modules lazily), which places the array in
+ * device memory and can synchronise: make one warm-up call at start-up,
+ * outside render loops and before any stream capture.  All calls share the
+ * one array: calls whose work overlaps on the GPU (other streams or host
+ * threads) race and must be serialised by the caller.  Returns after the
+ * build has finished. */
 CPVS_API cpvs_status cpvs_shadow_build_noalloc(const float* depth, uint32_t n, uint32_t z_tile_index,
                                                uint32_t z_tile_num, uint32_t flags, uint32_t* dag_out,
                                                uint64_t dag_capacity, uint64_t* dag_words, void* stream);

@@ -170,6 +170,52 @@ def test_c1_config_matches_oracle(cp, oracle):
     assert np.array_equal(sh.lookup_ndc(q), oracle.lookup_ndc(want.dag, want.num_levels, True, q, threads=8))
 
 
+def _sha(a):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def test_c0_config_matches_reference(cp, golden_configs):
+    """The 1024^2 workload against the reference's own output
+    (tests/golden/make_golden_configs.py): DAG words, per-level counts, and
+    the reference's traverse answers on 2^16 mixed NDC points and on the
+    voxel centres of the first 2^16 voxel queries (voxel and NDC input)."""
+    g = golden_configs
+    d = scene.rasterise(scene.config_scene("c0"))
+    assert _sha(d) == str(g["c0/map_sha256"])
+    sh = cp.CompressedShadow.from_depth(d)
+    nl, tv, words = g["c0/meta"].tolist()
+    assert sh.get_num_levels() == nl and sh.get_total_visibility() == tv
+    assert np.array_equal(sh.get_dag(), g["c0/dag"])
+    tree, uniq = sh.level_counts()
+    assert tree == g["c0/tree_nodes"].tolist() and uniq == g["c0/unique_nodes"].tolist()
+    q = scene.ndc_queries_mixed(d, 1 << 16, int(g["c0/ndc_seed"]))
+    assert np.array_equal(sh.lookup_ndc(q), g["c0/ndc_vis"])
+    v = scene.voxel_queries(1 << 20, 1024, 0)[:1 << 16]
+    assert _sha(v) == str(g["c0/voxel_sha256"])
+    assert np.array_equal(sh.lookup_voxel(v), g["c0/voxel_vis"])
+
+
+def test_c1_config_matches_reference(cp, golden_configs):
+    """The 8192^2 workload against the reference's own output: DAG length
+    and SHA-256, per-level tree and unique node counts, numLevels, total
+    visibility, and the reference's traverse answers on 2^16 mixed NDC
+    points."""
+    import torch
+    g = golden_configs
+    d = scene.rasterise(scene.config_scene("c1"))
+    assert _sha(d) == str(g["c1/map_sha256"])
+    sh = cp.CompressedShadow.from_depth(torch.from_numpy(d).cuda())
+    nl, tv, words = g["c1/meta"].tolist()
+    assert sh.get_num_levels() == nl and sh.get_total_visibility() == tv
+    dag = sh.get_dag()
+    assert dag.size == words and _sha(dag) == str(g["c1/dag_sha256"])
+    tree, uniq = sh.level_counts()
+    assert tree == g["c1/tree_nodes"].tolist() and uniq == g["c1/unique_nodes"].tolist()
+    q = scene.ndc_queries_mixed(d, 1 << 16, int(g["c1/ndc_seed"]))
+    assert np.array_equal(sh.lookup_ndc(q), g["c1/ndc_vis"])
+
+
 def test_lookup_variants_agree(cp, oracle):
     """Every queries-per-thread variant of the lookup kernel (and the tuned
     choice) answers exactly like the oracle, for NDC and voxel input."""

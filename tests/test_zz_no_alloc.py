@@ -2,9 +2,10 @@
 ABI.  It serves callers that may not allocate device memory (a render loop
 that must not stall on cudaMalloc/cudaFree, a plugin inside an application
 that owns all GPU memory): its scratch is a fixed array inside the library.
-Its DAG must equal the one the allocating build makes, call after call,
-although every call reuses the same array.  This file is collected last so
-that a run stopping at the first failure has run everything else first."""
+Its DAG must equal the one the allocating build makes and the oracle's,
+call after call, although every call reuses the same array.  This file is
+collected last so that a run stopping at the first failure has run
+everything else first."""
 import ctypes as C
 
 import numpy as np
@@ -52,12 +53,47 @@ def test_noalloc_without_leafmasks_and_small_maps(cp):
         assert np.array_equal(got, want)
 
 
+def test_noalloc_matches_oracle(cp, oracle):
+    """Random maps of five kinds and maps whose depths sit on or beside voxel
+    boundaries, with and without z-tiles, against the oracle's DAG words
+    (the multi-pass kernels this build runs are used by no other path)."""
+    import torch
+    from test_gpu_parity import boundary_map, random_map
+    lib = cp.load_library()
+    rng = np.random.default_rng(4321)
+    cases = [(random_map(rng, int(rng.choice([16, 32, 64, 128, 256])), kind), kind)
+             for kind in range(5) for _ in range(3)]
+    for n, zn in ((64, 1), (64, 3), (128, 8), (256, 1), (32, 5)):
+        cases.append((boundary_map(rng, n, n * zn), zn))
+    for t, (depth, zk) in enumerate(cases):
+        n = depth.shape[0]
+        zn = zk if t >= 15 else int(rng.choice([1, 1, 2, 3]))
+        zi = int(rng.integers(0, zn))
+        want = oracle.build(depth, zi, zn)
+        status, got, words = build_noalloc(lib, torch.from_numpy(depth).cuda(), n, 1 << 22, zi, zn)
+        assert status == 0, lib.cpvs_last_error()
+        assert words == want.dag.size and np.array_equal(got, want.dag), (t, n, zi, zn)
+    for n in (16, 32, 64):
+        depth = random_map(rng, n, 2)
+        want = oracle.build(depth, leafmasks=False)
+        status, got, _ = build_noalloc(lib, torch.from_numpy(depth).cuda(), n, 1 << 22, leafmasks=False)
+        assert status == 0 and np.array_equal(got, want.dag), n
+
+
 def test_noalloc_limits(cp):
     import torch
     lib = cp.load_library()
     big = torch.zeros((512, 512), dtype=torch.float32, device="cuda")
     status, _, _ = build_noalloc(lib, big, 512, 1 << 16)
     assert status == 1 and b"256" in lib.cpvs_last_error()      # beyond the fixed maximum
+    small = torch.zeros((128, 128), dtype=torch.float32, device="cuda")
+    status, _, _ = build_noalloc(lib, small, 128, 1 << 16, leafmasks=False)
+    assert status == 1 and b"64" in lib.cpvs_last_error()       # without leafmasks: at most 64
+    words = C.c_uint64(0)
+    out = torch.zeros(1 << 16, dtype=torch.int32, device="cuda")
+    status = lib.cpvs_shadow_build_noalloc(small.data_ptr(), 128, 0, 1, 0x1 | 0x100, out.data_ptr(), 1 << 16,
+                                           C.byref(words), None)
+    assert status == 1 and b"flag" in lib.cpvs_last_error()     # unknown flag bits
     depth = torch.from_numpy(scene.rasterise(scene.make_scene(128, 0.9, 20, 2, 5))).cuda()
     status, _, words = build_noalloc(lib, depth, 128, 4)
     assert status == 8 and words > 4                             # output too small: size reported
