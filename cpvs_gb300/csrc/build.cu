@@ -610,6 +610,7 @@ __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long lon
 struct LeafGroupDev {      // one source map and z_num; its jobs' z-tiles are distinct
     const float2* lvl3;    // pyramid level 3 of the map: (n/8)^2 (min, max) pairs
     const float* depth;    // the map, n x n
+    const uint32_t* nan_flag;  // nonzero if the map holds a NaN (null: unknown)
     uint32_t n, z_num;
     uint32_t job_lo, job_cnt;  // its jobs in the z-tile table, ordered by z_idx
     uint64_t col_base;         // its first column record
@@ -631,7 +632,19 @@ struct LeafColumns {
     uint32_t njobs;             // uniform classes: id run_cap + 9 * job + k (all counts k)
     uint32_t* pending;          // run entries of non-uniform leaves, for k_leaf_classes
     unsigned int* pending_ctr;  // their count (zeroed per build)
+    uint4* heavy;               // columns whose walk needs their texels: (column, job index, z-cell, entry)
+    unsigned int* heavy_ctr;    // their count (zeroed per build)
 };
+
+// The last z-cell (at most zmax) through which a texel with value v (the
+// count functions' v: the raw depth for power-of-two heights, else
+// fl(d * H)) stays fully lit: floor(v / 8 - 0.9375), see column_counts.
+__device__ __forceinline__ uint32_t full_run_end(float v, float s, uint32_t zmax) {
+    float t;
+    asm("fma.rm.f32 %0, %1, %2, %3;" : "=f"(t) : "f"(v), "f"(s), "f"(-0.9375f));
+    t = floorf(t);
+    return t >= __uint2float_rn(zmax) ? zmax : (uint32_t)t;  // t >= zc here (the texel is full at zc)
+}
 
 // Lit counts of the column at (row0, row stride nmap) for the leaf of
 // z-cell zc (W as leaf_rows gives them), and the last z-cell through which
@@ -674,10 +687,7 @@ __device__ __forceinline__ uint32_t column_counts(const float* row0, uint32_t nm
         part |= W[y] & 0x77777777u;  // some count in 1..7
     }
     if (part) return zc;
-    float t;
-    asm("fma.rm.f32 %0, %1, %2, %3;" : "=f"(t) : "f"(vfull), "f"(s), "f"(-0.9375f));
-    t = floorf(t);
-    return t >= __uint2float_rn(zmax) ? zmax : (uint32_t)t;  // t >= zc here (the texel is full at zc)
+    return full_run_end(vfull, s, zmax);
 }
 
 // Inserts the class of run entry `cid` (job j, masks M, hash h) into the
@@ -757,6 +767,7 @@ __device__ __forceinline__ void column_partial_range(float2 b, uint32_t H3, uint
 // Column q of the batch: its group, its coordinates and its partial range.
 struct ColumnAt {
     uint32_t g, C, cx, cy, zlo, zhi;
+    float2 b;  // the column's level-3 (min, max)
 };
 __device__ __forceinline__ ColumnAt column_at(const LeafColumns& lc, uint32_t ngroups, uint64_t q) {
     uint32_t lo = 0, hi = ngroups;  // the last group whose first column is <= q
@@ -771,7 +782,8 @@ __device__ __forceinline__ ColumnAt column_at(const LeafColumns& lc, uint32_t ng
     const uint32_t local = (uint32_t)(q - __ldg(&G.col_base)), lg = 31u - (uint32_t)__clz((int)c.C);
     c.cx = local & (c.C - 1u);
     c.cy = local >> lg;
-    column_partial_range(__ldg(G.lvl3 + local), c.C * __ldg(&G.z_num), c.zlo, c.zhi);
+    c.b = __ldg(G.lvl3 + local);
+    column_partial_range(c.b, c.C * __ldg(&G.z_num), c.zlo, c.zhi);
     return c;
 }
 
@@ -788,22 +800,112 @@ __device__ __forceinline__ uint32_t column_cells(const LeafColumns& lc, const Co
     return cells;
 }
 
-// The runs of every column of the batch's maps.  A block takes a chunk of
-// kColChunk columns, kColItems per thread: it counts their partial leaf
-// cells, reserves that many run entries with one atomic add, then each
-// thread walks the runs of its columns in one flat loop -- a lane that
-// finishes a column moves on to its next one while its neighbours are still
-// inside theirs, so the warp steps through runs, not through the longest
-// column of each round.  Uniform leaves (all 64 counts equal to k: flat
-// surface, the most frequent classes) take the fixed class id
-// run_cap + 9 * job + k; the first block writes those classes' masks and
-// empty records.  Every other run stores its masks at its own entry and
-// joins the pending list that k_leaf_classes deduplicates.
+// One run of column c at z-cell zc (range end e, job `job`), written to run
+// entry cid: its last z-cell is returned.  A lit count is monotone in the
+// depth, so when the column's lowest and highest depth have the same count
+// at zc every texel has it (a uniform leaf) and the texels need not be read
+// (`minmax`: the map holds no NaN, which the min/max reduction may hide).
+// LIGHT: a run that needs the texels is not taken (returns false); else the
+// texels are read, and a non-uniform run stores its masks, job and an empty
+// record at its own entry and joins the pending list of k_leaf_classes.
+template <bool POW2, bool LIGHT>
+__device__ __forceinline__ bool column_run(const LeafColumns& lc, const ColumnAt& c, const float* row0, uint32_t nmap,
+                                           float H0, bool minmax, uint32_t zc, uint32_t e, uint32_t job, uint32_t cid,
+                                           uint32_t& last) {
+    uint32_t k0 = 0;
+    bool uni = false;
+    if (minmax) {
+        const float s = POW2 ? __fmul_rn(H0, 0.125f) : 0.125f;
+        const float c8 = __fmul_rn(__fsub_rn(0.5f, __uint2float_rn(8u * zc)), 0.125f);
+        const float vlo = POW2 ? c.b.x : __fmul_rn(c.b.x, H0), vhi = POW2 ? c.b.y : __fmul_rn(c.b.y, H0);
+        const uint32_t clo = lit_count_bits(vlo, s, c8), chi = lit_count_bits(vhi, s, c8);
+        if (clo == chi) {
+            uni = true;
+            k0 = clo - kCountBias;
+            last = k0 == 8u ? full_run_end(vlo, s, e) : (k0 == 0u ? e : zc);
+        }
+    }
+    if (LIGHT && !uni) return false;
+    uint32_t W[8];
+    if (!uni) {
+        last = column_counts<POW2>(row0, nmap, H0, zc, e, W);
+        uni = leaf_uniform(W, k0);
+    }
+    uint32_t id, mask;
+    if (uni) {
+        id = lc.run_cap + 9u * job + k0;
+        mask = uniform_class_mask(k0);
+    } else {
+        uint64_t M[8];
+        leaf_masks_from_counts(W, M, mask);
+        ulonglong2* o = reinterpret_cast<ulonglong2*>(lc.cls_slices + (size_t)cid * 8);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) o[q] = make_ulonglong2(M[2 * q], M[2 * q + 1]);
+        lc.cls_job[cid] = job;
+        lc.crec[cid] = kEmptySlot;
+        id = cid;
+    }
+    if (!LIGHT) {
+        // the non-uniform runs of the warp's active lanes join the pending
+        // list with one atomic add
+        const unsigned act = __activemask();
+        const unsigned want = __ballot_sync(act, !uni);
+        if (want) {
+            const int lead = __ffs((int)want) - 1;
+            const uint32_t lane = threadIdx.x & 31u;
+            uint32_t at = 0;
+            if ((int)lane == lead) at = atomicAdd(lc.pending_ctr, (unsigned)__popc(want));
+            at = __shfl_sync(act, at, lead);
+            if (!uni) lc.pending[at + __popc(want & ((1u << lane) - 1u))] = id;
+        }
+    }
+    lc.runs[cid] = make_uint4(last, id, mask, job);
+    return true;
+}
+
+// Walks the runs of column c from job index k and z-cell zc on, writing run
+// entries from off + nrun; LIGHT stops at the first run that needs the
+// texels and returns false with (k, zc) at that run.
+template <bool POW2, bool LIGHT>
+__device__ __forceinline__ bool column_walk(const LeafColumns& lc, const ColumnAt& c, uint32_t off, uint32_t& nrun,
+                                            uint32_t& k, uint32_t& zc) {
+    const LeafGroupDev& G = lc.groups[c.g];
+    const uint32_t jl = __ldg(&G.job_lo), jc = __ldg(&G.job_cnt), nmap = __ldg(&G.n);
+    const float* row0 = G.depth + (size_t)(c.cy * 8u) * nmap + c.cx * 8u;
+    const float H0 = __uint2float_rn(nmap * __ldg(&G.z_num));
+    const uint32_t* nf = G.nan_flag;
+    const bool minmax = nf && __ldg(nf) == 0u;
+    for (; k < jc; ++k) {
+        const uint2 zt = __ldg(&lc.ztiles[jl + k]);
+        const uint32_t z0 = zt.x * c.C;
+        const uint32_t e = min(c.zhi, z0 + c.C - 1u);
+        zc = max(zc, max(c.zlo, z0));
+        while (zc <= e) {
+            uint32_t last;
+            if (!column_run<POW2, LIGHT>(lc, c, row0, nmap, H0, minmax, zc, e, zt.y, off + nrun, last)) return false;
+            ++nrun;
+            zc = last + 1u;
+        }
+        zc = 0;
+    }
+    return true;
+}
+
+// The runs of every column of the batch's maps, first pass.  A block takes
+// a chunk of kColChunk columns, kColItems per thread: it counts their
+// partial leaf cells, reserves that many run entries with one atomic add,
+// and walks each column's runs as far as the min/max shortcut carries
+// them.  Uniform leaves (all 64 counts equal to k: flat surface, 77% of the
+// 8192^2 workload's runs) take the fixed class id run_cap + 9 * job + k;
+// the first block writes those classes' masks and empty records.  A column
+// that reaches a run needing its texels is queued, with the state to
+// resume from, for k_leaf_columns_heavy, so the texel work runs on full
+// warps instead of on the few lanes of each warp that have it.
 constexpr int kColItems = 2;
 constexpr uint32_t kColChunk = kThreads * kColItems;
 
 template <bool POW2>
-__global__ void __launch_bounds__(kThreads, 2) k_leaf_columns(LeafColumns lc, uint32_t* err) {
+__global__ void __launch_bounds__(kThreads) k_leaf_columns(LeafColumns lc, uint32_t* err) {
     __shared__ uint32_t sm[64];
     __shared__ uint32_t s_base;
     const uint32_t ngroups = lc.meta[0];
@@ -834,92 +936,46 @@ __global__ void __launch_bounds__(kThreads, 2) k_leaf_columns(LeafColumns lc, ui
         __syncthreads();
         const bool fits = (uint64_t)base + tot.x <= lc.run_cap;
         if (!fits && threadIdx.x == 0) atomicOr(err, 1u);  // more runs than the plan holds: reported, the plan grows
-        // flat walk: column `it` of this thread, job `k` of its group, the
-        // current range [zc, e] of that job's z-tile
-        uint32_t off = base + pre;  // entry base of the current column
-        int it = 0;
-        bool open = false;  // column `it` is open: its record is not written yet
-        uint64_t q = 0;
-        ColumnAt c{};
-        uint32_t cells = 0, nrun = 0, jl = 0, jc = 0, k = 0, zc = 1, e = 0, job = 0, nmap = 0;
-        const float* row0 = nullptr;
-        float H0 = 0.f;
-        for (;;) {
-            // the next non-empty range: the next job of the open column, or
-            // the next column
-            while (zc > e) {
-                if (open) {
-                    if (++k < jc) {
-                        const uint2 zt = __ldg(&lc.ztiles[jl + k]);
-                        const uint32_t z0 = zt.x * c.C;
-                        zc = max(c.zlo, z0);
-                        e = min(c.zhi, z0 + c.C - 1u);
-                        job = zt.y;
-                        continue;
-                    }
-                    lc.colrec[q] = make_uint2(off, nrun);
-                    off += cells;
-                    open = false;
-                    ++it;
-                }
-                if (it >= kColItems) break;
-                q = q0 + (uint64_t)it * kThreads;
-                if (q >= ncols) {
-                    it = kColItems;
-                    break;
-                }
-                c = column_at(lc, ngroups, q);
+        uint32_t off = base + pre;
+#pragma unroll 1
+        for (int it = 0; it < kColItems; ++it) {
+            const uint64_t q = q0 + (uint64_t)it * kThreads;
+            bool queue = false;
+            uint32_t k = 0, zc = 0, nrun = 0, cells = 0;
+            if (q < ncols) {
+                const ColumnAt c = column_at(lc, ngroups, q);
                 cells = column_cells(lc, c);
-                nrun = 0;
-                const LeafGroupDev& G = lc.groups[c.g];
-                jl = __ldg(&G.job_lo);
-                jc = (cells && fits) ? __ldg(&G.job_cnt) : 0u;  // no cells: the record only
-                nmap = __ldg(&G.n);
-                row0 = G.depth + (size_t)(c.cy * 8u) * nmap + c.cx * 8u;
-                H0 = __uint2float_rn(nmap * __ldg(&G.z_num));
-                open = true;
-                k = ~0u;  // the next ++k is job 0
-                zc = 1;
-                e = 0;
+                if (cells && fits) queue = !column_walk<POW2, true>(lc, c, off, nrun, k, zc);
+                lc.colrec[q] = make_uint2(off, nrun);
             }
-            if (it >= kColItems) break;
-            // one run: the leaf at z-cell zc and every following one equal to it
-            uint32_t W[8];
-            const uint32_t last = column_counts<POW2>(row0, nmap, H0, zc, e, W);
-            const uint32_t cid = off + nrun;
-            uint32_t id, mask, k0;
-            const bool uni = leaf_uniform(W, k0);
-            if (uni) {
-                id = lc.run_cap + 9u * job + k0;
-                mask = uniform_class_mask(k0);
-            } else {
-                // masks, job and an empty record at the run's own entry; the
-                // class id follows in k_leaf_classes
-                uint64_t M[8];
-                leaf_masks_from_counts(W, M, mask);
-                ulonglong2* o = reinterpret_cast<ulonglong2*>(lc.cls_slices + (size_t)cid * 8);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) o[q] = make_ulonglong2(M[2 * q], M[2 * q + 1]);
-                lc.cls_job[cid] = job;
-                lc.crec[cid] = kEmptySlot;
-                id = cid;
-            }
-            // the non-uniform runs of the warp's active lanes join the
-            // pending list with one atomic add
-            const unsigned act = __activemask();
-            const unsigned want = __ballot_sync(act, !uni);
+            // queue the columns that need their texels, one atomic per warp
+            const unsigned want = __ballot_sync(0xffffffffu, queue);
             if (want) {
                 const int lead = __ffs((int)want) - 1;
                 const uint32_t lane = threadIdx.x & 31u;
                 uint32_t at = 0;
-                if ((int)lane == lead) at = atomicAdd(lc.pending_ctr, (unsigned)__popc(want));
-                at = __shfl_sync(act, at, lead);
-                if (!uni) lc.pending[at + __popc(want & ((1u << lane) - 1u))] = cid;
+                if ((int)lane == lead) at = atomicAdd(lc.heavy_ctr, (unsigned)__popc(want));
+                at = __shfl_sync(0xffffffffu, at, lead);
+                if (queue) lc.heavy[at + __popc(want & ((1u << lane) - 1u))] = make_uint4((uint32_t)q, k, zc, off + nrun);
             }
-            lc.runs[cid] = make_uint4(last, id, mask, job);
-            ++nrun;
-            zc = last + 1u;
+            off += cells;
         }
+    }
+}
+
+// Second pass: one thread per queued column resumes its walk where the
+// first pass stopped, reading the texels where a run needs them.
+template <bool POW2>
+__global__ void __launch_bounds__(kThreads, 2) k_leaf_columns_heavy(LeafColumns lc) {
+    const uint32_t ngroups = lc.meta[0];
+    const uint32_t nh = *lc.heavy_ctr;
+    for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += gridDim.x * blockDim.x) {
+        const uint4 w = lc.heavy[h];
+        const ColumnAt c = column_at(lc, ngroups, w.x);
+        const uint32_t off = lc.colrec[w.x].x;
+        uint32_t nrun = w.w - off, k = w.y, zc = w.z;
+        column_walk<POW2, false>(lc, c, off, nrun, k, zc);
+        lc.colrec[w.x].y = nrun;
     }
 }
 
@@ -2368,7 +2424,7 @@ inline StageLayout stage_layout(uint32_t njobs) {
     L.inj = o; o += a16(njobs * sizeof(Injected));
     L.groups = o; o += a16(njobs * sizeof(LeafGroupDev));
     L.ztiles = o; o += a16(njobs * sizeof(uint2));
-    L.meta = o; o += 16;
+    L.meta = o; o += 32;
     L.bytes = o;
     return L;
 }
@@ -2412,10 +2468,12 @@ struct BuildPlan {
     // region; the level's own `table` is the class records)
     LeafGroupDev* groups_dev = nullptr;
     uint2* ztiles_dev = nullptr;
-    uint32_t* lmeta = nullptr;  // [0] groups, [1] columns, [2] run entries reserved, [3] pending runs
+    uint32_t* lmeta = nullptr;  // [0] groups, [1] columns, [2] run entries reserved, [3] pending runs,
+                                // [4] queued columns
     uint32_t* pending = nullptr;  // non-uniform run entries (cap[2])
     uint4* runs = nullptr;
-    uint2* colrec = nullptr;
+    uint2* colrec = nullptr;  // per column (colrec_cap), followed by the queue of columns
+    uint4* heavy = nullptr;   // that need their texels (colrec_cap)
     uint64_t colrec_cap = 0;
     unsigned long long* ltable = nullptr;
     uint64_t ltable_mask = 0;
@@ -2456,8 +2514,9 @@ void plan_release(Ctx& ctx, BuildPlan* P) {
     for (cudaEvent_t* e : {&P->join, &P->start, &P->tables})
         if (*e) cudaEventDestroy(*e), *e = nullptr;
     if (P->arena) ctx.release(P->arena, P->arena_bytes, true, nullptr);
-    if (P->colrec) ctx.release(P->colrec, P->colrec_cap * sizeof(uint2), true, nullptr);
+    if (P->colrec) ctx.release(P->colrec, P->colrec_cap * (sizeof(uint2) + sizeof(uint4)), true, nullptr);
     P->colrec = nullptr;
+    P->heavy = nullptr;
     P->colrec_cap = 0;
     if (P->table) ctx.release(P->table, P->table_slots * 8, true, nullptr);
     P->arena = nullptr;
@@ -2680,6 +2739,8 @@ LeafColumns plan_leaf_columns(const BuildPlan* P) {
     lc.njobs = P->njobs;
     lc.pending = P->pending;
     lc.pending_ctr = P->lmeta + 3;
+    lc.heavy = P->heavy;
+    lc.heavy_ctr = P->lmeta + 4;
     return lc;
 }
 
@@ -2717,7 +2778,7 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
     const LeafColumns lc = plan_leaf_columns(P);
     if (P->leafmasks) {
         KernelTimer kt(tm, K_LEAF_COLUMNS, rank_st);
-        CPVS_CUDA(cudaMemsetAsync(P->lmeta + 2, 0, 8, rank_st));
+        CPVS_CUDA(cudaMemsetAsync(P->lmeta + 2, 0, 12, rank_st));
         // one block per chunk of columns (the column records are sized to
         // the batch's columns; a larger batch re-captures the sequence)
         const uint32_t cg = (uint32_t)std::max<uint64_t>(
@@ -2726,6 +2787,12 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
             k_leaf_columns<true><<<cg, kThreads, 0, rank_st>>>(lc, err);
         else
             k_leaf_columns<false><<<cg, kThreads, 0, rank_st>>>(lc, err);
+        CPVS_CUDA(cudaGetLastError());
+        const uint32_t hg = plan_grid(P, P->colrec_cap, kThreads);
+        if (P->pow2)
+            k_leaf_columns_heavy<true><<<hg, kThreads, 0, rank_st>>>(lc);
+        else
+            k_leaf_columns_heavy<false><<<hg, kThreads, 0, rank_st>>>(lc);
         CPVS_CUDA(cudaGetLastError());
     }
     if (P->leafmasks) {
@@ -3027,12 +3094,14 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         if (leafmasks && ncols > P->colrec_cap) {
             if (P->colrec) {
                 CPVS_CUDA(cudaStreamSynchronize(st));
-                ctx.release(P->colrec, P->colrec_cap * sizeof(uint2), true, nullptr);
+                ctx.release(P->colrec, P->colrec_cap * (sizeof(uint2) + sizeof(uint4)), true, nullptr);
                 P->colrec = nullptr;
+                P->heavy = nullptr;
                 P->colrec_cap = 0;
             }
-            cpvs_status r = ctx.alloc((void**)&P->colrec, ncols * sizeof(uint2), true, st);
+            cpvs_status r = ctx.alloc((void**)&P->colrec, ncols * (sizeof(uint2) + sizeof(uint4)), true, st);
             if (r != CPVS_OK) return r;
+            P->heavy = reinterpret_cast<uint4*>(P->colrec + ((ncols + 1) & ~1ull));
             P->colrec_cap = ncols;
             if (P->exec) {
                 cudaGraphExecDestroy(P->exec);
@@ -3061,8 +3130,8 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
             uint64_t cb = 0;
             for (size_t g = 0; g < grp_source.size(); ++g) {
                 const SourceSpec& S = sources[grp_source[g]];
-                hg[g] = LeafGroupDev{S.levels + pyramid_level_offset(S.n, 3), S.depth, S.n, grp_znum[g], zo,
-                                     (uint32_t)grp_tiles[g].size(), cb};
+                hg[g] = LeafGroupDev{S.levels + pyramid_level_offset(S.n, 3), S.depth, S.nan_flag, S.n, grp_znum[g],
+                                     zo, (uint32_t)grp_tiles[g].size(), cb};
                 for (const uint2& t : grp_tiles[g]) hz[zo++] = t;
                 cb += (uint64_t)(S.n / 8) * (S.n / 8);
             }

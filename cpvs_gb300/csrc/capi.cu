@@ -415,14 +415,16 @@ cpvs_status hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n, uint
     }
     if (r == CPVS_OK) {
         if (in_place) {
-            r = cpvs::launch_pyramid(in_place, n, h->levels, st, &c.timing, h->depth, first_level);
+            r = cpvs::launch_pyramid(in_place, n, h->levels, st, &c.timing, h->depth, first_level,
+                                     cpvs::pyramid_nan_flag(h->levels, n));
             // the caller may reuse its buffer on return: wait for the read
             if (r == CPVS_OK) {
                 const cudaError_t e = cudaStreamSynchronize(st);
                 if (e != cudaSuccess) r = cpvs::cuda_fail(e, "hierarchy read of the host map");
             }
         } else {
-            r = cpvs::launch_pyramid(h->depth, n, h->levels, st, &c.timing, nullptr, first_level);
+            r = cpvs::launch_pyramid(h->depth, n, h->levels, st, &c.timing, nullptr, first_level,
+                                     cpvs::pyramid_nan_flag(h->levels, n));
         }
     }
     h->touch(st);
@@ -567,7 +569,7 @@ cpvs_status cpvs_shadow_create(cpvs_ctx* ctx, const cpvs_hierarchy* h, uint32_t 
     if (r != CPVS_OK) return r;
     const uint32_t nl = (uint32_t)cpvs::log2_u32(h->n) + 1;
     const bool leaf = (flags & CPVS_FLAG_LEAFMASKS) && (nl - 3 >= 2);
-    std::vector<cpvs::SourceSpec> src{{h->depth, h->levels, h->n}};
+    std::vector<cpvs::SourceSpec> src{{h->depth, h->levels, h->n, cpvs::pyramid_nan_flag(h->levels, h->n)}};
     std::vector<cpvs::JobSpec> jobs{{0, z_tile_index, z_tile_num}};
     DagBlock* block = nullptr;
     std::vector<cpvs_shadow*> shadows;
@@ -589,7 +591,8 @@ cpvs_status cpvs_shadow_create_batch(cpvs_ctx* ctx, const cpvs_hierarchy* const*
         if (!sources[i]) return fail(CPVS_ERR_INVALID_ARG, "create_batch: null hierarchy");
         cpvs_status r = check_map_size(sources[i]->n, 8);
         if (r != CPVS_OK) return r;
-        src[i] = cpvs::SourceSpec{sources[i]->depth, sources[i]->levels, sources[i]->n};
+        src[i] = cpvs::SourceSpec{sources[i]->depth, sources[i]->levels, sources[i]->n,
+                                  cpvs::pyramid_nan_flag(sources[i]->levels, sources[i]->n)};
     }
     // jobs grouped by leafmask mode (maps below 16^2 cannot use leafmasks)
     std::vector<cpvs::JobSpec> group[2];
@@ -876,7 +879,7 @@ cpvs_status cpvs_grid_build(cpvs_grid* g, const cpvs_hierarchy* const* xy_tiles,
         if (h->n != xy_tiles[0]->n) return fail(CPVS_ERR_INVALID_ARG, "grid_build: tiles differ in size");
         cpvs_status r = check_map_size(h->n, 8);
         if (r != CPVS_OK) return r;
-        src[i] = cpvs::SourceSpec{h->depth, h->levels, h->n};
+        src[i] = cpvs::SourceSpec{h->depth, h->levels, h->n, cpvs::pyramid_nan_flag(h->levels, h->n)};
     }
     if ((uint64_t)src[0].n * L > (1ull << 23)) return fail(CPVS_ERR_INVALID_ARG, "grid_build: n * length must not exceed 2^23");
     cpvs_status r = set_device(g->ctx);

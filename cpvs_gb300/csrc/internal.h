@@ -46,8 +46,14 @@ inline uint64_t pyramid_texels(uint32_t n) {
     return o;
 }
 // Device bytes of a pyramid: its texels plus 16 bytes, so that reads
-// rounded up to 16-byte chunks stay inside the allocation.
-inline uint64_t pyramid_bytes(uint32_t n) { return pyramid_texels(n) * 8 + 16; }
+// rounded up to 16-byte chunks stay inside the allocation, plus 16 bytes
+// that hold the map's NaN flag.
+inline uint64_t pyramid_bytes(uint32_t n) { return pyramid_texels(n) * 8 + 32; }
+// The word after a pyramid's padding: nonzero when its map holds a NaN
+// (set by launch_pyramid when it is given the word).
+inline uint32_t* pyramid_nan_flag(float2* levels, uint32_t n) {
+    return reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(levels) + pyramid_texels(n) * 8 + 16);
+}
 inline int log2_u32(uint32_t n) {
     int l = 0;
     while ((1u << l) < n) ++l;
@@ -59,8 +65,9 @@ struct Timing;
 // `depth_copy` (optional): the map is also copied there while it is read.
 // Levels below `store_from` are reduced but not stored (the first pass must
 // still store its last level, which the next pass reads: store_from <= 3).
+// `nan_flag` (optional): zeroed, then set when the map holds a NaN.
 cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaStream_t st, Timing* timing = nullptr,
-                           float* depth_copy = nullptr, int store_from = 1);
+                           float* depth_copy = nullptr, int store_from = 1, uint32_t* nan_flag = nullptr);
 
 // One z-tile of a source map whose per-level node bounds are wanted.
 struct BoundJob {
@@ -90,6 +97,7 @@ struct SourceSpec {
     const float* depth;    // device, n*n
     const float2* levels;  // device pyramid (levels 1..log2 n)
     uint32_t n;
+    const uint32_t* nan_flag;  // device word, nonzero if the map holds a NaN (null: unknown)
 };
 struct JobSpec {
     uint32_t source;

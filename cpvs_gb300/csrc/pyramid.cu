@@ -33,7 +33,7 @@ constexpr int kThreads = 256;
 template <bool FROM_DEPTH>
 __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ in, uint32_t S, float2* __restrict__ out,
                                                       uint32_t n, int L0, uint32_t T, float* __restrict__ copy,
-                                                      int store_from) {
+                                                      int store_from, uint32_t* nan_flag) {
     chain_enter();
     __shared__ float2 buf0[(kTile / 2) * (kTile / 2)];
     __shared__ float2 buf1[(kTile / 4) * (kTile / 4)];
@@ -42,6 +42,7 @@ __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ i
 
     // first level: (T/2)^2 outputs of this tile
     uint32_t half = T / 2;
+    int nan = 0;  // a NaN among the depths this thread read
     {
         const uint32_t So = S / 2;
         float2* dst = out + pyramid_level_offset_dev(n, L0);
@@ -59,6 +60,7 @@ __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ i
                 }
                 lo = pmin(pmin(r0.x, r0.y), pmin(r1.x, r1.y));
                 hi = pmax(pmax(r0.x, r0.y), pmax(r1.x, r1.y));
+                nan |= (r0.x != r0.x) | (r0.y != r0.y) | (r1.x != r1.x) | (r1.y != r1.y);
             } else {
                 const float2* p = static_cast<const float2*>(in);
                 const float4 r0 = *reinterpret_cast<const float4*>(p + (size_t)iy * S + ix);
@@ -71,6 +73,7 @@ __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ i
             buf0[o] = v;
         }
     }
+    if (FROM_DEPTH && nan_flag && __any_sync(0xffffffffu, nan) && (threadIdx.x & 31u) == 0) atomicOr(nan_flag, 1u);
     // remaining levels of the tile in shared memory (ping-pong buf0 <-> buf1)
     uint32_t So = S / 2;
     int L = L0 + 1;
@@ -108,12 +111,13 @@ __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ i
 // `store_from` stay in shared memory.
 __global__ void __launch_bounds__(kThreads)
     k_pyramid64(const float* __restrict__ in, uint32_t S, float2* __restrict__ out, uint32_t n,
-                float* __restrict__ copy, int store_from) {
+                float* __restrict__ copy, int store_from, uint32_t* nan_flag) {
     chain_enter();
     __shared__ float2 buf0[32 * 32];
     __shared__ float2 buf1[16 * 16];
     const uint32_t tiles_x = S >> 6;
     const uint32_t tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+    int nan = 0;  // a NaN among the depths this thread read
     {
         const uint32_t So = S >> 1;
         float2* dst = out;  // level 1 starts the pyramid array
@@ -130,6 +134,8 @@ __global__ void __launch_bounds__(kThreads)
             }
             const float2 v0 = make_float2(pmin(pmin(a.x, a.y), pmin(b.x, b.y)), pmax(pmax(a.x, a.y), pmax(b.x, b.y)));
             const float2 v1 = make_float2(pmin(pmin(a.z, a.w), pmin(b.z, b.w)), pmax(pmax(a.z, a.w), pmax(b.z, b.w)));
+            nan |= (a.x != a.x) | (a.y != a.y) | (a.z != a.z) | (a.w != a.w) | (b.x != b.x) | (b.y != b.y) |
+                   (b.z != b.z) | (b.w != b.w);
             if (store_from <= 1)
                 *reinterpret_cast<float4*>(dst + (size_t)(ty * 32 + oy) * So + tx * 32 + 2 * px) =
                     make_float4(v0.x, v0.y, v1.x, v1.y);
@@ -137,6 +143,7 @@ __global__ void __launch_bounds__(kThreads)
             buf0[oy * 32 + 2 * px + 1] = v1;
         }
     }
+    if (nan_flag && __any_sync(0xffffffffu, nan) && (threadIdx.x & 31u) == 0) atomicOr(nan_flag, 1u);
     uint32_t So = S >> 1;
     float2* src = buf0;
     float2* nxt = buf1;
@@ -207,8 +214,9 @@ __global__ void __launch_bounds__(kBoundThreads)
 }  // namespace
 
 cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaStream_t st, Timing* timing,
-                           float* depth_copy, int store_from) {
+                           float* depth_copy, int store_from, uint32_t* nan_flag) {
     KernelTimer kt(timing, K_PYRAMID, st);
+    if (nan_flag) CPVS_CUDA(cudaMemsetAsync(nan_flag, 0, sizeof(uint32_t), st));
     uint32_t S = n;
     int L0 = 1;
     bool first = true;
@@ -219,14 +227,14 @@ cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaS
         // the stream drains, and waits for it at its start
         if (first && T == (uint32_t)kTile)
             CPVS_CUDA(launch_kernel(k_pyramid64, tiles, kThreads, 0, st, true, 0, depth, S, levels, n, depth_copy,
-                                    store_from));
+                                    store_from, nan_flag));
         else if (first)
             CPVS_CUDA(launch_kernel(k_pyramid<true>, tiles, kThreads, 0, st, true, 0, static_cast<const void*>(depth), S,
-                                    levels, n, L0, T, depth_copy, store_from));
+                                    levels, n, L0, T, depth_copy, store_from, nan_flag));
         else
             CPVS_CUDA(launch_kernel(k_pyramid<false>, tiles, kThreads, 0, st, true, 0,
                                     static_cast<const void*>(levels + pyramid_level_offset(n, L0 - 1)), S, levels, n,
-                                    L0, T, static_cast<float*>(nullptr), store_from));
+                                    L0, T, static_cast<float*>(nullptr), store_from, static_cast<uint32_t*>(nullptr)));
         first = false;
         L0 += log2_u32(T);
         S /= T;
