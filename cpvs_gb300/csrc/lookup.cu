@@ -128,22 +128,35 @@ __global__ void __launch_bounds__(kThreads)
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     const float scale = (float)((1u << (num_levels - 1)) - 1u);
     if (Q == 1) {
-        // one query per thread, each descending on its own
-        for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwords; w += nw) {
+        // one query per thread, each descending on its own; the point of the
+        // thread's next query is requested before the current one descends
+        uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+        uint32_t nx = 0, ny = 0, nz = 0;
+        auto fetch = [&](uint64_t wq) {
+            const uint64_t iq = wq * 32 + (uint64_t)lane;
+            if (wq < nwords && iq < n) {
+                const uint32_t* p = static_cast<const uint32_t*>(q) + 3 * iq;
+                nx = __ldcs(p);
+                ny = __ldcs(p + 1);
+                nz = __ldcs(p + 2);
+            }
+        };
+        fetch(w);
+        for (; w < nwords; w += nw) {
             const uint64_t i = w * 32 + (uint64_t)lane;
+            const uint32_t rx = nx, ry = ny, rz = nz;
+            fetch(w + nw);
             bool lit = false;
             if (i < n) {
                 int32_t px, py, pz;
                 if (NDC) {
-                    const float* p = static_cast<const float*>(q) + 3 * i;
-                    px = quantise(__ldcs(p), scale);
-                    py = quantise(__ldcs(p + 1), scale);
-                    pz = quantise(__ldcs(p + 2), scale);
+                    px = quantise(__uint_as_float(rx), scale);
+                    py = quantise(__uint_as_float(ry), scale);
+                    pz = quantise(__uint_as_float(rz), scale);
                 } else {
-                    const int32_t* p = static_cast<const int32_t*>(q) + 3 * i;
-                    px = __ldcs(p);
-                    py = __ldcs(p + 1);
-                    pz = __ldcs(p + 2);
+                    px = (int32_t)rx;
+                    py = (int32_t)ry;
+                    pz = (int32_t)rz;
                 }
                 uint32_t off = 0;
                 int level = root;
