@@ -150,6 +150,38 @@ def kernel_alg_bytes(name: str, n: int, tree: list, uniq: list, dag_words: int) 
     return 0.0
 
 
+def config_dict(config: str, n: int, dag_words: int, nq: int, world: int) -> dict:
+    """The workload description both arms print (GPU and reference)."""
+    wl = WORKLOADS[config]
+    return {"workload": f"{config}: {wl['desc']}", "map_side": n, "voxels_per_dag": n ** 3,
+            "dag_words": int(dag_words), "lookups_per_batch": nq,
+            "l2": "inputs larger than L2 (256 MiB map read per step)" if n >= 8192 else
+                  "map smaller than L2: later steps may hit L2",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
+
+
+def host_link(torch, dev, stream, nbytes=256 << 20, reps=5) -> dict:
+    """Copy rate of the host link: pinned host <-> device, one
+    cudaMemcpyAsync of 256 MiB per direction, best of `reps` (CUDA events)."""
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    out = {}
+    for name, dst, src in (("h2d_gbs", d, h), ("d2h_gbs", h, d)):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        best = 1e30
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            dst.copy_(src, non_blocking=True)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            best = min(best, e0.elapsed_time(e1))
+        out[name] = round(nbytes / (best * 1e-3) / 1e9, 1)
+    out["how"] = "one pinned cudaMemcpyAsync of 256 MiB per direction, best of 5, CUDA events"
+    return out
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     import cpvs_gb300 as cp
@@ -235,6 +267,12 @@ def run_ours(args, rank, world, local_rank):
     sh = keep["sh"]
     tree, uniq = sh.level_counts()
     dag_words = sh.dag_size()
+    # the library's record of the last graph build: its internal-check word
+    # must be 0 (any other bit fails the build), plus its re-plans and the
+    # launch shapes the plan's tuner kept
+    build_step()
+    report = ctx.last_build()
+    assert report["error_word"] == 0, report
 
     # lookups against the resident DAG, queries resident in HBM
     for _ in range(args.warmup):
@@ -261,6 +299,20 @@ def run_ours(args, rank, world, local_rank):
         barrier()
         variants[str(qpt)] = round(e0.elapsed_time(e1) / 3, 4)
     ctx.set_option(ctx.OPT_LOOKUP_QUERIES_PER_THREAD, 0)
+    # a build followed by its first lookup batch, the serving pattern: the
+    # first lookup also builds the DAG's top grid (k_top_index)
+    first = []
+    ctx.enable_timing(True)
+    for _ in range(3):
+        e0.record(stream)
+        s2 = cp.CompressedShadow.from_depth(depth_dev, ctx=ctx, stream=stream)
+        s2.lookup_ndc(q_dev, bits_dev, stream=stream)
+        e1.record(stream)
+        barrier()
+        first.append(e0.elapsed_time(e1))
+        del s2
+    top_kt = ctx.kernel_times().get("k_top_index", (0.0, 0))
+    ctx.enable_timing(False)
 
     # end to end through the public API with host buffers
     # the DAG is read back into one reused pinned buffer, as the lookup bits are
@@ -292,6 +344,7 @@ def run_ours(args, rank, world, local_rank):
     frame = (measure_frame(cp, torch, ctx, sh, q_dev, stream, args.steps, args.warmup, barrier)
              if world == 1 and nq >= 3840 * 2160 else None)
     clk = clocks.stop()
+    link = host_link(torch, dev, stream) if world == 1 else None
 
     # slowest rank
     t = torch.tensor([build_ms, lookup_ms, e2e_build_ms, e2e_lookup_ms], dtype=torch.float64, device=dev)
@@ -334,11 +387,7 @@ def run_ours(args, rank, world, local_rank):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic: seeded scene rasterised to a float32 depth map (no dataset involved)",
-        "config": {"workload": f"{args.config}: {wl['desc']}", "map_side": n, "voxels_per_dag": int(voxels),
-                   "dag_words": dag_words, "lookups_per_batch": nq,
-                   "l2": "inputs larger than L2 (256 MiB map read per step)" if n >= 8192 else
-                         "map smaller than L2: later steps may hit L2",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "config": config_dict(args.config, n, dag_words, nq, world),
         "e2e": {"value": round(world * voxels / (e2e_build_ms * 1e-3) / 1e9, 1), "unit": "Gvoxel/s",
                 "h2d_bytes_per_step": int(depth.nbytes), "d2h_bytes_per_step": int(dag_bytes),
                 "ms_per_step": round(e2e_build_ms, 3),
@@ -358,18 +407,48 @@ def run_ours(args, rank, world, local_rank):
                    "e2e": {"value": round(world * nq / (e2e_lookup_ms * 1e-3) / 1e9, 2), "unit": "Glookups/s",
                            "h2d_bytes_per_step": int(q_host.nbytes), "d2h_bytes_per_step": int(bits_host.numel() * 4),
                            "ms_per_step": round(e2e_lookup_ms, 3)}},
+        "build_then_first_lookup": {"ms": round(statistics.median(first), 4),
+                                    "steady_build_plus_lookup_ms": round(build_ms + lookup_ms, 4),
+                                    "k_top_index_ms": round(top_kt[0] / max(top_kt[1], 1), 4),
+                                    "path": "cpvs_shadow_create_from_depth, then the first cpvs_shadow_lookup_ndc "
+                                            "on the new shadow (builds its top grid), median of 3"},
+        "build_report": report,
         "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in build_kernels.items()},
         "kernel_timing": "CUDA events around every library launch, in a pass of the same steps right after the "
                          "timed region (the timed region itself replays the captured build graph)",
         "gpu_launches": int(launches),
         "clocks": clk,
     }
+    if link is not None:
+        # end to end against the host link: the bytes each step moves across
+        # it, at the link's measured copy rate, bound the step from below
+        def link_roofline(h2d, d2h, ms):
+            floor = (h2d / (link["h2d_gbs"] * 1e9) + d2h / (link["d2h_gbs"] * 1e9)) * 1e3
+            return {"bound": "host link", "floor_ms": round(floor, 4), "frac": round(floor / ms, 4),
+                    "achieved_gbs": round((h2d + d2h) / (ms * 1e-3) / 1e9, 1)}
+        line["host_link"] = link
+        line["e2e"]["roofline"] = link_roofline(depth.nbytes, dag_bytes, e2e_build_ms)
+        line["lookup"]["e2e"]["roofline"] = link_roofline(q_host.nbytes, bits_host.numel() * 4, e2e_lookup_ms)
     if frame is not None:
         fr = frame["shade_roofline"]
         fr.update({"peak": peak, "unit": "GB/s", "frac": round(fr["achieved"] / peak, 4), "peak_kind": peak_kind})
         line["frame"] = frame
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(depth, q_host, args.config, sample_queries=1 << 22)
+    if world == 1 and not args.no_extras:
+        # the batched and served forms on the same GPU, each against the
+        # plain per-request path (their own clocks; not part of `value`)
+        drop = ("n_gpus", "higher_is_better", "scaling", "vs_baseline", "dtype", "data")
+        del q_dev, bits_dev, depth_dev
+        keep.clear()
+        torch.cuda.empty_cache()
+        xs = min(args.steps, 10)
+        for key, cfg in (("batched", "c3"), ("grid", "c2")):
+            r = measure_batched(cfg, xs, 3, cpu=not args.no_cpu_baseline)
+            line[key] = {k: v for k, v in r.items() if k not in drop}
+            torch.cuda.empty_cache()
+        r = measure_served()
+        line["served"] = {k: v for k, v in r.items() if k not in drop}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -504,9 +583,10 @@ def run_reference(args, rank, world):
     O = Oracle()
     threads = os.cpu_count() or 1
     # each step: one full build (the reference builds one DAG per thread) plus
-    # one bounded lookup sample over all host cores
-    steps = max(1, min(args.steps, 5))
-    warm = min(args.warmup, 1)
+    # one bounded lookup sample over all host cores; the driver's steps and
+    # warm-up (20 and 5 builds of ~3 s each at 8192^2)
+    steps = max(1, args.steps)
+    warm = max(0, args.warmup)
     sample = min(wl["queries"], 1 << 23)
     for _ in range(warm):
         O.build(depth, threads=4)
@@ -526,8 +606,7 @@ def run_reference(args, rank, world):
         "steps": steps, "warmup": warm, "ms_per_step": round(build_s * 1e3, 2), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded scene rasterised to a float32 depth map (no dataset involved)",
-        "config": {"workload": f"{args.config}: {wl['desc']}", "map_side": n, "dag_words": int(b.dag.size),
-                   "note": f"steps capped at {steps} (bounded CPU sample)"},
+        "config": config_dict(args.config, n, int(b.dag.size), wl["queries"], world),
         "cpu_baseline": {"value": round(v, 3), "unit": "Gvoxel/s", "cores": 4, "kind": "port",
                          "sample": f"full {n}^2 build per step: pyramid on 4 threads, SVO/merge/compress on 1 thread "
                                    f"(the reference's threading); hash-indexed first-occurrence merge",
@@ -572,20 +651,20 @@ def surface_queries_device(torch, maps, n_total, count, gen, tile_of=None):
     return out, which
 
 
-def run_batched(args):
+def measure_batched(config: str, steps: int, warmup: int, cpu: bool = True) -> dict:
     """c2 / c3: many DAGs per step in one batched build (one plan, one graph
     launch) against the plain path (one build call per DAG)."""
     import torch
     import cpvs_gb300 as cp
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(0)
-    wl = WORKLOADS[args.config]
+    wl = WORKLOADS[config]
     ctx = cp.Context(0)
     stream = torch.cuda.current_stream(dev)
     gen = torch.Generator(device=dev)
     gen.manual_seed(7)
     nq = wl["queries"]
-    if args.config == "c2":
+    if config == "c2":
         sc = scene.config_scene("c2")
         T, L = 4096, 8
         maps = [cp.raster_depth(sc, x * T, y * T, T, T, ctx=ctx) for y in range(L) for x in range(L)]
@@ -671,11 +750,11 @@ def run_batched(args):
 
     clocks = ClockSampler(0)
     clocks.start()
-    res_b, tb = timed(batched, args.steps, args.warmup)
-    res_p, tp = timed(plain, max(2, args.steps // 4), 1)
+    res_b, tb = timed(batched, steps, warmup)
+    res_p, tp = timed(plain, max(2, steps // 4), 1)
     # correctness of the batched form against the plain one on the same maps
     same = None
-    if args.config == "c3":
+    if config == "c3":
         same = all(np.array_equal(a.get_dag(), b.get_dag()) for a, b in zip(res_b, res_p))
     else:
         da, _ = res_b.words()
@@ -686,32 +765,32 @@ def run_batched(args):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         look(res_b, out)
     e1.record(stream)
     torch.cuda.synchronize()
-    look_ms = e0.elapsed_time(e1) / args.steps
+    look_ms = e0.elapsed_time(e1) / steps
     clk = clocks.stop()
     ms_b = statistics.median(tb)
     ms_p = statistics.median(tp)
     line = {
-        "metric": METRIC + (" -- batched grid build" if args.config == "c2" else " -- batched multi-light build"),
-        "value": round(voxels / (ms_b * 1e-3) / 1e9, 1), "unit": "Gvoxel/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(ms_b, 3), "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC + (" -- batched grid build" if config == "c2" else " -- batched multi-light build"),
+        "value": round(voxels / (ms_b * 1e-3) / 1e9, 1), "unit": "Gvoxel/s", "n_gpus": 1, "steps": steps,
+        "warmup": warmup, "ms_per_step": round(ms_b, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded scenes rasterised on the GPU (no dataset)",
-        "config": {"workload": f"{args.config}: {wl['desc']}", "dags_per_step": ndags, "voxels_per_step": voxels},
+        "config": {"workload": f"{config}: {wl['desc']}", "dags_per_step": ndags, "voxels_per_step": voxels},
         "plain": {"value": round(voxels / (ms_p * 1e-3) / 1e9, 1), "unit": "Gvoxel/s", "ms_per_step": round(ms_p, 3),
-                  "path": "one cpvs_shadow_create per DAG" + (" + grid finalize" if args.config == "c2" else "")},
+                  "path": "one cpvs_shadow_create per DAG" + (" + grid finalize" if config == "c2" else "")},
         "batched_over_plain": round(ms_p / ms_b, 2),
         "p50_ms": {"batched": round(ms_b, 3), "plain": round(ms_p, 3)},
         "p99_ms": {"batched": round(float(np.percentile(tb, 99)), 3), "plain": round(float(np.percentile(tp, 99)), 3)},
         "dags_identical_to_plain": same,
         "lookup": {"value": round(nq / (look_ms * 1e-3) / 1e9, 2), "unit": "Glookups/s", "ms_per_batch": round(look_ms, 4),
-                   "path": "cpvs_grid_lookup_ndc" if args.config == "c2" else "cpvs_lookup_ndc_multi"},
+                   "path": "cpvs_grid_lookup_ndc" if config == "c2" else "cpvs_lookup_ndc_multi"},
         "clocks": clk,
     }
-    if not args.no_cpu_baseline:
-        if args.config == "c2":
+    if cpu:
+        if config == "c2":
             # the 8 z-tile DAGs of the 8 xy tiles on the grid's diagonal (1/8 of the DAGs)
             diag = [t * (L + 1) for t in range(L)]
             jobs = [(maps[t].cpu().numpy(), z, L) for t in diag for z in range(L)]
@@ -719,12 +798,19 @@ def run_batched(args):
         else:
             jobs = [(m.cpu().numpy(), 0, 1) for m in maps[:16]]
             line["cpu_baseline"] = cpu_parallel_builds(jobs, "the first 16 of the 64 lights")
-    print(json.dumps(line), flush=True)
+    return line
 
 
-def run_served(args):
+def run_batched(args):
+    print(json.dumps(measure_batched(args.config, args.steps, args.warmup, not args.no_cpu_baseline)), flush=True)
+
+
+def measure_served() -> dict:
     """c4: the same request trace through the server (continuous batching)
-    and through serial plain-path handling on the same GPU."""
+    and through serial plain-path handling on the same GPU; then a trace
+    whose lookups go to the 6 most recent builds through a server with a
+    12 MiB budget (the trace builds ~16 MB of DAGs), so that older DAGs are
+    evicted (LRU) and builds admitted by bytes."""
     import threading
     import torch
     import cpvs_gb300 as cp
@@ -741,7 +827,8 @@ def run_served(args):
     meta = np.random.Generator(np.random.PCG64(45))
     nreq = 4000
 
-    def make_trace(rate):
+    def make_trace(rate, recent=0):
+        # recent > 0: lookups pick one of the `recent` latest builds
         t, trace, built = 0.0, [], []
         for i in range(nreq):
             t += meta.exponential(1.0 / rate)
@@ -752,7 +839,8 @@ def run_served(args):
             else:
                 cnt = 1 << int(round(12 + 10 * meta.random()))
                 off = int(meta.integers(0, pts_pool.shape[0] - cnt + 1))
-                trace.append(("lookup", t, built[int(meta.integers(0, len(built)))], pts_pool[off:off + cnt]))
+                pick = built[-recent:] if recent else built
+                trace.append(("lookup", t, pick[int(meta.integers(0, len(pick)))], pts_pool[off:off + cnt]))
         return trace
 
     def plain_run(trace):
@@ -770,10 +858,10 @@ def run_served(args):
             lat[kind].append((time.perf_counter() - t0 - at) * 1e3)
         return lat, time.perf_counter() - t0
 
-    def served_run(trace):
+    def served_run(trace, budget=120 << 30):
         """The trace through the server; latency counts from the scheduled
         arrival (a late submission counts against the server)."""
-        srv = cp.Server(cp.Context(0), budget_bytes=120 << 30)
+        srv = cp.Server(cp.Context(0), budget_bytes=budget)
         tickets = []
         t0 = time.perf_counter()
 
@@ -792,15 +880,21 @@ def run_served(args):
         th = threading.Thread(target=submitter)
         th.start()
         lat = {"build": [], "lookup": []}
+        failed = 0
         for got in range(len(trace)):
             while got >= len(tickets):
                 time.sleep(0.0001)
             kind, late, t = tickets[got]
-            ms, _ = srv.wait(t, packed=True)
+            try:
+                ms, _ = srv.wait(t, packed=True)
+            except cp.CpvsError:
+                failed += 1  # e.g. a lookup whose DAG was evicted: the client would rebuild
+                continue
             lat[kind].append(late + ms)
         wall = time.perf_counter() - t0
         th.join()
         stats = srv.stats()
+        stats["requests_failed"] = failed
         srv.close()
         return lat, wall, stats
 
@@ -829,14 +923,26 @@ def run_served(args):
         loads[str(load)] = {"offered_req_s": round(rate, 1), "served": summ(lat_s, wall_s),
                             "plain_serial": summ(lat_p, wall_p),
                             "server_stats": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in stats.items()}}
+    # under a budget that holds a few DAGs: evictions and admission by bytes
+    budget = 12 << 20
+    trace = make_trace(0.8 * cap_plain, recent=6)
+    lat_p, wall_p = plain_run(trace)
+    lat_s, wall_s, stats = served_run(trace, budget)
+    budgeted = {"budget_bytes": budget, "offered_req_s": round(0.8 * cap_plain, 1),
+                "lookups_target": "one of the 6 most recent builds",
+                "served": summ(lat_s, wall_s), "plain_serial": summ(lat_p, wall_p),
+                "server_stats": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in stats.items()}}
     head = loads["0.8"]
-    line = {"metric": "served p99 latency ms (c4)", "value": head["served"]["p99_ms"], "unit": "ms", "n_gpus": 1,
+    return {"metric": "served p99 latency ms (c4)", "value": head["served"]["p99_ms"], "unit": "ms", "n_gpus": 1,
             "steps": nreq, "warmup": 100, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic: seeded scenes and Poisson request traces (no dataset)",
             "config": {"workload": "c4: " + WORKLOADS["c4"]["desc"], "requests_per_trace": nreq},
             "capacity_req_s": {"served": round(cap_served, 1), "plain_serial": round(cap_plain, 1)},
-            "loads": loads}
-    print(json.dumps(line), flush=True)
+            "loads": loads, "budget_limited": budgeted}
+
+
+def run_served(args):
+    print(json.dumps(measure_served()), flush=True)
 
 
 def main():
@@ -847,6 +953,8 @@ def main():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--config", choices=tuple(WORKLOADS), default="c1")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="c1 line without the batched (c3), grid (c2) and served (c4) measurements")
     ap.add_argument("--part", choices=("all", "build", "lookup", "frame"), default="all",
                     help="profiling aid: run only the build steps or only the lookup batches (no JSON line)")
     args = ap.parse_args()

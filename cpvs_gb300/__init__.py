@@ -51,6 +51,7 @@ _SIGS = {
     "cpvs_ctx_bytes_in_use": (_u64, [_vp]),
     "cpvs_ctx_set_option": (C.c_int, [_vp, C.c_int, C.c_int64]),
     "cpvs_ctx_get_option": (C.c_int64, [_vp, C.c_int]),
+    "cpvs_ctx_last_build": (C.c_int, [_vp, _vp]),
     "cpvs_ctx_enable_timing": (C.c_int, [_vp, C.c_int]),
     "cpvs_ctx_kernel_times": (C.c_int, [_vp, _vp, _vp, _u32, C.POINTER(_u32)]),
     "cpvs_kernel_name": (C.c_char_p, [_u32]),
@@ -230,12 +231,25 @@ class Context:
         return int(_lib.cpvs_ctx_bytes_in_use(self.handle))
 
     OPT_LOOKUP_QUERIES_PER_THREAD = 1
+    OPT_BUILD_CLUSTER_CAP = 2
+    OPT_BUILD_INSERT_WAVES = 3
 
     def set_option(self, key: int, value: int):
         _check(_lib.cpvs_ctx_set_option(self.handle, key, int(value)))
 
     def get_option(self, key: int) -> int:
         return int(_lib.cpvs_ctx_get_option(self.handle, key))
+
+    def last_build(self) -> dict:
+        """What the last successful build did (cpvs_ctx_last_build): its
+        final internal-check word (0), plan re-growths, launch shapes, and
+        whether it timed the candidate shapes (a plan's first build)."""
+        class _Report(C.Structure):
+            _fields_ = [("error_word", C.c_uint32), ("replans", C.c_uint32), ("cluster_cap", C.c_uint32),
+                        ("insert_waves", C.c_uint32), ("tuned", C.c_uint32), ("tuning_ms", C.c_float)]
+        r = _Report()
+        _check(_lib.cpvs_ctx_last_build(self.handle, C.byref(r)))
+        return {f: getattr(r, f) for f, _ in _Report._fields_}
 
     def enable_timing(self, on: bool = True):
         _check(_lib.cpvs_ctx_enable_timing(self.handle, int(on)))

@@ -1605,7 +1605,8 @@ __global__ void __launch_bounds__(kThreads)
 constexpr int kClusterThreads = 1024;
 constexpr int kClusterItems = 4;
 constexpr int kClusterMaxBlocks = 16;
-constexpr uint64_t kClusterLevelCap = 8192;  // planned nodes of a level that the cluster kernels take, at most
+constexpr uint32_t kClusterLevelCap = 8192;  // default: planned nodes of a level that the cluster kernels take, at most
+constexpr uint32_t kClusterCaps[] = {2048, 4096, 8192, 16384};  // the candidates a plan's tuner times
 
 struct SmallLevels {
     uint32_t inj_off[CPVS_MAX_LEVELS];
@@ -2444,6 +2445,12 @@ struct BuildPlan {
     uint64_t inj_off[CPVS_MAX_LEVELS + 1] = {0};
     uint32_t max_grid = 0;
     uint32_t insert_grid = 0;  // one wave of the inner insert kernel
+    // launch shapes (tuned on the plan's first build, or fixed by the
+    // context's options): the largest level the cluster kernels take, and
+    // the inner insert's grid in resident waves
+    uint32_t cluster_cap = kClusterLevelCap;
+    uint32_t insert_waves = 1;
+    bool shapes_set = false;
     // device memory
     char* arena = nullptr;
     size_t arena_bytes = 0;
@@ -2534,7 +2541,7 @@ void plan_release(Ctx& ctx, BuildPlan* P) {
 void plan_bind_tables(BuildPlan* P) {
     // a level of more nodes runs faster as its own launches over every SM
     const uint64_t small_cap =
-        std::min<uint64_t>((uint64_t)P->cluster_blocks * kClusterThreads * kClusterItems, kClusterLevelCap);
+        std::min<uint64_t>((uint64_t)P->cluster_blocks * kClusterThreads * kClusterItems, P->cluster_cap);
     uint64_t off = 0;
     for (int L = P->bottom; L <= P->maxR; ++L) {
         P->lv[L].table = P->table + off;
@@ -2864,7 +2871,8 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
         const LevelDev child = (L > P->bottom) ? P->lv[L - 1] : P->lv[L];
         if (!leaf) {
             KernelTimer kt(tm, K_INSERT_INNER, st);
-            CPVS_CUDA(launch_kernel(k_dedup_insert<false>, std::min(plan_grid(P, P->cap[L], kThreads), P->insert_grid),
+            CPVS_CUDA(launch_kernel(k_dedup_insert<false>,
+                                    std::min(plan_grid(P, P->cap[L], kThreads), P->insert_grid * P->insert_waves),
                                     kThreads, 0, st, ch, 0,
                                    P->lv[L], child, P->counts, L, P->lv[L].table, P->lv[L].table_mask, err));
         }
@@ -2904,6 +2912,97 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
     }
     CPVS_CUDA(cudaMemcpyAsync(P->hout, P->res, result_bytes(njobs), cudaMemcpyDeviceToHost, st));
     return CPVS_OK;
+}
+
+// Captures the plan's launch sequence into P->exec.
+cpvs_status plan_capture(Ctx& ctx, BuildPlan* P) {
+    if (!ctx.capture_stream) CPVS_CUDA(cudaStreamCreateWithFlags(&ctx.capture_stream, cudaStreamNonBlocking));
+    if (!ctx.capture_rank_stream) CPVS_CUDA(cudaStreamCreateWithFlags(&ctx.capture_rank_stream, cudaStreamNonBlocking));
+    if (P->exec) {
+        cudaGraphExecDestroy(P->exec);
+        P->exec = nullptr;
+    }
+    cudaGraph_t graph = nullptr;
+    CPVS_CUDA(cudaStreamBeginCapture(ctx.capture_stream, cudaStreamCaptureModeThreadLocal));
+    cpvs_status r = plan_enqueue(P, ctx.capture_stream, ctx.capture_rank_stream, nullptr);
+    cudaError_t ec = cudaStreamEndCapture(ctx.capture_stream, &graph);
+    if (r != CPVS_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return r;
+    }
+    if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture");
+    ec = cudaGraphInstantiate(&P->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ec != cudaSuccess) return cuda_fail(ec, "cudaGraphInstantiate");
+    return CPVS_OK;
+}
+
+// Launch shapes of a plan: (cluster cap, insert waves).
+void plan_set_shapes(BuildPlan* P, uint32_t cap, uint32_t waves) {
+    if (P->cluster_cap == cap && P->insert_waves == waves) return;
+    P->cluster_cap = cap;
+    P->insert_waves = waves;
+    plan_bind_tables(P);  // the split between cluster and multi-block levels
+    if (P->exec) {
+        cudaGraphExecDestroy(P->exec);
+        P->exec = nullptr;
+    }
+}
+
+// The plan's autotuner: after the plan's first build (its inputs still
+// staged, its hash tables sized), every (cluster cap, insert waves) pair is
+// captured and its launch sequence timed -- one warm-up and the best of
+// three CUDA-event-timed replays on `st` -- and the fastest pair kept.  A
+// pair whose replay reports an internal check (a level or table overflow)
+// is not taken.  Runs after this build's emission in stream order; the
+// replays only rewrite the plan's own scratch.
+cpvs_status plan_tune(Ctx& ctx, BuildPlan* P, cudaStream_t st, float& tuning_ms) {
+    cudaEvent_t a = nullptr, b = nullptr, t0 = nullptr, t1 = nullptr;
+    CPVS_CUDA(cudaEventCreate(&a));
+    CPVS_CUDA(cudaEventCreate(&b));
+    CPVS_CUDA(cudaEventCreate(&t0));
+    CPVS_CUDA(cudaEventCreate(&t1));
+    CPVS_CUDA(cudaEventRecord(t0, st));
+    const uint32_t cap0 = P->cluster_cap, waves0 = P->insert_waves;
+    uint32_t best_cap = cap0, best_waves = waves0;
+    float best = 1e30f;
+    cpvs_status r = CPVS_OK;
+    for (uint32_t cap : kClusterCaps) {
+        for (uint32_t waves : {1u, 2u}) {
+            plan_set_shapes(P, cap, waves);
+            r = plan_capture(ctx, P);
+            if (r != CPVS_OK) break;
+            float t_min = 1e30f;
+            bool clean = true;
+            for (int rep = 0; rep < 4 && clean; ++rep) {
+                cudaEventRecord(a, st);
+                cudaGraphLaunch(P->exec, st);
+                cudaEventRecord(b, st);
+                if (cudaEventSynchronize(b) != cudaSuccess) {
+                    r = cuda_fail(cudaGetLastError(), "build tuning");
+                    break;
+                }
+                clean = *result_view(P->hout, P->njobs).err == 0;
+                float t = 0.f;
+                cudaEventElapsedTime(&t, a, b);
+                if (rep > 0 && t < t_min) t_min = t;  // the first replay warms the caches
+            }
+            if (r != CPVS_OK) break;
+            if (clean && t_min < best) {
+                best = t_min;
+                best_cap = cap;
+                best_waves = waves;
+            }
+        }
+        if (r != CPVS_OK) break;
+    }
+    plan_set_shapes(P, r == CPVS_OK ? best_cap : cap0, r == CPVS_OK ? best_waves : waves0);
+    cudaEventRecord(t1, st);
+    cudaEventSynchronize(t1);
+    cudaEventElapsedTime(&tuning_ms, t0, t1);
+    for (cudaEvent_t e : {a, b, t0, t1}) cudaEventDestroy(e);
+    if (P->done) cudaEventRecord(P->done, st);  // the next build waits for the replays too
+    return r;
 }
 
 bool same_shape(const BuildPlan* P, bool leafmasks, bool pow2, const std::vector<uint32_t>& job_n) {
@@ -3056,6 +3155,14 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
     }
 
     if (!P->done) CPVS_CUDA(cudaEventCreateWithFlags(&P->done, cudaEventDisableTiming));
+    // launch shapes fixed by the context's options take effect at once;
+    // otherwise the plan's first graph build times the candidates (below)
+    if (ctx.build_cluster_cap || ctx.build_insert_waves) {
+        plan_set_shapes(P, ctx.build_cluster_cap ? (uint32_t)ctx.build_cluster_cap : kClusterLevelCap,
+                        ctx.build_insert_waves ? (uint32_t)ctx.build_insert_waves : 1u);
+        P->shapes_set = true;
+    }
+    uint32_t replans = 0;
     // the previous build with this plan may still be emitting from its
     // scratch on another stream
     CPVS_CUDA(cudaStreamWaitEvent(st, P->done, 0));
@@ -3149,21 +3256,8 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
             if (r != CPVS_OK) return r;
         } else {
             if (!P->exec) {
-                if (!ctx.capture_stream) CPVS_CUDA(cudaStreamCreateWithFlags(&ctx.capture_stream, cudaStreamNonBlocking));
-                if (!ctx.capture_rank_stream)
-                    CPVS_CUDA(cudaStreamCreateWithFlags(&ctx.capture_rank_stream, cudaStreamNonBlocking));
-                cudaGraph_t graph = nullptr;
-                CPVS_CUDA(cudaStreamBeginCapture(ctx.capture_stream, cudaStreamCaptureModeThreadLocal));
-                cpvs_status r = plan_enqueue(P, ctx.capture_stream, ctx.capture_rank_stream, nullptr);
-                cudaError_t ec = cudaStreamEndCapture(ctx.capture_stream, &graph);
-                if (r != CPVS_OK) {
-                    if (graph) cudaGraphDestroy(graph);
-                    return r;
-                }
-                if (ec != cudaSuccess) return cuda_fail(ec, "cudaStreamEndCapture");
-                ec = cudaGraphInstantiate(&P->exec, graph, 0);
-                cudaGraphDestroy(graph);
-                if (ec != cudaSuccess) return cuda_fail(ec, "cudaGraphInstantiate");
+                cpvs_status r = plan_capture(ctx, P);
+                if (r != CPVS_OK) return r;
             }
             CPVS_CUDA(cudaGraphLaunch(P->exec, st));
         }
@@ -3178,6 +3272,7 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         const bool overflow = (herr & (1u | 16u)) != 0;
         if (!overflow || (herr & 2u) || attempt >= 2)
             return fail(CPVS_ERR_DEVICE, "build_dags: internal check " + std::to_string(herr));
+        ++replans;
         std::vector<unsigned long long> bounds;
         {
             cpvs_status r = prepass_bounds(ctx, sources, jobs, (leafmasks ? 2 : 0) + 1, st, bounds);
@@ -3254,6 +3349,19 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
             CPVS_CUDA(cudaMemcpyAsync(P->lvt, P->lv, sizeof(P->lv), cudaMemcpyHostToDevice, st));
         }
     }
+    float tuning_ms = 0.f;
+    bool tuned = false;
+    if (!P->shapes_set && !ctx.timing.on && ctx.tune_builds) {
+        cpvs_status r = plan_tune(ctx, P, st, tuning_ms);
+        if (r != CPVS_OK) return r;
+        P->shapes_set = tuned = true;
+    }
+    ctx.last_build.error_word = 0;
+    ctx.last_build.replans = replans;
+    ctx.last_build.cluster_cap = P->cluster_cap;
+    ctx.last_build.insert_waves = P->insert_waves;
+    ctx.last_build.tuned = tuned ? 1u : 0u;
+    ctx.last_build.tuning_ms = tuning_ms;
     return CPVS_OK;
 }
 

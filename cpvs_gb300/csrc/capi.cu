@@ -210,6 +210,7 @@ void ensure_top(const cpvs_shadow* cs, cudaStream_t st, uint32_t max_factor = kT
     cpvs_shadow* s = const_cast<cpvs_shadow*>(cs);
     if (s->top || s->top_bytes == ~0ull) return;
     const int depth = cpvs::top_index_depth(s->num_levels, s->leafmasks, s->words, max_factor);
+    cpvs::KernelTimer kt(&s->ctx->c.timing, cpvs::K_TOP_INDEX, st);
     if (depth <= 0 || s->ctx->c.alloc((void**)&s->top, uint64_t(4) << (3 * depth), true, st) != CPVS_OK ||
         cpvs::launch_top_index(s->dag, s->words, depth, s->top, st) != CPVS_OK) {
         if (s->top) s->ctx->c.release(s->top, uint64_t(4) << (3 * depth), true, st);
@@ -335,14 +336,32 @@ cpvs_status cpvs_ctx_set_option(cpvs_ctx* ctx, cpvs_option key, int64_t value) {
                 return fail(CPVS_ERR_INVALID_ARG, "lookup queries per thread must be 0 (tuned), 1, 2 or 4");
             ctx->c.lookup_qpt = (int)value;
             return CPVS_OK;
+        case CPVS_OPT_BUILD_CLUSTER_CAP:
+            if (value != 0 && value != 2048 && value != 4096 && value != 8192 && value != 16384)
+                return fail(CPVS_ERR_INVALID_ARG, "build cluster cap must be 0 (tuned), 2048, 4096, 8192 or 16384");
+            ctx->c.build_cluster_cap = (int)value;
+            return CPVS_OK;
+        case CPVS_OPT_BUILD_INSERT_WAVES:
+            if (value < 0 || value > 2) return fail(CPVS_ERR_INVALID_ARG, "build insert waves must be 0 (tuned), 1 or 2");
+            ctx->c.build_insert_waves = (int)value;
+            return CPVS_OK;
     }
     return fail(CPVS_ERR_INVALID_ARG, "unknown option");
+}
+
+cpvs_status cpvs_ctx_last_build(const cpvs_ctx* ctx, cpvs_build_report* out) {
+    if (!ctx || !out) return fail(CPVS_ERR_INVALID_ARG, "last_build: null argument");
+    const auto& b = ctx->c.last_build;
+    *out = cpvs_build_report{b.error_word, b.replans, b.cluster_cap, b.insert_waves, b.tuned, b.tuning_ms};
+    return CPVS_OK;
 }
 
 int64_t cpvs_ctx_get_option(const cpvs_ctx* ctx, cpvs_option key) {
     if (!ctx) return -1;
     switch (key) {
         case CPVS_OPT_LOOKUP_QUERIES_PER_THREAD: return ctx->c.lookup_qpt;
+        case CPVS_OPT_BUILD_CLUSTER_CAP: return ctx->c.build_cluster_cap;
+        case CPVS_OPT_BUILD_INSERT_WAVES: return ctx->c.build_insert_waves;
     }
     return -1;
 }

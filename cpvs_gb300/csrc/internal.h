@@ -203,6 +203,7 @@ enum KernelId : int {
     K_EVALUATE,
     K_SHADE,
     K_LEAF_CLASSES,
+    K_TOP_INDEX,
     K_COUNT
 };
 const char* kernel_name(int id);
@@ -244,6 +245,17 @@ struct Ctx {
     // once per (DAG levels, NDC or voxel input)
     int lookup_qpt = 0;
     int lookup_qpt_tuned[CPVS_MAX_LEVELS][2] = {{0}};
+    // build launch shapes fixed by cpvs_ctx_set_option (0: timed per plan on
+    // its first build): the largest level the cluster kernels take, and the
+    // inner-level insert's grid in resident waves
+    int build_cluster_cap = 0;
+    int build_insert_waves = 0;
+    bool tune_builds = true;  // a server's context does not time candidates inside its loop
+    // what the last build did (cpvs_ctx_last_build)
+    struct BuildReport {
+        uint32_t error_word = 0, replans = 0, cluster_cap = 0, insert_waves = 0, tuned = 0;
+        float tuning_ms = 0.f;
+    } last_build;
     uint64_t budget = 0;   // 0 = unlimited
     uint64_t in_use = 0;   // persistent bytes (hierarchies, DAGs, grids)
     uint64_t scratch = 0;  // stream-ordered build / staging scratch

@@ -111,6 +111,7 @@ struct cpvs_server {
     std::vector<Req> builds_pending;
     std::unordered_map<uint64_t, EntryP> resident;
     uint64_t resident_bytes = 0, tick = 0;
+    uint64_t dag_bytes_seen[17] = {0};  // largest DAG built so far per log2 map side (admission estimate)
     std::unordered_map<uint64_t, uint64_t> gen_submitted, gen_done;
     std::vector<cpvs_shadow*> graveyard;  // unpinned after being dropped: the builder destroys them
     std::vector<double> lat[2];
@@ -356,10 +357,14 @@ struct cpvs_server {
     }
 
     void build_batch(std::vector<Req>& batch) {
-        // admission: room for the new DAGs (estimated at n^2/4 bytes each)
+        // admission: room for the new DAGs, each estimated at the largest
+        // DAG built so far from a map of its side (n^2/4 bytes before any)
         if (cfg.budget_bytes) {
             uint64_t estimate = 0;
-            for (const Req& r : batch) estimate += (uint64_t)r->n * r->n / 4;
+            for (const Req& r : batch) {
+                const uint64_t seen = dag_bytes_seen[cpvs::log2_u32(r->n)];
+                estimate += seen ? seen : (uint64_t)r->n * r->n / 4;
+            }
             std::vector<cpvs_shadow*> dead;
             {
                 std::lock_guard<std::mutex> lock(mu);
@@ -406,6 +411,8 @@ struct cpvs_server {
             for (size_t i = 0; i < ok.size(); ++i) {
                 const Req& r = ok[i];
                 const uint64_t bytes = out[i]->words * 4;
+                uint64_t& seen = dag_bytes_seen[cpvs::log2_u32(r->n)];
+                if (bytes > seen) seen = bytes;
                 if (cfg.budget_bytes && bytes > cfg.budget_bytes) {
                     dead.push_back(out[i]);
                     complete_locked(r, CPVS_ERR_BUDGET, "build: the DAG alone exceeds the server's budget");
@@ -483,6 +490,9 @@ cpvs_status cpvs_server_create(cpvs_ctx* ctx, const cpvs_server_config* cfg, cpv
     CPVS_CUDA(cudaSetDevice(ctx->c.device));
     auto s = std::make_unique<cpvs_server>();
     s->ctx = ctx;
+    // the server's builds keep the default launch shapes (or those the
+    // context's options fix): timing candidates would stall the loop
+    ctx->c.tune_builds = false;
     if (cfg) s->cfg = *cfg;
     if (!s->cfg.max_batch_builds) s->cfg.max_batch_builds = 16;
     if (!s->cfg.max_batch_lookups) s->cfg.max_batch_lookups = 256;

@@ -10,7 +10,7 @@ const char* kernel_name(int id) {
         "k_classify_bottom", "table_clear",    "k_leaf_resolve", "k_dedup_insert", "k_dedup_resolve",
         "k_merge_scan",      "k_dedup_remap",  "k_layout",       "k_emit_all",     "k_lookup",
         "k_grid_lookup",     "k_raster",       "k_multi_lookup", "k_grid_evaluate", "k_shade",
-        "k_leaf_classes"};
+        "k_leaf_classes", "k_top_index"};
     return (id >= 0 && id < K_COUNT) ? names[id] : "";
 }
 

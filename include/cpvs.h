@@ -84,14 +84,39 @@ CPVS_API void cpvs_ctx_destroy(cpvs_ctx* ctx);
  * CPVS_ERR_BUDGET. */
 CPVS_API cpvs_status cpvs_ctx_set_budget(cpvs_ctx* ctx, uint64_t bytes);
 CPVS_API uint64_t cpvs_ctx_bytes_in_use(const cpvs_ctx* ctx);
-/* Tunable launch shapes.  CPVS_OPT_LOOKUP_QUERIES_PER_THREAD: independent
- * descents each lookup thread carries (1, 2 or 4); 0 (default) = tuned per
- * DAG depth by timing the three on the first lookup batch of that depth. */
+/* Tunable launch shapes; 0 (the default) = timed by the library.
+ * CPVS_OPT_LOOKUP_QUERIES_PER_THREAD: independent descents each lookup
+ * thread carries (1, 2 or 4); tuned per DAG depth by timing the three on the
+ * first lookup batch of that depth.
+ * CPVS_OPT_BUILD_CLUSTER_CAP: the largest level (planned nodes) that the
+ * small-level cluster kernels take (2048, 4096, 8192 or 16384); larger
+ * levels run in the multi-block kernels.
+ * CPVS_OPT_BUILD_INSERT_WAVES: grid of the inner-level merge insert, in
+ * waves of resident blocks (1 or 2).
+ * The two build shapes are tuned per build plan (one per batch shape) by
+ * timing every pair on the plan's first build; setting either fixes both
+ * (the other at its default: 8192, 1).  The DAG does not depend on them. */
 typedef enum cpvs_option {
-    CPVS_OPT_LOOKUP_QUERIES_PER_THREAD = 1
+    CPVS_OPT_LOOKUP_QUERIES_PER_THREAD = 1,
+    CPVS_OPT_BUILD_CLUSTER_CAP = 2,
+    CPVS_OPT_BUILD_INSERT_WAVES = 3
 } cpvs_option;
 CPVS_API cpvs_status cpvs_ctx_set_option(cpvs_ctx* ctx, cpvs_option key, int64_t value);
 CPVS_API int64_t cpvs_ctx_get_option(const cpvs_ctx* ctx, cpvs_option key);
+/* What the context's last successful build did: the internal-check word of
+ * its final pass (always 0: any other bit fails the build), the plan
+ * re-growths it needed (a level or hash table outgrew the plan), the launch
+ * shapes it ran with, and whether it timed the candidate shapes (a plan's
+ * first build) and for how long.  No counterpart in the reference. */
+typedef struct cpvs_build_report {
+    uint32_t error_word;
+    uint32_t replans;
+    uint32_t cluster_cap;
+    uint32_t insert_waves;
+    uint32_t tuned;
+    float tuning_ms;
+} cpvs_build_report;
+CPVS_API cpvs_status cpvs_ctx_last_build(const cpvs_ctx* ctx, cpvs_build_report* out);
 
 /* Per-kernel CUDA-event timing (off by default).  When on, every kernel the
  * context launches is bracketed by an event pair on its stream;
@@ -401,6 +426,12 @@ typedef struct cpvs_server_stats {
     double lookup_p50_ms, lookup_p99_ms;
 } cpvs_server_stats;
 
+/* The server takes over `ctx`.  Its builds keep the default launch shapes
+ * or those fixed by the context's options (the build tuner does not run
+ * inside the serving loop).  Admission by bytes: before a batch of builds,
+ * least-recently-used unpinned DAGs are evicted until the batch fits the
+ * budget, each new DAG estimated at the largest DAG the server has built
+ * from a map of its side (n^2/4 bytes before the first). */
 CPVS_API cpvs_status cpvs_server_create(cpvs_ctx* ctx, const cpvs_server_config* cfg, cpvs_server** out);
 /* Cancels queued requests, finishes running ones, frees the resident DAGs. */
 CPVS_API void cpvs_server_destroy(cpvs_server* s);

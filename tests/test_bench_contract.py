@@ -22,6 +22,11 @@ def test_reference_arm_prints_one_contract_line():
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert d["e2e"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    # the driver's steps and warm-up, and the GPU arm's config dict (bench.config_dict)
+    assert d["steps"] == 1 and d["warmup"] == 1
+    assert set(d["config"]) == {"workload", "map_side", "voxels_per_dag", "dag_words", "lookups_per_batch", "l2",
+                                "parallelism"}
+    assert d["config"]["map_side"] == 1024 and d["config"]["lookups_per_batch"] == 1 << 20
 
 
 def test_reference_arm_under_torchrun_prints_once():

@@ -417,3 +417,46 @@ def test_plan_grows_for_a_busier_map(cp, oracle):
         want = oracle.build(d)
         assert np.array_equal(sh.get_dag(), want.dag)
         assert sh.level_counts() == (want.tree_nodes, want.unique_nodes)
+
+
+def test_every_build_shape_gives_the_oracles_dag(cp, oracle):
+    """The build tuner times every (cluster cap, insert waves) pair on a
+    plan's first build; each pair, fixed through the context options, must
+    build the same DAG (the oracle's) on maps whose level sizes fall on both
+    sides of every cap, including the 8192^2 workload."""
+    import torch
+    rng = np.random.default_rng(21)
+    maps = [scene.rasterise(scene.config_scene("c0")), random_map(rng, 256, 0),
+            scene.rasterise(scene.make_scene(2048, 0.9, 80, 8, 9)), scene.rasterise(scene.config_scene("c1"))]
+    wants = [oracle.build(d, threads=4).dag for d in maps]
+    devs = [torch.from_numpy(d).cuda() for d in maps]
+    for cap in (2048, 4096, 8192, 16384):
+        for waves in (1, 2):
+            ctx = cp.Context(0)
+            ctx.set_option(ctx.OPT_BUILD_CLUSTER_CAP, cap)
+            ctx.set_option(ctx.OPT_BUILD_INSERT_WAVES, waves)
+            for d, want in zip(devs, wants):
+                sh = cp.CompressedShadow.from_depth(d, ctx=ctx)
+                assert np.array_equal(sh.get_dag(), want), (cap, waves, d.shape)
+                rep = ctx.last_build()
+                assert rep["error_word"] == 0 and rep["tuned"] == 0
+                assert rep["cluster_cap"] == cap and rep["insert_waves"] == waves
+
+
+def test_build_tuner_times_once_per_plan(cp, oracle):
+    """A fresh context's first build of a shape times the candidates and
+    keeps one; the next build of that shape reuses it; both DAGs equal the
+    oracle's."""
+    d = scene.rasterise(scene.config_scene("c0"))
+    want = oracle.build(d).dag
+    ctx = cp.Context(0)
+    sh = cp.CompressedShadow.from_depth(d, ctx=ctx)
+    first = ctx.last_build()
+    assert first["tuned"] == 1 and first["tuning_ms"] > 0 and first["error_word"] == 0
+    assert first["cluster_cap"] in (2048, 4096, 8192, 16384) and first["insert_waves"] in (1, 2)
+    assert np.array_equal(sh.get_dag(), want)
+    sh = cp.CompressedShadow.from_depth(d, ctx=ctx)
+    again = ctx.last_build()
+    assert again["tuned"] == 0
+    assert (again["cluster_cap"], again["insert_waves"]) == (first["cluster_cap"], first["insert_waves"])
+    assert np.array_equal(sh.get_dag(), want)
