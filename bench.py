@@ -205,6 +205,10 @@ def run_ours(args, rank, world, local_rank):
     bits_host = torch.empty((nq + 31) // 32, dtype=torch.int32).pin_memory()
 
     ctx = cp.Context(local_rank)
+    if args.fixed_shapes:
+        # profiling aid: the default launch shapes, no tuning replays
+        ctx.set_option(ctx.OPT_BUILD_CLUSTER_CAP, 8192)
+        ctx.set_option(ctx.OPT_BUILD_INSERT_WAVES, 1)
     stream = torch.cuda.current_stream(dev)
     keep = {}
 
@@ -220,6 +224,9 @@ def run_ours(args, rank, world, local_rank):
             torch.distributed.barrier()
         torch.cuda.synchronize(dev)
 
+    if args.part in ("grid", "multi", "serve", "raster"):
+        profile_part(args.part, cp, torch, ctx, dev, stream, args.warmup + args.steps)
+        return
     if args.part == "frame":
         # profiling aid: the 4K frame (evaluate + shade) alone
         fr = measure_frame(cp, torch, ctx, build_step(), q_dev, stream, args.steps, args.warmup, barrier)
@@ -366,10 +373,27 @@ def run_ours(args, rank, world, local_rank):
     dom_launches_per_step = build_kernels[dom][1] / args.steps
     dom_bytes = kernel_alg_bytes(dom, n, tree, uniq, dag_words) / dom_launches_per_step
     achieved = dom_bytes / (dom_ms_launch * 1e-3) / 1e9
-    traffic = None
+    # DRAM bytes per launch from the committed ncu launch list of this
+    # workload (profiles/traffic_<config>.json), when it has one
     prof = os.path.join(ROOT, "profiles", f"traffic_{args.config}.json")
-    if os.path.exists(prof):
-        traffic = json.load(open(prof)).get(dom)
+    measured = json.load(open(prof)) if os.path.exists(prof) else {}
+
+    def traffic_of(k):
+        t = measured.get(k)
+        return int(t["dram_bytes_per_build"] / max(t["launches_per_build"], 1)) if isinstance(t, dict) else None
+    traffic = traffic_of(dom)
+    # every build kernel's roofline on its own algorithmic bytes
+    kernel_rooflines = {}
+    for k, (tot_ms, launches) in build_kernels.items():
+        per = launches / args.steps
+        alg = kernel_alg_bytes(k, n, tree, uniq, dag_words)
+        if not alg or not per:
+            continue
+        ms_l = tot_ms / launches
+        ach = alg / per / (ms_l * 1e-3) / 1e9
+        kernel_rooflines[k] = {"launches_per_step": round(per, 2), "ms_per_launch": round(ms_l, 4),
+                               "alg_bytes_per_launch": int(alg / per), "achieved_gbs": round(ach, 1),
+                               "frac": round(ach / peak, 4), "traffic_per_launch": traffic_of(k)}
     # the map once, the stored pyramid levels (3 and up for a leafmask build) once, the DAG once
     build_alg = 4.0 * n * n + 8.0 * sum((n >> L) ** 2 for L in range(3, int(np.log2(n)) + 1)) + 4.0 * dag_words
     lookup_alg = nq * 12.125 + 4.0 * dag_words
@@ -413,6 +437,7 @@ def run_ours(args, rank, world, local_rank):
                                     "path": "cpvs_shadow_create_from_depth, then the first cpvs_shadow_lookup_ndc "
                                             "on the new shadow (builds its top grid), median of 3"},
         "build_report": report,
+        "kernel_rooflines": kernel_rooflines,
         "kernels_ms_per_step": {k: round(v[0] / args.steps, 4) for k, v in build_kernels.items()},
         "kernel_timing": "CUDA events around every library launch, in a pass of the same steps right after the "
                          "timed region (the timed region itself replays the captured build graph)",
@@ -452,6 +477,59 @@ def run_ours(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def profile_part(part, cp, torch, ctx, dev, stream, reps):
+    """Profiling aids for the kernels outside the c1 build and lookup, on
+    small cases (inputs above L2, a few GB on the device at most):
+    grid   -- a 4x4 grid of 2048^2 xy tiles of the c2 scene, 4 z-tiles each
+              (64 DAGs, one batched build), 2^24 NDC lookups routed through it
+              (k_grid_top_index, k_grid_lookup);
+    multi  -- 16 of the c3 lights in one batch, 2^24 points spread over them
+              (k_top_index per DAG, k_multi_lookup);
+    serve  -- 64 lookup requests of 2^18 points through a server holding 4
+              DAGs, in one segmented launch each round (k_segment_lookup);
+    raster -- the c1 scene rasterised to an 8192^2 depth map (k_raster)."""
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(11)
+    if part == "raster":
+        sc = scene.config_scene("c1")
+        for _ in range(reps):
+            cp.raster_depth(sc, ctx=ctx)
+    elif part == "grid":
+        sc = scene.config_scene("c2", n=8192)
+        T, L = 2048, 4
+        maps = [cp.raster_depth(sc, x * T, y * T, T, T, ctx=ctx) for y in range(L) for x in range(L)]
+        hs = [cp.MinMaxHierarchy(m, ctx=ctx, stream=stream, borrow=True) for m in maps]
+        grid = cp.CompressedShadowContainer(L, ctx=ctx)
+        grid.build(hs, stream=stream)
+        q = (torch.rand((1 << 24, 3), generator=gen, device=dev) * 2 - 1).contiguous()
+        out = torch.empty((1 << 24) // 32, dtype=torch.int32, device=dev)
+        for _ in range(reps):
+            grid.lookup_ndc(q, out, stream=stream)
+    elif part == "multi":
+        scs = c3_scenes()[:16]
+        maps = [cp.raster_depth(s, ctx=ctx) for s in scs]
+        hs = [cp.MinMaxHierarchy(m, ctx=ctx, stream=stream, borrow=True) for m in maps]
+        shs = cp.CompressedShadow.create_batch(hs, [(i, 0, 1) for i in range(len(hs))], stream=stream)
+        ids = torch.randint(0, len(shs), (1 << 24,), generator=gen, device=dev, dtype=torch.int32)
+        q = (torch.rand((1 << 24, 3), generator=gen, device=dev) * 2 - 1).contiguous()
+        out = torch.empty((1 << 24) // 32, dtype=torch.int32, device=dev)
+        for _ in range(reps):
+            cp.lookup_ndc_multi(shs, ids, q, out, stream=stream)
+    elif part == "serve":
+        srv = cp.Server(cp.Context(dev.index or 0), budget_bytes=1 << 30)
+        for key in range(4):
+            d = scene.rasterise(scene.make_scene(2048, 0.9, 40, 0, 500 + key))
+            srv.wait(srv.submit_build(key, torch.from_numpy(d).pin_memory()))
+        pts = torch.from_numpy((np.random.default_rng(3).random((1 << 18, 3)) * 2 - 1).astype(np.float32)).pin_memory()
+        for _ in range(reps):
+            tickets = [srv.submit_lookup(k % 4, pts) for k in range(64)]
+            for t in tickets:
+                srv.wait(t, packed=True)
+        srv.close()
+    torch.cuda.synchronize(dev)
+    print(json.dumps({"part": part, "reps": reps}), flush=True)
 
 
 def measure_frame(cp, torch, ctx, sh, q_dev, stream, steps, warmup, barrier, width=3840, height=2160):
@@ -955,8 +1033,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="c1 line without the batched (c3), grid (c2) and served (c4) measurements")
-    ap.add_argument("--part", choices=("all", "build", "lookup", "frame"), default="all",
-                    help="profiling aid: run only the build steps or only the lookup batches (no JSON line)")
+    ap.add_argument("--part", choices=("all", "build", "lookup", "frame", "grid", "multi", "serve", "raster"),
+                    default="all",
+                    help="profiling aid: run one part alone (no contract line); see profile_part")
+    ap.add_argument("--fixed-shapes", action="store_true",
+                    help="profiling aid: default build launch shapes, no tuning replays")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         ap.error("--warmup must be at least 3")

@@ -3120,6 +3120,7 @@ void destroy_plans(Ctx& ctx) {
 
 cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const std::vector<JobSpec>& jobs,
                        bool leafmasks, cudaStream_t st, BuildOutput& out) {
+    NvtxRange range("cpvs build");
     const uint32_t njobs = (uint32_t)jobs.size();
     if (njobs == 0) return fail(CPVS_ERR_INVALID_ARG, "build_dags: no jobs");
     std::vector<uint32_t> job_n(njobs);
@@ -3138,6 +3139,7 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
     for (BuildPlan* q : ctx.plans->plans)
         if (same_shape(q, leafmasks, pow2, job_n)) P = q;
     if (!P) {
+        NvtxRange plan_range("cpvs build: new plan");
         std::vector<unsigned long long> bounds;
         cpvs_status r = prepass_bounds(ctx, sources, jobs, (leafmasks ? 2 : 0) + 1, st, bounds);
         if (r != CPVS_OK) return r;
@@ -3251,6 +3253,7 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
             CPVS_CUDA(cudaMemcpyAsync(P->stage_dev, P->hin, SL.bytes, cudaMemcpyHostToDevice, st));
             P->staged.assign(P->hin, P->hin + SL.bytes);
         }
+        NvtxRange pass_range("cpvs build: levels");
         if (ctx.timing.on) {
             cpvs_status r = plan_enqueue(P, st, nullptr, &ctx.timing);
             if (r != CPVS_OK) return r;
@@ -3318,6 +3321,7 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         CPVS_CUDA(cudaMemsetAsync(out.dag + total, 0, kDagPad * 4, st));
     }
     {
+        NvtxRange emit_range("cpvs build: emission");
         KernelTimer kt(&ctx.timing, K_EMIT, st);
         const uint32_t U = el.ustart[P->maxR + 1];
         if (U)
@@ -3352,6 +3356,7 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
     float tuning_ms = 0.f;
     bool tuned = false;
     if (!P->shapes_set && !ctx.timing.on && ctx.tune_builds) {
+        NvtxRange tune_range("cpvs build: tuning");
         cpvs_status r = plan_tune(ctx, P, st, tuning_ms);
         if (r != CPVS_OK) return r;
         P->shapes_set = tuned = true;

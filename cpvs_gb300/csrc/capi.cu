@@ -711,6 +711,7 @@ cpvs_status cpvs_shadow_level_counts(const cpvs_shadow* s, uint64_t* tree, uint6
 cpvs_status cpvs_shadow_lookup_ndc(const cpvs_shadow* s, const float* xyz, uint64_t n, uint32_t* bits_out,
                                    uint32_t flags, void* stream) {
     if (!s) return fail(CPVS_ERR_INVALID_ARG, "lookup_ndc: null shadow");
+    cpvs::NvtxRange range("cpvs lookup");
     cudaStream_t st = (cudaStream_t)stream;
     return lookup_common(s->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
         ensure_top(s, st);
@@ -725,6 +726,7 @@ cpvs_status cpvs_shadow_lookup_ndc(const cpvs_shadow* s, const float* xyz, uint6
 cpvs_status cpvs_shadow_lookup_voxel(const cpvs_shadow* s, const int32_t* xyz, uint64_t n, uint32_t* bits_out,
                                      uint32_t flags, void* stream) {
     if (!s) return fail(CPVS_ERR_INVALID_ARG, "lookup_voxel: null shadow");
+    cpvs::NvtxRange range("cpvs lookup");
     cudaStream_t st = (cudaStream_t)stream;
     return lookup_common(s->ctx, xyz, n, bits_out, flags, st, [&](const void* q, uint32_t* bits) {
         ensure_top(s, st);

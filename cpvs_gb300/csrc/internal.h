@@ -7,6 +7,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/cpvs.h"
 
 #define CPVS_MAX_LEVELS 18
@@ -222,6 +224,15 @@ struct Timing {
     void collect();  // waits for pending events and accumulates
     void reset();
     ~Timing();
+};
+
+// An NVTX range over its scope (host phases of builds, lookups and the
+// server's batches, for a timeline profiler; a no-op without one).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
 // Records an event pair around the launches in its scope.

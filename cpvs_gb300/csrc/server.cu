@@ -194,6 +194,7 @@ struct cpvs_server {
 
     // One segmented launch for every runnable lookup (up to max_batch_lookups).
     void launch_lookups() {
+        cpvs::NvtxRange range("cpvs server: lookup launch");
         if (lookups_pending.empty()) return;
         if (inflight.size() >= kRingSlots) retire_finished(true);  // frees the oldest slot
         std::vector<Req> run, keep;
@@ -357,6 +358,7 @@ struct cpvs_server {
     }
 
     void build_batch(std::vector<Req>& batch) {
+        cpvs::NvtxRange range("cpvs server: build batch");
         // admission: room for the new DAGs, each estimated at the largest
         // DAG built so far from a map of its side (n^2/4 bytes before any)
         if (cfg.budget_bytes) {
