@@ -71,6 +71,7 @@ struct JobDev {
     uint32_t n, num_levels, z_idx, z_num;
     uint32_t group;      // leaf column group of its source (build plans with leafmasks)
     uint32_t pad;
+    uint64_t col_base;   // that group's first column record
 };
 
 // Per-level node arrays (capacity `cap`).
@@ -620,7 +621,7 @@ struct LeafColumns {
     const LeafGroupDev* groups;
     const uint2* ztiles;        // (z_idx, job) per job, by group, ordered by z_idx
     const uint32_t* meta;       // [0] groups, [1] column records in use
-    uint2* colrec;              // per column: first run entry, run count
+    uint4* colrec;              // per column q: [2q] (first run entry, run count), [2q+1] a copy of its first run
     uint4* runs;                // per run: last z-cell, class id, class mask, job
     uint32_t run_cap;
     unsigned int* run_ctr;      // run entries reserved (zeroed per build)
@@ -630,7 +631,8 @@ struct LeafColumns {
     unsigned long long* table;  // class hash table: tag << 32 | class id
     uint64_t table_mask;
     uint32_t njobs;             // uniform classes: id run_cap + 9 * job + k (all counts k)
-    uint32_t* pending;          // run entries of non-uniform leaves, for k_leaf_classes
+    uint2* pending;             // non-uniform runs for k_leaf_classes: (run entry, index of the
+                                // column record's copy of it, or 0)
     unsigned int* pending_ctr;  // their count (zeroed per build)
     uint4* heavy;               // columns whose walk needs their texels: (column, job index, z-cell, entry)
     unsigned int* heavy_ctr;    // their count (zeroed per build)
@@ -729,7 +731,8 @@ __device__ __forceinline__ uint32_t leaf_class_insert(const LeafColumns& lc, uin
 __global__ void __launch_bounds__(kThreads) k_leaf_classes(LeafColumns lc, uint32_t* err) {
     const uint32_t np = *lc.pending_ctr;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
-        const uint32_t cid = lc.pending[p];
+        const uint2 pe = lc.pending[p];
+        const uint32_t cid = pe.x;
         if (cid >= lc.run_cap) {
             atomicOr(err, 512u);
             continue;
@@ -743,7 +746,9 @@ __global__ void __launch_bounds__(kThreads) k_leaf_classes(LeafColumns lc, uint3
             M[2 * q + 1] = t.y;
         }
         const uint32_t j = lc.cls_job[cid];
-        lc.runs[cid].y = leaf_class_insert(lc, leaf_hash(j, M), j, M, cid, err);
+        const uint32_t id = leaf_class_insert(lc, leaf_hash(j, M), j, M, cid, err);
+        lc.runs[cid].y = id;
+        if (pe.y) lc.colrec[pe.y].y = id;  // the column record's copy of its first run
     }
 }
 
@@ -808,10 +813,12 @@ __device__ __forceinline__ uint32_t column_cells(const LeafColumns& lc, const Co
 // LIGHT: a run that needs the texels is not taken (returns false); else the
 // texels are read, and a non-uniform run stores its masks, job and an empty
 // record at its own entry and joins the pending list of k_leaf_classes.
+// `first` (non-null for a column's first run): where the column record keeps
+// a copy of the entry.
 template <bool POW2, bool LIGHT>
 __device__ __forceinline__ bool column_run(const LeafColumns& lc, const ColumnAt& c, const float* row0, uint32_t nmap,
                                            float H0, bool minmax, uint32_t zc, uint32_t e, uint32_t job, uint32_t cid,
-                                           uint32_t& last) {
+                                           uint32_t& last, uint4* first) {
     uint32_t k0 = 0;
     bool uni = false;
     if (minmax) {
@@ -856,10 +863,14 @@ __device__ __forceinline__ bool column_run(const LeafColumns& lc, const ColumnAt
             uint32_t at = 0;
             if ((int)lane == lead) at = atomicAdd(lc.pending_ctr, (unsigned)__popc(want));
             at = __shfl_sync(act, at, lead);
-            if (!uni) lc.pending[at + __popc(want & ((1u << lane) - 1u))] = id;
+            if (!uni)
+                lc.pending[at + __popc(want & ((1u << lane) - 1u))] =
+                    make_uint2(id, first ? (uint32_t)(first - lc.colrec) : 0u);
         }
     }
-    lc.runs[cid] = make_uint4(last, id, mask, job);
+    const uint4 entry = make_uint4(last, id, mask, job);
+    lc.runs[cid] = entry;
+    if (first) *first = entry;
     return true;
 }
 
@@ -867,8 +878,8 @@ __device__ __forceinline__ bool column_run(const LeafColumns& lc, const ColumnAt
 // entries from off + nrun; LIGHT stops at the first run that needs the
 // texels and returns false with (k, zc) at that run.
 template <bool POW2, bool LIGHT>
-__device__ __forceinline__ bool column_walk(const LeafColumns& lc, const ColumnAt& c, uint32_t off, uint32_t& nrun,
-                                            uint32_t& k, uint32_t& zc) {
+__device__ __forceinline__ bool column_walk(const LeafColumns& lc, const ColumnAt& c, uint64_t q, uint32_t off,
+                                            uint32_t& nrun, uint32_t& k, uint32_t& zc) {
     const LeafGroupDev& G = lc.groups[c.g];
     const uint32_t jl = __ldg(&G.job_lo), jc = __ldg(&G.job_cnt), nmap = __ldg(&G.n);
     const float* row0 = G.depth + (size_t)(c.cy * 8u) * nmap + c.cx * 8u;
@@ -882,7 +893,9 @@ __device__ __forceinline__ bool column_walk(const LeafColumns& lc, const ColumnA
         zc = max(zc, max(c.zlo, z0));
         while (zc <= e) {
             uint32_t last;
-            if (!column_run<POW2, LIGHT>(lc, c, row0, nmap, H0, minmax, zc, e, zt.y, off + nrun, last)) return false;
+            if (!column_run<POW2, LIGHT>(lc, c, row0, nmap, H0, minmax, zc, e, zt.y, off + nrun, last,
+                                         nrun ? nullptr : lc.colrec + 2 * q + 1))
+                return false;
             ++nrun;
             zc = last + 1u;
         }
@@ -945,8 +958,8 @@ __global__ void __launch_bounds__(kThreads) k_leaf_columns(LeafColumns lc, uint3
             if (q < ncols) {
                 const ColumnAt c = column_at(lc, ngroups, q);
                 cells = column_cells(lc, c);
-                if (cells && fits) queue = !column_walk<POW2, true>(lc, c, off, nrun, k, zc);
-                lc.colrec[q] = make_uint2(off, nrun);
+                if (cells && fits) queue = !column_walk<POW2, true>(lc, c, q, off, nrun, k, zc);
+                lc.colrec[2 * q] = make_uint4(off, nrun, 0u, 0u);
             }
             // queue the columns that need their texels, one atomic per warp
             const unsigned want = __ballot_sync(0xffffffffu, queue);
@@ -972,10 +985,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_leaf_columns_heavy(LeafColumns 
     for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += gridDim.x * blockDim.x) {
         const uint4 w = lc.heavy[h];
         const ColumnAt c = column_at(lc, ngroups, w.x);
-        const uint32_t off = lc.colrec[w.x].x;
+        const uint32_t off = lc.colrec[2 * (uint64_t)w.x].x;
         uint32_t nrun = w.w - off, k = w.y, zc = w.z;
-        column_walk<POW2, false>(lc, c, off, nrun, k, zc);
-        lc.colrec[w.x].y = nrun;
+        column_walk<POW2, false>(lc, c, w.x, off, nrun, k, zc);
+        lc.colrec[2 * (uint64_t)w.x].y = nrun;
     }
 }
 
@@ -983,31 +996,42 @@ __global__ void __launch_bounds__(kThreads, 2) k_leaf_columns_heavy(LeafColumns 
 // class id (its merged identity for level 3) and class mask; then the
 // class's first-occurrence index is lowered to the leaf's if smaller.
 // Leaves of one class in one warp: only the first (lowest index) updates.
+// The column record's two halves (run count, first run) arrive together, so
+// a leaf whose z-cell the first run covers (most) costs one round trip.
 __device__ __forceinline__ uint32_t leaf_class_of(const LeafColumns& lc, const JobDev* __restrict__ jobs,
                                                   uint32_t njobs, uint64_t c, uint32_t j, uint32_t& mask, bool& ok) {
     ok = false;
     mask = 0;
     if (j >= njobs) return 0;
-    const LeafGroupDev& G = lc.groups[__ldg(&jobs[j].group)];
-    const uint32_t C = __ldg(&G.n) >> 3;
+    const uint32_t C = __ldg(&jobs[j].n) >> 3;
     const uint32_t cx = unpack_x(c) >> 1, cy = unpack_y(c) >> 1, zc = unpack_z(c) >> 1;
     if (cx >= C || cy >= C) return 0;
-    const uint2 rec = lc.colrec[__ldg(&G.col_base) + (uint64_t)cy * C + cx];
-    for (uint32_t k = 0; k < rec.y; ++k) {
-        const uint4 e = lc.runs[rec.x + k];
-        if (zc <= e.x) {
-            ok = e.w == j && e.y < lc.run_cap + 9u * lc.njobs;
-            mask = e.z;
-            return e.y;
-        }
-    }
-    return 0;
+    const uint4* rp = lc.colrec + 2 * (__ldg(&jobs[j].col_base) + (uint64_t)cy * C + cx);
+    const uint4 h = rp[0], e0 = rp[1];
+    if (h.y == 0) return 0;
+    uint4 e = e0;
+    for (uint32_t k = 1; zc > e.x && k < h.y; ++k) e = lc.runs[h.x + k];
+    if (zc > e.x) return 0;
+    ok = e.w == j && e.y < lc.run_cap + 9u * lc.njobs;
+    mask = e.z;
+    return e.y;
 }
+
+// The uniform classes (9 per job, the most frequent) keep their smallest
+// leaf index per block in shared memory and lower the class record once per
+// block; other classes lower it per warp (the warp's lowest lane of each).
+constexpr uint32_t kResUniform = 9 * 64;
 
 __global__ void __launch_bounds__(kThreads)
     k_leaf_resolve(LevelDev lv, const uint32_t* __restrict__ counts, const JobDev* __restrict__ jobs, uint32_t njobs,
                    SegDev seg, LeafColumns lc, uint32_t* err) {
     chain_enter();
+    __shared__ uint32_t s_umin[kResUniform];
+    const uint32_t nu = 9u * lc.njobs;
+    const bool block_uniform = nu <= kResUniform;
+    if (block_uniform)
+        for (uint32_t t = threadIdx.x; t < nu; t += blockDim.x) s_umin[t] = ~0u;
+    __syncthreads();
     const uint32_t n = counts[2];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         uint32_t j = lv.job[i], mask = 0;
@@ -1023,12 +1047,24 @@ __global__ void __launch_bounds__(kThreads)
         lv.slot[i] = id;
         lv.mask[i] = mask;
         leaf_segments(lv, seg, i, n, j, 2, njobs, err);
-        const unsigned same = __match_any_sync(__activemask(), id);
-        if ((threadIdx.x & 31u) == (uint32_t)(__ffs((int)same) - 1)) {
-            const uint32_t r = __ldcg(reinterpret_cast<const uint32_t*>(lc.crec + id));
-            if (r > i) atomicMin(lc.crec + id, 0xFFFFFFFF00000000ull | i);
+        if (block_uniform && id >= lc.run_cap) {
+            atomicMin(&s_umin[id - lc.run_cap], i);
+        } else {
+            const unsigned same = __match_any_sync(__activemask(), id);
+            if ((threadIdx.x & 31u) == (uint32_t)(__ffs((int)same) - 1)) {
+                const uint32_t r = __ldcg(reinterpret_cast<const uint32_t*>(lc.crec + id));
+                if (r > i) atomicMin(lc.crec + id, 0xFFFFFFFF00000000ull | i);
+            }
         }
     }
+    __syncthreads();
+    if (block_uniform)
+        for (uint32_t t = threadIdx.x; t < nu; t += blockDim.x) {
+            const uint32_t v = s_umin[t];
+            if (v == ~0u) continue;
+            unsigned long long* rec = lc.crec + lc.run_cap + t;
+            if (__ldcg(reinterpret_cast<const uint32_t*>(rec)) > v) atomicMin(rec, 0xFFFFFFFF00000000ull | v);
+        }
 }
 
 // --------------------------------------------------------------- bottom-up
@@ -2477,9 +2513,9 @@ struct BuildPlan {
     uint2* ztiles_dev = nullptr;
     uint32_t* lmeta = nullptr;  // [0] groups, [1] columns, [2] run entries reserved, [3] pending runs,
                                 // [4] queued columns
-    uint32_t* pending = nullptr;  // non-uniform run entries (cap[2])
+    uint2* pending = nullptr;  // non-uniform runs (cap[2])
     uint4* runs = nullptr;
-    uint2* colrec = nullptr;  // per column (colrec_cap), followed by the queue of columns
+    uint4* colrec = nullptr;  // two per column (colrec_cap), followed by the queue of columns
     uint4* heavy = nullptr;   // that need their texels (colrec_cap)
     uint64_t colrec_cap = 0;
     unsigned long long* ltable = nullptr;
@@ -2521,7 +2557,7 @@ void plan_release(Ctx& ctx, BuildPlan* P) {
     for (cudaEvent_t* e : {&P->join, &P->start, &P->tables})
         if (*e) cudaEventDestroy(*e), *e = nullptr;
     if (P->arena) ctx.release(P->arena, P->arena_bytes, true, nullptr);
-    if (P->colrec) ctx.release(P->colrec, P->colrec_cap * (sizeof(uint2) + sizeof(uint4)), true, nullptr);
+    if (P->colrec) ctx.release(P->colrec, P->colrec_cap * 3 * sizeof(uint4), true, nullptr);
     P->colrec = nullptr;
     P->heavy = nullptr;
     P->colrec_cap = 0;
@@ -2582,7 +2618,7 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
             add(cls, 8);      // class records
             add(cls, 4);      // class jobs
             add(c, 16);       // run entries
-            add(c, 4);        // pending run list
+            add(c, 8);        // pending run list
         }
     }
     add(CPVS_MAX_LEVELS, sizeof(LevelDev));
@@ -2635,7 +2671,7 @@ cpvs_status plan_allocate(Ctx& ctx, BuildPlan* P, cudaStream_t st) {
             l.hash = A.take<uint64_t>(cls);
             l.uid = A.take<uint32_t>(cls);
             P->runs = A.take<uint4>(c);
-            P->pending = A.take<uint32_t>(c);
+            P->pending = A.take<uint2>(c);
         }
     }
     P->lvt = A.take<LevelDev>(CPVS_MAX_LEVELS);
@@ -3172,6 +3208,7 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
     // distinct z-tiles (a repeated z-tile starts another group)
     std::vector<uint32_t> job_group(njobs, 0);
     std::vector<uint32_t> grp_source, grp_znum;
+    std::vector<uint64_t> grp_colbase;
     std::vector<std::vector<uint2>> grp_tiles;  // (z_idx, job)
     uint64_t ncols = 0;
     if (leafmasks) {
@@ -3187,6 +3224,7 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
                 grp_source.push_back(jobs[j].source);
                 grp_znum.push_back(jobs[j].z_num);
                 grp_tiles.emplace_back();
+                grp_colbase.push_back(ncols);
                 const uint64_t c = sources[jobs[j].source].n / 8;
                 ncols += c * c;
             }
@@ -3194,7 +3232,7 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
             job_group[j] = g;
         }
         for (auto& t : grp_tiles) std::sort(t.begin(), t.end(), [](uint2 a, uint2 b) { return a.x < b.x; });
-        if (ncols >= (1ull << 32)) return fail(CPVS_ERR_BUDGET, "build_dags: more than 2^32 leaf columns");
+        if (ncols >= (1ull << 31)) return fail(CPVS_ERR_BUDGET, "build_dags: more than 2^31 leaf columns");
     }
     ResultView hv{};
     for (int attempt = 0;; ++attempt) {
@@ -3203,14 +3241,14 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         if (leafmasks && ncols > P->colrec_cap) {
             if (P->colrec) {
                 CPVS_CUDA(cudaStreamSynchronize(st));
-                ctx.release(P->colrec, P->colrec_cap * (sizeof(uint2) + sizeof(uint4)), true, nullptr);
+                ctx.release(P->colrec, P->colrec_cap * 3 * sizeof(uint4), true, nullptr);
                 P->colrec = nullptr;
                 P->heavy = nullptr;
                 P->colrec_cap = 0;
             }
-            cpvs_status r = ctx.alloc((void**)&P->colrec, ncols * (sizeof(uint2) + sizeof(uint4)), true, st);
+            cpvs_status r = ctx.alloc((void**)&P->colrec, ncols * 3 * sizeof(uint4), true, st);
             if (r != CPVS_OK) return r;
-            P->heavy = reinterpret_cast<uint4*>(P->colrec + ((ncols + 1) & ~1ull));
+            P->heavy = P->colrec + 2 * ncols;
             P->colrec_cap = ncols;
             if (P->exec) {
                 cudaGraphExecDestroy(P->exec);
@@ -3227,7 +3265,8 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         std::vector<uint64_t> fill(CPVS_MAX_LEVELS, 0);
         for (uint32_t j = 0; j < njobs; ++j) {
             const SourceSpec& S = sources[jobs[j].source];
-            hj[j] = JobDev{S.levels, S.depth, S.n, P->root_level[j] + 2, jobs[j].z_idx, jobs[j].z_num, job_group[j], 0};
+            hj[j] = JobDev{S.levels,         S.depth,       S.n, P->root_level[j] + 2, jobs[j].z_idx, jobs[j].z_num,
+                           job_group[j],     0,             leafmasks ? grp_colbase[job_group[j]] : 0ull};
             const int R = (int)P->root_level[j];
             hi[P->inj_off[R] + fill[R]++] = Injected{pack_xyz(0, 0, 2 * jobs[j].z_idx), j, 0};
         }
