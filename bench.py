@@ -122,7 +122,13 @@ class ClockSampler:
 # once and every output written once; reads that the kernel repeats from
 # cache (a depth texel shared by the leaves above it, a hot hash slot) count
 # once.  These divide the kernel's CUDA-event time for `roofline.achieved`.
-def kernel_alg_bytes(name: str, n: int, tree: list, uniq: list, dag_words: int) -> float:
+def kernel_alg_bytes(name: str, n: int, tree: list, uniq: list, dag_words: int, fused_leaves: bool = False) -> float:
+    """Algorithmic bytes of one build's launches of kernel `name`.  With
+    `fused_leaves` (no k_leaf_resolve launch: the expansion of level 3 looks
+    each leaf's class up as it writes the leaf) the expansion also reads
+    every column's 32-byte record once and writes job, class id and class
+    mask per leaf (12 B, as many as the coordinate and job it no longer
+    writes)."""
     leaves = tree[2] if len(tree) > 2 else 0
     # a build with leafmasks stores pyramid levels 3 and up (levels 1-2 stay on chip)
     first = 3 if leaves else 1
@@ -140,7 +146,7 @@ def kernel_alg_bytes(name: str, n: int, tree: list, uniq: list, dag_words: int) 
         return leaves * (8 + 4 + 4 + 4) + cols * 8
     if name == "k_expand":         # per inner node coord + job + 2x2 pyramid texels in, mask + first out;
         # 12 B per child written
-        return inner * (8 + 4 + 32 + 8) + (leaves + inner) * 12
+        return inner * (8 + 4 + 32 + 8) + (leaves + inner) * 12 + (cols * 32 if fused_leaves else 0)
     if name == "k_dedup_insert":   # per inner node mask + job + first + slot probe + slot out; 4 B per child id
         return inner * (4 + 4 + 4 + 8 + 4) + (leaves + inner) * 4
     if name == "k_merge_scan":     # per node slot + mask + job + table entry in; rank, offset out
@@ -371,7 +377,8 @@ def run_ours(args, rank, world, local_rank):
     dom = max(build_kernels, key=lambda k: build_kernels[k][0])
     dom_ms_launch = build_kernels[dom][0] / build_kernels[dom][1]
     dom_launches_per_step = build_kernels[dom][1] / args.steps
-    dom_bytes = kernel_alg_bytes(dom, n, tree, uniq, dag_words) / dom_launches_per_step
+    fused_leaves = "k_leaf_resolve" not in build_kernels
+    dom_bytes = kernel_alg_bytes(dom, n, tree, uniq, dag_words, fused_leaves) / dom_launches_per_step
     achieved = dom_bytes / (dom_ms_launch * 1e-3) / 1e9
     # DRAM bytes per launch from the committed ncu launch list of this
     # workload (profiles/traffic_<config>.json), when it has one
@@ -386,7 +393,7 @@ def run_ours(args, rank, world, local_rank):
     kernel_rooflines = {}
     for k, (tot_ms, launches) in build_kernels.items():
         per = launches / args.steps
-        alg = kernel_alg_bytes(k, n, tree, uniq, dag_words)
+        alg = kernel_alg_bytes(k, n, tree, uniq, dag_words, fused_leaves)
         if not alg or not per:
             continue
         ms_l = tot_ms / launches

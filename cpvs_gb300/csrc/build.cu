@@ -21,18 +21,31 @@
 //      slice's leafmask).
 //
 // Pipeline per build (all DAGs of a batch at once; each node carries its
-// job id and never merges across jobs):
-//   top-down, per level L:  expand_count + expand_write  (classify, scan,
-//                           write children)            -- breadth-first order
-//   leaf level:             leaf_masks (one warp per leaf, 16 ballots)
-//   bottom-up, per level L: dedup_insert (open-addressing hash, 64-bit keys
-//                           = 32-bit tag | node index, atomicMin keeps the
-//                           first occurrence, full-signature compare on tag
-//                           match), dedup_resolve, dedup_scan (ranks and word
-//                           offsets in one pair scan), dedup_remap
-//   layout:                 per-job level bases, then emit per level.
-// Scans are reduce-then-scan over contiguous per-CTA chunks: no CTA waits on
-// another, so nothing can hang.
+// job id and never merges across jobs), captured once per plan as a CUDA
+// graph of chained (programmatic dependent) launches:
+//   k_clear                 per-build counters, look-back flags and tickets
+//   top-down expansion:     k_expand_cluster for the levels of at most the
+//                           plan's cluster cap of nodes (one thread-block
+//                           cluster), then k_expand_lb per level (classify,
+//                           block scan + decoupled look-back, write
+//                           children)                  -- breadth-first order
+//   leaf level (beside the expansion, from the map and pyramid level 3):
+//                           k_leaf_columns + k_leaf_columns_heavy (runs of
+//                           equal leaves per texel column), k_leaf_classes
+//                           (hash insert of the non-uniform runs' classes);
+//                           then k_leaf_resolve (each listed leaf's class)
+//   bottom-up merge:        k_dedup_insert per inner level (open-addressing
+//                           hash; a class's slot is its merged identity,
+//                           atomicMin keeps its first occurrence), with
+//                           k_merge_scan_lb per level on a forked stream
+//                           (ranks and word offsets of the kept nodes), and
+//                           k_merge_cluster for the cluster levels
+//   layout:                 k_layout (per-job level bases, root masks)
+// then one host synchronisation (the DAG's size) and k_emit_all.  Every
+// look-back wait is bounded in time and reports an error bit instead of
+// hanging.  The allocation-free build at the end of this file uses separate
+// multi-pass kernels (k_expand_count/k_expand_write, k_leaf_masks,
+// k_dedup_insert/resolve/scan/remap, k_emit) that need no plan.
 #include <algorithm>
 #include <cstring>
 #include <string>
@@ -598,7 +611,10 @@ __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long lon
 //
 // k_leaf_columns (one thread per column, beside the expansion) walks the
 // runs of every column of the batch's maps over the z-tiles of the jobs that
-// use it, computes each run's masks once from the map, and inserts the
+// use it: a run whose leaves are uniform (every texel's count equal) takes
+// a fixed class per (job, count) from the column's min/max alone; the other
+// runs' masks are computed once from the map (k_leaf_columns_heavy, for
+// the columns that reach one), and k_leaf_classes inserts each such run's
 // class (job, masks) into a hash table; a class's identity is the index of
 // the run entry that first claimed it.  k_leaf_resolve (after the expansion
 // has listed the leaves in breadth-first order) looks each leaf's run up
@@ -998,20 +1014,38 @@ __global__ void __launch_bounds__(kThreads, 2) k_leaf_columns_heavy(LeafColumns 
 // Leaves of one class in one warp: only the first (lowest index) updates.
 // The column record's two halves (run count, first run) arrive together, so
 // a leaf whose z-cell the first run covers (most) costs one round trip.
-__device__ __forceinline__ uint32_t leaf_class_of(const LeafColumns& lc, const JobDev* __restrict__ jobs,
-                                                  uint32_t njobs, uint64_t c, uint32_t j, uint32_t& mask, bool& ok) {
+struct LeafRec {  // a leaf's column record, fetched ahead of its use
+    uint4 h, e0;     // (first run entry, run count), the first run
+    uint32_t zc;     // the leaf's level-3 z-cell
+    bool in;         // the job and column exist
+};
+
+__device__ __forceinline__ LeafRec leaf_rec_fetch(const LeafColumns& lc, const JobDev* __restrict__ jobs,
+                                                  uint32_t njobs, uint64_t c, uint32_t j) {
+    LeafRec r;
+    r.in = false;
+    r.zc = 0;
+    r.h = r.e0 = make_uint4(0u, 0u, 0u, 0u);
+    if (j >= njobs) return r;
+    const uint32_t C = __ldg(&jobs[j].n) >> 3;
+    const uint32_t cx = unpack_x(c) >> 1, cy = unpack_y(c) >> 1;
+    if (cx >= C || cy >= C) return r;
+    const uint4* rp = lc.colrec + 2 * (__ldg(&jobs[j].col_base) + (uint64_t)cy * C + cx);
+    r.h = rp[0];
+    r.e0 = rp[1];
+    r.zc = unpack_z(c) >> 1;
+    r.in = true;
+    return r;
+}
+
+__device__ __forceinline__ uint32_t leaf_class_of(const LeafColumns& lc, const LeafRec& r, uint32_t j, uint32_t& mask,
+                                                  bool& ok) {
     ok = false;
     mask = 0;
-    if (j >= njobs) return 0;
-    const uint32_t C = __ldg(&jobs[j].n) >> 3;
-    const uint32_t cx = unpack_x(c) >> 1, cy = unpack_y(c) >> 1, zc = unpack_z(c) >> 1;
-    if (cx >= C || cy >= C) return 0;
-    const uint4* rp = lc.colrec + 2 * (__ldg(&jobs[j].col_base) + (uint64_t)cy * C + cx);
-    const uint4 h = rp[0], e0 = rp[1];
-    if (h.y == 0) return 0;
-    uint4 e = e0;
-    for (uint32_t k = 1; zc > e.x && k < h.y; ++k) e = lc.runs[h.x + k];
-    if (zc > e.x) return 0;
+    if (!r.in || r.h.y == 0) return 0;
+    uint4 e = r.e0;
+    for (uint32_t k = 1; r.zc > e.x && k < r.h.y; ++k) e = lc.runs[r.h.x + k];
+    if (r.zc > e.x) return 0;
     ok = e.w == j && e.y < lc.run_cap + 9u * lc.njobs;
     mask = e.z;
     return e.y;
@@ -1022,49 +1056,82 @@ __device__ __forceinline__ uint32_t leaf_class_of(const LeafColumns& lc, const J
 // block; other classes lower it per warp (the warp's lowest lane of each).
 constexpr uint32_t kResUniform = 9 * 64;
 
+struct LeafFirst {  // a block's running minima of the uniform classes
+    uint32_t* umin;  // shared, kResUniform entries
+    bool on;         // 9 * njobs <= kResUniform
+};
+
+__device__ __forceinline__ LeafFirst leaf_first_begin(uint32_t* umin, uint32_t njobs) {
+    LeafFirst f{umin, 9u * njobs <= kResUniform};
+    if (f.on)
+        for (uint32_t t = threadIdx.x; t < 9u * njobs; t += blockDim.x) umin[t] = ~0u;
+    return f;  // the caller synchronises the block before the first update
+}
+
+// Leaf i of class `id`: lowers the class's first occurrence.
+__device__ __forceinline__ void leaf_first_update(const LeafColumns& lc, const LeafFirst& f, uint32_t id, uint32_t i) {
+    if (f.on && id >= lc.run_cap) {
+        atomicMin(&f.umin[id - lc.run_cap], i);
+    } else {
+        const unsigned same = __match_any_sync(__activemask(), id);
+        if ((threadIdx.x & 31u) == (uint32_t)(__ffs((int)same) - 1)) {
+            const uint32_t r = __ldcg(reinterpret_cast<const uint32_t*>(lc.crec + id));
+            if (r > i) atomicMin(lc.crec + id, 0xFFFFFFFF00000000ull | i);
+        }
+    }
+}
+
+// After the block's last update (the caller synchronises the block first).
+__device__ __forceinline__ void leaf_first_flush(const LeafColumns& lc, const LeafFirst& f) {
+    if (!f.on) return;
+    for (uint32_t t = threadIdx.x; t < 9u * lc.njobs; t += blockDim.x) {
+        const uint32_t v = f.umin[t];
+        if (v == ~0u) continue;
+        unsigned long long* rec = lc.crec + lc.run_cap + t;
+        if (__ldcg(reinterpret_cast<const uint32_t*>(rec)) > v) atomicMin(rec, 0xFFFFFFFF00000000ull | v);
+    }
+}
+
+// Leaf i (job j, column record r) of the level: its class id into slot,
+// its class mask, its first occurrence; returns its job (0 when out of
+// range).
+__device__ __forceinline__ uint32_t leaf_resolve_one(const LevelDev& lv, uint32_t njobs, const LeafColumns& lc,
+                                                     const LeafFirst& f, uint32_t i, const LeafRec& r, uint32_t j,
+                                                     uint32_t* err) {
+    uint32_t mask = 0;
+    bool ok;
+    uint32_t id = leaf_class_of(lc, r, j, mask, ok);
+    if (!ok) {
+        atomicOr(err, 512u);  // a leaf outside its column's runs: reported, not followed
+        j = j < njobs ? j : 0u;
+        id = 0;
+        mask = 0;
+    }
+    lv.slot[i] = id;
+    lv.mask[i] = mask;
+    if (ok) leaf_first_update(lc, f, id, i);
+    return j;
+}
+
+// One thread per listed leaf (used where the expansion of level 3 runs in
+// the cluster kernel; else k_expand_lb<true> resolves the leaves as it
+// writes them).
 __global__ void __launch_bounds__(kThreads)
     k_leaf_resolve(LevelDev lv, const uint32_t* __restrict__ counts, const JobDev* __restrict__ jobs, uint32_t njobs,
                    SegDev seg, LeafColumns lc, uint32_t* err) {
     chain_enter();
     __shared__ uint32_t s_umin[kResUniform];
-    const uint32_t nu = 9u * lc.njobs;
-    const bool block_uniform = nu <= kResUniform;
-    if (block_uniform)
-        for (uint32_t t = threadIdx.x; t < nu; t += blockDim.x) s_umin[t] = ~0u;
+    const LeafFirst f = leaf_first_begin(s_umin, lc.njobs);
     __syncthreads();
     const uint32_t n = counts[2];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t j = lv.job[i], mask = 0;
-        bool ok;
-        uint32_t id = leaf_class_of(lc, jobs, njobs, lv.coord[i], j, mask, ok);
-        if (!ok) {
-            atomicOr(err, 512u);  // a leaf outside its column's runs: reported, not followed
-            j = j < njobs ? j : 0u;
-            lv.job[i] = j;
-            id = 0;
-            mask = 0;
-        }
-        lv.slot[i] = id;
-        lv.mask[i] = mask;
+        const uint32_t j0 = lv.job[i];
+        const uint32_t j = leaf_resolve_one(lv, njobs, lc, f, i, leaf_rec_fetch(lc, jobs, njobs, lv.coord[i], j0), j0, err);
+        if (j != j0) lv.job[i] = j;
         leaf_segments(lv, seg, i, n, j, 2, njobs, err);
-        if (block_uniform && id >= lc.run_cap) {
-            atomicMin(&s_umin[id - lc.run_cap], i);
-        } else {
-            const unsigned same = __match_any_sync(__activemask(), id);
-            if ((threadIdx.x & 31u) == (uint32_t)(__ffs((int)same) - 1)) {
-                const uint32_t r = __ldcg(reinterpret_cast<const uint32_t*>(lc.crec + id));
-                if (r > i) atomicMin(lc.crec + id, 0xFFFFFFFF00000000ull | i);
-            }
-        }
     }
     __syncthreads();
-    if (block_uniform)
-        for (uint32_t t = threadIdx.x; t < nu; t += blockDim.x) {
-            const uint32_t v = s_umin[t];
-            if (v == ~0u) continue;
-            unsigned long long* rec = lc.crec + lc.run_cap + t;
-            if (__ldcg(reinterpret_cast<const uint32_t*>(rec)) > v) atomicMin(rec, 0xFFFFFFFF00000000ull | v);
-        }
+    leaf_first_flush(lc, f);
 }
 
 // --------------------------------------------------------------- bottom-up
@@ -1344,16 +1411,25 @@ __device__ __forceinline__ uint32_t partial_set(uint32_t m) {
 // after the tile's scan and look-back, thread t writes children t, t + 256,
 // ... of the tile from that map, so the child arrays are written in
 // coalesced runs.
+// LEAVES (level 3 into the leaf level of a leafmask build, after the leaf
+// column passes): each leaf takes its class from its column's runs as it is
+// written (leaf_resolve_one), instead of its coordinate, and the leaf
+// level's job ranges follow from the parents' (a job's leaves are its
+// level-3 nodes' children, contiguous), so no pass re-reads the leaf list.
+template <bool LEAVES>
 __global__ void __launch_bounds__(kThreads)
     k_expand_lb(LevelDev cur, LevelDev nxt, uint32_t* counts, const JobDev* __restrict__ jobs, uint32_t njobs,
                 int L, const Injected* __restrict__ inj, uint32_t ninj, SegDev seg, uint32_t cap_next,
-                unsigned int* ticket, unsigned long long* flags, uint32_t* err) {
+                unsigned int* ticket, unsigned long long* flags, LeafColumns lc, uint32_t* err) {
     chain_enter();
     __shared__ uint32_t sm[64];
     __shared__ uint32_t s_tile, s_excl;
     __shared__ uint64_t s_coord[kExpTile];
     __shared__ uint32_t s_job[kExpTile];
     __shared__ uint16_t s_child[8 * kExpTile];  // tile child c: parent (local index) << 3 | child slot
+    __shared__ uint32_t s_umin[LEAVES ? kResUniform : 1];
+    LeafFirst lf{};
+    if (LEAVES) lf = leaf_first_begin(s_umin, lc.njobs);  // synchronised by the first ticket's barrier
     const uint32_t n = counts[L];
     const uint32_t ntiles = n ? (n + kExpTile - 1) / kExpTile : 1u;
     for (;;) {
@@ -1364,7 +1440,17 @@ __global__ void __launch_bounds__(kThreads)
         if (tile == 0)
             for (uint32_t r = threadIdx.x; r < ninj; r += blockDim.x) {
                 nxt.coord[r] = inj[r].coord;
-                nxt.job[r] = inj[r].job;
+                if (LEAVES) {
+                    // a job whose root is a leaf: its leaf range is that root
+                    const Injected q = inj[r];
+                    const uint32_t j = leaf_resolve_one(nxt, njobs, lc, lf, r, leaf_rec_fetch(lc, jobs, njobs, q.coord, q.job),
+                                                        q.job, err);
+                    nxt.job[r] = j;
+                    seg.nstart[seg_index(j, L - 1)] = r;
+                    seg.nend[seg_index(j, L - 1)] = r + 1;
+                } else {
+                    nxt.job[r] = inj[r].job;
+                }
             }
         const uint32_t l0 = threadIdx.x * kExpItems;  // first node of this thread within the tile
         const uint32_t b0 = tile * kExpTile + l0;
@@ -1444,21 +1530,43 @@ __global__ void __launch_bounds__(kThreads)
             cur.mask[i] = m[it];
             if (jv[it] != cur.job[i]) cur.job[i] = jv[it];
             const uint32_t j = jv[it];
-            if (i == 0 || cur.job[i - 1] != j) seg.nstart[seg_index(j, L)] = i;
-            if (i == n - 1 || cur.job[i + 1] != j) seg.nend[seg_index(j, L)] = i + 1;
+            const bool jfirst = i == 0 || cur.job[i - 1] != j, jlast = i == n - 1 || cur.job[i + 1] != j;
+            if (jfirst) seg.nstart[seg_index(j, L)] = i;
+            if (jlast) seg.nend[seg_index(j, L)] = i + 1;
+            if (LEAVES) {
+                // the job's leaves: from its first node's first child to
+                // its last node's last child
+                if (jfirst) seg.nstart[seg_index(j, L - 1)] = f;
+                if (jlast) seg.nend[seg_index(j, L - 1)] = f + k;
+            }
         }
         // cs::getChildCoordinates (src/CompressedShadowUtil.cpp:101-117),
         // one child per thread and step
         const uint32_t C = tot.x;
-        for (uint32_t c = threadIdx.x; c < C; c += blockDim.x) {
-            const uint32_t dst = f0 + c;
-            if (dst >= cap_next) break;
+        auto child_coord = [&](uint32_t c, uint32_t& j) {
             const uint32_t e = s_child[c];
             const uint32_t lo = e >> 3, ch = e & 7u;
             const uint64_t pc = s_coord[lo];
             const uint32_t x = unpack_x(pc), y = unpack_y(pc), z = unpack_z(pc);
-            nxt.coord[dst] = pack_xyz((x + (ch & 1u)) * 2u, (y + ((ch >> 1) & 1u)) * 2u, (z + (ch >> 2)) * 2u);
-            nxt.job[dst] = s_job[lo];
+            j = s_job[lo];
+            return pack_xyz((x + (ch & 1u)) * 2u, (y + ((ch >> 1) & 1u)) * 2u, (z + (ch >> 2)) * 2u);
+        };
+        const uint32_t Cw = min(C, cap_next > f0 ? cap_next - f0 : 0u);  // children that fit the level
+        if (LEAVES) {
+            // one leaf per thread and step (requesting several leaves'
+            // column records together measured slower: the registers it
+            // takes cost more occupancy than the overlap gains)
+            for (uint32_t c = threadIdx.x; c < Cw; c += blockDim.x) {
+                uint32_t j;
+                const uint64_t cc = child_coord(c, j);
+                nxt.job[f0 + c] = leaf_resolve_one(nxt, njobs, lc, lf, f0 + c, leaf_rec_fetch(lc, jobs, njobs, cc, j), j, err);
+            }
+        } else {
+            for (uint32_t c = threadIdx.x; c < Cw; c += blockDim.x) {
+                uint32_t j;
+                nxt.coord[f0 + c] = child_coord(c, j);
+                nxt.job[f0 + c] = j;
+            }
         }
         if (tile == ntiles - 1 && threadIdx.x == 0) {
             const uint32_t total = f0 + tot.x;
@@ -1466,6 +1574,10 @@ __global__ void __launch_bounds__(kThreads)
             counts[L - 1] = total < cap_next ? total : cap_next;
         }
         __syncthreads();
+    }
+    if (LEAVES) {
+        __syncthreads();
+        leaf_first_flush(lc, lf);
     }
 }
 
@@ -2882,15 +2994,22 @@ cpvs_status plan_enqueue(BuildPlan* P, cudaStream_t st, cudaStream_t rank_st, Ti
         CPVS_CUDA(launch_kernel(k_init_top, 1, 256, 0, st, ch, 0, P->lv[P->maxR], P->counts, P->maxR,
                                P->inj_dev + P->inj_off[P->maxR], (uint32_t)P->ninj[P->maxR]));
     }
+    // a leafmask build whose level 3 expands over every SM resolves its
+    // leaves in that pass (after the leaf column passes); else k_leaf_resolve
+    const bool fuse_leaves = P->leafmasks && std::min(exp_lo - 1, P->maxR) >= 3;
     for (int L = std::min(exp_lo - 1, P->maxR); L > P->bottom; --L) {
+        const bool leaves = fuse_leaves && L == 3;
+        if (leaves && forked) CPVS_CUDA(cudaStreamWaitEvent(st, P->tables, 0));
         KernelTimer kt(tm, K_EXPAND_WRITE, st);
-        CPVS_CUDA(launch_kernel(k_expand_lb, plan_grid(P, P->cap[L], kExpTile), kThreads, 0, st, ch, 0, P->lv[L],
-                               P->lv[L - 1], P->counts, P->jobs_dev, njobs, L, P->inj_dev + P->inj_off[L - 1],
-                               (uint32_t)P->ninj[L - 1], P->seg, (uint32_t)P->cap[L - 1], P->tickets + L,
-                               P->flags + P->exp_flag_off[L], err));
+        CPVS_CUDA(launch_kernel(leaves ? k_expand_lb<true> : k_expand_lb<false>, plan_grid(P, P->cap[L], kExpTile),
+                               kThreads, 0, st, ch, 0, P->lv[L], P->lv[L - 1], P->counts, P->jobs_dev, njobs, L,
+                               P->inj_dev + P->inj_off[L - 1], (uint32_t)P->ninj[L - 1], P->seg,
+                               (uint32_t)P->cap[L - 1], P->tickets + L, P->flags + P->exp_flag_off[L], lc, err));
     }
-    if (forked) CPVS_CUDA(cudaStreamWaitEvent(st, P->tables, 0));
-    if (P->leafmasks) {
+    if (forked && !fuse_leaves) CPVS_CUDA(cudaStreamWaitEvent(st, P->tables, 0));
+    if (fuse_leaves) {
+        // resolved by the expansion
+    } else if (P->leafmasks) {
         KernelTimer kt(tm, K_LEAF_RESOLVE, st);
         CPVS_CUDA(launch_kernel(k_leaf_resolve, plan_grid(P, P->cap[2], kThreads), kThreads, 0, st, ch, 0, P->lv[2],
                                 P->counts, P->jobs_dev, njobs, P->seg, lc, err));
