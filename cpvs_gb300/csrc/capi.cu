@@ -237,11 +237,15 @@ MultiDag shadow_table_entry(const cpvs_shadow* s) {
 namespace {
 
 // Queries per thread for a lookup on `s`: the context's fixed choice, or the
-// tuned one for this DAG depth (tuned on the first batch that needs it).
-int lookup_qpt(const cpvs_shadow* s, const void* q, bool ndc, uint64_t n, uint32_t* bits, cudaStream_t st) {
+// tuned one for this DAG depth and input kind (tuned on the first batch that
+// needs it).  Points read in place from host memory cross the host link with
+// its latency, which favours more queries in flight per thread than points
+// in device memory do, so the two kinds are tuned apart.
+int lookup_qpt(const cpvs_shadow* s, const void* q, bool ndc, bool host_in, uint64_t n, uint32_t* bits,
+               cudaStream_t st) {
     cpvs::Ctx& c = s->ctx->c;
     if (c.lookup_qpt) return c.lookup_qpt;
-    int& t = c.lookup_qpt_tuned[s->num_levels % CPVS_MAX_LEVELS][ndc ? 1 : 0];
+    int& t = c.lookup_qpt_tuned[s->num_levels % CPVS_MAX_LEVELS][ndc ? 1 : 0][host_in ? 1 : 0];
     if (!t)
         t = cpvs::tune_lookup(s->dag, s->words, s->num_levels, s->leafmasks, s->top, s->top_depth, q, ndc, n, bits, st);
     return t;
@@ -717,7 +721,8 @@ cpvs_status cpvs_shadow_lookup_ndc(const cpvs_shadow* s, const float* xyz, uint6
         ensure_top(s, st);
         cpvs_status r =
             cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, s->top, s->top_depth, q, true, n, bits,
-                                st, &s->ctx->c.timing, lookup_qpt(s, q, true, n, bits, st));
+                                st, &s->ctx->c.timing, lookup_qpt(s, q, true, q == xyz && !(flags & CPVS_IO_DEVICE), n,
+                                                                  bits, st));
         s->touch(st);
         return r;
     });
@@ -732,7 +737,8 @@ cpvs_status cpvs_shadow_lookup_voxel(const cpvs_shadow* s, const int32_t* xyz, u
         ensure_top(s, st);
         cpvs_status r =
             cpvs::launch_lookup(s->dag, s->words, s->num_levels, s->leafmasks, s->top, s->top_depth, q, false, n,
-                                bits, st, &s->ctx->c.timing, lookup_qpt(s, q, false, n, bits, st));
+                                bits, st, &s->ctx->c.timing,
+                                lookup_qpt(s, q, false, q == xyz && !(flags & CPVS_IO_DEVICE), n, bits, st));
         s->touch(st);
         return r;
     });

@@ -255,7 +255,7 @@ struct Ctx {
     // lookup queries per thread: fixed by cpvs_ctx_set_option, else tuned
     // once per (DAG levels, NDC or voxel input)
     int lookup_qpt = 0;
-    int lookup_qpt_tuned[CPVS_MAX_LEVELS][2] = {{0}};
+    int lookup_qpt_tuned[CPVS_MAX_LEVELS][2][2] = {};  // [levels][ndc][points in host memory]
     // build launch shapes fixed by cpvs_ctx_set_option (0: timed per plan on
     // its first build): the largest level the cluster kernels take, and the
     // inner-level insert's grid in resident waves

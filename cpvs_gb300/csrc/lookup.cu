@@ -285,6 +285,135 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// The common case in straight-line code: a leafmask DAG with a top grid
+// and NL inner levels below it (the c1 workload: levels 4 and 3), fewer
+// than 2^31 queries.  The levels are unrolled, each query carries an
+// `alive` flag instead of leaving a loop, and indices are 32-bit, so a
+// query costs fewer instructions than in k_lookup; Q queries per thread are
+// interleaved level by level, so each level issues Q independent loads with
+// no lockstep loop around them.  The next group's points are requested
+// before the current group descends.  Same answers as k_lookup: every node
+// offset is checked against `words` before its mask is read, and the zeroed
+// tail keeps a node's pointer and leaf words inside the buffer.
+template <bool NDC, int Q, int NL>
+__global__ void __launch_bounds__(kThreads)
+    k_lookup_fixed(const uint32_t* __restrict__ dag, uint32_t words, int num_levels, const uint32_t* __restrict__ top,
+                   int depth, const void* __restrict__ q, uint32_t n, uint32_t* __restrict__ bits) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const int root = num_levels - 2;
+    const int shift = root - depth + 1;  // the top grid takes bits root .. shift of each coordinate
+    const int low = shift - NL;          // bit of the last inner level (3)
+    const uint32_t nwords = (n + 31u) / 32u;
+    const uint32_t ngroups = (nwords + Q - 1u) / Q;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const float scale = (float)((1u << (num_levels - 1)) - 1u);
+    uint32_t nx[Q] = {}, ny[Q] = {}, nz[Q] = {};
+    auto fetch = [&](uint32_t g) {
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            const uint32_t i = (g * Q + k) * 32u + lane;
+            if (g < ngroups && i < n) {
+                const uint32_t* p = static_cast<const uint32_t*>(q) + 3u * (size_t)i;
+                nx[k] = __ldcs(p);
+                ny[k] = __ldcs(p + 1);
+                nz[k] = __ldcs(p + 2);
+            }
+        }
+    };
+    uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    fetch(g);
+    for (; g < ngroups; g += nw) {
+        // this group's points, then the next group's requested before these
+        // are used (two groups' reads in flight while a point arrives)
+        uint32_t rx[Q], ry[Q], rz[Q];
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            rx[k] = nx[k];
+            ry[k] = ny[k];
+            rz[k] = nz[k];
+        }
+        fetch(g + nw);
+        int32_t px[Q], py[Q], pz[Q];
+        uint32_t off[Q];
+        bool alive[Q], lit[Q];
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            const uint32_t i = (g * Q + k) * 32u + lane;
+            if (NDC) {
+                px[k] = quantise(__uint_as_float(rx[k]), scale);
+                py[k] = quantise(__uint_as_float(ry[k]), scale);
+                pz[k] = quantise(__uint_as_float(rz[k]), scale);
+            } else {
+                px[k] = (int32_t)rx[k];
+                py[k] = (int32_t)ry[k];
+                pz[k] = (int32_t)rz[k];
+            }
+            alive[k] = i < n;
+            lit[k] = false;
+            off[k] = 0;
+        }
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            const uint32_t e = alive[k] ? __ldg(top + top_cell(px[k], py[k], pz[k], shift, depth)) : kCellShadow;
+            if (e >= kCellLit) {
+                lit[k] = alive[k] && e == kCellLit;
+                alive[k] = false;
+            } else {
+                off[k] = e;
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < NL; ++s) {
+            const int b = NL - 1 - s;  // this level's bit above `low`
+            uint32_t m[Q];
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                if (alive[k] && off[k] >= words) alive[k] = false;  // malformed DAG: shadow
+                m[k] = alive[k] ? __ldg(dag + off[k]) : 0u;
+            }
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                if (!alive[k]) continue;
+                const uint32_t c2 = child2(px[k] >> low, py[k] >> low, pz[k] >> low, b);
+                const uint32_t v = (m[k] >> c2) & 3u;
+                if (v != kPartial) {
+                    lit[k] = v == kVisible;
+                    alive[k] = false;
+                } else {
+                    off[k] = __ldg(dag + off[k] + 1u + __popc(m[k] & 0xAAAAu & ((1u << c2) - 1u)));
+                }
+            }
+        }
+        // the leaf: slice z & 7, bit (x & 7) + 8 (y & 7) of its mask pair
+        uint32_t m[Q];
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            if (alive[k] && off[k] >= words) alive[k] = false;
+            m[k] = alive[k] ? __ldg(dag + off[k]) : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            if (alive[k]) {
+                const uint32_t c2 = ((uint32_t)pz[k] & 7u) * 2u;
+                const uint32_t v = (m[k] >> c2) & 3u;
+                if (v != kPartial) {
+                    lit[k] = v == kVisible;
+                } else {
+                    const uint32_t rank = __popc(m[k] & 0xAAAAu & ((1u << c2) - 1u));
+                    const uint32_t bb = ((uint32_t)px[k] & 7u) + 8u * ((uint32_t)py[k] & 7u);
+                    lit[k] = (__ldg(dag + off[k] + 1u + 2u * rank + (bb >> 5)) >> (bb & 31u)) & 1u;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            const uint32_t word = __ballot_sync(0xffffffffu, lit[k]);
+            const uint32_t wi = g * Q + k;
+            if (lane == 0 && wi < nwords) __stcs(bits + wi, word);
+        }
+    }
+}
+
 // One grid sample at an integer path (shader/traverse.cs:75-88 routing):
 // outside the grid answers lit, a uniform cell its class, else the descent
 // of the cell's DAG with pointers relative to its first word.
@@ -558,9 +687,34 @@ cpvs_status launch_top_index(const uint32_t* dag, uint64_t words, int depth, uin
     return CPVS_OK;
 }
 
+// Inner levels below the top grid that k_lookup_fixed unrolls (0 ..
+// kFixedLevels); other DAGs take k_lookup.
+constexpr int kFixedLevels = 6;
+
+template <bool NDC, int Q, int NL>
+bool launch_fixed_nl(int nl, uint32_t g, cudaStream_t st, const uint32_t* dag, uint64_t words, uint32_t num_levels,
+                     const uint32_t* top, int depth, const void* xyz, uint64_t n, uint32_t* bits) {
+    if (nl == NL) {
+        k_lookup_fixed<NDC, Q, NL><<<g, kThreads, 0, st>>>(dag, (uint32_t)words, (int)num_levels, top, depth, xyz,
+                                                           (uint32_t)n, bits);
+        return true;
+    }
+    if constexpr (NL < kFixedLevels) {
+        return launch_fixed_nl<NDC, Q, NL + 1>(nl, g, st, dag, words, num_levels, top, depth, xyz, n, bits);
+    } else {
+        return false;
+    }
+}
+
 template <bool NDC, int Q>
 void launch_lookup_q(uint32_t g, cudaStream_t st, const uint32_t* dag, uint64_t words, uint32_t num_levels,
                      bool leafmasks, const uint32_t* top, int depth, const void* xyz, uint64_t n, uint32_t* bits) {
+    // the straight-line kernel where it applies: leafmasks, a top grid, at
+    // most kFixedLevels inner levels below it, fewer than 2^31 queries
+    const int nl = (int)num_levels - 2 - depth - 3 + 1;
+    if (Q <= 2 && leafmasks && top && depth > 0 && nl >= 0 && n < (1ull << 31) &&
+        launch_fixed_nl<NDC, (Q <= 2 ? Q : 2), 0>(nl, g, st, dag, words, num_levels, top, depth, xyz, n, bits))
+        return;
     k_lookup<NDC, Q><<<g, kThreads, 0, st>>>(dag, (uint32_t)words, (int)num_levels, leafmasks, top, depth, xyz, n,
                                              bits);
 }
