@@ -396,9 +396,14 @@ const char* cpvs_kernel_name(uint32_t id) { return cpvs::kernel_name((int)id); }
 // ------------------------------------------------------------- hierarchy
 namespace {
 // `first_level`: the lowest pyramid level stored (1 for a hierarchy handed to
-// the caller).
+// the caller).  A host map that the GPU reads in place must not change
+// before the pyramid has read it: the call waits for that read, unless
+// `host_read` is given, which then receives an event recorded after the read
+// (null when nothing reads host memory); the caller waits for it before it
+// returns to its own caller.
 cpvs_status hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n, uint32_t flags, void* stream,
-                             int first_level, cpvs_hierarchy** out) {
+                             int first_level, cpvs_hierarchy** out, cudaEvent_t* host_read = nullptr) {
+    if (host_read) *host_read = nullptr;
     if (!ctx || !depth || !out) return fail(CPVS_ERR_INVALID_ARG, "hierarchy_create: null argument");
     *out = nullptr;
     cpvs_status r = check_map_size(n, 2);
@@ -441,9 +446,15 @@ cpvs_status hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n, uint
             r = cpvs::launch_pyramid(in_place, n, h->levels, st, &c.timing, h->depth, first_level,
                                      cpvs::pyramid_nan_flag(h->levels, n));
             // the caller may reuse its buffer on return: wait for the read
-            if (r == CPVS_OK) {
-                const cudaError_t e = cudaStreamSynchronize(st);
+            // (or hand the wait to the caller)
+            if (r == CPVS_OK && host_read) {
+                cudaError_t e = cudaEventCreateWithFlags(host_read, cudaEventDisableTiming);
+                if (e == cudaSuccess) e = cudaEventRecord(*host_read, st);
                 if (e != cudaSuccess) r = cpvs::cuda_fail(e, "hierarchy read of the host map");
+            }
+            if (r != CPVS_OK || !host_read) {
+                const cudaError_t e = cudaStreamSynchronize(st);
+                if (e != cudaSuccess && r == CPVS_OK) r = cpvs::cuda_fail(e, "hierarchy read of the host map");
             }
         } else {
             r = cpvs::launch_pyramid(h->depth, n, h->levels, st, &c.timing, nullptr, first_level,
@@ -452,6 +463,10 @@ cpvs_status hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n, uint
     }
     h->touch(st);
     if (r != CPVS_OK) {
+        if (host_read && *host_read) {
+            cudaEventDestroy(*host_read);
+            *host_read = nullptr;
+        }
         cpvs_hierarchy_destroy(h);
         return r;
     }
@@ -658,11 +673,23 @@ cpvs_status cpvs_shadow_create_from_depth(cpvs_ctx* ctx, const float* depth, uin
     if (r != CPVS_OK) return r;
     // The temporary hierarchy is gone before this call returns, so a device
     // map can be read in place.
+    // A host map read in place is waited for once, at the end: the build is
+    // queued behind the pyramid instead of after a host round trip.
     cpvs_hierarchy* h = nullptr;
-    r = cpvs::hierarchy_create_for_build(ctx, depth, n, flags | CPVS_FLAG_BORROW_INPUT, flags, stream, &h);
+    cudaEvent_t host_read = nullptr;
+    r = cpvs::hierarchy_create_for_build(ctx, depth, n, flags | CPVS_FLAG_BORROW_INPUT, flags, stream, &h, &host_read);
     if (r != CPVS_OK) return r;
     r = cpvs_shadow_create(ctx, h, z_tile_index, z_tile_num, flags, stream, out);
     cpvs_hierarchy_destroy(h);
+    if (host_read) {
+        const cudaError_t e = cudaEventSynchronize(host_read);
+        cudaEventDestroy(host_read);
+        if (e != cudaSuccess && r == CPVS_OK) {
+            cpvs_shadow_destroy(*out);
+            *out = nullptr;
+            r = cpvs::cuda_fail(e, "hierarchy read of the host map");
+        }
+    }
     return r;
 }
 
@@ -1107,9 +1134,10 @@ namespace cpvs {
 // the map itself): levels 1 and 2, the bulk of the pyramid, are reduced on
 // chip but never stored.
 cpvs_status hierarchy_create_for_build(cpvs_ctx* ctx, const float* depth, uint32_t n, uint32_t flags,
-                                       uint32_t build_flags, void* stream, cpvs_hierarchy** out) {
+                                       uint32_t build_flags, void* stream, cpvs_hierarchy** out,
+                                       cudaEvent_t* host_read) {
     const uint32_t nl = (uint32_t)log2_u32(n) + 1;
     const bool leaf = (build_flags & CPVS_FLAG_LEAFMASKS) && n >= 2 && (nl - 3 >= 2);
-    return hierarchy_create(ctx, depth, n, flags, stream, leaf ? 3 : 1, out);
+    return hierarchy_create(ctx, depth, n, flags, stream, leaf ? 3 : 1, out, host_read);
 }
 }  // namespace cpvs

@@ -93,7 +93,11 @@ void shadow_ensure_top(const cpvs_shadow* s, cudaStream_t st, uint32_t max_facto
 // The shadow as an entry of a multi-DAG lookup table (with its top grid).
 MultiDag shadow_table_entry(const cpvs_shadow* s);
 // A hierarchy that only feeds builds with the given flags (destroyed after
-// them): with leafmasks, pyramid levels 1 and 2 are not stored.
+// them): with leafmasks, pyramid levels 1 and 2 are not stored.  With
+// `host_read`, a host map read in place is not waited for: the event
+// recorded after the read is returned, and the caller waits for it before
+// its own caller may reuse the map.
 cpvs_status hierarchy_create_for_build(cpvs_ctx* ctx, const float* depth, uint32_t n, uint32_t flags,
-                                       uint32_t build_flags, void* stream, cpvs_hierarchy** out);
+                                       uint32_t build_flags, void* stream, cpvs_hierarchy** out,
+                                       cudaEvent_t* host_read = nullptr);
 }  // namespace cpvs
