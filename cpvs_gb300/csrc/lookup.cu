@@ -82,16 +82,21 @@ __device__ __forceinline__ uint32_t top_cell(int32_t px, int32_t py, int32_t pz,
            (((uint32_t)px >> shift) & m);
 }
 
+// One thread per cell of depth `depth` - 1: its descent, then the eight
+// cells below it from one mask load and up to eight independent pointer
+// loads (neighbouring cells share all but their last level, so walking
+// each cell alone would repeat the same chain eight times).
 __global__ void k_top_index(const uint32_t* __restrict__ dag, uint32_t words, int depth, uint32_t* __restrict__ out) {
-    const uint32_t cells = 1u << (3 * depth);
-    const uint32_t m = (1u << depth) - 1u;
-    for (uint32_t cell = blockIdx.x * blockDim.x + threadIdx.x; cell < cells; cell += gridDim.x * blockDim.x) {
-        const uint32_t cx = cell & m, cy = (cell >> depth) & m, cz = cell >> (2 * depth);
+    const int dp = depth - 1;
+    const uint32_t pcells = 1u << (3 * dp);
+    const uint32_t pm = (1u << dp) - 1u;
+    for (uint32_t pc = blockIdx.x * blockDim.x + threadIdx.x; pc < pcells; pc += gridDim.x * blockDim.x) {
+        const uint32_t px = pc & pm, py = (pc >> dp) & pm, pz = pc >> (2 * dp);
         uint32_t off = 0, entry = 0;
         bool done = false;
-        for (int d = 0; d < depth; ++d) {
-            const int b = depth - 1 - d;
-            const uint32_t c = ((cx >> b) & 1u) | (((cy >> b) & 1u) << 1) | (((cz >> b) & 1u) << 2);
+        for (int d = 0; d < dp; ++d) {
+            const int b = dp - 1 - d;
+            const uint32_t c = ((px >> b) & 1u) | (((py >> b) & 1u) << 1) | (((pz >> b) & 1u) << 2);
             if (off >= words) {
                 entry = kCellShadow;
                 done = true;
@@ -106,7 +111,26 @@ __global__ void k_top_index(const uint32_t* __restrict__ dag, uint32_t words, in
             }
             off = dag[off + 1u + __popc(m & 0xAAAAu & ((1u << (2u * c)) - 1u))];
         }
-        out[cell] = done ? entry : off;
+        uint32_t m = 0;
+        if (!done) {
+            if (off >= words) {
+                entry = kCellShadow;
+                done = true;
+            } else {
+                m = dag[off];
+            }
+        }
+#pragma unroll
+        for (uint32_t c = 0; c < 8; ++c) {
+            uint32_t e = entry;
+            if (!done) {
+                const uint32_t v = (m >> (2u * c)) & 3u;
+                e = v == kPartial ? dag[off + 1u + __popc(m & 0xAAAAu & ((1u << (2u * c)) - 1u))]
+                                  : (v == kVisible ? kCellLit : kCellShadow);
+            }
+            const uint32_t cx = 2u * px + (c & 1u), cy = 2u * py + ((c >> 1) & 1u), cz = 2u * pz + (c >> 2);
+            out[(cz << (2 * depth)) | (cy << depth) | cx] = e;
+        }
     }
 }
 
@@ -490,6 +514,59 @@ __global__ void k_grid_top_index(const uint32_t* __restrict__ dag, uint32_t word
     }
 }
 
+// The same index from one thread per entry of resolution bits - 1 (depth
+// >= 1): the descent to its node, then its eight entries from one mask load
+// and up to eight independent pointer loads.
+__global__ void k_grid_top_index_parents(const uint32_t* __restrict__ dag, uint32_t words,
+                                         const uint32_t* __restrict__ cells, uint32_t length, int depth, int bits,
+                                         uint32_t* __restrict__ out) {
+    const int pb = bits - 1, dp = depth - 1;
+    const uint64_t total = 1ull << (3 * pb);
+    const uint32_t m = (1u << pb) - 1u;
+    for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t px = (uint32_t)t & m, py = (uint32_t)(t >> pb) & m, pz = (uint32_t)(t >> (2 * pb));
+        const uint32_t cell = cells[((size_t)(pz >> dp) * length + (py >> dp)) * length + (px >> dp)];
+        uint32_t entry = cell, off = cell, mk = 0;
+        bool done = cell >= kCellLit;  // a uniform cell: every entry is its sentinel
+        for (int d = 0; d < dp && !done; ++d) {
+            const int b = dp - 1 - d;
+            const uint32_t c = ((px >> b) & 1u) | (((py >> b) & 1u) << 1) | (((pz >> b) & 1u) << 2);
+            if (off >= words) {
+                entry = kCellShadow;
+                done = true;
+                break;
+            }
+            const uint32_t w = dag[off];
+            const uint32_t v = (w >> (2u * c)) & 3u;
+            if (v != kPartial) {
+                entry = (v == kVisible) ? kCellLit : kCellShadow;
+                done = true;
+                break;
+            }
+            off = cell + dag[off + 1u + __popc(w & 0xAAAAu & ((1u << (2u * c)) - 1u))];
+        }
+        if (!done) {
+            if (off >= words) {
+                entry = kCellShadow;
+                done = true;
+            } else {
+                mk = dag[off];
+            }
+        }
+#pragma unroll
+        for (uint32_t c = 0; c < 8; ++c) {
+            uint32_t e = entry;
+            if (!done) {
+                const uint32_t v = (mk >> (2u * c)) & 3u;
+                e = v == kPartial ? cell + dag[off + 1u + __popc(mk & 0xAAAAu & ((1u << (2u * c)) - 1u))]
+                                  : (v == kVisible ? kCellLit : kCellShadow);
+            }
+            const uint64_t gx = 2ull * px + (c & 1u), gy = 2ull * py + ((c >> 1) & 1u), gz = 2ull * pz + (c >> 2);
+            out[(gz << (2 * bits)) | (gy << bits) | gx] = e;
+        }
+    }
+}
+
 // Grid routing (shader/traverse.cs:75-88): the path at resolution
 // 2^(dag_levels+grid_levels-1), its top bits select the cell, the cell word
 // holds the DAG offset or a uniform-cell sentinel; then the cell's descent
@@ -681,8 +758,8 @@ int top_index_depth(uint32_t num_levels, bool leafmasks, uint64_t words, uint32_
 
 cpvs_status launch_top_index(const uint32_t* dag, uint64_t words, int depth, uint32_t* out, cudaStream_t st) {
     if (depth <= 0) return CPVS_OK;
-    const uint32_t cells = 1u << (3 * depth);
-    k_top_index<<<(cells + 255) / 256, 256, 0, st>>>(dag, (uint32_t)words, depth, out);
+    const uint32_t parents = 1u << (3 * (depth - 1));  // one thread per cell of depth - 1
+    k_top_index<<<(parents + 255) / 256, 256, 0, st>>>(dag, (uint32_t)words, depth, out);
     CPVS_CUDA(cudaGetLastError());
     return CPVS_OK;
 }
@@ -822,9 +899,15 @@ int grid_top_depth(uint32_t length, uint32_t dag_levels, bool leafmasks, uint64_
 cpvs_status launch_grid_top_index(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
                                   uint32_t dag_levels, int depth, uint32_t* out, cudaStream_t st) {
     const int bits = log2_u32(length) + depth;
-    const uint64_t total = 1ull << (3 * bits);
-    const uint32_t g = (uint32_t)std::min<uint64_t>((total + 255) / 256, 152ull * 32);
-    k_grid_top_index<<<g, 256, 0, st>>>(dag, (uint32_t)words, cells, length, (int)dag_levels, depth, bits, out);
+    if (depth >= 1) {
+        const uint64_t parents = 1ull << (3 * (bits - 1));
+        const uint32_t g = (uint32_t)std::min<uint64_t>((parents + 255) / 256, 152ull * 32);
+        k_grid_top_index_parents<<<g, 256, 0, st>>>(dag, (uint32_t)words, cells, length, depth, bits, out);
+    } else {
+        const uint64_t total = 1ull << (3 * bits);
+        const uint32_t g = (uint32_t)std::min<uint64_t>((total + 255) / 256, 152ull * 32);
+        k_grid_top_index<<<g, 256, 0, st>>>(dag, (uint32_t)words, cells, length, (int)dag_levels, depth, bits, out);
+    }
     CPVS_CUDA(cudaGetLastError());
     return CPVS_OK;
 }
