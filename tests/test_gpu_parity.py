@@ -235,6 +235,30 @@ def test_lookup_variants_agree(cp, oracle):
         ctx.set_option(ctx.OPT_LOOKUP_QUERIES_PER_THREAD, 3)
 
 
+def test_lookup_every_depth_and_input_kind(cp, oracle):
+    """Maps of sides 16..2048 put the top grid at different depths, so the
+    straight-line lookup runs with 0 to several inner levels below it (and
+    the looped kernel where it does not apply).  Every variant, the tuned
+    choice, points in host and in device memory, and points a little
+    outside [-1, 1] answer like the oracle."""
+    torch = pytest.importorskip("torch")
+    for n, seed in ((16, 1), (32, 2), (64, 3), (128, 4), (256, 5), (512, 6), (2048, 7)):
+        d = scene.rasterise(scene.make_scene(n, 0.9, 12, 3, 600 + seed))
+        want = oracle.build(d)
+        ctx = cp.Context(0)
+        sh = cp.CompressedShadow.from_depth(d, ctx=ctx)
+        q = scene.ndc_queries_mixed(d, 20_001, seed)
+        g = np.random.Generator(np.random.PCG64(seed))
+        q[-2000:] = (g.random((2000, 3)) * 2.4 - 1.2).astype(np.float32)  # partly outside the volume
+        ref = oracle.lookup_ndc(want.dag, want.num_levels, True, q, threads=8)
+        qd = torch.from_numpy(q).cuda()
+        for qpt in (0, 1, 2, 4):
+            ctx.set_option(ctx.OPT_LOOKUP_QUERIES_PER_THREAD, qpt)
+            assert np.array_equal(sh.lookup_ndc(q), ref), (n, qpt, "host")
+            words = sh.lookup_ndc(qd).cpu().numpy().view(np.uint32)
+            assert np.array_equal(cp.unpack_bits(words, q.shape[0]), ref), (n, qpt, "device")
+
+
 def test_repeated_builds_are_identical(cp):
     d = scene.rasterise(scene.config_scene("c0", n=512))
     a = cp.CompressedShadow.from_depth(d).get_dag()
