@@ -647,10 +647,26 @@ class CompressedShadowContainer:
         return c
 
     def set(self, shadow: CompressedShadow, x: int, y: int, z: int):
-        """Cell (x,y,z) takes ownership of the shadow's DAG."""
+        """Cell (x,y,z) takes ownership of the shadow (the reference moves a
+        unique_ptr in): the shadow object stays usable while the container
+        holds it, and is released with the container, when its cell is
+        replaced, or by move_to_gpu and build.  A released shadow, or one that
+        a cell already holds, is refused."""
+        if getattr(shadow, "handle", None) is None:
+            raise ValueError("set: the shadow has been released (its container took it)")
+        if not shadow._owned and self._cells.get((x, y, z)) is not shadow:
+            raise ValueError("set: the shadow already belongs to a container cell")
         _check(_lib.cpvs_grid_set(self.handle, x, y, z, shadow.handle))
+        old = self._cells.get((x, y, z))
+        if old is not None and old is not shadow:
+            old.handle = None  # destroyed by the grid
         shadow._owned = False
         self._cells[(x, y, z)] = shadow
+
+    def _release_cells(self):
+        for s in self._cells.values():
+            s.handle = None
+        self._cells.clear()
 
     def get(self, x: int, y: int, z: int) -> Optional[CompressedShadow]:
         return self._cells.get((x, y, z))
@@ -660,16 +676,14 @@ class CompressedShadowContainer:
         xy_tiles[y*length+x] (MinMaxHierarchy objects of one size)."""
         hs = (_vp * len(xy_tiles))(*[m.handle for m in xy_tiles])
         _check(_lib.cpvs_grid_build(self.handle, hs, FLAG_LEAFMASKS if leafmasks else 0, _stream(stream)))
-        self._cells.clear()
+        self._release_cells()  # the grid destroyed the cells' previous shadows
 
     def copy_to_gpu(self, stream=None):
         _check(_lib.cpvs_grid_finalize(self.handle, 0, _stream(stream)))
 
     def move_to_gpu(self, stream=None):
         _check(_lib.cpvs_grid_finalize(self.handle, 1, _stream(stream)))
-        for s in self._cells.values():
-            s.handle = None
-        self._cells.clear()
+        self._release_cells()
 
     copyToGPU, moveToGPU = copy_to_gpu, move_to_gpu
 
@@ -767,6 +781,7 @@ class CompressedShadowContainer:
 
     def __del__(self):
         if getattr(self, "handle", None) and _live():
+            self._release_cells()
             _lib.cpvs_grid_destroy(self.handle)
             self.handle = None
 

@@ -848,8 +848,13 @@ cpvs_status cpvs_grid_set(cpvs_grid* g, uint32_t x, uint32_t y, uint32_t z, cpvs
     if (!g) return fail(CPVS_ERR_INVALID_ARG, "grid_set: null grid");
     if (x >= g->length || y >= g->length || z >= g->length) return fail(CPVS_ERR_INVALID_ARG, "grid_set: cell out of range");
     const size_t i = ((size_t)z * g->length + y) * g->length + x;
+    // a cell owns its shadow: a shadow that a cell already holds (this
+    // grid's other cells or another grid's) would be destroyed twice
+    if (s && s->owner && !(s->owner == g && g->cells[i] == s))
+        return fail(CPVS_ERR_INVALID_ARG, "grid_set: the shadow already belongs to a grid cell");
     if (g->cells[i] && g->cells[i] != s) cpvs_shadow_destroy(g->cells[i]);
     g->cells[i] = s;
+    if (s) s->owner = g;
     return CPVS_OK;
 }
 
@@ -979,7 +984,10 @@ cpvs_status cpvs_grid_build(cpvs_grid* g, const cpvs_hierarchy* const* xy_tiles,
     block->refs++;
     g->dag = block->base;
     g->words = total;
-    for (size_t i = 0; i < jobs.size(); ++i) g->cells[i] = shadows[i];
+    for (size_t i = 0; i < jobs.size(); ++i) {
+        g->cells[i] = shadows[i];
+        shadows[i]->owner = g;
+    }
     g->dag_levels = nl;
     g->leafmasks = leaf;
     g->finalized = true;

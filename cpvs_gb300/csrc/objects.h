@@ -64,6 +64,7 @@ struct cpvs_shadow : DeviceObject {
     bool leafmasks = false;
     uint32_t root_mask = 0;
     std::vector<uint64_t> tree, uniq;
+    const cpvs_grid* owner = nullptr;  // the grid whose cell holds it (and destroys it)
 };
 
 struct cpvs_grid : DeviceObject {

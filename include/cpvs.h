@@ -297,7 +297,10 @@ CPVS_API cpvs_status cpvs_grid_create(cpvs_ctx* ctx, uint32_t length, cpvs_grid*
 CPVS_API void cpvs_grid_destroy(cpvs_grid* g);
 CPVS_API uint32_t cpvs_grid_length(const cpvs_grid* g);
 /* CompressedShadowContainer::set (src/CompressedShadowContainer.h:34-39):
- * cell (x,y,z) takes ownership of `s` (destroys any previous DAG there). */
+ * cell (x,y,z) takes ownership of `s` (destroys any previous DAG there);
+ * the grid destroys it, so the caller must not, and must not use `s` after
+ * the grid is destroyed.  A shadow that a cell already holds (of this grid or
+ * another) is refused with CPVS_ERR_INVALID_ARG. */
 CPVS_API cpvs_status cpvs_grid_set(cpvs_grid* g, uint32_t x, uint32_t y, uint32_t z, cpvs_shadow* s);
 /* CompressedShadowContainer::get: the DAG at (x,y,z), or NULL. */
 CPVS_API const cpvs_shadow* cpvs_grid_get(const cpvs_grid* g, uint32_t x, uint32_t y, uint32_t z);

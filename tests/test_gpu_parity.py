@@ -259,6 +259,41 @@ def test_lookup_every_depth_and_input_kind(cp, oracle):
             assert np.array_equal(cp.unpack_bits(words, q.shape[0]), ref), (n, qpt, "device")
 
 
+def test_container_owns_its_shadows(cp):
+    """A container takes its shadows the way the reference moves a
+    unique_ptr in: a shadow stays usable while a cell holds it; one that its
+    container released (container gone, cell replaced) raises on use instead
+    of reaching freed memory; and a shadow cannot sit in two cells (the
+    Python mirror and the C ABI both refuse)."""
+    import gc
+    d = scene.rasterise(scene.config_scene("c0", n=64))
+    ctx = cp.Context(0)
+    q = scene.ndc_queries_mixed(d, 1000, 3)
+    sh = cp.CompressedShadow.from_depth(d, ctx=ctx)
+    want = sh.lookup_ndc(q)
+    g = cp.CompressedShadowContainer.of(sh)
+    assert g.get(0, 0, 0) is sh and np.array_equal(sh.lookup_ndc(q), want)
+    with pytest.raises(ValueError):
+        cp.CompressedShadowContainer.of(sh)  # a cell already holds it
+    other = cp.CompressedShadowContainer(2, ctx)
+    with pytest.raises(ValueError):
+        other.set(sh, 1, 0, 0)
+    assert cp._lib.cpvs_grid_set(other.handle, 1, 0, 0, sh.handle) != 0  # the C ABI refuses too
+    del g
+    gc.collect()
+    with pytest.raises(ValueError):
+        cp.CompressedShadowContainer.of(sh)  # released with its container
+    with pytest.raises(cp.CpvsError):
+        sh.lookup_ndc(q)
+    a = cp.CompressedShadow.from_depth(d, ctx=ctx)
+    b = cp.CompressedShadow.from_depth(d, ctx=ctx)
+    other.set(a, 0, 0, 0)
+    other.set(b, 0, 0, 0)  # replaces (and destroys) a
+    with pytest.raises(cp.CpvsError):
+        a.lookup_ndc(q)
+    assert np.array_equal(b.lookup_ndc(q), want)
+
+
 def test_repeated_builds_are_identical(cp):
     d = scene.rasterise(scene.config_scene("c0", n=512))
     a = cp.CompressedShadow.from_depth(d).get_dag()
