@@ -24,6 +24,7 @@
 // batch streams hundreds of MB past L2 and would otherwise push the DAG and
 // its top grid out of it.
 #include <algorithm>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -61,6 +62,33 @@ __device__ __forceinline__ bool descend(const uint32_t* __restrict__ dag, uint32
         off = base + __ldg(dag + off + 1u + rank);
     }
     if (!leafmasks) return true;  // unreachable: level 0 has no partial children
+    if (off >= words) return false;
+    const uint32_t c2 = ((uint32_t)pz & 7u) * 2u;
+    const uint32_t m = __ldg(dag + off);
+    const uint32_t v = (m >> c2) & 3u;
+    if (v != kPartial) return v == kVisible;
+    const uint32_t rank = __popc(m & 0xAAAAu & ((1u << c2) - 1u));
+    const uint32_t b = ((uint32_t)px & 7u) + 8u * ((uint32_t)py & 7u);
+    const uint32_t w = __ldg(dag + off + 1u + 2u * rank + (b >> 5));
+    return (w >> (b & 31u)) & 1u;
+}
+
+// descend() for a leafmask DAG whose NL inner levels above the leaves are
+// known at compile time (the levels below a grid index): the same reads and
+// checks, unrolled, with constant shifts.
+template <int NL>
+__device__ __forceinline__ bool descend_fixed(const uint32_t* __restrict__ dag, uint32_t words, uint32_t base,
+                                              uint32_t off, int32_t px, int32_t py, int32_t pz) {
+#pragma unroll
+    for (int s = 0; s < NL; ++s) {
+        const int level = 3 + NL - 1 - s;
+        if (off >= words) return false;
+        const uint32_t c2 = child2(px, py, pz, level);
+        const uint32_t m = __ldg(dag + off);
+        const uint32_t v = (m >> c2) & 3u;
+        if (v != kPartial) return v == kVisible;
+        off = base + __ldg(dag + off + 1u + __popc(m & 0xAAAAu & ((1u << c2) - 1u)));
+    }
     if (off >= words) return false;
     const uint32_t c2 = ((uint32_t)pz & 7u) * 2u;
     const uint32_t m = __ldg(dag + off);
@@ -449,6 +477,9 @@ struct GridTop {
     int bits;             // log2(length) + depth: index bits per axis
 };
 
+// NL >= 0: a leafmask grid with an index, NL inner levels below it
+// (descend_fixed); -1: any grid.
+template <int NL = -1>
 __device__ __forceinline__ bool grid_sample(const uint32_t* __restrict__ dag, uint32_t words,
                                             const uint32_t* __restrict__ cells, uint32_t length, int dag_levels,
                                             bool leafmasks, GridTop gt, int64_t px, int64_t py, int64_t pz) {
@@ -463,6 +494,7 @@ __device__ __forceinline__ bool grid_sample(const uint32_t* __restrict__ dag, ui
         const uint32_t e = __ldg(gt.top + ((((uint64_t)pz >> s) << (2 * gt.bits)) | (((uint64_t)py >> s) << gt.bits) |
                                            ((uint64_t)px >> s)));
         if (e >= kCellLit) return e == kCellLit;  // uniform cell, or the descent ended in the top levels
+        if constexpr (NL >= 0) return descend_fixed<NL>(dag, words, cell, e, (int32_t)px, (int32_t)py, (int32_t)pz);
         off = e;
         level -= gt.depth;
     } else {
@@ -571,6 +603,7 @@ __global__ void k_grid_top_index_parents(const uint32_t* __restrict__ dag, uint3
 // 2^(dag_levels+grid_levels-1), its top bits select the cell, the cell word
 // holds the DAG offset or a uniform-cell sentinel; then the cell's descent
 // (grid_sample, with the grid top index when there is one).
+template <int NL>
 __global__ void __launch_bounds__(kThreads)
     k_grid_lookup(const uint32_t* __restrict__ dag, uint32_t words, const uint32_t* __restrict__ cells,
                   uint32_t length, int dag_levels, int grid_levels, bool leafmasks, GridTop gt,
@@ -585,7 +618,7 @@ __global__ void __launch_bounds__(kThreads)
         if (i < n) {
             const float* p = q + 3 * i;
             const int32_t px = quantise(__ldcs(p), scale), py = quantise(__ldcs(p + 1), scale), pz = quantise(__ldcs(p + 2), scale);
-            lit = grid_sample(dag, words, cells, length, dag_levels, leafmasks, gt, px, py, pz);
+            lit = grid_sample<NL>(dag, words, cells, length, dag_levels, leafmasks, gt, px, py, pz);
         }
         const uint32_t word = __ballot_sync(0xffffffffu, lit);
         if (lane == 0) __stcs(bits + w, word);
@@ -607,7 +640,7 @@ struct EvalMatrix {
     float m[16];
 };
 
-template <bool U8>
+template <bool U8, int NL>
 __global__ void __launch_bounds__(kThreads)
     k_grid_evaluate(const uint32_t* __restrict__ dag, uint32_t words, const uint32_t* __restrict__ cells,
                     uint32_t length, int dag_levels, int grid_levels, bool leafmasks, GridTop gt,
@@ -619,13 +652,36 @@ __global__ void __launch_bounds__(kThreads)
     const float scale = (float)((1u << (dag_levels + grid_levels - 1)) - 1u);
     const int lo = -((filter - 1) / 2), hi = filter / 2;
     const uint32_t f2 = (uint32_t)(filter * filter);
-    for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nwords; w += nw) {
+    // four floats per pixel on a 16-byte boundary: one load per position
+    const bool vec4 = fpp == 4 && (reinterpret_cast<uintptr_t>(pos) & 15u) == 0;
+    float nx = 0.f, ny = 0.f, nz = 0.f;
+    auto fetch = [&](uint64_t wq) {
+        const uint64_t iq = wq * 32 + (uint64_t)lane;
+        if (wq < nwords && iq < n) {
+            const float* p = pos + (size_t)fpp * iq;
+            if (vec4) {
+                const float4 v = __ldcs(reinterpret_cast<const float4*>(p));
+                nx = v.x;
+                ny = v.y;
+                nz = v.z;
+            } else {
+                nx = __ldcs(p);
+                ny = __ldcs(p + 1);
+                nz = __ldcs(p + 2);
+            }
+        }
+    };
+    uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    fetch(w);
+    for (; w < nwords; w += nw) {
         const uint64_t i = w * 32 + (uint64_t)lane;
+        // this pixel's position, then the next one's requested before this
+        // one descends
+        const float x = nx, y = ny, z = nz;
+        fetch(w + nw);
         bool lit = false;
         uint32_t cnt = 0;
         if (i < n) {
-            const float* p = pos + (size_t)fpp * i;
-            const float x = __ldcs(p), y = __ldcs(p + 1), z = __ldcs(p + 2);
             float c[4];
 #pragma unroll
             for (int r = 0; r < 4; ++r)
@@ -636,12 +692,13 @@ __global__ void __launch_bounds__(kThreads)
             const int64_t py = quantise(__fdiv_rn(c[1], c[3]), scale);
             const int64_t pz = quantise(__fdiv_rn(c[2], c[3]), scale);
             if (filter <= 1) {
-                lit = grid_sample(dag, words, cells, length, dag_levels, leafmasks, gt, px, py, pz);
+                lit = grid_sample<NL>(dag, words, cells, length, dag_levels, leafmasks, gt, px, py, pz);
                 cnt = lit ? 1u : 0u;
             } else {
                 for (int dy = lo; dy <= hi; ++dy)
                     for (int dx = lo; dx <= hi; ++dx)
-                        cnt += grid_sample(dag, words, cells, length, dag_levels, leafmasks, gt, px + dx, py + dy, pz)
+                        cnt += grid_sample<NL>(dag, words, cells, length, dag_levels, leafmasks, gt, px + dx,
+                                               py + dy, pz)
                                    ? 1u
                                    : 0u;
             }
@@ -889,11 +946,37 @@ int grid_top_depth(uint32_t length, uint32_t dag_levels, bool leafmasks, uint64_
     const int gl = log2_u32(length);
     int d = root - min_level + 1;
     if (d > kTopIndexDepth) d = kTopIndexDepth;
-    // no larger than the combined DAG (at least 64 KiB, at most 64 MiB)
-    uint64_t limit = words * 4 > 65536 ? words * 4 : 65536;
+    // no larger than 8x the combined DAG (at least 64 KiB, at most 64 MiB),
+    // as a shadow's own top grid: one more level in the index (8 instead of
+    // 7 for an 8192^2 map's 9.4 MB DAG) took a 4K frame's evaluate from
+    // 0.147 to 0.126 ms
+    uint64_t limit = words * 32 > 65536 ? words * 32 : 65536;
     if (limit > (64ull << 20)) limit = 64ull << 20;
     while (d > 0 && (uint64_t(4) << (3 * (gl + d))) > limit) --d;
     return d < 0 ? 0 : d;
+}
+
+// Inner levels below a grid index that the grid kernels unroll (0 ..
+// kFixedLevels), or -1: leafmask cell DAGs with an index only.
+int grid_fixed_levels(uint32_t dag_levels, bool leafmasks, const GridTop& gt) {
+    if (!leafmasks || !gt.top || gt.depth <= 0) return -1;
+    const int nl = (int)dag_levels - 2 - gt.depth - 3 + 1;
+    return nl >= 0 && nl <= kFixedLevels ? nl : -1;
+}
+
+// Calls f(std::integral_constant<int, nl>) for nl in [NL, kFixedLevels];
+// false when nl is outside.
+template <int NL, typename F>
+bool dispatch_levels(int nl, F&& f) {
+    if (nl == NL) {
+        f(std::integral_constant<int, NL>());
+        return true;
+    }
+    if constexpr (NL < kFixedLevels) {
+        return dispatch_levels<NL + 1>(nl, f);
+    } else {
+        return false;
+    }
 }
 
 cpvs_status launch_grid_top_index(const uint32_t* dag, uint64_t words, const uint32_t* cells, uint32_t length,
@@ -922,14 +1005,20 @@ cpvs_status launch_grid_evaluate(const uint32_t* dag, uint64_t words, const uint
     EvalMatrix M;
     for (int k = 0; k < 16; ++k) M.m[k] = light_view_proj[k];
     const uint32_t g = lookup_grid(device_sms(), n);
-    if (u8)
-        k_grid_evaluate<true><<<g, kThreads, 0, st>>>(dag, (uint32_t)words, cells, length, (int)dag_levels,
-                                                      log2_u32(length), leafmasks, gt, positions, fpp, n, M,
-                                                      (int)filter, out);
-    else
-        k_grid_evaluate<false><<<g, kThreads, 0, st>>>(dag, (uint32_t)words, cells, length, (int)dag_levels,
-                                                       log2_u32(length), leafmasks, gt, positions, fpp, n, M,
-                                                       (int)filter, out);
+    const int gl = log2_u32(length);
+    auto launch = [&](auto nlc) {
+        constexpr int NLv = decltype(nlc)::value;
+        if (u8)
+            k_grid_evaluate<true, NLv><<<g, kThreads, 0, st>>>(dag, (uint32_t)words, cells, length, (int)dag_levels,
+                                                               gl, leafmasks, gt, positions, fpp, n, M, (int)filter,
+                                                               out);
+        else
+            k_grid_evaluate<false, NLv><<<g, kThreads, 0, st>>>(dag, (uint32_t)words, cells, length,
+                                                                (int)dag_levels, gl, leafmasks, gt, positions, fpp, n,
+                                                                M, (int)filter, out);
+    };
+    if (!dispatch_levels<0>(grid_fixed_levels(dag_levels, leafmasks, gt), launch))
+        launch(std::integral_constant<int, -1>());
     CPVS_CUDA(cudaGetLastError());
     return CPVS_OK;
 }
@@ -941,8 +1030,13 @@ cpvs_status launch_grid_lookup(const uint32_t* dag, uint64_t words, const uint32
     KernelTimer kt(timing, K_GRID_LOOKUP, st);
     const GridTop gt{gtop, gtop ? gdepth : 0, (int)log2_u32(length) + (gtop ? gdepth : 0)};
     const uint32_t g = lookup_grid(device_sms(), n);
-    k_grid_lookup<<<g, kThreads, 0, st>>>(dag, (uint32_t)words, cells, length, (int)dag_levels, log2_u32(length),
-                                          leafmasks, gt, xyz, n, bits);
+    auto launch = [&](auto nlc) {
+        k_grid_lookup<decltype(nlc)::value><<<g, kThreads, 0, st>>>(dag, (uint32_t)words, cells, length,
+                                                                    (int)dag_levels, log2_u32(length), leafmasks, gt,
+                                                                    xyz, n, bits);
+    };
+    if (!dispatch_levels<0>(grid_fixed_levels(dag_levels, leafmasks, gt), launch))
+        launch(std::integral_constant<int, -1>());
     CPVS_CUDA(cudaGetLastError());
     return CPVS_OK;
 }
