@@ -13,8 +13,6 @@
 // memory with 16-byte loads, the rest in shared memory.  Three launches cover
 // an 8192^2 map (levels 1-6, 7-12, 13).  HBM-bound: the map is read once and
 // every pyramid texel written once.
-#include <algorithm>
-
 #include "common.cuh"
 
 namespace cpvs {
@@ -169,94 +167,6 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
-// k_pyramid64 as a persistent pipeline for a device map on a 16-byte
-// boundary: each block takes tiles t, t + gridDim.x, ... and copies the next
-// tile into shared memory (cp.async, 16 bytes per copy) while it reduces the
-// current one, so every block keeps a tile's loads in flight instead of
-// loading once and then only reducing.  Same outputs as k_pyramid64 (no map
-// copy: a device map is read where it lies).
-constexpr int kPipeTileFloats = 64 * 64;
-
-__device__ __forceinline__ void pipe_issue(float* dst, const float* __restrict__ in, uint32_t S, uint32_t tile) {
-    const uint32_t tiles_x = S >> 6;
-    const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
-    // 64 rows x 16 chunks of 16 bytes; 4 chunks per thread
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const uint32_t c = threadIdx.x + k * kThreads, row = c >> 4, col = (c & 15u) * 4u;
-        const float* g = in + (size_t)(ty * 64 + row) * S + tx * 64 + col;
-        const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst + row * 64 + col);
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(g) : "memory");
-    }
-    asm volatile("cp.async.commit_group;" ::: "memory");
-}
-
-__global__ void __launch_bounds__(kThreads)
-    k_pyramid64_pipe(const float* __restrict__ in, uint32_t S, float2* __restrict__ out, uint32_t n, int store_from,
-                     uint32_t* nan_flag) {
-    chain_enter();
-    extern __shared__ float4 pipe_smem[];
-    float* tile_buf = reinterpret_cast<float*>(pipe_smem);  // 2 tiles of 64 x 64 floats
-    __shared__ float2 buf0[32 * 32];
-    __shared__ float2 buf1[16 * 16];
-    const uint32_t tiles_x = S >> 6, ntiles = tiles_x * tiles_x;
-    int nan = 0;
-    uint32_t t = blockIdx.x;
-    if (t < ntiles) pipe_issue(tile_buf, in, S, t);
-    for (uint32_t k = 0; t < ntiles; ++k, t += gridDim.x) {
-        const uint32_t tn = t + gridDim.x;
-        if (tn < ntiles) {
-            pipe_issue(tile_buf + ((k + 1) & 1u) * kPipeTileFloats, in, S, tn);
-            asm volatile("cp.async.wait_group 1;" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
-        }
-        __syncthreads();  // every thread's copies of tile t have landed
-        const float* T = tile_buf + (k & 1u) * kPipeTileFloats;
-        const uint32_t tx = t % tiles_x, ty = t / tiles_x;
-        const uint32_t So1 = S >> 1;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const uint32_t pidx = threadIdx.x + h * kThreads;  // 512 texel pairs: 32 rows x 16
-            const uint32_t oy = pidx >> 4, px = pidx & 15u;
-            const float4 a = *reinterpret_cast<const float4*>(T + (2 * oy) * 64 + 4 * px);
-            const float4 b = *reinterpret_cast<const float4*>(T + (2 * oy + 1) * 64 + 4 * px);
-            const float2 v0 = make_float2(pmin(pmin(a.x, a.y), pmin(b.x, b.y)), pmax(pmax(a.x, a.y), pmax(b.x, b.y)));
-            const float2 v1 = make_float2(pmin(pmin(a.z, a.w), pmin(b.z, b.w)), pmax(pmax(a.z, a.w), pmax(b.z, b.w)));
-            nan |= (a.x != a.x) | (a.y != a.y) | (a.z != a.z) | (a.w != a.w) | (b.x != b.x) | (b.y != b.y) |
-                   (b.z != b.z) | (b.w != b.w);
-            if (store_from <= 1)
-                *reinterpret_cast<float4*>(out + (size_t)(ty * 32 + oy) * So1 + tx * 32 + 2 * px) =
-                    make_float4(v0.x, v0.y, v1.x, v1.y);
-            buf0[oy * 32 + 2 * px] = v0;
-            buf0[oy * 32 + 2 * px + 1] = v1;
-        }
-        uint32_t So = So1;
-        float2* src = buf0;
-        float2* nxt = buf1;
-#pragma unroll
-        for (int lvl = 2; lvl <= 6; ++lvl) {
-            __syncthreads();
-            const uint32_t h = 64u >> lvl, lh = 6 - lvl;
-            So >>= 1;
-            float2* dst = out + pyramid_level_offset_dev(n, lvl);
-            if (threadIdx.x < h * h) {
-                const uint32_t o = threadIdx.x, ox = o & (h - 1), oy = o >> lh, w = 2 * h;
-                const float2 a = src[(2 * oy) * w + 2 * ox], b = src[(2 * oy) * w + 2 * ox + 1];
-                const float2 c = src[(2 * oy + 1) * w + 2 * ox], d = src[(2 * oy + 1) * w + 2 * ox + 1];
-                const float2 v = make_float2(pmin(pmin(a.x, b.x), pmin(c.x, d.x)), pmax(pmax(a.y, b.y), pmax(c.y, d.y)));
-                if (lvl >= store_from) dst[(size_t)(ty * h + oy) * So + tx * h + ox] = v;
-                nxt[o] = v;
-            }
-            float2* tmp = src;
-            src = nxt;
-            nxt = tmp;
-        }
-        __syncthreads();  // the tile buffer and buf0/buf1 are reused by the next tile
-    }
-    if (nan_flag && __any_sync(0xffffffffu, nan) && (threadIdx.x & 31u) == 0) atomicOr(nan_flag, 1u);
-}
-
 // Partial-cell count of one texel for a z range [lo, hi): the cells z with
 // NOT(z+1 <= a) and NOT(z >= b), i.e. z in [floor(a), ceil(b)), where a and
 // b are the scaled min and max; a NaN bound excludes nothing (the
@@ -315,23 +225,7 @@ cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaS
         const uint32_t tiles = (S / T) * (S / T);
         // chained: each pass may be scheduled while the work before it in
         // the stream drains, and waits for it at its start
-        if (first && T == (uint32_t)kTile && !depth_copy && (reinterpret_cast<uintptr_t>(depth) & 15u) == 0) {
-            // a device map: the pipelined pass, one wave of persistent blocks
-            static int pipe_blocks = 0;  // resident blocks per SM (occupancy query, once)
-            constexpr size_t smem = 2 * kPipeTileFloats * sizeof(float);
-            if (!pipe_blocks) {
-                cudaFuncSetAttribute(k_pyramid64_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                int b = 0;
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pyramid64_pipe, kThreads, smem);
-                pipe_blocks = b > 0 ? b : 1;
-            }
-            int dev = 0, sms = 0;
-            cudaGetDevice(&dev);
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-            const uint32_t grid = (uint32_t)std::min<uint64_t>(tiles, (uint64_t)pipe_blocks * (sms > 0 ? sms : 1));
-            CPVS_CUDA(launch_kernel(k_pyramid64_pipe, grid, kThreads, smem, st, true, 0, depth, S, levels, n,
-                                    store_from, nan_flag));
-        } else if (first && T == (uint32_t)kTile)
+        if (first && T == (uint32_t)kTile)
             CPVS_CUDA(launch_kernel(k_pyramid64, tiles, kThreads, 0, st, true, 0, depth, S, levels, n, depth_copy,
                                     store_from, nan_flag));
         else if (first)

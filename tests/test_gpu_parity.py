@@ -30,6 +30,30 @@ def test_pyramid_matches_reference(cp, golden, golden_cases):
         assert np.array_equal(got.view(np.uint32), golden[f"{name}/pyramid"].view(np.uint32)), name
 
 
+def test_device_map_pyramid_equals_host_map_pyramid(cp):
+    """A map in device memory is reduced where it lies, a host map by the
+    pass that also copies it as it reads it: both give the same bits, signed
+    zeros, infinities and NaN included (the NaN flag too, through the DAG)."""
+    torch = pytest.importorskip("torch")
+    g = np.random.Generator(np.random.PCG64(17))
+    for n in (64, 128, 256, 1024, 4096):
+        d = g.random((n, n)).astype(np.float32)
+        k = max(n * n // 50, 4)
+        idx = g.integers(0, n * n, size=(4, k))
+        flat = d.reshape(-1)
+        flat[idx[0]] = -0.0
+        flat[idx[1]] = 0.0
+        flat[idx[2]] = np.inf if n % 2 == 0 else -np.inf
+        if n != 1024:
+            flat[idx[3]] = np.nan  # one size without NaN keeps the min/max shortcut on
+        host = hierarchy_levels(cp, cp.MinMaxHierarchy(d))
+        dev = hierarchy_levels(cp, cp.MinMaxHierarchy(torch.from_numpy(d).cuda()))
+        assert np.array_equal(host.view(np.uint32), dev.view(np.uint32)), n
+        a = cp.CompressedShadow.from_depth(d).get_dag()
+        b = cp.CompressedShadow.from_depth(torch.from_numpy(d).cuda()).get_dag()
+        assert np.array_equal(a, b), n
+
+
 def test_build_matches_reference(cp, golden, golden_cases):
     for key in golden_cases:
         name, zi, zn = split_key(key)
