@@ -767,7 +767,8 @@ def measure_batched(config: str, steps: int, warmup: int, cpu: bool = True) -> d
         q = torch.cat([qs, qu]).contiguous()
 
         def batched():
-            hs = [cp.MinMaxHierarchy(m, ctx=ctx, stream=stream, borrow=True) for m in maps]
+            # every tile's pyramid in one launch per pass, then one grid build
+            hs = cp.MinMaxHierarchy.create_batch(maps, ctx=ctx, stream=stream, borrow=True)
             grid = cp.CompressedShadowContainer(L, ctx=ctx)
             grid.build(hs, stream=stream)
             return grid
@@ -809,7 +810,8 @@ def measure_batched(config: str, steps: int, warmup: int, cpu: bool = True) -> d
         q = q.contiguous()
 
         def batched():
-            hs = [cp.MinMaxHierarchy(m, ctx=ctx, stream=stream, borrow=True) for m in maps]
+            # every light's pyramid in one launch per pass, then one batch build
+            hs = cp.MinMaxHierarchy.create_batch(maps, ctx=ctx, stream=stream, borrow=True)
             return cp.CompressedShadow.create_batch(hs, [(i, 0, 1) for i in range(len(hs))], stream=stream)
 
         def plain():

@@ -52,6 +52,7 @@ _SIGS = {
     "cpvs_ctx_set_option": (C.c_int, [_vp, C.c_int, C.c_int64]),
     "cpvs_ctx_get_option": (C.c_int64, [_vp, C.c_int]),
     "cpvs_ctx_last_build": (C.c_int, [_vp, _vp]),
+    "cpvs_hierarchy_create_batch": (C.c_int, [_vp, _vp, _vp, _u32, _u32, _vp, _vp]),
     "cpvs_ctx_enable_timing": (C.c_int, [_vp, C.c_int]),
     "cpvs_ctx_kernel_times": (C.c_int, [_vp, _vp, _vp, _u32, C.POINTER(_u32)]),
     "cpvs_kernel_name": (C.c_char_p, [_u32]),
@@ -398,6 +399,47 @@ class MinMaxHierarchy:
         self.handle = h.value
         self.n = n
         self._levels = {}
+
+    @classmethod
+    def create_batch(cls, maps, ctx: Optional[Context] = None, stream=None, borrow: bool = False) -> list:
+        """One hierarchy per map (cpvs_hierarchy_create_batch): the maps'
+        pyramids in one launch per pass.  `maps`: square power-of-two float32
+        maps, all numpy arrays or all CUDA tensors (`borrow` as in the
+        constructor)."""
+        ctx = ctx or Context.default()
+        maps = list(maps)
+        if not maps:
+            return []
+        dev = _is_device(maps[0])
+        if any(_is_device(m) != dev for m in maps):
+            raise ValueError("create_batch: maps must all be host arrays or all CUDA tensors")
+        keep = []
+        for m in maps:
+            n = int(m.shape[0])
+            if tuple(m.shape) != (n, n):
+                raise ValueError("depth map must be square")
+            if dev:
+                if not m.is_contiguous():
+                    raise ValueError("device depth map must be contiguous")
+                _checked(m, np.float32, n * n, "map", ctx.device)
+                keep.append(m)
+            else:
+                keep.append(_host_array(m, np.float32))
+        ptrs = (_vp * len(keep))(*[_ptr(m) for m in keep])
+        sides = (_u32 * len(keep))(*[int(m.shape[0]) for m in keep])
+        out = (_vp * len(keep))()
+        flags = (IO_DEVICE | (FLAG_BORROW_INPUT if borrow else 0)) if dev else 0
+        _check(_lib.cpvs_hierarchy_create_batch(ctx.handle, ptrs, sides, len(keep), flags, _stream(stream), out))
+        hs = []
+        for i, m in enumerate(keep):
+            h = cls.__new__(cls)
+            h.ctx = ctx
+            h._borrowed = m if (dev and borrow) else None
+            h.handle = out[i]
+            h.n = int(m.shape[0])
+            h._levels = {}
+            hs.append(h)
+        return hs
 
     def get_num_levels(self) -> int:
         return int(_lib.cpvs_hierarchy_num_levels(self.handle))

@@ -480,6 +480,66 @@ cpvs_status cpvs_hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n,
     return hierarchy_create(ctx, depth, n, flags, stream, 1, out);
 }
 
+cpvs_status cpvs_hierarchy_create_batch(cpvs_ctx* ctx, const float* const* depths, const uint32_t* sides,
+                                        uint32_t count, uint32_t flags, void* stream, cpvs_hierarchy** out) {
+    if (!ctx || (count && (!depths || !sides || !out)))
+        return fail(CPVS_ERR_INVALID_ARG, "hierarchy_create_batch: null argument");
+    for (uint32_t i = 0; i < count; ++i) out[i] = nullptr;
+    for (uint32_t i = 0; i < count; ++i) {
+        if (!depths[i]) return fail(CPVS_ERR_INVALID_ARG, "hierarchy_create_batch: null map " + std::to_string(i));
+        cpvs_status r = check_map_size(sides[i], 2);
+        if (r != CPVS_OK) return r;
+    }
+    cpvs_status r = set_device(ctx);
+    if (r != CPVS_OK || count == 0) return r;
+    cudaStream_t st = (cudaStream_t)stream;
+    cpvs::Ctx& c = ctx->c;
+    const bool dev = (flags & CPVS_IO_DEVICE) != 0, borrow = dev && (flags & CPVS_FLAG_BORROW_INPUT);
+    std::vector<cpvs_hierarchy*> hs;
+    std::vector<cpvs::PyramidMap> maps;
+    hs.reserve(count);
+    maps.reserve(count);
+    for (uint32_t i = 0; i < count && r == CPVS_OK; ++i) {
+        const uint32_t n = sides[i];
+        auto* h = new cpvs_hierarchy;
+        h->ctx = ctx;
+        h->n = n;
+        h->first_level = 1;
+        hs.push_back(h);
+        const uint64_t dbytes = (uint64_t)n * n * 4, lbytes = cpvs::pyramid_bytes(n);
+        if (borrow) {
+            h->depth = const_cast<float*>(depths[i]);
+            h->owns_depth = false;
+        } else {
+            r = c.alloc((void**)&h->depth, dbytes, true, st);
+            if (r == CPVS_OK) {
+                h->bytes += dbytes;
+                const cudaError_t e = cudaMemcpyAsync(h->depth, depths[i], dbytes,
+                                                      dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st);
+                if (e != cudaSuccess) r = cpvs::cuda_fail(e, "hierarchy_create_batch: map upload");
+            }
+        }
+        if (r == CPVS_OK) r = c.alloc((void**)&h->levels, lbytes, true, st);
+        if (r == CPVS_OK) {
+            h->bytes += lbytes;
+            maps.push_back(cpvs::PyramidMap{h->depth, n, h->levels, 1, cpvs::pyramid_nan_flag(h->levels, n)});
+        }
+    }
+    if (r == CPVS_OK) r = cpvs::launch_pyramid_batch(maps, st, &c.timing);
+    for (cpvs_hierarchy* h : hs) h->touch(st);
+    // host maps were copied from the caller's buffers: done before return
+    if (!dev || r != CPVS_OK) {
+        const cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess && r == CPVS_OK) r = cpvs::cuda_fail(e, "hierarchy_create_batch");
+    }
+    if (r != CPVS_OK) {
+        for (cpvs_hierarchy* h : hs) cpvs_hierarchy_destroy(h);
+        return r;
+    }
+    for (uint32_t i = 0; i < count; ++i) out[i] = hs[i];
+    return CPVS_OK;
+}
+
 
 void cpvs_hierarchy_destroy(cpvs_hierarchy* h) {
     if (!h) return;

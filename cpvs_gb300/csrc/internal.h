@@ -70,6 +70,16 @@ struct Timing;
 // `nan_flag` (optional): zeroed, then set when the map holds a NaN.
 cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaStream_t st, Timing* timing = nullptr,
                            float* depth_copy = nullptr, int store_from = 1, uint32_t* nan_flag = nullptr);
+// Many device maps' pyramids at once: pass k of every map in one launch
+// (up to three launches per 256 maps, plus one that zeroes the NaN flags).
+struct PyramidMap {
+    const float* depth;  // device, n x n
+    uint32_t n;
+    float2* levels;
+    int store_from;
+    uint32_t* nan_flag;
+};
+cpvs_status launch_pyramid_batch(const std::vector<PyramidMap>& maps, cudaStream_t st, Timing* timing = nullptr);
 
 // One z-tile of a source map whose per-level node bounds are wanted.
 struct BoundJob {

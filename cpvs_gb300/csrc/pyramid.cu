@@ -13,6 +13,8 @@
 // memory with 16-byte loads, the rest in shared memory.  Three launches cover
 // an 8192^2 map (levels 1-6, 7-12, 13).  HBM-bound: the map is read once and
 // every pyramid texel written once.
+#include <vector>
+
 #include "common.cuh"
 
 namespace cpvs {
@@ -30,15 +32,15 @@ constexpr int kThreads = 256;
 // `copy` (FROM_DEPTH only) the depth map is also written there as it is
 // read: a map in host memory that the GPU reads in place crosses the host
 // link once, while it is reduced, instead of in a separate copy first.
+// Tile `tile` of the pass, with the block's shared buffers buf0
+// ((kTile/2)^2 pairs) and buf1 ((kTile/4)^2 pairs).
 template <bool FROM_DEPTH>
-__global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ in, uint32_t S, float2* __restrict__ out,
-                                                      uint32_t n, int L0, uint32_t T, float* __restrict__ copy,
-                                                      int store_from, uint32_t* nan_flag) {
-    chain_enter();
-    __shared__ float2 buf0[(kTile / 2) * (kTile / 2)];
-    __shared__ float2 buf1[(kTile / 4) * (kTile / 4)];
+__device__ __forceinline__ void pyramid_tile(const void* __restrict__ in, uint32_t S, float2* __restrict__ out,
+                                             uint32_t n, int L0, uint32_t T, float* __restrict__ copy,
+                                             int store_from, uint32_t* nan_flag, uint32_t tile, float2* buf0,
+                                             float2* buf1) {
     const uint32_t tiles_x = S / T;
-    const uint32_t tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+    const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
 
     // first level: (T/2)^2 outputs of this tile
     uint32_t half = T / 2;
@@ -102,6 +104,16 @@ __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ i
     }
 }
 
+template <bool FROM_DEPTH>
+__global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ in, uint32_t S, float2* __restrict__ out,
+                                                      uint32_t n, int L0, uint32_t T, float* __restrict__ copy,
+                                                      int store_from, uint32_t* nan_flag) {
+    chain_enter();
+    __shared__ float2 buf0[(kTile / 2) * (kTile / 2)];
+    __shared__ float2 buf1[(kTile / 4) * (kTile / 4)];
+    pyramid_tile<FROM_DEPTH>(in, S, out, n, L0, T, copy, store_from, nan_flag, blockIdx.x, buf0, buf1);
+}
+
 // Levels 1-6 of a 64x64 tile straight from the depth map, with the tile
 // size fixed at compile time: each thread reduces two horizontally adjacent
 // level-1 texels per step from two 16-byte loads (one per input row) and
@@ -109,14 +121,11 @@ __global__ void __launch_bounds__(kThreads) k_pyramid(const void* __restrict__ i
 // contiguous bytes of each input row.  Levels 2-6 reduce in shared memory.
 // With `copy` the map is also written there as it is read; levels below
 // `store_from` stay in shared memory.
-__global__ void __launch_bounds__(kThreads)
-    k_pyramid64(const float* __restrict__ in, uint32_t S, float2* __restrict__ out, uint32_t n,
-                float* __restrict__ copy, int store_from, uint32_t* nan_flag) {
-    chain_enter();
-    __shared__ float2 buf0[32 * 32];
-    __shared__ float2 buf1[16 * 16];
+__device__ __forceinline__ void pyramid64_tile(const float* __restrict__ in, uint32_t S, float2* __restrict__ out,
+                                               uint32_t n, float* __restrict__ copy, int store_from,
+                                               uint32_t* nan_flag, uint32_t tile, float2* buf0, float2* buf1) {
     const uint32_t tiles_x = S >> 6;
-    const uint32_t tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+    const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
     int nan = 0;  // a NaN among the depths this thread read
     {
         const uint32_t So = S >> 1;
@@ -165,6 +174,58 @@ __global__ void __launch_bounds__(kThreads)
         src = nxt;
         nxt = t;
     }
+}
+
+__global__ void __launch_bounds__(kThreads)
+    k_pyramid64(const float* __restrict__ in, uint32_t S, float2* __restrict__ out, uint32_t n,
+                float* __restrict__ copy, int store_from, uint32_t* nan_flag) {
+    chain_enter();
+    __shared__ float2 buf0[32 * 32];
+    __shared__ float2 buf1[16 * 16];
+    pyramid64_tile(in, S, out, n, copy, store_from, nan_flag, blockIdx.x, buf0, buf1);
+}
+
+// Many maps' pyramids, one pass over all of them per launch: entry j of
+// the table covers tiles [first, next entry's first) of one map's pass.
+// The same per-tile code as k_pyramid64 / k_pyramid, so the bits are the
+// same as the maps' own passes.
+struct PyrPass {
+    const void* in;     // the map (FROM_DEPTH) or its level L0 - 1
+    float2* out;        // the map's pyramid
+    uint32_t* nan_flag;
+    uint32_t S, n, T, first;
+    int L0, store_from;
+};
+constexpr int kPyrBatch = 256;
+struct PyrPassTable {
+    PyrPass p[kPyrBatch];
+    uint32_t count;
+};
+
+template <bool FROM_DEPTH>
+__global__ void __launch_bounds__(kThreads) k_pyramid_batch(const __grid_constant__ PyrPassTable tab) {
+    chain_enter();
+    __shared__ float2 buf0[(kTile / 2) * (kTile / 2)];
+    __shared__ float2 buf1[(kTile / 4) * (kTile / 4)];
+    uint32_t lo = 0, hi = tab.count;  // the last entry whose first tile is <= blockIdx.x
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (tab.p[mid].first <= blockIdx.x) lo = mid; else hi = mid;
+    }
+    const PyrPass& P = tab.p[lo];
+    const uint32_t tile = blockIdx.x - P.first;
+    if (FROM_DEPTH && P.T == (uint32_t)kTile)
+        pyramid64_tile(static_cast<const float*>(P.in), P.S, P.out, P.n, nullptr, P.store_from, P.nan_flag, tile,
+                       buf0, buf1);
+    else
+        pyramid_tile<FROM_DEPTH>(P.in, P.S, P.out, P.n, P.L0, P.T, nullptr, P.store_from, P.nan_flag, tile, buf0,
+                                 buf1);
+}
+
+// Zeroes the maps' NaN flags before their first pass.
+__global__ void k_zero_flags(const __grid_constant__ PyrPassTable tab) {
+    for (uint32_t j = threadIdx.x; j < tab.count; j += blockDim.x)
+        if (tab.p[j].nan_flag) *tab.p[j].nan_flag = 0;
 }
 
 // Partial-cell count of one texel for a z range [lo, hi): the cells z with
@@ -238,6 +299,64 @@ cpvs_status launch_pyramid(const float* depth, uint32_t n, float2* levels, cudaS
         first = false;
         L0 += log2_u32(T);
         S /= T;
+    }
+    return CPVS_OK;
+}
+
+cpvs_status launch_pyramid_batch(const std::vector<PyramidMap>& maps, cudaStream_t st, Timing* timing) {
+    KernelTimer kt(timing, K_PYRAMID, st);
+    // per map its passes: (S, T, L0) while S > 1, as launch_pyramid runs them
+    struct MapPass {
+        uint32_t S, T;
+        int L0;
+    };
+    std::vector<std::vector<MapPass>> passes(maps.size());
+    size_t npass = 0;
+    for (size_t m = 0; m < maps.size(); ++m) {
+        uint32_t S = maps[m].n;
+        int L0 = 1;
+        while (S > 1) {
+            const uint32_t T = S < (uint32_t)kTile ? S : (uint32_t)kTile;
+            passes[m].push_back(MapPass{S, T, L0});
+            L0 += log2_u32(T);
+            S /= T;
+        }
+        npass = std::max(npass, passes[m].size());
+    }
+    // pass k of every map in launches of up to kPyrBatch maps
+    for (size_t m0 = 0; m0 < maps.size(); m0 += kPyrBatch) {
+        const size_t m1 = std::min(maps.size(), m0 + (size_t)kPyrBatch);
+        PyrPassTable flags{};
+        for (size_t m = m0; m < m1; ++m) flags.p[flags.count++].nan_flag = maps[m].nan_flag;
+        k_zero_flags<<<1, 256, 0, st>>>(flags);
+        CPVS_CUDA(cudaGetLastError());
+        for (size_t k = 0; k < npass; ++k) {
+            PyrPassTable tab{};
+            uint32_t tiles = 0;
+            for (size_t m = m0; m < m1; ++m) {
+                if (k >= passes[m].size()) continue;
+                const MapPass& q = passes[m][k];
+                PyrPass& P = tab.p[tab.count++];
+                P.in = k == 0 ? static_cast<const void*>(maps[m].depth)
+                              : static_cast<const void*>(maps[m].levels + pyramid_level_offset(maps[m].n, q.L0 - 1));
+                P.out = maps[m].levels;
+                P.nan_flag = k == 0 ? maps[m].nan_flag : nullptr;
+                P.S = q.S;
+                P.n = maps[m].n;
+                P.T = q.T;
+                P.L0 = q.L0;
+                // the first pass stores from the map's first stored level;
+                // later passes read their predecessor's last level, stored
+                P.store_from = maps[m].store_from;
+                P.first = tiles;
+                tiles += (q.S / q.T) * (q.S / q.T);
+            }
+            if (!tab.count) continue;
+            if (k == 0)
+                CPVS_CUDA(launch_kernel(k_pyramid_batch<true>, tiles, kThreads, 0, st, true, 0, tab));
+            else
+                CPVS_CUDA(launch_kernel(k_pyramid_batch<false>, tiles, kThreads, 0, st, true, 0, tab));
+        }
     }
     return CPVS_OK;
 }

@@ -141,6 +141,15 @@ CPVS_API int cpvs_abi_version(void);
  * depth map is copied; the caller's buffer may be reused on return. */
 CPVS_API cpvs_status cpvs_hierarchy_create(cpvs_ctx* ctx, const float* depth, uint32_t n, uint32_t flags, void* stream,
                                   cpvs_hierarchy** out);
+/* `count` hierarchies at once, map i of side sides[i] (sides may differ):
+ * the same pyramids as cpvs_hierarchy_create per map, from one launch per
+ * pyramid pass over every map's tiles (at most three per 256 maps) instead
+ * of up to three per map -- the many-lights case, where the maps' own
+ * launches dominate small maps.  flags: CPVS_IO_DEVICE (maps in device
+ * memory), CPVS_FLAG_BORROW_INPUT with it (read in place; the maps must
+ * outlive the hierarchies).  On failure no hierarchy is returned. */
+CPVS_API cpvs_status cpvs_hierarchy_create_batch(cpvs_ctx* ctx, const float* const* depths, const uint32_t* sides,
+                                                 uint32_t count, uint32_t flags, void* stream, cpvs_hierarchy** out);
 CPVS_API void cpvs_hierarchy_destroy(cpvs_hierarchy* h);
 /* numLevels including the depth map itself (MinMaxHierarchy::getNumLevels,
  * src/MinMaxHierarchy.h:60-62). */

@@ -58,6 +58,7 @@ def test_null_arguments_are_rejected(lib):
     import ctypes as C
     h = C.c_void_p()
     assert lib.cpvs_hierarchy_create(None, None, 64, 0, None, C.byref(h)) == 1
+    assert lib.cpvs_hierarchy_create_batch(None, None, None, 2, 0, None, C.byref(h)) == 1
     assert lib.cpvs_shadow_create(None, None, 0, 1, 1, None, C.byref(h)) == 1
     assert lib.cpvs_grid_create(None, 4, C.byref(h)) == 1
     assert b"null" in lib.cpvs_last_error()

@@ -54,6 +54,36 @@ def test_device_map_pyramid_equals_host_map_pyramid(cp):
         assert np.array_equal(a, b), n
 
 
+def test_hierarchy_batch_equals_single_hierarchies(cp):
+    """cpvs_hierarchy_create_batch over maps of many sides (one launch per
+    pass for all of them) gives each map the pyramid of its own
+    cpvs_hierarchy_create, bit for bit, from host or device maps, and the
+    same DAGs (so the same NaN flags)."""
+    torch = pytest.importorskip("torch")
+    g = np.random.Generator(np.random.PCG64(23))
+    sides = [2, 4, 8, 16, 32, 64, 128, 256, 512, 1024, 2048, 64, 8, 256]
+    maps = []
+    for i, n in enumerate(sides):
+        d = g.random((n, n)).astype(np.float32)
+        flat = d.reshape(-1)
+        k = max(n * n // 40, 1)
+        flat[g.integers(0, n * n, k)] = (-0.0, 0.0, np.inf, -np.inf, np.nan)[i % 5]
+        maps.append(d)
+    single = [hierarchy_levels(cp, cp.MinMaxHierarchy(d)) for d in maps]
+    for kind in ("host", "device", "borrow"):
+        src = maps if kind == "host" else [torch.from_numpy(d).cuda() for d in maps]
+        hs = cp.MinMaxHierarchy.create_batch(src, borrow=kind == "borrow")
+        assert len(hs) == len(maps)
+        for i, h in enumerate(hs):
+            assert h.get_num_levels() == int(np.log2(sides[i])) + 1
+            assert np.array_equal(hierarchy_levels(cp, h).view(np.uint32), single[i].view(np.uint32)), (kind, i)
+        big = [i for i, n in enumerate(sides) if n >= 8]
+        batch = cp.CompressedShadow.create_batch([hs[i] for i in big], [(j, 0, 1) for j in range(len(big))])
+        for j, i in enumerate(big):
+            want = cp.CompressedShadow.create(cp.MinMaxHierarchy(maps[i])).get_dag()
+            assert np.array_equal(batch[j].get_dag(), want), (kind, i)
+
+
 def test_build_matches_reference(cp, golden, golden_cases):
     for key in golden_cases:
         name, zi, zn = split_key(key)
