@@ -376,13 +376,19 @@ struct cpvs_server {
         }
         std::vector<cpvs_hierarchy*> hs;
         std::vector<Req> ok;
+        // each request keeps its map until it completes, so the pyramids'
+        // reads of the maps are waited for once, after the batch build
+        std::vector<cudaEvent_t> reads;
         for (const Req& r : batch) {
             cpvs_hierarchy* h = nullptr;
-            const cpvs_status st = cpvs::hierarchy_create_for_build(ctx, r->depth, r->n, 0, cfg.flags, s_build, &h);
+            cudaEvent_t read = nullptr;
+            const cpvs_status st =
+                cpvs::hierarchy_create_for_build(ctx, r->depth, r->n, 0, cfg.flags, s_build, &h, &read);
             if (st != CPVS_OK) {
                 complete(r, st, cpvs_last_error());
                 continue;
             }
+            if (read) reads.push_back(read);
             hs.push_back(h);
             ok.push_back(r);
         }
@@ -393,6 +399,10 @@ struct cpvs_server {
         const cpvs_status st = cpvs_shadow_create_batch(ctx, hs.data(), (uint32_t)hs.size(), jobs.data(),
                                                         (uint32_t)jobs.size(), cfg.flags, s_build, out.data());
         const std::string msg = st == CPVS_OK ? "" : cpvs_last_error();
+        for (cudaEvent_t e : reads) {
+            cudaEventSynchronize(e);
+            cudaEventDestroy(e);
+        }
         for (cpvs_hierarchy* h : hs) cpvs_hierarchy_destroy(h);
         if (st != CPVS_OK) {
             for (const Req& r : ok) complete(r, st, msg);
