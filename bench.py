@@ -230,7 +230,7 @@ def run_ours(args, rank, world, local_rank):
             torch.distributed.barrier()
         torch.cuda.synchronize(dev)
 
-    if args.part in ("grid", "multi", "serve", "raster"):
+    if args.part in ("grid", "multi", "serve", "raster", "batch"):
         profile_part(args.part, cp, torch, ctx, dev, stream, args.warmup + args.steps)
         return
     if args.part == "frame":
@@ -507,7 +507,9 @@ def profile_part(part, cp, torch, ctx, dev, stream, reps):
               (k_top_index per DAG, k_multi_lookup);
     serve  -- 64 lookup requests of 2^18 points through a server holding 4
               DAGs, in one segmented launch each round (k_segment_lookup);
-    raster -- the c1 scene rasterised to an 8192^2 depth map (k_raster)."""
+    raster -- the c1 scene rasterised to an 8192^2 depth map (k_raster);
+    batch  -- 16 of the c3 lights' hierarchies in one batched call, then one
+              batch build (k_zero_flags, k_pyramid_batch)."""
     gen = torch.Generator(device=dev)
     gen.manual_seed(11)
     if part == "raster":
@@ -525,6 +527,13 @@ def profile_part(part, cp, torch, ctx, dev, stream, reps):
         out = torch.empty((1 << 24) // 32, dtype=torch.int32, device=dev)
         for _ in range(reps):
             grid.lookup_ndc(q, out, stream=stream)
+    elif part == "batch":
+        # 16 of the c3 lights: their hierarchies in one batched call, then
+        # one batch build
+        maps = [cp.raster_depth(s, ctx=ctx) for s in c3_scenes()[:16]]
+        for _ in range(reps):
+            hs = cp.MinMaxHierarchy.create_batch(maps, ctx=ctx, stream=stream, borrow=True)
+            cp.CompressedShadow.create_batch(hs, [(i, 0, 1) for i in range(len(hs))], stream=stream)
     elif part == "multi":
         scs = c3_scenes()[:16]
         maps = [cp.raster_depth(s, ctx=ctx) for s in scs]
@@ -1053,7 +1062,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="c1 line without the batched (c3), grid (c2) and served (c4) measurements")
-    ap.add_argument("--part", choices=("all", "build", "lookup", "frame", "grid", "multi", "serve", "raster"),
+    ap.add_argument("--part", choices=("all", "build", "lookup", "frame", "grid", "multi", "serve", "raster", "batch"),
                     default="all",
                     help="profiling aid: run one part alone (no contract line); see profile_part")
     ap.add_argument("--fixed-shapes", action="store_true",
