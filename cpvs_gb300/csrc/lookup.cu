@@ -18,11 +18,15 @@
 // z: the node offset the descent reaches after those levels, or a lit /
 // shadow sentinel.  It lives in global memory (L2-resident; up to 8 levels,
 // at most 8x the DAG's size), so one load replaces up to 8 dependent hops --
-// and each thread carries Q independent queries (Q picked per DAG depth by
-// timing Q = 1, 2, 4 on the first batch).  Query points and answer words are
-// touched once, so they go through the caches evict-first (ld/st .cs): a
-// batch streams hundreds of MB past L2 and would otherwise push the DAG and
-// its top grid out of it.
+// and each thread carries Q independent queries (Q picked per DAG depth and
+// input kind, device or host memory, by timing Q = 1, 2, 4 on the first
+// batch).  A leafmask DAG with a top grid and few levels below it takes
+// k_lookup_fixed (the levels unrolled, 32-bit indices); any other DAG
+// k_lookup.  Query points and answer words are touched once, so they go
+// through the caches evict-first (ld/st .cs): a batch streams hundreds of MB
+// past L2 and would otherwise push the DAG and its top grid out of it.  The
+// grid lookups and evaluate (k_grid_lookup, k_grid_evaluate) route through
+// the grid's cells and a grid index the same way.
 #include <algorithm>
 #include <type_traits>
 
