@@ -406,18 +406,19 @@ class MinMaxHierarchy:
         pyramids in one launch per pass.  `maps`: square power-of-two float32
         maps, all numpy arrays or all CUDA tensors (`borrow` as in the
         constructor)."""
-        ctx = ctx or Context.default()
         maps = list(maps)
         if not maps:
             return []
         dev = _is_device(maps[0])
         if any(_is_device(m) != dev for m in maps):
             raise ValueError("create_batch: maps must all be host arrays or all CUDA tensors")
+        for m in maps:
+            if len(m.shape) != 2 or m.shape[0] != m.shape[1]:
+                raise ValueError("depth map must be square")
+        ctx = ctx or Context.default()
         keep = []
         for m in maps:
             n = int(m.shape[0])
-            if tuple(m.shape) != (n, n):
-                raise ValueError("depth map must be square")
             if dev:
                 if not m.is_contiguous():
                     raise ValueError("device depth map must be contiguous")

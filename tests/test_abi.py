@@ -103,6 +103,27 @@ def test_python_buffers_are_checked_before_the_call():
         _checked(torch.zeros(4, 4)[:, 1], np.float32, 4, "t")
 
 
+def test_hierarchy_batch_checks_maps_before_any_device_work():
+    """MinMaxHierarchy.create_batch refuses non-square maps before it touches
+    a context; an empty batch is empty."""
+    import numpy as np
+    import cpvs_gb300 as cp
+    assert cp.MinMaxHierarchy.create_batch([]) == []
+    with pytest.raises(ValueError, match="square"):
+        cp.MinMaxHierarchy.create_batch([np.zeros((8, 8), np.float32), np.zeros((4, 8), np.float32)])
+    with pytest.raises(ValueError, match="square"):
+        cp.MinMaxHierarchy.create_batch([np.zeros(16, np.float32)])
+
+
+@pytest.mark.gpu
+def test_hierarchy_batch_refuses_mixed_host_and_device_maps():
+    import numpy as np
+    import torch
+    import cpvs_gb300 as cp
+    with pytest.raises(ValueError, match="all host arrays or all CUDA tensors"):
+        cp.MinMaxHierarchy.create_batch([np.zeros((8, 8), np.float32), torch.zeros((8, 8), device="cuda")])
+
+
 def test_every_entry_point_refuses_null_handles(lib):
     """Every entry point called with null handles and pointers (sizes 1)
     returns CPVS_ERR_INVALID_ARG, or a neutral value for the queries, without
