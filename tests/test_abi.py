@@ -120,7 +120,7 @@ def test_hierarchy_batch_refuses_mixed_host_and_device_maps():
     import numpy as np
     import torch
     import cpvs_gb300 as cp
-    with pytest.raises(ValueError, match="all host arrays or all CUDA tensors"):
+    with pytest.raises(ValueError, match="host arrays or all CUDA tensors"):
         cp.MinMaxHierarchy.create_batch([np.zeros((8, 8), np.float32), torch.zeros((8, 8), device="cuda")])
 
 
