@@ -1029,16 +1029,20 @@ cpvs_status cpvs_grid_build(cpvs_grid* g, const cpvs_hierarchy* const* xy_tiles,
         const uint32_t m = shadows[i]->root_mask;
         cellw[i] = (m == 0u) ? 0xFFFFFFFFu : (m == 0x5555u ? 0xFFFFFFFEu : (uint32_t)offsets[i]);
     }
+    // the new cell words are allocated before the old cells go, so that a
+    // failed build leaves the grid (and every handle to its cells) as it was
+    uint32_t* cell_words = nullptr;
+    r = g->ctx->c.alloc((void**)&cell_words, g->cells.size() * 4, true, st);
+    if (r != CPVS_OK) {
+        for (auto* sh : shadows) cpvs_shadow_destroy(sh);
+        return r;
+    }
     for (auto*& c : g->cells) {
         cpvs_shadow_destroy(c);
         c = nullptr;
     }
     grid_release_device(g);
-    r = g->ctx->c.alloc((void**)&g->cell_words, g->cells.size() * 4, true, st);
-    if (r != CPVS_OK) {
-        for (auto* sh : shadows) cpvs_shadow_destroy(sh);
-        return r;
-    }
+    g->cell_words = cell_words;
     CPVS_CUDA(cudaMemcpyAsync(g->cell_words, cellw.data(), cellw.size() * 4, cudaMemcpyHostToDevice, st));
     g->block = block;
     block->refs++;

@@ -122,6 +122,36 @@ public:
     MinMaxHierarchy(const MinMaxHierarchy&) = delete;
     MinMaxHierarchy& operator=(const MinMaxHierarchy&) = delete;
 
+    /* One hierarchy per map (cpvs_hierarchy_create_batch): every map's
+     * pyramid in one launch per pass, the many-lights case.  Each image is
+     * square with one channel; sides may differ. */
+    static std::vector<std::unique_ptr<MinMaxHierarchy>> createBatch(const std::vector<const ImageF*>& maps,
+                                                                     Context& ctx = Context::shared()) {
+        std::vector<const float*> depths;
+        std::vector<uint32_t> sides;
+        for (const ImageF* m : maps) {
+            if (!m || m->getWidth() != m->getHeight() || m->getNumChannels() != 1)
+                throw Error(CPVS_ERR_INVALID_ARG,
+                            "MinMaxHierarchy::createBatch: every image must be square with one channel");
+            depths.push_back(m->data());
+            sides.push_back((uint32_t)m->getWidth());
+        }
+        std::vector<std::unique_ptr<MinMaxHierarchy>> out;
+        if (maps.empty()) return out;
+        std::vector<cpvs_hierarchy*> hs(maps.size(), nullptr);
+        check(cpvs_hierarchy_create_batch(ctx.get(), depths.data(), sides.data(), (uint32_t)maps.size(), 0, nullptr,
+                                          hs.data()));
+        size_t i = 0;
+        try {
+            out.reserve(maps.size());
+            for (; i < maps.size(); ++i) out.emplace_back(new MinMaxHierarchy(hs[i], *maps[i], ctx));
+        } catch (...) {
+            for (; i < maps.size(); ++i) cpvs_hierarchy_destroy(hs[i]);
+            throw;
+        }
+        return out;
+    }
+
     float getMin(size_t level, size_t x, size_t y) const { return texel(level, x, y, 0); }
     float getMax(size_t level, size_t x, size_t y) const { return texel(level, x, y, 1); }
     int getNumLevels() const { return (int)cpvs_hierarchy_num_levels(m_h); }
@@ -130,6 +160,11 @@ public:
     Context& context() const { return *m_ctx; }
 
 private:
+    /* Takes ownership of h, built from orig, once constructed (createBatch
+     * destroys h if this throws); the copy of orig answers level 0. */
+    MinMaxHierarchy(cpvs_hierarchy* h, const ImageF& orig, Context& ctx) : m_ctx(&ctx), m_h(h) {
+        m_depth.assign(orig.data(), orig.data() + orig.getWidth() * orig.getHeight());
+    }
     float texel(size_t level, size_t x, size_t y, int channel) const {
         const uint32_t n = cpvs_hierarchy_size(m_h);
         if (level == 0) return m_depth[y * n + x];
@@ -169,6 +204,36 @@ public:
         check(cpvs_shadow_create_from_depth(ctx.get(), depth.data(), (uint32_t)depth.getWidth(), zTileIndex,
                                             zTileNum, leafmasks ? CPVS_FLAG_LEAFMASKS : 0u, nullptr, &s));
         return std::unique_ptr<CompressedShadow>(new CompressedShadow(s));
+    }
+    /* Many DAGs in one batch (cpvs_shadow_create_batch): DAG j is z-tile
+     * jobs[j].z_tile_index of jobs[j].z_tile_num of sources[jobs[j].source],
+     * equal to what create() builds for it.  The sources share one context. */
+    static std::vector<std::unique_ptr<CompressedShadow>> createBatch(
+        const std::vector<const MinMaxHierarchy*>& sources, const std::vector<cpvs_build_job>& jobs,
+        bool leafmasks = true) {
+        std::vector<std::unique_ptr<CompressedShadow>> out;
+        if (jobs.empty()) return out;
+        if (sources.empty()) throw Error(CPVS_ERR_INVALID_ARG, "CompressedShadow::createBatch: no sources");
+        std::vector<const cpvs_hierarchy*> hs;
+        for (const MinMaxHierarchy* m : sources) {
+            if (!m) throw Error(CPVS_ERR_INVALID_ARG, "CompressedShadow::createBatch: null source");
+            if (&m->context() != &sources[0]->context())
+                throw Error(CPVS_ERR_INVALID_ARG, "CompressedShadow::createBatch: sources differ in context");
+            hs.push_back(m->handle());
+        }
+        std::vector<cpvs_shadow*> s(jobs.size(), nullptr);
+        check(cpvs_shadow_create_batch(sources[0]->context().get(), hs.data(), (uint32_t)hs.size(), jobs.data(),
+                                       (uint32_t)jobs.size(), leafmasks ? CPVS_FLAG_LEAFMASKS : 0u, nullptr,
+                                       s.data()));
+        size_t j = 0;
+        try {
+            out.reserve(jobs.size());
+            for (; j < jobs.size(); ++j) out.emplace_back(new CompressedShadow(s[j]));
+        } catch (...) {
+            for (; j < jobs.size(); ++j) cpvs_shadow_destroy(s[j]);
+            throw;
+        }
+        return out;
     }
     ~CompressedShadow() {
         if (m_owned) cpvs_shadow_destroy(m_s);
@@ -238,6 +303,22 @@ public:
     /* Drops the host-side handles; get() then returns NULL. */
     void freeOnCPU() {
         for (auto& p : m_data) p.reset();
+    }
+    /* Builds every cell in one batch and finalizes the grid (cpvs_grid_build):
+     * cell (x,y,z) is z-tile z of length of xyTiles[y*length+x], tiles of one
+     * size.  It replaces the cells set before, so get() returns NULL for every
+     * cell afterwards, as after moveToGPU().  A build refused by its checks or
+     * short of memory leaves the cells as they were. */
+    void build(const std::vector<const MinMaxHierarchy*>& xyTiles, bool leafmasks = true) {
+        if (xyTiles.size() != (size_t)m_length * m_length)
+            throw Error(CPVS_ERR_INVALID_ARG, "CompressedShadowContainer::build: needs length^2 xy tiles");
+        std::vector<const cpvs_hierarchy*> hs;
+        for (const MinMaxHierarchy* m : xyTiles) {
+            if (!m) throw Error(CPVS_ERR_INVALID_ARG, "CompressedShadowContainer::build: null tile");
+            hs.push_back(m->handle());
+        }
+        check(cpvs_grid_build(m_g, hs.data(), leafmasks ? CPVS_FLAG_LEAFMASKS : 0u, nullptr));
+        freeOnCPU();  // the grid destroyed the cells' previous DAGs
     }
     void copyToGPU() { check(cpvs_grid_finalize(m_g, 0, nullptr)); }
     void moveToGPU() {
