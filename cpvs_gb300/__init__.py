@@ -539,6 +539,11 @@ class CompressedShadow:
         """Many DAGs in one batch.  `sources`: MinMaxHierarchy list; `jobs`:
         (source index, z_tile_index, z_tile_num) per DAG.  Returns one
         CompressedShadow per job."""
+        sources, jobs = list(sources), list(jobs)
+        if not jobs:
+            return []
+        if not sources:
+            raise ValueError("create_batch: no sources")
         ctx = sources[0].ctx
         hs = (_vp * len(sources))(*[m.handle for m in sources])
         jb = (_BuildJob * len(jobs))(*[_BuildJob(*j) for j in jobs])
@@ -717,6 +722,9 @@ class CompressedShadowContainer:
     def build(self, xy_tiles, leafmasks: bool = True, stream=None):
         """Builds every cell in one batch: cell (x,y,z) = z-tile z of
         xy_tiles[y*length+x] (MinMaxHierarchy objects of one size)."""
+        xy_tiles = list(xy_tiles)
+        if len(xy_tiles) != self.length ** 2:
+            raise ValueError(f"build: needs length^2 = {self.length ** 2} xy tiles, got {len(xy_tiles)}")
         hs = (_vp * len(xy_tiles))(*[m.handle for m in xy_tiles])
         _check(_lib.cpvs_grid_build(self.handle, hs, FLAG_LEAFMASKS if leafmasks else 0, _stream(stream)))
         self._release_cells()  # the grid destroyed the cells' previous shadows

@@ -115,6 +115,19 @@ def test_hierarchy_batch_checks_maps_before_any_device_work():
         cp.MinMaxHierarchy.create_batch([np.zeros(16, np.float32)])
 
 
+def test_batch_builds_check_their_lists_before_any_device_work():
+    """cpvs_grid_build reads length^2 tile handles with no count beside them,
+    so the Python mirror checks the count itself; a shadow batch with no jobs
+    is empty and one with no sources is refused."""
+    import types
+    import cpvs_gb300 as cp
+    with pytest.raises(ValueError, match=r"length\^2 = 4 xy tiles, got 3"):
+        cp.CompressedShadowContainer.build(types.SimpleNamespace(length=2), [object()] * 3)
+    assert cp.CompressedShadow.create_batch([], []) == []
+    with pytest.raises(ValueError, match="no sources"):
+        cp.CompressedShadow.create_batch([], [(0, 0, 1)])
+
+
 @pytest.mark.gpu
 def test_hierarchy_batch_refuses_mixed_host_and_device_maps():
     import numpy as np
