@@ -863,16 +863,27 @@ class Server:
         self._keep = {}  # ticket -> buffers that must outlive it
 
     def submit_build(self, key: int, depth) -> int:
-        d = _host_array(depth, np.float32)
+        """Queues a build of the square host map `depth` into DAG `key`."""
+        if _is_device(depth):
+            raise ValueError("submit_build: the depth map must be in host memory")
+        if len(depth.shape) != 2 or depth.shape[0] != depth.shape[1]:
+            raise ValueError("depth map must be square")
+        n = int(depth.shape[0])
+        d = _checked(_host_array(depth, np.float32), np.float32, n * n, "depth")
         t = C.c_uint64()
-        _check(_lib.cpvs_server_submit_build(self.handle, key, _ptr(d), int(depth.shape[0]), C.byref(t)))
+        _check(_lib.cpvs_server_submit_build(self.handle, key, _ptr(d), n, C.byref(t)))
         self._keep[t.value] = (d,)
         return t.value
 
     def submit_lookup(self, key: int, points, out=None) -> int:
-        pts = _host_array(points, np.float32)
+        """Queues a lookup of the (n, 3) host points in DAG `key`; `out`, if
+        given, is a host uint32 buffer of at least ceil(n/32) words."""
+        if _is_device(points) or (out is not None and _is_device(out)):
+            raise ValueError("submit_lookup: points and out must be in host memory")
         n = int(points.shape[0])
+        pts = _checked(_host_array(points, np.float32), np.float32, 3 * n, "points")
         words = out if out is not None else np.zeros(max((n + 31) // 32, 1), np.uint32)
+        _checked(words, np.uint32, (n + 31) // 32, "out")
         t = C.c_uint64()
         _check(_lib.cpvs_server_submit_lookup(self.handle, key, _ptr(pts), n, _ptr(words), C.byref(t)))
         self._keep[t.value] = (pts, words, n)

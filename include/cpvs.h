@@ -322,7 +322,9 @@ CPVS_API cpvs_status cpvs_grid_finalize(cpvs_grid* g, int release_cells, void* s
 /* Builds every cell of the grid in one batch and finalizes it: cell
  * (x,y,z) is z-tile z of length of the xy tile hierarchy xy_tiles[y*length+x]
  * (the reference's tiled precompute, src/DeferredRenderer.cpp:150-187, and
- * copyToGPU).  Replaces any cells set before; tiles must share one size. */
+ * copyToGPU).  xy_tiles holds exactly length^2 handles (the call has no count
+ * to check it against).  Replaces any cells set before, once the build has
+ * succeeded; tiles must share one size. */
 CPVS_API cpvs_status cpvs_grid_build(cpvs_grid* g, const cpvs_hierarchy* const* xy_tiles, uint32_t flags,
                                      void* stream);
 /* Size in words of the concatenated DAG, and its copy (after finalize). */

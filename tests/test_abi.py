@@ -128,6 +128,24 @@ def test_batch_builds_check_their_lists_before_any_device_work():
         cp.CompressedShadow.create_batch([], [(0, 0, 1)])
 
 
+def test_server_checks_its_buffers_before_any_device_work():
+    """The server reads the map and points and writes the bits after submit
+    returns, from its own thread, so a buffer too small for the request is
+    refused at submission."""
+    import types
+    import numpy as np
+    import cpvs_gb300 as cp
+    srv = types.SimpleNamespace(handle=None, _keep={})
+    with pytest.raises(ValueError, match="square"):
+        cp.Server.submit_build(srv, 0, np.zeros((4, 8), np.float32))
+    with pytest.raises(ValueError, match="points"):
+        cp.Server.submit_lookup(srv, 0, np.zeros((64, 2), np.float32))
+    with pytest.raises(ValueError, match="out: 1 elements, at least 2"):
+        cp.Server.submit_lookup(srv, 0, np.zeros((64, 3), np.float32), np.zeros(1, np.uint32))
+    with pytest.raises(ValueError, match="integers"):
+        cp.Server.submit_lookup(srv, 0, np.zeros((64, 3), np.float32), np.zeros(2, np.float32))
+
+
 @pytest.mark.gpu
 def test_hierarchy_batch_refuses_mixed_host_and_device_maps():
     import numpy as np
