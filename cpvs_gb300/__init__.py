@@ -363,11 +363,12 @@ def raster_triangles(tris, n: int, plane: float, x0: int = 0, y0: int = 0, w: Op
     m = int(tris.shape[0])
     if _is_device(tris):
         import torch
+        _checked(tris, np.float32, 9 * m, "tris", ctx.device)
         out = torch.empty((h, w), dtype=torch.float32, device=tris.device)
         _check(_lib.cpvs_raster_triangles(ctx.handle, _ptr(tris) if m else None, m, float(plane), n, x0, y0, w, h,
                                           _ptr(out), IO_DEVICE, _stream(stream)))
         return out
-    t = np.ascontiguousarray(tris, np.float32)
+    t = _checked(np.ascontiguousarray(tris, np.float32), np.float32, 9 * m, "tris")
     out = np.empty((h, w), np.float32)
     _check(_lib.cpvs_raster_triangles(ctx.handle, t.ctypes.data if m else None, m, float(plane), n, x0, y0, w, h,
                                       out.ctypes.data, 0, _stream(stream)))
@@ -390,8 +391,8 @@ class MinMaxHierarchy:
         dev = _is_device(depth)
         if not dev:
             depth = _host_array(depth, np.float32)
-        elif not depth.is_contiguous():
-            raise ValueError("device depth map must be contiguous")
+        else:
+            _checked(depth, np.float32, n * n, "depth", self.ctx.device)
         flags = (IO_DEVICE | (FLAG_BORROW_INPUT if borrow else 0)) if dev else 0
         self._borrowed = depth if (dev and borrow) else None
         h = _vp()
@@ -498,10 +499,14 @@ class CompressedShadow:
     def from_depth(depth, z_tile_index: int = 0, z_tile_num: int = 1, leafmasks: bool = True,
                    ctx: Optional[Context] = None, stream=None) -> "CompressedShadow":
         """CompressedShadow::create(const ShadowMap*, ...): depth map -> DAG."""
-        ctx = ctx or Context.default()
         n = int(depth.shape[0])
+        if tuple(depth.shape) != (n, n):
+            raise ValueError("depth map must be square")
+        ctx = ctx or Context.default()
         dev = _is_device(depth)
-        if not dev:
+        if dev:
+            _checked(depth, np.float32, n * n, "depth", ctx.device)
+        else:
             depth = _host_array(depth, np.float32)
         flags = (FLAG_LEAFMASKS if leafmasks else 0) | (IO_DEVICE if dev else 0)
         h = _vp()
@@ -615,7 +620,8 @@ class CompressedShadow:
             _checked(out, np.int32, (n + 31) // 32, "out", self.ctx.device)
             _check(fn(self.handle, _ptr(points), n, _ptr(out), IO_DEVICE, _stream(stream)))
             return out
-        pts = np.ascontiguousarray(points, np.float32 if ndc else np.int32)
+        pts = _checked(np.ascontiguousarray(points, np.float32 if ndc else np.int32), np.float32 if ndc else np.int32,
+                       3 * n, "points")
         words = np.zeros(max((n + 31) // 32, 1), np.uint32)
         _check(fn(self.handle, pts.ctypes.data, n, words.ctypes.data, 0, _stream(stream)))
         return unpack_bits(words, n)
@@ -756,7 +762,7 @@ class CompressedShadowContainer:
             _checked(out, np.int32, (n + 31) // 32, "out", self.ctx.device)
             _check(_lib.cpvs_grid_lookup_ndc(self.handle, _ptr(points), n, _ptr(out), IO_DEVICE, _stream(stream)))
             return out
-        pts = np.ascontiguousarray(points, np.float32)
+        pts = _checked(np.ascontiguousarray(points, np.float32), np.float32, 3 * n, "points")
         words = np.zeros(max((n + 31) // 32, 1), np.uint32)
         _check(_lib.cpvs_grid_lookup_ndc(self.handle, pts.ctypes.data, n, words.ctypes.data, 0, _stream(stream)))
         return unpack_bits(words, n)

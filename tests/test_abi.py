@@ -128,6 +128,25 @@ def test_batch_builds_check_their_lists_before_any_device_work():
         cp.CompressedShadow.create_batch([], [(0, 0, 1)])
 
 
+def test_host_inputs_are_checked_by_shape(lib):
+    """Maps, points and triangles whose shape holds fewer values than the
+    call reads are refused before the call."""
+    import types
+    import numpy as np
+    import cpvs_gb300 as cp
+    with pytest.raises(ValueError, match="square"):
+        cp.CompressedShadow.from_depth(np.zeros((4, 8), np.float32))
+    fake = types.SimpleNamespace(handle=None, ctx=types.SimpleNamespace(handle=None, device=0))
+    with pytest.raises(ValueError, match="points: 128 elements, at least 192"):
+        cp.CompressedShadow._lookup(fake, np.zeros((64, 2), np.float32), True, None, None)
+    with pytest.raises(ValueError, match="points: 128 elements, at least 192"):
+        cp.CompressedShadow._lookup(fake, np.zeros((64, 2), np.int32), False, None, None)
+    with pytest.raises(ValueError, match="points: 128 elements, at least 192"):
+        cp.CompressedShadowContainer.lookup_ndc(fake, np.zeros((64, 2), np.float32))
+    with pytest.raises(ValueError, match="tris: 24 elements, at least 36"):
+        cp.raster_triangles(np.zeros((4, 6), np.float32), 64, 0.5, ctx=fake.ctx)
+
+
 def test_server_checks_its_buffers_before_any_device_work():
     """The server reads the map and points and writes the bits after submit
     returns, from its own thread, so a buffer too small for the request is
