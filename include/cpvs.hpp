@@ -200,6 +200,8 @@ public:
     /* Replaces create(const ShadowMap*, ...): straight from a depth image. */
     static std::unique_ptr<CompressedShadow> create(const ImageF& depth, uint zTileIndex = 0, uint zTileNum = 1,
                                                     bool leafmasks = true, Context& ctx = Context::shared()) {
+        if (depth.getWidth() != depth.getHeight() || depth.getNumChannels() != 1)
+            throw Error(CPVS_ERR_INVALID_ARG, "CompressedShadow::create: the image must be square with one channel");
         cpvs_shadow* s = nullptr;
         check(cpvs_shadow_create_from_depth(ctx.get(), depth.data(), (uint32_t)depth.getWidth(), zTileIndex,
                                             zTileNum, leafmasks ? CPVS_FLAG_LEAFMASKS : 0u, nullptr, &s));
@@ -337,6 +339,10 @@ public:
                                  CPVS_EVAL_U8, visibilities, nullptr));
     }
     void evaluate(const ImageF& positions, const mat4& lightViewProj, Image<uint8_t>& visibilities) const {
+        if (visibilities.getWidth() != positions.getWidth() || visibilities.getHeight() != positions.getHeight() ||
+            visibilities.getNumChannels() != 1)
+            throw Error(CPVS_ERR_INVALID_ARG,
+                        "CompressedShadowContainer::evaluate: visibilities must have the positions' size, one channel");
         evaluate(positions.data(), (uint)positions.getWidth(), (uint)positions.getHeight(),
                  (uint)positions.getNumChannels(), lightViewProj, visibilities.data());
     }
