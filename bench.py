@@ -166,6 +166,21 @@ def config_dict(config: str, n: int, dag_words: int, nq: int, world: int) -> dic
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
 
 
+def slowest_rank(torch, values, world: int, device) -> list:
+    """Each per-rank time's maximum over the ranks: the job takes as long as
+    its slowest replica."""
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return t.tolist()
+
+
+def whole_job_rate(world: int, units_per_rank: float, ms: float) -> float:
+    """Billions of units per second for the whole job: every replica
+    processes `units_per_rank` per step, in `ms` of the slowest rank."""
+    return world * units_per_rank / (ms * 1e-3) / 1e9
+
+
 def host_link(torch, dev, stream, nbytes=256 << 20, reps=5) -> dict:
     """Copy rate of the host link: pinned host <-> device, one
     cudaMemcpyAsync of 256 MiB per direction, best of `reps` (CUDA events)."""
@@ -360,10 +375,8 @@ def run_ours(args, rank, world, local_rank):
     link = host_link(torch, dev, stream) if world == 1 else None
 
     # slowest rank
-    t = torch.tensor([build_ms, lookup_ms, e2e_build_ms, e2e_lookup_ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    build_ms, lookup_ms, e2e_build_ms, e2e_lookup_ms = t.tolist()
+    build_ms, lookup_ms, e2e_build_ms, e2e_lookup_ms = slowest_rank(
+        torch, [build_ms, lookup_ms, e2e_build_ms, e2e_lookup_ms], world, dev)
     voxels = float(n) ** 3
 
     # kernels launched in the timed region: the eager pass's timing scopes,
@@ -413,7 +426,7 @@ def run_ours(args, rank, world, local_rank):
     lk_ms_launch = lk[0] / max(lk[1], 1)
     line = {
         "metric": METRIC,
-        "value": round(world * voxels / (build_ms * 1e-3) / 1e9, 1),
+        "value": round(whole_job_rate(world, voxels, build_ms), 1),
         "unit": "Gvoxel/s",
         "n_gpus": world,
         "steps": args.steps,
@@ -425,7 +438,7 @@ def run_ours(args, rank, world, local_rank):
         "dtype": "f32",
         "data": "synthetic: seeded scene rasterised to a float32 depth map (no dataset involved)",
         "config": config_dict(args.config, n, dag_words, nq, world),
-        "e2e": {"value": round(world * voxels / (e2e_build_ms * 1e-3) / 1e9, 1), "unit": "Gvoxel/s",
+        "e2e": {"value": round(whole_job_rate(world, voxels, e2e_build_ms), 1), "unit": "Gvoxel/s",
                 "h2d_bytes_per_step": int(depth.nbytes), "d2h_bytes_per_step": int(dag_bytes),
                 "ms_per_step": round(e2e_build_ms, 3),
                 "path": "cpvs_shadow_create_from_depth (pinned host map) + cpvs_shadow_dag_words (into pinned host memory)"},
@@ -440,13 +453,13 @@ def run_ours(args, rank, world, local_rank):
                                         "all_levels_model": {
                                             "alg_bytes": int(build_alg_all),
                                             "frac": round(build_alg_all / (build_ms * 1e-3) / 1e9 / peak, 4)}}},
-        "lookup": {"value": round(world * nq / (lookup_ms * 1e-3) / 1e9, 2), "unit": "Glookups/s",
+        "lookup": {"value": round(whole_job_rate(world, nq, lookup_ms), 2), "unit": "Glookups/s",
                    "ms_per_batch": round(lookup_ms, 4), "ms_by_queries_per_thread": variants,
                    "roofline": {"bound": "hbm", "achieved": round(lookup_alg / (lk_ms_launch * 1e-3) / 1e9, 1),
                                 "peak": peak, "unit": "GB/s",
                                 "frac": round(lookup_alg / (lk_ms_launch * 1e-3) / 1e9 / peak, 4),
                                 "alg_bytes_per_launch": int(lookup_alg)},
-                   "e2e": {"value": round(world * nq / (e2e_lookup_ms * 1e-3) / 1e9, 2), "unit": "Glookups/s",
+                   "e2e": {"value": round(whole_job_rate(world, nq, e2e_lookup_ms), 2), "unit": "Glookups/s",
                            "h2d_bytes_per_step": int(q_host.nbytes), "d2h_bytes_per_step": int(bits_host.numel() * 4),
                            "ms_per_step": round(e2e_lookup_ms, 3)}},
         "build_then_first_lookup": {"ms": round(statistics.median(first), 4),

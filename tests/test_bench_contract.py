@@ -46,3 +46,40 @@ def test_reference_arm_under_torchrun_prints_once():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+
+
+def _replica_rank(rank, port, q):
+    import torch
+    import torch.distributed as dist
+    sys.path.insert(0, ROOT)
+    import bench
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=2)
+    try:
+        # rank 1 is the slower replica on the first time, rank 0 on the second
+        ms = bench.slowest_rank(torch, [1.0 + rank, 4.0 - rank], 2, "cpu")
+        q.put((rank, ms, bench.whole_job_rate(2, 1e9, ms[0])))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_replicas_report_the_slowest_rank_over_gloo():
+    """The N>1 form of the GPU arm: every replica builds its own workload, the
+    job's time is the slowest rank's (an all-reduce of the times, the one
+    collective), and the rate counts every replica's units."""
+    import multiprocessing as mp
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_replica_rank, args=(r, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, ms, rate in got:
+        assert ms == [2.0, 4.0], (rank, ms)
+        assert rate == 2 * 1e9 / 2e-3 / 1e9  # two replicas' units in the slowest 2 ms
