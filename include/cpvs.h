@@ -17,7 +17,8 @@
  *     A plain pointer carries no size: each buffer must hold the elements
  *     its call documents, and a CPVS_IO_DEVICE pointer must be device memory
  *     of the context's device, which the call uses as given.  (The Python
- *     and C++ front ends check their arrays' sizes before they call.)
+ *     front end checks its arrays, and the C++ classes their images, before
+ *     they call.)
  *   - Handles are immutable after creation and may be read from several host
  *     threads; a cpvs_ctx must not be used by two host threads at once.
  *   - Visibility classes follow the reference's NodeVisibility
