@@ -402,6 +402,10 @@ def run_ours(args, rank, world, local_rank):
     # workload (profiles/traffic_<config>.json), when it has one
     prof = os.path.join(ROOT, "profiles", f"traffic_{args.config}.json")
     measured = json.load(open(prof)) if os.path.exists(prof) else {}
+    # the lookup kernel's DRAM and L2 figures from its committed ncu capture
+    # (profiles/lookup_<config>.json), when this workload has one
+    lk_prof_path = os.path.join(ROOT, "profiles", f"lookup_{args.config}.json")
+    lk_prof = json.load(open(lk_prof_path)) if os.path.exists(lk_prof_path) else {}
 
     def traffic_of(k):
         t = measured.get(k)
@@ -458,7 +462,10 @@ def run_ours(args, rank, world, local_rank):
                    "roofline": {"bound": "hbm", "achieved": round(lookup_alg / (lk_ms_launch * 1e-3) / 1e9, 1),
                                 "peak": peak, "unit": "GB/s",
                                 "frac": round(lookup_alg / (lk_ms_launch * 1e-3) / 1e9 / peak, 4),
-                                "alg_bytes_per_launch": int(lookup_alg)},
+                                "alg_bytes_per_launch": int(lookup_alg),
+                                "traffic": lk_prof.get("dram_bytes_per_launch"),
+                                "l2_throughput_frac_ncu": lk_prof.get("l2_throughput_frac"),
+                                "l2_hit_rate_ncu": lk_prof.get("l2_hit_rate")},
                    "e2e": {"value": round(whole_job_rate(world, nq, e2e_lookup_ms), 2), "unit": "Glookups/s",
                            "h2d_bytes_per_step": int(q_host.nbytes), "d2h_bytes_per_step": int(bits_host.numel() * 4),
                            "ms_per_step": round(e2e_lookup_ms, 3)}},
