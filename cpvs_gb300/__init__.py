@@ -28,7 +28,7 @@ IO_DEVICE = 0x100
 FLAG_BORROW_INPUT = 0x200
 EVAL_U8 = 0x400
 
-STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "device wait timed out",
+STATUS = {0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "timed out",
           4: "CUDA device error", 5: "unimplemented", 6: "memory budget exceeded", 7: "cancelled",
           8: "output buffer too small"}
 

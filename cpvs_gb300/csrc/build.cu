@@ -3450,10 +3450,12 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
         // bit 1 (a level outgrew the plan) or 16 (a hash table did): re-plan
         // from these maps' level bounds and retry; the rejected stale slots
         // that an overflow leaves behind (bits 4, 8) go with it.  Anything
-        // else is an internal fault.
+        // else is an internal fault, reported as a timeout when a bounded
+        // wait on another CTA gave up (bit 32).
         const bool overflow = (herr & (1u | 16u)) != 0;
         if (!overflow || (herr & 2u) || attempt >= 2)
-            return fail(CPVS_ERR_DEVICE, "build_dags: internal check " + std::to_string(herr));
+            return fail((herr & 32u) ? CPVS_ERR_TIMEOUT : CPVS_ERR_DEVICE,
+                        "build_dags: internal check " + std::to_string(herr));
         ++replans;
         std::vector<unsigned long long> bounds;
         {

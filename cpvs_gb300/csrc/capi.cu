@@ -260,7 +260,7 @@ const char* cpvs_status_string(cpvs_status s) {
         case CPVS_OK: return "ok";
         case CPVS_ERR_INVALID_ARG: return "invalid argument";
         case CPVS_ERR_OOM: return "out of device memory";
-        case CPVS_ERR_TIMEOUT: return "device wait timed out";
+        case CPVS_ERR_TIMEOUT: return "timed out";
         case CPVS_ERR_DEVICE: return "CUDA device error";
         case CPVS_ERR_UNIMPLEMENTED: return "unimplemented";
         case CPVS_ERR_BUDGET: return "memory budget exceeded";

@@ -48,7 +48,7 @@ typedef enum cpvs_status {
     CPVS_OK = 0,
     CPVS_ERR_INVALID_ARG = 1,  /* a size, flag or pointer the call cannot accept */
     CPVS_ERR_OOM = 2,          /* device allocation failed */
-    CPVS_ERR_TIMEOUT = 3,      /* a bounded device wait gave up */
+    CPVS_ERR_TIMEOUT = 3,      /* a bounded wait ended first: cpvs_server_wait's timeout */
     CPVS_ERR_DEVICE = 4,       /* CUDA error, or no usable device */
     CPVS_ERR_UNIMPLEMENTED = 5,
     CPVS_ERR_BUDGET = 6,       /* request exceeds the context's memory budget */
