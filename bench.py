@@ -708,8 +708,8 @@ def run_reference(args, rank, world):
     O = Oracle()
     threads = os.cpu_count() or 1
     # each step: one full build (the reference builds one DAG per thread) plus
-    # one bounded lookup sample over all host cores; the driver's steps and
-    # warm-up (20 and 5 builds of ~3 s each at 8192^2)
+    # one bounded lookup sample over all host cores; --steps and --warmup as
+    # given (20 and 5 builds of ~3 s each at 8192^2 take about 75 s)
     steps = max(1, args.steps)
     warm = max(0, args.warmup)
     sample = min(wl["queries"], 1 << 23)

@@ -3111,7 +3111,7 @@ void plan_set_shapes(BuildPlan* P, uint32_t cap, uint32_t waves) {
 // a clock ramp or a neighbour's load falls on every pair alike -- and the
 // pair with the lowest replay time is kept with its graph.  A pair whose
 // replay reports an internal check (a level or table overflow) is not taken.
-// Runs after this build's emission in stream order; the replays only rewrite
+// Runs after the current DAG build's emission in stream order; the replays only rewrite
 // the plan's own scratch.
 constexpr int kTuneRounds = 3;
 constexpr int kTuneShapes = (int)(sizeof(kClusterCaps) / sizeof(kClusterCaps[0])) * 2;
@@ -3528,7 +3528,7 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
                 cudaGraphExecDestroy(P->exec);
                 P->exec = nullptr;
             }
-            // after this build's emission (stream order), which reads the
+            // after the current DAG build's emission (stream order), which reads the
             // level table
             plan_bind_tables(P);
             CPVS_CUDA(cudaMemcpyAsync(P->lvt, P->lv, sizeof(P->lv), cudaMemcpyHostToDevice, st));
@@ -3572,7 +3572,7 @@ cpvs_status build_dags(Ctx& ctx, const std::vector<SourceSpec>& sources, const s
 // k_dedup_resolve, k_dedup_scan and k_dedup_remap, then k_layout and k_emit
 // per level.  It is those kernels' only user, so a change to the node
 // layout, the error bits or the segment bookkeeping of the main path must be
-// mirrored there; tests/test_zz_no_alloc.py compares this build word for
+// mirrored there; tests/test_zz_no_alloc.py compares the allocation-free build word for
 // word with the allocating build and with the oracle.
 // ---------------------------------------------------------------------------
 namespace cpvs {

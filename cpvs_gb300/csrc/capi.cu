@@ -290,7 +290,7 @@ cpvs_status cpvs_ctx_create(int device, cpvs_ctx** out) {
     props.location.id = device;
     cudaMemPool_t pool = nullptr;
     CPVS_CUDA(cudaMemPoolCreate(&pool, &props));
-    uint64_t keep = ~0ull;  // never hand freed blocks back to the driver
+    uint64_t keep = ~0ull;  // freed blocks stay in the pool: never returned to the CUDA driver
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
     cudaStream_t fs = nullptr;
     cudaError_t e2 = cudaStreamCreateWithFlags(&fs, cudaStreamNonBlocking);

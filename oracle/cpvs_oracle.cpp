@@ -2,7 +2,7 @@
  * cpvs_oracle.cpp -- CPU restatement of the reference's shadow build and
  * visibility lookup (TobiasRp/cpvs).
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker the CUDA path is compared
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle the CUDA path is compared
  * against: only tests/, __graft_entry__.smoke() and bench.py's CPU baseline
  * leg load it.  The product never links or calls it.
  *
@@ -18,9 +18,9 @@
  *
  * Parity unpinned: the shader restatements (oracle_grid_evaluate's float
  * transform and oracle_shade) follow the GLSL of shader/traverse.cs and
- * shader/shade.frag, which cannot run here (no graphics stack on this machine);
- * their float32 operation order is this build's definition, and the GPU path
- * is checked against it bit for bit.  The lookup part of evaluate is pinned
+ * shader/shade.frag, which need a GL context that no machine here provides;
+ * GLSL leaves their float32 operation order open, so the order is defined
+ * here, and the GPU path is checked against it bit for bit.  The lookup part of evaluate is pinned
  * like the other lookups.
  */
 #include <algorithm>

@@ -22,7 +22,7 @@ def test_reference_arm_prints_one_contract_line():
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert d["e2e"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
-    # the driver's steps and warm-up, and the GPU arm's config dict (bench.config_dict)
+    # the steps and warm-up given, and the GPU arm's config dict (bench.config_dict)
     assert d["steps"] == 1 and d["warmup"] == 1
     assert set(d["config"]) == {"workload", "map_side", "voxels_per_dag", "dag_words", "lookups_per_batch", "l2",
                                 "parallelism"}

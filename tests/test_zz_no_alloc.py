@@ -56,7 +56,8 @@ def test_noalloc_without_leafmasks_and_small_maps(cp):
 def test_noalloc_matches_oracle(cp, oracle):
     """Random maps of five kinds and maps whose depths sit on or beside voxel
     boundaries, with and without z-tiles, against the oracle's DAG words
-    (the multi-pass kernels this build runs are used by no other path)."""
+    (the multi-pass kernels the allocation-free build runs are used by no
+    other path)."""
     import torch
     from test_gpu_parity import boundary_map, random_map
     lib = cp.load_library()
