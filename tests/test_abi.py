@@ -145,9 +145,67 @@ def test_host_inputs_are_checked_by_shape(lib):
         cp.CompressedShadowContainer.lookup_ndc(fake, np.zeros((64, 2), np.float32))
     with pytest.raises(ValueError, match="tris: 24 elements, at least 36"):
         cp.raster_triangles(np.zeros((4, 6), np.float32), 64, 0.5, ctx=fake.ctx)
+    # well-formed inputs pass the checks and meet the null handles in the library
+    for call in (lambda: cp.CompressedShadow._lookup(fake, np.zeros((64, 3), np.float32), True, None, None),
+                 lambda: cp.CompressedShadow._lookup(fake, np.zeros((64, 3), np.int32), False, None, None),
+                 lambda: cp.CompressedShadowContainer.lookup_ndc(fake, np.zeros((64, 3), np.float32)),
+                 lambda: cp.raster_triangles(np.zeros((4, 9), np.float32), 64, 0.5, ctx=fake.ctx)):
+        with pytest.raises(cp.CpvsError) as e:
+            call()
+        assert e.value.status == 1
 
 
-def test_server_checks_its_buffers_before_any_device_work():
+class _DeviceLike:
+    """Stands in for a CUDA tensor on device 0 (host memory behind it), so the
+    mirror's device-input checks run without a GPU.  A call that gets past
+    them reaches the C ABI with a null context and is refused there."""
+    is_cuda = True
+
+    def __init__(self, arr):
+        import types
+        self.a = arr
+        self.shape = arr.shape
+        self.device = types.SimpleNamespace(index=0)
+        self.dtype = types.SimpleNamespace(is_floating_point=arr.dtype.kind == "f")
+
+    def is_contiguous(self):
+        return self.a.flags.c_contiguous
+
+    def element_size(self):
+        return self.a.itemsize
+
+    def numel(self):
+        return self.a.size
+
+    def data_ptr(self):
+        return self.a.ctypes.data
+
+
+def test_device_maps_are_checked_before_the_call(lib):
+    """A square float32 contiguous device map passes the checks (and meets
+    the null context in the library); a map of another element type, a
+    strided one or one on another device is refused first."""
+    import types
+    import numpy as np
+    import cpvs_gb300 as cp
+    ctx = types.SimpleNamespace(handle=None, device=0)
+    good = _DeviceLike(np.zeros((64, 64), np.float32))
+    for make in (lambda d: cp.CompressedShadow.from_depth(d, ctx=ctx), lambda d: cp.MinMaxHierarchy(d, ctx=ctx)):
+        with pytest.raises(cp.CpvsError, match="null argument") as e:
+            make(good)
+        assert e.value.status == 1
+        with pytest.raises(ValueError, match="4-byte floats"):
+            make(_DeviceLike(np.zeros((64, 64), np.float64)))
+        with pytest.raises(ValueError, match="contiguous"):
+            make(_DeviceLike(np.zeros((64, 128), np.float32)[:, ::2]))
+    other = types.SimpleNamespace(handle=None, device=1)
+    with pytest.raises(ValueError, match="device 1"):
+        cp.CompressedShadow.from_depth(good, ctx=other)
+    with pytest.raises(ValueError, match="device 1"):
+        cp.MinMaxHierarchy(good, ctx=other)
+
+
+def test_server_checks_its_buffers_before_any_device_work(lib):
     """The server reads the map and points and writes the bits after submit
     returns, from its own thread, so a buffer too small for the request is
     refused at submission."""
@@ -163,6 +221,13 @@ def test_server_checks_its_buffers_before_any_device_work():
         cp.Server.submit_lookup(srv, 0, np.zeros((64, 3), np.float32), np.zeros(1, np.uint32))
     with pytest.raises(ValueError, match="integers"):
         cp.Server.submit_lookup(srv, 0, np.zeros((64, 3), np.float32), np.zeros(2, np.float32))
+    # well-formed requests pass the checks and meet the null server in the library
+    for call in (lambda: cp.Server.submit_build(srv, 0, np.zeros((64, 64), np.float32)),
+                 lambda: cp.Server.submit_lookup(srv, 0, np.zeros((64, 3), np.float32)),
+                 lambda: cp.Server.submit_lookup(srv, 0, np.zeros((64, 3), np.float32), np.zeros(2, np.uint32))):
+        with pytest.raises(cp.CpvsError) as e:
+            call()
+        assert e.value.status == 1
 
 
 @pytest.mark.gpu
