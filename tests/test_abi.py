@@ -264,3 +264,33 @@ def test_every_entry_point_refuses_null_handles(lib):
         elif res is not None and name != "cpvs_abi_version":
             assert not r, (name, r)  # sizes and counts of nothing are 0, handles null
     assert called >= 50
+
+
+def test_header_is_plain_c(lib, tmp_path):
+    """include/cpvs.h compiles as strict C99 and links from C; without a GPU
+    the context call reports the device error (no fallback) and the program
+    still exits cleanly."""
+    import shutil
+    import torch
+    if not shutil.which("gcc"):
+        pytest.skip("no gcc")
+    src = tmp_path / "abi.c"
+    src.write_text(
+        '#include "cpvs.h"\n#include <stdio.h>\n'
+        "int main(void) {\n"
+        "    cpvs_ctx* ctx = NULL;\n"
+        "    cpvs_build_job job = {0, 0, 1};\n"
+        "    cpvs_server_config cfg = {0, 0, 0, CPVS_FLAG_LEAFMASKS};\n"
+        "    cpvs_status s = cpvs_ctx_create(0, &ctx);\n"
+        "    (void)job; (void)cfg;\n"
+        '    if (s != CPVS_OK) { printf("%s\\n", cpvs_status_string(s)); return 0; }\n'
+        '    printf("ok\\n");\n'
+        "    cpvs_ctx_destroy(ctx);\n"
+        "    return 0;\n"
+        "}\n")
+    libdir = os.path.join(ROOT, "cpvs_gb300")
+    exe = str(tmp_path / "abi")
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-L", libdir, "-lcpvs_gb300", f"-Wl,-rpath,{libdir}", "-o", exe], check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=120, check=True).stdout.strip()
+    assert out == ("ok" if torch.cuda.is_available() else "CUDA device error")
