@@ -294,3 +294,20 @@ def test_header_is_plain_c(lib, tmp_path):
                     str(src), "-L", libdir, "-lcpvs_gb300", f"-Wl,-rpath,{libdir}", "-o", exe], check=True)
     out = subprocess.run([exe], capture_output=True, text=True, timeout=120, check=True).stdout.strip()
     assert out == ("ok" if torch.cuda.is_available() else "CUDA device error")
+
+
+def test_product_never_uses_the_oracle(lib):
+    """The library links nothing of oracle/ and the package imports nothing
+    from it: the oracle is test infrastructure only."""
+    from cpvs_gb300 import LIB_PATH
+    needed = subprocess.run(["readelf", "-d", LIB_PATH], capture_output=True, text=True, check=True).stdout
+    assert "oracle" not in needed and "cpvs_ref" not in needed
+    pkg = os.path.join(ROOT, "cpvs_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".h", ".hpp")):
+                src = open(os.path.join(dirpath, f)).read()
+                assert not re.search(r"^\s*(import oracle|from oracle)", src, re.M), f
+                assert not re.search(r'#include\s*[<"][^>"]*oracle', src), f
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        assert "oracle" not in open(os.path.join(ROOT, "include", f)).read(), f
